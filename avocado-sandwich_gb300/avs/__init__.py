@@ -1,0 +1,302 @@
+"""Python host mirror of the reference's tiled singular-value entry point.
+
+Binds ``libavs.so`` (the C-ABI library built from ``../csrc``) with ctypes and
+mirrors the reference's Julia interface for this path
+(evelyne-ringoot/Avocado-sandwich):
+
+* ``my_CU_svdval(A, block_size)`` -- CUDAbasedSVD/SVD_GPU.jl:257-283: host
+  (numpy) or device (CUDA torch tensor) matrix in, singular values out
+  (descending).  Raises ``NotImplementedError("Not implemented")`` exactly where
+  the reference calls ``error("Not implemented")`` (non-square, tile not a
+  power of two, tile < 16, tile not dividing n).
+* ``Blockbidiag(A, tile)`` -- Blockbidiag! on a TiledMatrix
+  (KAbasedSVD/src/tiledalgos.jl:17-34, TiledMatrix.jl:41-67), in place on a
+  device matrix.
+* ``bidiagonalize(band, bw)`` -- KAbasedSVD/src/bulgechasing.jl:33-42 on the GPU.
+* ``diag_lapack(d, e)`` -- bulgechasing.jl:50-53 (bdsdc('U','N')), by FP64
+  bisection on the GPU.
+* ``geqrt_tile`` / ``tsqrt_tile`` -- the tile kernels of
+  KAbasedSVD/src/QRkernels.jl:3-129.
+
+Device matrices are column-major like Julia's: a torch tensor ``t`` of shape
+(n, n) stores the column-major matrix ``t.T``.  ``to_device`` / ``from_device``
+convert numpy arrays.  There is no CPU fallback: every call runs the CUDA
+library, and a missing library raises at import of the binding.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = [
+    "AvsError", "Handle", "lib", "library_path", "my_CU_svdval", "svdvals", "Blockbidiag", "extract_band",
+    "bidiagonalize", "diag_lapack", "geqrt_tile", "tsqrt_tile", "to_device", "from_device", "PREC",
+    "NOT_IMPLEMENTED", "EXPORTED_SYMBOLS", "Report",
+]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_HANDLES = {}
+
+NOT_IMPLEMENTED = -100
+PREC = {"default": 0, "fp64": 1, "fp32": 2, "tf32": 3, "tf32x3": 4, "bf16": 5, "bf16x3": 6}
+
+EXPORTED_SYMBOLS = [
+    "avs_create", "avs_destroy", "avs_reserve", "avs_strerror", "avs_version",
+    "avs_svdvals_s", "avs_svdvals_d", "avs_svdvals_dev_s", "avs_svdvals_dev_d",
+    "avs_blockbidiag_dev_s", "avs_blockbidiag_dev_d", "avs_extract_band_dev_s", "avs_extract_band_dev_d",
+    "avs_band_to_bidiag_dev", "avs_bidiag_svals_dev",
+    "avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d", "avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d",
+]
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int32), ("flags", ctypes.c_int32), ("bisect_rel_tol", ctypes.c_double),
+                ("stream", ctypes.c_void_p)]
+
+
+class Report(ctypes.Structure):
+    _fields_ = [("t_total_ms", ctypes.c_double), ("t_stage1_ms", ctypes.c_double), ("t_stage2_ms", ctypes.c_double),
+                ("t_stage3_ms", ctypes.c_double), ("t_h2d_ms", ctypes.c_double), ("t_d2h_ms", ctypes.c_double),
+                ("kernel_launches", ctypes.c_int64), ("workspace_bytes", ctypes.c_int64),
+                ("precision", ctypes.c_int32), ("status", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class AvsError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        msg = lib().avs_strerror(status).decode() if _LIB is not None else str(status)
+        super().__init__("%s: %s (status %d)" % (what, msg, status) if what else "%s (status %d)" % (msg, status))
+
+
+def library_path():
+    return os.path.join(_HERE, "libavs.so")
+
+
+def lib():
+    """Load libavs.so (raises OSError if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        path = library_path()
+        if not os.path.exists(path):
+            raise OSError("libavs.so not built: run __graft_entry__.build() (or avs/build.py)")
+        L = ctypes.CDLL(path)
+        P, I64, I32, I = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_int
+        OP, RP = ctypes.POINTER(Opts), ctypes.POINTER(Report)
+        L.avs_create.argtypes = [ctypes.POINTER(P), I]
+        L.avs_destroy.argtypes = [P]
+        L.avs_reserve.argtypes = [P, I64, I32, I32]
+        L.avs_strerror.argtypes = [I]
+        L.avs_strerror.restype = ctypes.c_char_p
+        L.avs_version.restype = I
+        for nm in ("avs_svdvals_s", "avs_svdvals_d", "avs_svdvals_dev_s", "avs_svdvals_dev_d"):
+            getattr(L, nm).argtypes = [P, I64, I64, I64, I32, P, P, OP, RP]
+        for nm in ("avs_blockbidiag_dev_s", "avs_blockbidiag_dev_d"):
+            getattr(L, nm).argtypes = [P, I64, I64, I32, P, OP, RP]
+        for nm in ("avs_extract_band_dev_s", "avs_extract_band_dev_d"):
+            getattr(L, nm).argtypes = [P, I64, I64, I32, P, P, I64]
+        L.avs_band_to_bidiag_dev.argtypes = [P, I64, I32, P, I64, P, P, RP]
+        L.avs_bidiag_svals_dev.argtypes = [P, I64, P, P, P, ctypes.c_double, RP]
+        for nm in ("avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d"):
+            getattr(L, nm).argtypes = [P, I32, P, P]
+        for nm in ("avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d"):
+            getattr(L, nm).argtypes = [P, I32, P, P, P]
+        for nm in EXPORTED_SYMBOLS:
+            if nm not in ("avs_strerror",):
+                getattr(L, nm).restype = I
+        _LIB = L
+    return _LIB
+
+
+class Handle:
+    """One avs_handle (CUDA stream + grow-only workspace) on one device."""
+
+    def __init__(self, device=0):
+        self.ptr = ctypes.c_void_p()
+        rc = lib().avs_create(ctypes.byref(self.ptr), int(device))
+        if rc != 0:
+            raise AvsError(rc, "avs_create")
+        self.device = device
+
+    def close(self):
+        if self.ptr:
+            lib().avs_destroy(self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reserve(self, n, tile, precision="default"):
+        rc = lib().avs_reserve(self.ptr, int(n), int(tile), _prec(precision))
+        _check(rc, "avs_reserve")
+
+
+def default_handle(device=0):
+    h = _HANDLES.get(device)
+    if h is None:
+        h = _HANDLES[device] = Handle(device)
+    return h
+
+
+def _prec(p):
+    if p is None:
+        return 0
+    if isinstance(p, str):
+        return PREC[p.lower()]
+    return int(p)
+
+
+def _check(rc, what):
+    if rc == NOT_IMPLEMENTED:
+        raise NotImplementedError("Not implemented")
+    if rc != 0:
+        raise AvsError(rc, what)
+
+
+def _is_torch_cuda(x):
+    return hasattr(x, "is_cuda") and getattr(x, "is_cuda")
+
+
+def to_device(a, device=0):
+    """numpy (n x m) -> CUDA torch tensor holding the same matrix column-major."""
+    import torch
+    a = np.asarray(a)
+    return torch.from_numpy(np.ascontiguousarray(a.T)).to("cuda:%d" % device)
+
+
+def from_device(t):
+    """Inverse of to_device: CUDA tensor holding a column-major matrix -> numpy."""
+    return t.detach().cpu().numpy().T.copy()
+
+
+def my_CU_svdval(A, block_size, precision=None, report=None, handle=None, rel_tol=0.0):
+    """Singular values (descending) of the square matrix A with tile ``block_size``.
+
+    ``A`` is a numpy array (the ``Matrix{Float32}`` method, host copies inside
+    the call) or a CUDA torch tensor holding the matrix column-major (the
+    ``CuMatrix{Float32}`` method, result returned as a CUDA tensor).  float32
+    and float64 are supported; the input is never modified.
+    """
+    h = handle or default_handle()
+    o = Opts(_prec(precision), 0, float(rel_tol), None)
+    r = report if report is not None else Report()
+    if _is_torch_cuda(A):
+        import torch
+        if A.dim() != 2:
+            raise NotImplementedError("Not implemented")
+        if A.dtype not in (torch.float32, torch.float64):
+            raise TypeError("float32 / float64 only")
+        # tensor (c, r) row-major = column-major r x c matrix with ld = stride(0)
+        n_rows, n_cols = A.shape[1], A.shape[0]
+        if A.stride(1) != 1:
+            A = A.contiguous()
+        lda = max(A.stride(0), 1)
+        out = torch.empty(n_cols, dtype=A.dtype, device=A.device)
+        fn = lib().avs_svdvals_dev_d if A.dtype == torch.float64 else lib().avs_svdvals_dev_s
+        o.stream = ctypes.c_void_p(torch.cuda.current_stream(A.device).cuda_stream)
+        rc = fn(h.ptr, n_rows, n_cols, lda, int(block_size), ctypes.c_void_p(A.data_ptr()),
+                ctypes.c_void_p(out.data_ptr()), ctypes.byref(o), ctypes.byref(r))
+        _check(rc, "avs_svdvals_dev")
+        return out
+    a = np.asarray(A)
+    if a.ndim != 2:
+        raise NotImplementedError("Not implemented")
+    if a.dtype not in (np.float32, np.float64):
+        a = a.astype(np.float32)
+    a = np.asfortranarray(a)
+    m, n = a.shape
+    out = np.empty(n, dtype=a.dtype)
+    fn = lib().avs_svdvals_d if a.dtype == np.float64 else lib().avs_svdvals_s
+    rc = fn(h.ptr, m, n, max(m, 1), int(block_size), ctypes.c_void_p(a.ctypes.data),
+            ctypes.c_void_p(out.ctypes.data), ctypes.byref(o), ctypes.byref(r))
+    _check(rc, "avs_svdvals")
+    return out
+
+
+svdvals = my_CU_svdval
+
+
+def Blockbidiag(A, tile, handle=None):
+    """Blockbidiag! in place on a CUDA tensor holding a column-major n x n matrix."""
+    import torch
+    h = handle or default_handle()
+    n = A.shape[0]
+    if A.dim() != 2 or A.shape[0] != A.shape[1] or not A.is_contiguous():
+        raise NotImplementedError("Not implemented")
+    fn = lib().avs_blockbidiag_dev_d if A.dtype == torch.float64 else lib().avs_blockbidiag_dev_s
+    r = Report()
+    rc = fn(h.ptr, n, n, int(tile), ctypes.c_void_p(A.data_ptr()), None, ctypes.byref(r))
+    _check(rc, "avs_blockbidiag_dev")
+    return r
+
+
+def extract_band(A, bw, handle=None):
+    """Upper band (0 <= j - i <= bw) of a device column-major matrix -> dense FP64 device matrix."""
+    import torch
+    h = handle or default_handle()
+    n = A.shape[0]
+    B = torch.empty((n, n), dtype=torch.float64, device=A.device)
+    fn = lib().avs_extract_band_dev_d if A.dtype == torch.float64 else lib().avs_extract_band_dev_s
+    rc = fn(h.ptr, n, n, int(bw), ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()), n)
+    _check(rc, "avs_extract_band_dev")
+    return B
+
+
+def bidiagonalize(B, bw, handle=None):
+    """Dense FP64 device band matrix (column-major) -> (d, e) FP64 device vectors."""
+    import torch
+    h = handle or default_handle()
+    n = B.shape[0]
+    d = torch.empty(n, dtype=torch.float64, device=B.device)
+    e = torch.empty(max(n - 1, 1), dtype=torch.float64, device=B.device)
+    r = Report()
+    rc = lib().avs_band_to_bidiag_dev(h.ptr, n, int(bw), ctypes.c_void_p(B.data_ptr()), n,
+                                      ctypes.c_void_p(d.data_ptr()), ctypes.c_void_p(e.data_ptr()), ctypes.byref(r))
+    _check(rc, "avs_band_to_bidiag_dev")
+    return d, e[: max(n - 1, 0)]
+
+
+def diag_lapack(d, e, rel_tol=0.0, handle=None):
+    """Singular values (descending) of the upper bidiagonal (d, e) on the GPU."""
+    import torch
+    h = handle or default_handle()
+    n = d.shape[0]
+    s = torch.empty(n, dtype=torch.float64, device=d.device)
+    rc = lib().avs_bidiag_svals_dev(h.ptr, n, ctypes.c_void_p(d.data_ptr()),
+                                    ctypes.c_void_p(e.data_ptr()) if e.numel() else None,
+                                    ctypes.c_void_p(s.data_ptr()), float(rel_tol), None)
+    _check(rc, "avs_bidiag_svals_dev")
+    return s
+
+
+def geqrt_tile(a, handle=None):
+    """GEQRT of one b x b tile (numpy in, numpy factors + tau out), on the GPU."""
+    import torch
+    h = handle or default_handle()
+    a = np.asarray(a)
+    b = a.shape[0]
+    t = to_device(a)
+    tau = torch.zeros(b, dtype=t.dtype, device=t.device)
+    fn = lib().avs_geqrt_tile_dev_d if a.dtype == np.float64 else lib().avs_geqrt_tile_dev_s
+    _check(fn(h.ptr, b, ctypes.c_void_p(t.data_ptr()), ctypes.c_void_p(tau.data_ptr())), "avs_geqrt_tile_dev")
+    return from_device(t), tau.cpu().numpy()
+
+
+def tsqrt_tile(r, bt, handle=None):
+    """TSQRT of [triu(r); bt] (numpy in) -> (r', V, tau), on the GPU."""
+    import torch
+    h = handle or default_handle()
+    r = np.asarray(r)
+    b = r.shape[0]
+    tr, tb = to_device(r), to_device(np.asarray(bt, dtype=r.dtype))
+    tau = torch.zeros(b, dtype=tr.dtype, device=tr.device)
+    fn = lib().avs_tsqrt_tile_dev_d if r.dtype == np.float64 else lib().avs_tsqrt_tile_dev_s
+    _check(fn(h.ptr, b, ctypes.c_void_p(tr.data_ptr()), ctypes.c_void_p(tb.data_ptr()),
+              ctypes.c_void_p(tau.data_ptr())), "avs_tsqrt_tile_dev")
+    return from_device(tr), from_device(tb), tau.cpu().numpy()

@@ -1,0 +1,560 @@
+// C ABI of the GB300 tiled SVD: handle, workspace, argument checks and the
+// three-stage pipeline behind my_CU_svdval (CUDAbasedSVD/SVD_GPU.jl:257-283).
+#include <cfloat>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include "avs_common.cuh"
+
+namespace avs {
+static thread_local cudaError_t g_last_cuda = cudaSuccess;
+void set_last_cuda_error(cudaError_t e) { g_last_cuda = e; }
+}  // namespace avs
+
+using namespace avs;
+
+struct avs_handle {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    void *ws = nullptr;
+    size_t ws_bytes = 0;
+    cudaEvent_t ev[6] = {};
+    int *h_err = nullptr;  // pinned status word
+};
+
+namespace {
+
+constexpr int kMaxTile = 256;
+
+inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
+
+inline bool is_pow2(int64_t x) { return x > 0 && (x & (x - 1)) == 0; }
+
+// Workspace carve-up for one call.
+struct Layout {
+    size_t off_w, off_stage, off_tau, off_tblk, off_flags1, off_flags2, off_err, off_ab, off_d, off_e, off_sig,
+        off_scr, off_out, total;
+    int64_t ldab;
+};
+
+Layout make_layout(int64_t n, int b, size_t elem, size_t stage_elem) {
+    Layout L{};
+    const int64_t nt = n / b;
+    size_t o = 0;
+    L.off_err = o;
+    o = align_up(o + 64);
+    L.off_w = o;
+    o = align_up(o + elem * (size_t)n * (size_t)n);
+    L.off_stage = o;
+    o = align_up(o + stage_elem * (size_t)n * (size_t)n);
+    L.off_tau = o;
+    o = align_up(o + elem * (size_t)(nt + 1) * (size_t)b);
+    L.off_tblk = o;
+    o = align_up(o + elem * (size_t)(nt + 1) * (size_t)(b / 16) * 256);
+    L.off_flags1 = o;
+    o = align_up(o + sizeof(int) * (size_t)(nt + 4));
+    L.off_flags2 = o;
+    o = align_up(o + sizeof(int) * (size_t)(n + 4));
+    L.ldab = 3 * (int64_t)b;
+    L.off_ab = o;
+    o = align_up(o + sizeof(double) * (size_t)L.ldab * (size_t)n);
+    L.off_d = o;
+    o = align_up(o + sizeof(double) * (size_t)n);
+    L.off_e = o;
+    o = align_up(o + sizeof(double) * (size_t)(n + 1));
+    L.off_sig = o;
+    o = align_up(o + sizeof(double) * (size_t)n);
+    L.off_scr = o;
+    o = align_up(o + sizeof(double) * 8);
+    L.off_out = o;
+    o = align_up(o + sizeof(double) * (size_t)n);
+    L.total = o;
+    return L;
+}
+
+int ensure_ws(avs_handle *h, size_t bytes) {
+    if (h->ws_bytes >= bytes) return AVS_SUCCESS;
+    if (h->ws) {
+        cudaStreamSynchronize(h->stream);
+        cudaFree(h->ws);
+        h->ws = nullptr;
+        h->ws_bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&h->ws, bytes);
+    if (e != cudaSuccess) {
+        set_last_cuda_error(e);
+        cudaGetLastError();
+        return AVS_ERR_OOM;
+    }
+    h->ws_bytes = bytes;
+    return AVS_SUCCESS;
+}
+
+inline char *ws_at(avs_handle *h, size_t off) { return reinterpret_cast<char *>(h->ws) + off; }
+
+int resolve_precision(int32_t requested, bool input_double) {
+    if (requested == AVS_PREC_DEFAULT) return input_double ? AVS_PREC_FP64 : AVS_PREC_FP32;
+    return requested;
+}
+
+// Storage element size of the stage-1 tiles for a precision mode (0 = not provided by this build).
+size_t storage_elem(int prec) {
+    switch (prec) {
+        case AVS_PREC_FP64: return 8;
+        case AVS_PREC_FP32: return 4;
+        default: return 0;
+    }
+}
+
+int check_common(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const void *A, const void *sigma) {
+    if (!h) return -1;
+    if (m < 0) return -2;
+    if (n < 0) return -3;
+    if (lda < (m > 1 ? m : 1)) return -4;
+    if (m != n) return AVS_ERR_NOT_IMPLEMENTED;
+    if (!is_pow2(tile) || tile < 16 || (n > 0 && n % tile != 0)) return AVS_ERR_NOT_IMPLEMENTED;
+    if (tile > kMaxTile) return AVS_ERR_UNSUPPORTED;
+    if (n > 0 && !A) return -6;
+    if (n > 0 && !sigma) return -7;
+    return AVS_SUCCESS;
+}
+
+int finish_status(avs_handle *h, cudaStream_t s) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        set_last_cuda_error(e);
+        return AVS_ERR_CUDA;
+    }
+    int dev_err = *h->h_err;
+    if (dev_err == kDevTimeout) return AVS_ERR_TIMEOUT;
+    if (dev_err == kDevNonfinite) return AVS_ERR_NONFINITE;
+    if (dev_err != kDevOk) return AVS_ERR_INTERNAL;
+    return AVS_SUCCESS;
+}
+
+float ev_ms(cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+        cudaGetLastError();
+        return 0.f;
+    }
+    return ms;
+}
+
+// The pipeline on device data.  S = tile storage type.  src holds the input
+// (type TI, leading dimension lds) on the device; sigma_out (type TO) on the device.
+template <typename S, typename TI, typename TO>
+int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src, int64_t lds, TO *sigma_out,
+                 double rel_tol, cudaStream_t s, avs_report *rep) {
+    int rc;
+    int64_t launches = 0;
+    S *W = reinterpret_cast<S *>(ws_at(h, L.off_w));
+    int *err = reinterpret_cast<int *>(ws_at(h, L.off_err));
+    AVS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
+    if ((rc = copy_convert_2d<TI, S>(src, lds, W, n, n, n, s)) != AVS_SUCCESS) return rc;
+    ++launches;
+    Stage1Work w1;
+    w1.tau = ws_at(h, L.off_tau);
+    w1.tblk = ws_at(h, L.off_tblk);
+    w1.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags1));
+    w1.err = err;
+    if ((rc = stage1_ge2bnd<S>(W, n, n, b, w1, s, &launches)) != AVS_SUCCESS) return rc;
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
+    double *AB = reinterpret_cast<double *>(ws_at(h, L.off_ab));
+    double *dd = reinterpret_cast<double *>(ws_at(h, L.off_d));
+    double *de = reinterpret_cast<double *>(ws_at(h, L.off_e));
+    if ((rc = extract_band_compact<S>(W, n, n, b, AB, L.ldab, s)) != AVS_SUCCESS) return rc;
+    ++launches;
+    Stage2Work w2;
+    w2.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags2));
+    w2.err = err;
+    if ((rc = stage2_chase(AB, n, b, L.ldab, dd, de, w2, s, h->num_sms, &launches)) != AVS_SUCCESS) return rc;
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[2], s));
+    double *sig = reinterpret_cast<double *>(ws_at(h, L.off_sig));
+    if ((rc = stage3_bisect(dd, de, n, rel_tol, sig, reinterpret_cast<double *>(ws_at(h, L.off_scr)), s,
+                            &launches)) != AVS_SUCCESS)
+        return rc;
+    if ((rc = cast_from_double<TO>(sig, sigma_out, n, s)) != AVS_SUCCESS) return rc;
+    ++launches;
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[3], s));
+    AVS_CUDA_TRY(cudaMemcpyAsync(h->h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    rc = finish_status(h, s);
+    if (rep) {
+        rep->t_stage1_ms = ev_ms(h->ev[0], h->ev[1]);
+        rep->t_stage2_ms = ev_ms(h->ev[1], h->ev[2]);
+        rep->t_stage3_ms = ev_ms(h->ev[2], h->ev[3]);
+        rep->t_total_ms = ev_ms(h->ev[0], h->ev[3]);
+        rep->kernel_launches = launches;
+        rep->workspace_bytes = (int64_t)h->ws_bytes;
+        rep->status = rc;
+    }
+    return rc;
+}
+
+template <typename TI, typename TO>
+int svdvals_dev(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const TI *dA, TO *dsigma,
+                const avs_opts *opts, avs_report *rep) {
+    int rc = check_common(h, m, n, lda, tile, dA, dsigma);
+    if (rep) {
+        std::memset(rep, 0, sizeof(*rep));
+        rep->status = rc;
+    }
+    if (rc != AVS_SUCCESS || n == 0) return rc;
+    const int prec = resolve_precision(opts ? opts->precision : 0, sizeof(TI) == 8);
+    const size_t elem = storage_elem(prec);
+    if (elem == 0) return AVS_ERR_UNSUPPORTED;
+    if (rep) rep->precision = prec;
+    cudaStream_t s = (opts && opts->stream) ? reinterpret_cast<cudaStream_t>(opts->stream) : h->stream;
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    const Layout L = make_layout(n, tile, elem, 0);
+    if ((rc = ensure_ws(h, L.total)) != AVS_SUCCESS) return rc;
+    const double tol = (opts && opts->bisect_rel_tol > 0) ? opts->bisect_rel_tol : 2.0 * DBL_EPSILON;
+    if (elem == 8) return run_pipeline<double, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, s, rep);
+    return run_pipeline<float, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, s, rep);
+}
+
+template <typename T>
+int svdvals_host(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const T *A, T *sigma,
+                 const avs_opts *opts, avs_report *rep) {
+    int rc = check_common(h, m, n, lda, tile, A, sigma);
+    if (rep) {
+        std::memset(rep, 0, sizeof(*rep));
+        rep->status = rc;
+    }
+    if (rc != AVS_SUCCESS || n == 0) return rc;
+    const int prec = resolve_precision(opts ? opts->precision : 0, sizeof(T) == 8);
+    const size_t elem = storage_elem(prec);
+    if (elem == 0) return AVS_ERR_UNSUPPORTED;
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    const Layout L = make_layout(n, tile, elem, sizeof(T));
+    if ((rc = ensure_ws(h, L.total)) != AVS_SUCCESS) return rc;
+    cudaStream_t s = h->stream;
+    T *stage = reinterpret_cast<T *>(ws_at(h, L.off_stage));
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[4], s));
+    AVS_CUDA_TRY(cudaMemcpy2DAsync(stage, sizeof(T) * (size_t)n, A, sizeof(T) * (size_t)lda, sizeof(T) * (size_t)n,
+                                   (size_t)n, cudaMemcpyHostToDevice, s));
+    avs_opts o2 = opts ? *opts : avs_opts{};
+    o2.stream = s;
+    avs_report r2{};
+    const double tol = (o2.bisect_rel_tol > 0) ? o2.bisect_rel_tol : 2.0 * DBL_EPSILON;
+    T *dout = reinterpret_cast<T *>(ws_at(h, L.off_out));
+    if (elem == 8)
+        rc = run_pipeline<double, T, T>(h, L, n, tile, stage, n, dout, tol, s, &r2);
+    else
+        rc = run_pipeline<float, T, T>(h, L, n, tile, stage, n, dout, tol, s, &r2);
+    if (rc == AVS_SUCCESS) {
+        AVS_CUDA_TRY(cudaMemcpyAsync(sigma, dout, sizeof(T) * (size_t)n, cudaMemcpyDeviceToHost, s));
+        AVS_CUDA_TRY(cudaEventRecord(h->ev[5], s));
+        AVS_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    if (rep) {
+        *rep = r2;
+        rep->precision = prec;
+        if (rc == AVS_SUCCESS) {
+            rep->t_h2d_ms = ev_ms(h->ev[4], h->ev[0]);
+            rep->t_d2h_ms = ev_ms(h->ev[3], h->ev[5]);
+            rep->t_total_ms = ev_ms(h->ev[4], h->ev[5]);
+        }
+        rep->status = rc;
+    }
+    return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int avs_version(void) { return AVS_VERSION_MAJOR * 100 + AVS_VERSION_MINOR; }
+
+const char *avs_strerror(int status) {
+    switch (status) {
+        case AVS_SUCCESS: return "success";
+        case AVS_ERR_NOT_IMPLEMENTED: return "Not implemented";
+        case AVS_ERR_CUDA: return "CUDA runtime error";
+        case AVS_ERR_OOM: return "out of device memory";
+        case AVS_ERR_TIMEOUT: return "a bounded device-side wait timed out";
+        case AVS_ERR_NONFINITE: return "non-finite value met in the factorisation";
+        case AVS_ERR_NO_DEVICE: return "no usable CUDA device";
+        case AVS_ERR_UNSUPPORTED: return "valid request not provided by this build";
+        case AVS_ERR_INTERNAL: return "internal error";
+        default: return status < 0 ? "invalid argument" : "unknown error";
+    }
+}
+
+int avs_create(avs_handle **out, int device) {
+    if (!out) return -1;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        return AVS_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) return -2;
+    avs_handle *h = new (std::nothrow) avs_handle();
+    if (!h) return AVS_ERR_INTERNAL;
+    h->device = device;
+    AVS_CUDA_TRY(cudaSetDevice(device));
+    AVS_CUDA_TRY(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device));
+    AVS_CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    for (auto &e : h->ev) AVS_CUDA_TRY(cudaEventCreate(&e));
+    AVS_CUDA_TRY(cudaMallocHost(&h->h_err, sizeof(int)));
+    *h->h_err = 0;
+    *out = h;
+    return AVS_SUCCESS;
+}
+
+int avs_destroy(avs_handle *h) {
+    if (!h) return AVS_SUCCESS;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->ws) cudaFree(h->ws);
+    for (auto &e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->h_err) cudaFreeHost(h->h_err);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return AVS_SUCCESS;
+}
+
+int avs_reserve(avs_handle *h, int64_t n, int32_t tile, int32_t precision) {
+    if (!h) return -1;
+    if (n < 0) return -2;
+    if (!is_pow2(tile) || tile < 16 || (n > 0 && n % tile != 0)) return AVS_ERR_NOT_IMPLEMENTED;
+    if (tile > kMaxTile) return AVS_ERR_UNSUPPORTED;
+    const size_t elem = storage_elem(resolve_precision(precision, true));
+    if (elem == 0) return AVS_ERR_UNSUPPORTED;
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    return ensure_ws(h, make_layout(n, tile, elem, 8).total);
+}
+
+int avs_svdvals_s(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const float *A, float *sigma,
+                  const avs_opts *opts, avs_report *report) {
+    return svdvals_host<float>(h, m, n, lda, tile, A, sigma, opts, report);
+}
+int avs_svdvals_d(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const double *A, double *sigma,
+                  const avs_opts *opts, avs_report *report) {
+    return svdvals_host<double>(h, m, n, lda, tile, A, sigma, opts, report);
+}
+int avs_svdvals_dev_s(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const float *dA,
+                      float *dsigma, const avs_opts *opts, avs_report *report) {
+    return svdvals_dev<float, float>(h, m, n, lda, tile, dA, dsigma, opts, report);
+}
+int avs_svdvals_dev_d(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const double *dA,
+                      double *dsigma, const avs_opts *opts, avs_report *report) {
+    return svdvals_dev<double, double>(h, m, n, lda, tile, dA, dsigma, opts, report);
+}
+
+}  // extern "C"
+
+namespace {
+template <typename T>
+int blockbidiag_dev(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *dA, const avs_opts *opts,
+                    avs_report *rep) {
+    int rc = check_common(h, n, n, lda, tile, dA, dA);
+    if (rep) {
+        std::memset(rep, 0, sizeof(*rep));
+        rep->status = rc;
+    }
+    if (rc != AVS_SUCCESS || n == 0) return rc;
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    const Layout L = make_layout(n, tile, sizeof(T), 0);
+    if ((rc = ensure_ws(h, L.total)) != AVS_SUCCESS) return rc;
+    cudaStream_t s = (opts && opts->stream) ? reinterpret_cast<cudaStream_t>(opts->stream) : h->stream;
+    int *err = reinterpret_cast<int *>(ws_at(h, L.off_err));
+    AVS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+    Stage1Work w1;
+    w1.tau = ws_at(h, L.off_tau);
+    w1.tblk = ws_at(h, L.off_tblk);
+    w1.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags1));
+    w1.err = err;
+    int64_t launches = 0;
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
+    if ((rc = stage1_ge2bnd<T>(dA, n, lda, tile, w1, s, &launches)) != AVS_SUCCESS) return rc;
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
+    AVS_CUDA_TRY(cudaMemcpyAsync(h->h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    rc = finish_status(h, s);
+    if (rep) {
+        rep->t_stage1_ms = rep->t_total_ms = ev_ms(h->ev[0], h->ev[1]);
+        rep->kernel_launches = launches;
+        rep->precision = sizeof(T) == 8 ? AVS_PREC_FP64 : AVS_PREC_FP32;
+        rep->status = rc;
+    }
+    return rc;
+}
+
+template <typename T>
+int extract_band_dev(avs_handle *h, int64_t n, int64_t lda, int32_t bw, const T *dA, double *dB, int64_t ldb) {
+    if (!h) return -1;
+    if (n < 0) return -2;
+    if (lda < (n > 1 ? n : 1)) return -3;
+    if (bw < 0) return -4;
+    if (n > 0 && !dA) return -5;
+    if (n > 0 && !dB) return -6;
+    if (ldb < (n > 1 ? n : 1)) return -7;
+    if (n == 0) return AVS_SUCCESS;
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    int rc = extract_band_dense<T>(dA, n, lda, bw, dB, ldb, h->stream);
+    if (rc != AVS_SUCCESS) return rc;
+    AVS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    return AVS_SUCCESS;
+}
+
+template <typename T>
+int tile_kernel(avs_handle *h, int32_t b, T *dA, T *dB, T *dtau, bool ts) {
+    if (!h) return -1;
+    if (!is_pow2(b) || b < 16) return AVS_ERR_NOT_IMPLEMENTED;
+    if (b > kMaxTile) return AVS_ERR_UNSUPPORTED;
+    if (!dA) return -3;
+    if (ts && !dB) return -4;
+    if (!dtau) return ts ? -5 : -4;
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    const Layout L = make_layout(2 * b, b, sizeof(T), 0);
+    int rc = ensure_ws(h, L.total);
+    if (rc != AVS_SUCCESS) return rc;
+    cudaStream_t s = h->stream;
+    int *err = reinterpret_cast<int *>(ws_at(h, L.off_err));
+    AVS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+    Stage1Work w1;
+    w1.tau = ws_at(h, L.off_tau);
+    w1.tblk = ws_at(h, L.off_tblk);
+    w1.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags1));
+    w1.err = err;
+    if (!ts) {
+        rc = stage1_geqrt_tile<T>(dA, b, dtau, w1, s);
+    } else {
+        T *pair = reinterpret_cast<T *>(ws_at(h, L.off_w));  // 2b x b, ld 2b
+        AVS_CUDA_TRY(cudaMemcpy2DAsync(pair, sizeof(T) * 2 * b, dA, sizeof(T) * b, sizeof(T) * b, b,
+                                       cudaMemcpyDeviceToDevice, s));
+        AVS_CUDA_TRY(cudaMemcpy2DAsync(pair + b, sizeof(T) * 2 * b, dB, sizeof(T) * b, sizeof(T) * b, b,
+                                       cudaMemcpyDeviceToDevice, s));
+        rc = stage1_tsqrt_pair<T>(pair, b, dtau, w1, s);
+        if (rc == AVS_SUCCESS) {
+            AVS_CUDA_TRY(cudaMemcpy2DAsync(dA, sizeof(T) * b, pair, sizeof(T) * 2 * b, sizeof(T) * b, b,
+                                           cudaMemcpyDeviceToDevice, s));
+            AVS_CUDA_TRY(cudaMemcpy2DAsync(dB, sizeof(T) * b, pair + b, sizeof(T) * 2 * b, sizeof(T) * b, b,
+                                           cudaMemcpyDeviceToDevice, s));
+        }
+    }
+    if (rc != AVS_SUCCESS) return rc;
+    AVS_CUDA_TRY(cudaMemcpyAsync(h->h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return finish_status(h, s);
+}
+}  // namespace
+
+extern "C" {
+
+int avs_blockbidiag_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *dA, const avs_opts *opts,
+                          avs_report *report) {
+    return blockbidiag_dev<float>(h, n, lda, tile, dA, opts, report);
+}
+int avs_blockbidiag_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *dA, const avs_opts *opts,
+                          avs_report *report) {
+    return blockbidiag_dev<double>(h, n, lda, tile, dA, opts, report);
+}
+int avs_extract_band_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t bw, const float *dA, double *dB,
+                           int64_t ldb) {
+    return extract_band_dev<float>(h, n, lda, bw, dA, dB, ldb);
+}
+int avs_extract_band_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t bw, const double *dA, double *dB,
+                           int64_t ldb) {
+    return extract_band_dev<double>(h, n, lda, bw, dA, dB, ldb);
+}
+
+int avs_band_to_bidiag_dev(avs_handle *h, int64_t n, int32_t bw, const double *dB, int64_t ldb, double *dd,
+                           double *de, avs_report *rep) {
+    if (!h) return -1;
+    if (n < 0) return -2;
+    if (bw < 1) return -3;
+    if (n > 0 && !dB) return -4;
+    if (ldb < (n > 1 ? n : 1)) return -5;
+    if (n > 0 && !dd) return -6;
+    if (n > 1 && !de) return -7;
+    if (rep) std::memset(rep, 0, sizeof(*rep));
+    if (n == 0) return AVS_SUCCESS;
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    const Layout L = make_layout(n, 1, 8, 0);
+    const int64_t ldab = 3 * (int64_t)bw;
+    // compact band + flags after the standard layout
+    const size_t ab_off = align_up(L.total);
+    const size_t fl_off = align_up(ab_off + sizeof(double) * (size_t)ldab * (size_t)n);
+    const size_t d_off = align_up(fl_off + sizeof(int) * (size_t)(n + 4));
+    const size_t e_off = align_up(d_off + sizeof(double) * (size_t)n);
+    int rc = ensure_ws(h, align_up(e_off + sizeof(double) * (size_t)(n + 1)));
+    if (rc != AVS_SUCCESS) return rc;
+    cudaStream_t s = h->stream;
+    int *err = reinterpret_cast<int *>(ws_at(h, L.off_err));
+    AVS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+    double *AB = reinterpret_cast<double *>(ws_at(h, ab_off));
+    double *td = reinterpret_cast<double *>(ws_at(h, d_off));
+    double *te = reinterpret_cast<double *>(ws_at(h, e_off));
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
+    if ((rc = dense_band_to_compact(dB, n, ldb, bw, AB, ldab, s)) != AVS_SUCCESS) return rc;
+    Stage2Work w2;
+    w2.flags = reinterpret_cast<int *>(ws_at(h, fl_off));
+    w2.err = err;
+    int64_t launches = 1;
+    if ((rc = stage2_chase(AB, n, bw, ldab, td, te, w2, s, h->num_sms, &launches)) != AVS_SUCCESS) return rc;
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
+    AVS_CUDA_TRY(cudaMemcpyAsync(dd, td, sizeof(double) * (size_t)n, cudaMemcpyDeviceToDevice, s));
+    if (n > 1)
+        AVS_CUDA_TRY(cudaMemcpyAsync(de, te, sizeof(double) * (size_t)(n - 1), cudaMemcpyDeviceToDevice, s));
+    AVS_CUDA_TRY(cudaMemcpyAsync(h->h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    rc = finish_status(h, s);
+    if (rep) {
+        rep->t_stage2_ms = rep->t_total_ms = ev_ms(h->ev[0], h->ev[1]);
+        rep->kernel_launches = launches;
+        rep->status = rc;
+    }
+    return rc;
+}
+
+int avs_bidiag_svals_dev(avs_handle *h, int64_t n, const double *dd, const double *de, double *dsigma,
+                         double rel_tol, avs_report *rep) {
+    if (!h) return -1;
+    if (n < 0) return -2;
+    if (n > 0 && !dd) return -3;
+    if (n > 1 && !de) return -4;
+    if (n > 0 && !dsigma) return -5;
+    if (rep) std::memset(rep, 0, sizeof(*rep));
+    if (n == 0) return AVS_SUCCESS;
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    const Layout L = make_layout(n, 1, 8, 0);
+    const size_t e_off = align_up(L.total);
+    int rc = ensure_ws(h, align_up(e_off + sizeof(double) * (size_t)(n + 1)));
+    if (rc != AVS_SUCCESS) return rc;
+    cudaStream_t s = h->stream;
+    // e may have n-1 entries; pad a private copy to n.
+    double *te = reinterpret_cast<double *>(ws_at(h, e_off));
+    AVS_CUDA_TRY(cudaMemsetAsync(te, 0, sizeof(double) * (size_t)(n + 1), s));
+    if (n > 1) AVS_CUDA_TRY(cudaMemcpyAsync(te, de, sizeof(double) * (size_t)(n - 1), cudaMemcpyDeviceToDevice, s));
+    int64_t launches = 0;
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
+    rc = stage3_bisect(dd, te, n, rel_tol, dsigma, reinterpret_cast<double *>(ws_at(h, L.off_scr)), s, &launches);
+    if (rc != AVS_SUCCESS) return rc;
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
+    AVS_CUDA_TRY(cudaStreamSynchronize(s));
+    if (rep) {
+        rep->t_stage3_ms = rep->t_total_ms = ev_ms(h->ev[0], h->ev[1]);
+        rep->kernel_launches = launches;
+    }
+    return AVS_SUCCESS;
+}
+
+int avs_geqrt_tile_dev_s(avs_handle *h, int32_t b, float *dA, float *dtau) {
+    return tile_kernel<float>(h, b, dA, nullptr, dtau, false);
+}
+int avs_geqrt_tile_dev_d(avs_handle *h, int32_t b, double *dA, double *dtau) {
+    return tile_kernel<double>(h, b, dA, nullptr, dtau, false);
+}
+int avs_tsqrt_tile_dev_s(avs_handle *h, int32_t b, float *dR, float *dB, float *dtau) {
+    return tile_kernel<float>(h, b, dR, dB, dtau, true);
+}
+int avs_tsqrt_tile_dev_d(avs_handle *h, int32_t b, double *dR, double *dB, double *dtau) {
+    return tile_kernel<double>(h, b, dR, dB, dtau, true);
+}
+
+}  // extern "C"

@@ -1,0 +1,124 @@
+// Internal helpers shared by the stage kernels and the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "avs.h"
+
+namespace avs {
+
+// Error flag values written by kernels into the workspace's status word.
+enum DeviceError : int {
+    kDevOk = 0,
+    kDevTimeout = 1,   // a bounded spin on a progress flag ran out
+    kDevNonfinite = 2, // NaN/Inf met while generating a reflector
+};
+
+// Upper bound on the spin iterations of any dependency wait.  Each iteration
+// sleeps ~100-200 ns (__nanosleep), so the bound is on the order of tens of
+// seconds -- far beyond any legitimate wait, short enough that a lost
+// dependency returns AVS_ERR_TIMEOUT instead of hanging the GPU.
+constexpr long long kSpinLimit = 1ll << 27;
+
+// Column-major view of a matrix, optionally transposed: element (i, j) of the
+// view is a[i + j*lda] (LAYOUT 0) or a[j + i*lda] (LAYOUT 1).  The LQ half of
+// each GE2BND step is the QR half on the transposed view, as the reference
+// does with adjoint views (KAbasedSVD/src/TiledMatrix.jl:85-88).
+template <typename T, int LAYOUT>
+struct View {
+    T *a;
+    int64_t lda;
+    __device__ __forceinline__ T &operator()(int64_t i, int64_t j) const {
+        return LAYOUT == 0 ? a[i + j * lda] : a[j + i * lda];
+    }
+};
+
+// Acquire-load of a progress counter written by another CTA.
+__device__ __forceinline__ int ld_acquire(const int *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Release-store of a progress counter (after the CTA's writes are complete).
+__device__ __forceinline__ void st_release(int *p, int v) {
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Bounded wait until *flag >= target.  Called by one thread; returns false on
+// timeout (after recording kDevTimeout in *err) or when another CTA already
+// failed.  Never spins forever.
+__device__ __forceinline__ bool wait_geq(const int *flag, int target, int *err) {
+    long long it = 0;
+    while (ld_acquire(flag) < target) {
+        if (ld_acquire(err) != kDevOk) return false;
+        if (++it > kSpinLimit) {
+            atomicCAS(err, kDevOk, kDevTimeout);
+            return false;
+        }
+        __nanosleep(64);
+    }
+    return true;
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+}  // namespace avs
+
+#define AVS_CUDA_TRY(expr)                                   \
+    do {                                                     \
+        cudaError_t _e = (expr);                             \
+        if (_e != cudaSuccess) {                             \
+            avs::set_last_cuda_error(_e);                    \
+            return (_e == cudaErrorMemoryAllocation) ? AVS_ERR_OOM : AVS_ERR_CUDA; \
+        }                                                    \
+    } while (0)
+
+namespace avs {
+void set_last_cuda_error(cudaError_t e);
+
+// Host-side launchers (defined in the stage .cu files).
+struct Stage1Work {
+    void *tau;        // [nt][b] of T
+    void *tblk;       // [nt][b/ib][ib*ib] of T
+    int *flags;       // ticket (1) + progress (nt) + err (1), reset per launch
+    int *err;         // device status word (shared with other stages)
+};
+
+template <typename T>
+int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cudaStream_t s, int64_t *launches);
+
+template <typename T>
+int stage1_geqrt_tile(T *dA, int b, T *dtau, const Stage1Work &w, cudaStream_t s);
+template <typename T>
+int stage1_tsqrt_pair(T *dRB, int b, T *dtau, const Stage1Work &w, cudaStream_t s);
+
+template <typename T>
+int extract_band_compact(const T *dA, int64_t n, int64_t lda, int bw, double *dAB, int64_t ldab, cudaStream_t s);
+template <typename T>
+int extract_band_dense(const T *dA, int64_t n, int64_t lda, int bw, double *dB, int64_t ldb, cudaStream_t s);
+int dense_band_to_compact(const double *dB, int64_t n, int64_t ldb, int bw, double *dAB, int64_t ldab,
+                          cudaStream_t s);
+
+struct Stage2Work {
+    int *flags;  // ticket (1) + done (n) ; reset per launch
+    int *err;
+};
+int stage2_chase(double *dAB, int64_t n, int bw, int64_t ldab, double *dd, double *de, const Stage2Work &w,
+                 cudaStream_t s, int num_sms, int64_t *launches);
+
+int stage3_bisect(const double *dd, const double *de, int64_t n, double rel_tol, double *dsigma, double *dscratch,
+                  cudaStream_t s, int64_t *launches);
+
+template <typename T>
+int cast_from_double(const double *src, T *dst, int64_t n, cudaStream_t s);
+template <typename TI, typename TO>
+int copy_convert_2d(const TI *src, int64_t lds, TO *dst, int64_t ldd, int64_t rows, int64_t cols, cudaStream_t s);
+
+}  // namespace avs

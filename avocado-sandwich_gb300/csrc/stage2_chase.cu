@@ -1,0 +1,456 @@
+// Stage 2: upper band (width bw) -> upper bidiagonal by Householder bulge
+// chasing, FP64, on the GPU.
+//
+// Reference: bidiagonalize / block_bidiagonalize! (KAbasedSVD/src/
+// bulgechasing.jl:1-42), which the reference runs on the CPU with LAPACK on
+// views of the dense n x n array.  Here the band lives in a compact FP64 band
+// array with room for the bulges, and the chase is one persistent kernel.
+//
+// Sweep j (j = 0 .. n-2) makes row j bidiagonal.  Its step m works on the
+// pivot (rho, c0) -- (j, j+1) for m = 0, then (c0_prev, c0_prev + bw):
+//   R op: a right reflector of length <= bw annihilates A[rho, c0+1 .. c0+bw-1];
+//         it is applied to rows rho .. c0+bw-1;
+//   L op: a left reflector annihilates A[c0+1 .. c0+bw-1, c0]; it is applied to
+//         columns c0 .. c0+2bw-1.
+// Only the first row/column of each bulge is annihilated; what remains of a
+// bulge lies where the next sweep's reflectors annihilate it.  Step m of sweep
+// j touches nothing that steps >= m+3 of sweep j-1 touch, so sweep j may run
+// step m once sweep j-1 has finished step m+2: the sweeps form a wavefront,
+// each CTA owning one sweep at a time (sweeps handed out by an atomic ticket in
+// order, so a sweep waits only on sweeps already running; every wait bounded).
+// The result is bit-identical to running the sweeps one after another.
+//
+// For the tile sizes of the pipeline (bw = 16 .. 256) each sweep is owned by a
+// thread-block cluster of C CTAs (8 for bw >= 128): every CTA forms the
+// reflector itself from the pivot row/column, then applies it to its share of
+// the rows (R op) or columns (L op), holding its values in registers; a
+// cluster barrier separates the ops.  Dependencies are tracked per op: the
+// counter of sweep j counts finished ops (R, L, R, L, ...), and op k of sweep
+// j waits until sweep j-1 has finished op k+3 -- the tightest lag for which
+// the wavefront stays bit-identical to the sequential order.  Along the
+// critical path a sweep therefore costs 4 ops instead of 6.
+//
+// Band storage: A(r, c) at AB[(r - c + 2bw - 1) + c * ldab], ldab >= 3bw - 1,
+// which holds 0 <= c - r <= 2bw - 1 (band + upper bulge) and
+// 0 <= r - c <= bw - 1 (lower bulge).
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "avs_common.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace avs {
+namespace {
+
+constexpr int kChaseThreads = 256;
+
+struct Band {
+    double *ab;
+    int64_t ldab;
+    int ku;  // 2bw - 1
+    __device__ __forceinline__ double *at(int64_t r, int64_t c) const { return ab + (ku + r - c) + c * ldab; }
+};
+
+__device__ __forceinline__ double block_sum(double v, double *red) {
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x < 32) {
+        s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+        s = warp_sum(s);
+        if (threadIdx.x == 0) red[0] = s;
+    }
+    __syncthreads();
+    return red[0];
+}
+
+// Householder reflector of x (length L, x[0] = alpha) in shared memory, LAPACK
+// convention: beta = -sign(alpha) ||x||, v[0] = 1, v = x / (alpha - beta),
+// tau = (beta - alpha) / beta; tau = 0 when x[1..] == 0.  Overwrites x with v.
+__device__ void make_reflector(double *x, int L, double *red, double *out_tau, double *out_beta) {
+    double part = 0.0;
+    for (int i = 1 + threadIdx.x; i < L; i += blockDim.x) part += x[i] * x[i];
+    const double s = block_sum(part, red);
+    const double alpha = x[0];
+    double tau = 0.0, beta = alpha, scal = 0.0;
+    if (s > 0.0) {
+        const double nrm = sqrt(alpha * alpha + s);
+        beta = alpha >= 0.0 ? -nrm : nrm;
+        tau = (beta - alpha) / beta;
+        scal = 1.0 / (alpha - beta);
+    }
+    __syncthreads();
+    for (int i = 1 + threadIdx.x; i < L; i += blockDim.x) x[i] *= scal;
+    if (threadIdx.x == 0) x[0] = 1.0;
+    __syncthreads();
+    *out_tau = tau;
+    *out_beta = beta;
+}
+
+__global__ void __launch_bounds__(kChaseThreads) chase_kernel(double *ab, int64_t n, int bw, int64_t ldab,
+                                                              int *ticket, int *done, int *err) {
+    extern __shared__ double sv[];  // bw doubles: the current reflector
+    __shared__ double red[32];
+    __shared__ int s_j, s_ok;
+    Band A{ab, ldab, 2 * bw - 1};
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, wid = tid >> 5, nwarps = blockDim.x >> 5;
+
+    for (;;) {
+        if (tid == 0) s_j = atomicAdd(ticket, 1);
+        __syncthreads();
+        const int64_t j = s_j;
+        if (j >= n - 1) return;
+        const int nsteps = (int)((n - j - 2) / bw) + 1;
+        const int nsteps_prev = (j > 0) ? (int)((n - j - 1) / bw) + 1 : 0;
+        int64_t rho = j, c0 = j + 1;
+        for (int m = 0; m < nsteps; ++m) {
+            if (tid == 0) {
+                bool ok = true;
+                if (j > 0) ok = wait_geq(done + j - 1, min(m + 3, nsteps_prev), err);
+                s_ok = ok;
+            }
+            __syncthreads();
+            if (!s_ok) return;
+            const int64_t c1 = min(c0 + bw - 1, n - 1);
+            const int L = (int)(c1 - c0 + 1);
+            if (L >= 2) {
+                // ---- R op: row rho, columns c0..c1
+                for (int i = tid; i < L; i += blockDim.x) sv[i] = __ldcg(A.at(rho, c0 + i));
+                __syncthreads();
+                double tau, beta;
+                make_reflector(sv, L, red, &tau, &beta);
+                if (tau != 0.0) {
+                    for (int64_t r = rho + 1 + tid; r <= c1; r += blockDim.x) {
+                        double w = 0.0;
+                        for (int i = 0; i < L; ++i) w += __ldcg(A.at(r, c0 + i)) * sv[i];
+                        w *= tau;
+                        for (int i = 0; i < L; ++i) *A.at(r, c0 + i) -= w * sv[i];
+                    }
+                }
+                if (tid == 0) *A.at(rho, c0) = beta;
+                for (int i = 1 + tid; i < L; i += blockDim.x) *A.at(rho, c0 + i) = 0.0;
+                __syncthreads();
+                // ---- L op: column c0, rows c0..c1, applied to columns c0..c0+2bw-1
+                for (int i = tid; i < L; i += blockDim.x) sv[i] = __ldcg(A.at(c0 + i, c0));
+                __syncthreads();
+                make_reflector(sv, L, red, &tau, &beta);
+                if (tau != 0.0) {
+                    const int64_t cend = min(c0 + 2 * (int64_t)bw - 1, n - 1);
+                    for (int64_t c = c0 + 1 + wid; c <= cend; c += nwarps) {
+                        double w = 0.0;
+                        for (int i = lane; i < L; i += 32) w += sv[i] * __ldcg(A.at(c0 + i, c));
+                        w = warp_sum(w) * tau;
+                        for (int i = lane; i < L; i += 32) *A.at(c0 + i, c) -= w * sv[i];
+                    }
+                }
+                if (tid == 0) *A.at(c0, c0) = beta;
+                for (int i = 1 + tid; i < L; i += blockDim.x) *A.at(c0 + i, c0) = 0.0;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                __threadfence();
+                st_release(done + j, m + 1);
+            }
+            rho = c0;
+            c0 += bw;
+        }
+    }
+}
+
+template <int BW>
+struct ChaseCfg {
+    static constexpr int C = BW >= 128 ? 8 : (BW == 64 ? 4 : (BW == 32 ? 2 : 1));  // CTAs per cluster
+    static constexpr int NT = 512;
+    static constexpr int RPC = 2 * BW / C;          // R op: rows per CTA (64 or 32)
+    static constexpr int G = NT / RPC;              // R op: column groups
+    static constexpr int CPG = BW / G;              // R op: columns per group
+    static constexpr int CPC = 2 * BW / C;          // L op: columns per CTA
+    static constexpr int CPW = CPC / (NT / 32);     // L op: columns per warp
+    static constexpr int RPL = BW >= 32 ? BW / 32 : 1;  // L op: rows per lane
+    static_assert(CPG >= 1 && CPW >= 1, "chase configuration");
+};
+
+// Reflector of sv[0..L) (LAPACK convention, see make_reflector) computed by
+// every CTA of the cluster from the same global data.
+__device__ __forceinline__ void cluster_reflector(double *sv, int L, double *red, double *s_tau, double *s_beta) {
+    double part = 0.0;
+    for (int i = 1 + threadIdx.x; i < L; i += blockDim.x) part += sv[i] * sv[i];
+    const double s = block_sum(part, red);
+    const double alpha = sv[0];
+    double tau = 0.0, beta = alpha, scal = 0.0;
+    if (s > 0.0) {
+        const double nrm = sqrt(alpha * alpha + s);
+        beta = alpha >= 0.0 ? -nrm : nrm;
+        tau = (beta - alpha) / beta;
+        scal = 1.0 / (alpha - beta);
+    }
+    __syncthreads();  // every thread has read alpha = sv[0]
+    for (int i = 1 + threadIdx.x; i < L; i += blockDim.x) sv[i] *= scal;
+    if (threadIdx.x == 0) {
+        sv[0] = 1.0;
+        *s_tau = tau;
+        *s_beta = beta;
+    }
+    __syncthreads();
+}
+
+template <int BW>
+__global__ void __launch_bounds__(512) chase_cluster_kernel(double *ab, int64_t n, int64_t ldab, int *ticket,
+                                                            int *done, int *err) {
+    using Cfg = ChaseCfg<BW>;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int q = (int)cluster.block_rank();
+    __shared__ double sv[BW];
+    __shared__ double red[32];
+    __shared__ double part[Cfg::G][Cfg::RPC];
+    __shared__ double wrow[Cfg::RPC];
+    __shared__ double s_tau, s_beta;
+    __shared__ int s_j;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    Band A{ab, ldab, 2 * BW - 1};
+
+    for (;;) {
+        if (q == 0 && tid == 0) s_j = atomicAdd(ticket, 1);
+        cluster.sync();
+        const int64_t j = *cluster.map_shared_rank(&s_j, 0);
+        cluster.sync();
+        if (j >= n - 1) return;
+        const int nsteps = (int)((n - j - 2) / BW) + 1;
+        const int ops_prev = (j > 0) ? 2 * ((int)((n - j - 1) / BW) + 1) : 0;
+        int64_t rho = j, c0 = j + 1;
+        for (int m = 0; m < nsteps; ++m) {
+            const int64_t c1 = min(c0 + BW - 1, n - 1);
+            const int L = (int)(c1 - c0 + 1);
+            // ================= R op (op 2m) =================
+            if (tid == 0 && j > 0) wait_geq(done + j - 1, min(2 * m + 4, ops_prev), err);
+            __syncthreads();
+            if (L >= 2) {
+                for (int i = tid; i < L; i += blockDim.x) sv[i] = __ldcg(A.at(rho, c0 + i));
+                __syncthreads();
+                cluster_reflector(sv, L, red, &s_tau, &s_beta);
+                const double tau = s_tau;
+                if (tau != 0.0) {
+                    const int rr = tid % Cfg::RPC, g = tid / Cfg::RPC;
+                    const int64_t r = rho + 1 + (int64_t)q * Cfg::RPC + rr;
+                    const bool rv = (r <= c1);
+                    double vals[Cfg::CPG];
+                    double acc = 0.0;
+#pragma unroll
+                    for (int k = 0; k < Cfg::CPG; ++k) {
+                        const int ci = g * Cfg::CPG + k;
+                        vals[k] = (rv && ci < L) ? __ldcg(A.at(r, c0 + ci)) : 0.0;
+                        acc += vals[k] * ((ci < L) ? sv[ci] : 0.0);
+                    }
+                    part[g][rr] = acc;
+                    __syncthreads();
+                    if (g == 0) {
+                        double w = 0.0;
+#pragma unroll
+                        for (int gg = 0; gg < Cfg::G; ++gg) w += part[gg][rr];
+                        wrow[rr] = w * tau;
+                    }
+                    __syncthreads();
+                    const double w = wrow[rr];
+                    if (rv) {
+#pragma unroll
+                        for (int k = 0; k < Cfg::CPG; ++k) {
+                            const int ci = g * Cfg::CPG + k;
+                            if (ci < L) *A.at(r, c0 + ci) = vals[k] - w * sv[ci];
+                        }
+                    }
+                }
+                if (q == 0) {
+                    if (tid == 0) *A.at(rho, c0) = s_beta;
+                    for (int i = 1 + tid; i < L; i += blockDim.x) *A.at(rho, c0 + i) = 0.0;
+                }
+            }
+            __threadfence();
+            cluster.sync();
+            if (q == 0 && tid == 0) st_release(done + j, 2 * m + 1);
+            // ================= L op (op 2m+1) =================
+            if (tid == 0 && j > 0) wait_geq(done + j - 1, min(2 * m + 5, ops_prev), err);
+            __syncthreads();
+            if (L >= 2) {
+                for (int i = tid; i < L; i += blockDim.x) sv[i] = __ldcg(A.at(c0 + i, c0));
+                __syncthreads();
+                cluster_reflector(sv, L, red, &s_tau, &s_beta);
+                const double tau = s_tau;
+                if (tau != 0.0) {
+                    const int64_t cend = min(c0 + 2 * (int64_t)BW - 1, n - 1);
+                    const int64_t cbase = c0 + 1 + (int64_t)q * Cfg::CPC + (int64_t)wid * Cfg::CPW;
+                    double vals[Cfg::CPW][Cfg::RPL];
+#pragma unroll
+                    for (int k = 0; k < Cfg::CPW; ++k) {
+                        const int64_t c = cbase + k;
+#pragma unroll
+                        for (int t = 0; t < Cfg::RPL; ++t) {
+                            const int ri = lane + 32 * t;
+                            vals[k][t] = (c <= cend && ri < L) ? __ldcg(A.at(c0 + ri, c)) : 0.0;
+                        }
+                    }
+#pragma unroll
+                    for (int k = 0; k < Cfg::CPW; ++k) {
+                        const int64_t c = cbase + k;
+                        double acc = 0.0;
+#pragma unroll
+                        for (int t = 0; t < Cfg::RPL; ++t) {
+                            const int ri = lane + 32 * t;
+                            acc += (ri < L) ? sv[ri] * vals[k][t] : 0.0;
+                        }
+                        const double w = warp_sum(acc) * tau;
+                        if (c <= cend) {
+#pragma unroll
+                            for (int t = 0; t < Cfg::RPL; ++t) {
+                                const int ri = lane + 32 * t;
+                                if (ri < L) *A.at(c0 + ri, c) = vals[k][t] - w * sv[ri];
+                            }
+                        }
+                    }
+                }
+                if (q == 0) {
+                    if (tid == 0) *A.at(c0, c0) = s_beta;
+                    for (int i = 1 + tid; i < L; i += blockDim.x) *A.at(c0 + i, c0) = 0.0;
+                }
+            }
+            __threadfence();
+            cluster.sync();
+            if (q == 0 && tid == 0) st_release(done + j, 2 * m + 2);
+            rho = c0;
+            c0 += BW;
+        }
+    }
+}
+
+template <int BW>
+int launch_chase_cluster(double *dAB, int64_t n, int64_t ldab, const Stage2Work &w, cudaStream_t s, int num_sms) {
+    using Cfg = ChaseCfg<BW>;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = Cfg::C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.blockDim = dim3(Cfg::NT);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int max_clusters = 0;
+    cfg.gridDim = dim3(Cfg::C * 64);
+    if (cudaOccupancyMaxActiveClusters(&max_clusters, chase_cluster_kernel<BW>, &cfg) != cudaSuccess ||
+        max_clusters <= 0) {
+        cudaGetLastError();
+        max_clusters = std::max(1, num_sms / Cfg::C);
+    }
+    // Sweeps in flight are bounded by the wavefront: about (n / bw) / 2.
+    const int64_t want = std::max<int64_t>(1, (n / BW) / 2 + 2);
+    const int64_t clusters = std::min<int64_t>(std::min<int64_t>(want, max_clusters), n - 1);
+    cfg.gridDim = dim3((unsigned)(clusters * Cfg::C));
+    AVS_CUDA_TRY(cudaLaunchKernelEx(&cfg, chase_cluster_kernel<BW>, dAB, n, ldab, w.flags, w.flags + 1, w.err));
+    return AVS_SUCCESS;
+}
+
+template <typename T>
+__global__ void extract_band_compact_kernel(const T *a, int64_t n, int64_t lda, int bw, double *ab, int64_t ldab) {
+    const int64_t c = blockIdx.x;
+    const int ku = 2 * bw - 1;
+    for (int i = threadIdx.x; i <= bw; i += blockDim.x) {
+        const int64_t r = c - bw + i;
+        if (r >= 0) ab[(ku + r - c) + c * ldab] = (double)a[r + c * lda];
+    }
+}
+
+template <typename T>
+__global__ void extract_band_dense_kernel(const T *a, int64_t n, int64_t lda, int bw, double *bm, int64_t ldb) {
+    const int64_t c = blockIdx.x;
+    for (int64_t r = threadIdx.x; r < n; r += blockDim.x) {
+        const int64_t d = c - r;
+        bm[r + c * ldb] = (d >= 0 && d <= bw) ? (double)a[r + c * lda] : 0.0;
+    }
+}
+
+__global__ void dense_to_compact_kernel(const double *bm, int64_t n, int64_t ldb, int bw, double *ab, int64_t ldab) {
+    const int64_t c = blockIdx.x;
+    const int ku = 2 * bw - 1;
+    for (int i = threadIdx.x; i <= bw; i += blockDim.x) {
+        const int64_t r = c - bw + i;
+        if (r >= 0) ab[(ku + r - c) + c * ldab] = bm[r + c * ldb];
+    }
+}
+
+__global__ void bidiag_out_kernel(const double *ab, int64_t n, int bw, int64_t ldab, double *d, double *e) {
+    const int ku = 2 * bw - 1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        d[i] = ab[ku + i * ldab];
+        if (i + 1 < n) e[i] = ab[(ku - 1) + (i + 1) * ldab];
+    }
+}
+
+}  // namespace
+
+template <typename T>
+int extract_band_compact(const T *dA, int64_t n, int64_t lda, int bw, double *dAB, int64_t ldab, cudaStream_t s) {
+    AVS_CUDA_TRY(cudaMemsetAsync(dAB, 0, sizeof(double) * (size_t)ldab * (size_t)n, s));
+    extract_band_compact_kernel<T><<<(unsigned)n, 128, 0, s>>>(dA, n, lda, bw, dAB, ldab);
+    AVS_CUDA_TRY(cudaGetLastError());
+    return AVS_SUCCESS;
+}
+template int extract_band_compact<float>(const float *, int64_t, int64_t, int, double *, int64_t, cudaStream_t);
+template int extract_band_compact<double>(const double *, int64_t, int64_t, int, double *, int64_t, cudaStream_t);
+
+template <typename T>
+int extract_band_dense(const T *dA, int64_t n, int64_t lda, int bw, double *dB, int64_t ldb, cudaStream_t s) {
+    extract_band_dense_kernel<T><<<(unsigned)n, 256, 0, s>>>(dA, n, lda, bw, dB, ldb);
+    AVS_CUDA_TRY(cudaGetLastError());
+    return AVS_SUCCESS;
+}
+template int extract_band_dense<float>(const float *, int64_t, int64_t, int, double *, int64_t, cudaStream_t);
+template int extract_band_dense<double>(const double *, int64_t, int64_t, int, double *, int64_t, cudaStream_t);
+
+int dense_band_to_compact(const double *dB, int64_t n, int64_t ldb, int bw, double *dAB, int64_t ldab,
+                          cudaStream_t s) {
+    AVS_CUDA_TRY(cudaMemsetAsync(dAB, 0, sizeof(double) * (size_t)ldab * (size_t)n, s));
+    dense_to_compact_kernel<<<(unsigned)n, 128, 0, s>>>(dB, n, ldb, bw, dAB, ldab);
+    AVS_CUDA_TRY(cudaGetLastError());
+    return AVS_SUCCESS;
+}
+
+int stage2_chase(double *dAB, int64_t n, int bw, int64_t ldab, double *dd, double *de, const Stage2Work &w,
+                 cudaStream_t s, int num_sms, int64_t *launches) {
+    if (n >= 2 && bw >= 2) {
+        AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(n + 1), s));
+        int rc = AVS_SUCCESS;
+        switch (bw) {
+            case 16: rc = launch_chase_cluster<16>(dAB, n, ldab, w, s, num_sms); break;
+            case 32: rc = launch_chase_cluster<32>(dAB, n, ldab, w, s, num_sms); break;
+            case 64: rc = launch_chase_cluster<64>(dAB, n, ldab, w, s, num_sms); break;
+            case 128: rc = launch_chase_cluster<128>(dAB, n, ldab, w, s, num_sms); break;
+            case 256: rc = launch_chase_cluster<256>(dAB, n, ldab, w, s, num_sms); break;
+            default: {
+                // any other band width: one CTA per sweep, step-level lag 3
+                const int64_t sweeps = n - 1;
+                const int64_t want = std::max<int64_t>(1, (n / bw) / 3 + 4);
+                const int grid = (int)std::min<int64_t>(std::min<int64_t>(sweeps, want), (int64_t)num_sms * 2);
+                chase_kernel<<<grid, kChaseThreads, sizeof(double) * (size_t)bw, s>>>(dAB, n, bw, ldab, w.flags,
+                                                                                       w.flags + 1, w.err);
+                AVS_CUDA_TRY(cudaGetLastError());
+            }
+        }
+        if (rc != AVS_SUCCESS) return rc;
+        if (launches) *launches += 1;
+    }
+    const int nb = (int)std::min<int64_t>((n + 255) / 256, 4096);
+    bidiag_out_kernel<<<nb > 0 ? nb : 1, 256, 0, s>>>(dAB, n, bw, ldab, dd, de);
+    AVS_CUDA_TRY(cudaGetLastError());
+    if (launches) *launches += 1;
+    return AVS_SUCCESS;
+}
+
+}  // namespace avs

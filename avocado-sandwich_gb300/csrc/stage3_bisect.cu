@@ -1,0 +1,148 @@
+// Stage 3: singular values of an upper bidiagonal B (d, e) by per-value FP64
+// bisection on the Golub-Kahan tridiagonal TGK(B) (zero diagonal,
+// off-diagonal d0, e0, d1, e1, ..., d_{n-1}; eigenvalues +-sigma_i).
+//
+// Replaces LAPACK.bdsdc!('U','N', d, e) (KAbasedSVD/src/bulgechasing.jl:50-53,
+// CUDAbasedSVD/SVD_GPU.jl:267,281), which the reference runs on the CPU.
+// Method: Sturm counts from the LDL^T pivots of TGK - x I with the pivot guard
+// of LAPACK dstebz (Kahan's bisection); one thread per singular value, every
+// loop bounded.  Output is descending, like bdsdc.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+
+#include "avs_common.cuh"
+
+namespace avs {
+namespace {
+
+// scratch[0] = Gershgorin bound of TGK, scratch[1] = pivmin
+__global__ void tgk_bound_kernel(const double *d, const double *e, int64_t n, double *scratch) {
+    __shared__ double sb[32], sm[32];
+    double bound = 0.0, maxsq = 0.0;
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const double di = fabs(d[i]);
+        const double el = i > 0 ? fabs(e[i - 1]) : 0.0;
+        const double er = i + 1 < n ? fabs(e[i]) : 0.0;
+        bound = fmax(bound, di + el + er);
+        maxsq = fmax(maxsq, fmax(di * di, er * er));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        bound = fmax(bound, __shfl_xor_sync(0xffffffffu, bound, o));
+        maxsq = fmax(maxsq, __shfl_xor_sync(0xffffffffu, maxsq, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        sb[threadIdx.x >> 5] = bound;
+        sm[threadIdx.x >> 5] = maxsq;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b2 = 0.0, m2 = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            b2 = fmax(b2, sb[w]);
+            m2 = fmax(m2, sm[w]);
+        }
+        scratch[0] = b2;
+        scratch[1] = DBL_MIN * fmax(m2, 1.0);
+    }
+}
+
+__device__ __forceinline__ int tgk_count(const double *__restrict__ d, const double *__restrict__ e, int64_t n,
+                                         double x, double pivmin) {
+    int cnt = 0;
+    double q = -x;
+    if (fabs(q) < pivmin) q = -pivmin;
+    cnt += (q < 0.0);
+    for (int64_t i = 0; i < n; ++i) {
+        const double di = __ldg(d + i);
+        q = -x - (di * di) / q;
+        if (fabs(q) < pivmin) q = -pivmin;
+        cnt += (q < 0.0);
+        if (i + 1 < n) {
+            const double ei = __ldg(e + i);
+            q = -x - (ei * ei) / q;
+            if (fabs(q) < pivmin) q = -pivmin;
+            cnt += (q < 0.0);
+        }
+    }
+    return cnt;
+}
+
+__global__ void bisect_kernel(const double *d, const double *e, int64_t n, double rel_tol, const double *scratch,
+                              double *sigma) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double bound = scratch[0];
+    const double pivmin = scratch[1];
+    if (bound == 0.0) {
+        sigma[k] = 0.0;
+        return;
+    }
+    const double tol = rel_tol * bound;
+    const int64_t target = 2 * n - 1 - k;  // TGK index (ascending) of the k-th largest sigma
+    double lo = 0.0, hi = bound * (1.0 + 4.0 * DBL_EPSILON) + pivmin;
+    for (int it = 0; it < 128 && hi - lo > tol; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (mid <= lo || mid >= hi) break;
+        if (tgk_count(d, e, n, mid, pivmin) > target)
+            hi = mid;
+        else
+            lo = mid;
+    }
+    sigma[k] = 0.5 * (lo + hi);
+}
+
+template <typename T>
+__global__ void cast_kernel(const double *src, T *dst, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = (T)src[i];
+}
+
+template <typename TI, typename TO>
+__global__ void copy2d_kernel(const TI *src, int64_t lds, TO *dst, int64_t ldd, int64_t rows, int64_t cols) {
+    for (int64_t c = blockIdx.y; c < cols; c += gridDim.y)
+        for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x)
+            dst[r + c * ldd] = (TO)src[r + c * lds];
+}
+
+}  // namespace
+
+int stage3_bisect(const double *dd, const double *de, int64_t n, double rel_tol, double *dsigma, double *dscratch,
+                  cudaStream_t s, int64_t *launches) {
+    if (n <= 0) return AVS_SUCCESS;
+    if (!(rel_tol > 0.0)) rel_tol = 2.0 * DBL_EPSILON;
+    tgk_bound_kernel<<<1, 1024, 0, s>>>(dd, de, n, dscratch);
+    AVS_CUDA_TRY(cudaGetLastError());
+    const int threads = 128;
+    bisect_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, s>>>(dd, de, n, rel_tol, dscratch, dsigma);
+    AVS_CUDA_TRY(cudaGetLastError());
+    if (launches) *launches += 2;
+    return AVS_SUCCESS;
+}
+
+template <typename T>
+int cast_from_double(const double *src, T *dst, int64_t n, cudaStream_t s) {
+    const int nb = (int)std::min<int64_t>((n + 255) / 256, 1024);
+    cast_kernel<T><<<nb > 0 ? nb : 1, 256, 0, s>>>(src, dst, n);
+    AVS_CUDA_TRY(cudaGetLastError());
+    return AVS_SUCCESS;
+}
+template int cast_from_double<float>(const double *, float *, int64_t, cudaStream_t);
+template int cast_from_double<double>(const double *, double *, int64_t, cudaStream_t);
+
+template <typename TI, typename TO>
+int copy_convert_2d(const TI *src, int64_t lds, TO *dst, int64_t ldd, int64_t rows, int64_t cols, cudaStream_t s) {
+    dim3 grid((unsigned)std::min<int64_t>((rows + 255) / 256, 64), (unsigned)std::min<int64_t>(cols, 65535));
+    copy2d_kernel<TI, TO><<<grid, 256, 0, s>>>(src, lds, dst, ldd, rows, cols);
+    AVS_CUDA_TRY(cudaGetLastError());
+    return AVS_SUCCESS;
+}
+template int copy_convert_2d<float, float>(const float *, int64_t, float *, int64_t, int64_t, int64_t, cudaStream_t);
+template int copy_convert_2d<double, double>(const double *, int64_t, double *, int64_t, int64_t, int64_t,
+                                             cudaStream_t);
+template int copy_convert_2d<float, double>(const float *, int64_t, double *, int64_t, int64_t, int64_t,
+                                            cudaStream_t);
+template int copy_convert_2d<double, float>(const double *, int64_t, float *, int64_t, int64_t, int64_t,
+                                            cudaStream_t);
+
+}  // namespace avs

@@ -1,0 +1,155 @@
+/*
+ * avs.h -- C ABI of the GB300-native tiled SVD (singular values only).
+ *
+ * Drop-in for the tiled-matrix singular-value entry point of
+ * evelyne-ringoot/Avocado-sandwich:
+ *
+ *     my_CU_svdval(A::Matrix{Float32}, block_size)    CUDAbasedSVD/SVD_GPU.jl:257-270
+ *     my_CU_svdval(A::CuMatrix{Float32}, block_size)  CUDAbasedSVD/SVD_GPU.jl:272-283
+ *
+ * and for the KernelAbstractions building blocks behind it
+ * (TiledMatrix -> Blockbidiag! -> bidiagonalize -> diag_lapack,
+ *  KAbasedSVD/src/TiledMatrix.jl:41, tiledalgos.jl:17, bulgechasing.jl:33,50).
+ *
+ * Every function is plain C: pointers, sizes and status codes.  Matrices are
+ * column-major (Julia's layout) with a leading dimension.  "Host" entry points
+ * take host pointers and do the host<->device copies themselves (the
+ * Matrix{Float32} method); "_dev" entry points take device pointers that the
+ * caller owns (the CuMatrix{Float32} method).  The input matrix is never
+ * modified (the reference copies it first, SVD_GPU.jl:259,273).  Singular
+ * values are returned in descending order, like LAPACK bdsdc.
+ *
+ * Status codes: 0 success; -i the i-th argument is invalid (LAPACK info
+ * style); AVS_ERR_NOT_IMPLEMENTED for the reference's "Not implemented" cases
+ * (non-square, tile not a power of two, tile < 16, tile not dividing n); > 0
+ * runtime errors.  A Julia binding turns AVS_ERR_NOT_IMPLEMENTED into
+ * error("Not implemented").
+ *
+ * Threading: a handle owns one CUDA stream and a grow-only device workspace;
+ * calls on one handle are serialised by the caller (one handle per host
+ * thread).  Entry points block until their results are ready.
+ */
+#ifndef AVS_H
+#define AVS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AVS_VERSION_MAJOR 0
+#define AVS_VERSION_MINOR 1
+
+/* ---- status codes -------------------------------------------------------- */
+#define AVS_SUCCESS 0
+#define AVS_ERR_NOT_IMPLEMENTED (-100) /* SVD_GPU.jl:261-262 / 275-276 */
+#define AVS_ERR_CUDA 1                 /* a CUDA runtime call failed */
+#define AVS_ERR_OOM 2                  /* device memory exhausted */
+#define AVS_ERR_TIMEOUT 3              /* a bounded device-side wait gave up */
+#define AVS_ERR_NONFINITE 4            /* NaN/Inf met in the factorisation */
+#define AVS_ERR_NO_DEVICE 5            /* no usable CUDA device */
+#define AVS_ERR_UNSUPPORTED 6          /* valid request this build does not provide */
+#define AVS_ERR_INTERNAL 7
+
+/* ---- precision modes of the trailing WY updates (stage 1) ---------------- */
+/* Householder generation/scaling, bulge chase and bisection always run in FP64
+ * scalars; these modes select the storage type of the tiles and the arithmetic
+ * of the compact-WY trailing updates. */
+#define AVS_PREC_DEFAULT 0 /* FP64 for the _d entry points, FP32 for _s */
+#define AVS_PREC_FP64 1    /* plain path: FP64 tiles, FP64 updates */
+#define AVS_PREC_FP32 2    /* FP32 tiles, FP32 SIMT updates */
+#define AVS_PREC_TF32 3    /* FP32 tiles, TF32 tensor-core updates, FP32 accumulate */
+#define AVS_PREC_TF32X3 4  /* FP32 tiles, split TF32 (3 products) tensor-core updates */
+#define AVS_PREC_BF16 5    /* FP32 tiles, BF16 tensor-core updates, FP32 accumulate */
+#define AVS_PREC_BF16X3 6  /* FP32 tiles, split BF16 (3 products) tensor-core updates */
+
+typedef struct avs_handle avs_handle;
+
+typedef struct avs_opts {
+    int32_t precision;      /* AVS_PREC_* (0 = default for the entry point's type) */
+    int32_t flags;          /* reserved, 0 */
+    double bisect_rel_tol;  /* bisection width relative to ||B|| (0 = 2 * DBL_EPSILON) */
+    void *stream;           /* cudaStream_t for the _dev entry points (NULL = handle stream) */
+} avs_opts;
+
+typedef struct avs_report {
+    double t_total_ms;   /* device time of the whole call (events on the call's stream) */
+    double t_stage1_ms;  /* GE2BND: tile QR/LQ band reduction */
+    double t_stage2_ms;  /* band -> bidiagonal bulge chase (incl. band extraction) */
+    double t_stage3_ms;  /* bidiagonal singular values (bisection) */
+    double t_h2d_ms;     /* host entry points: input copy */
+    double t_d2h_ms;     /* host entry points: output copy */
+    int64_t kernel_launches;
+    int64_t workspace_bytes;
+    int32_t precision;   /* precision mode that ran */
+    int32_t status;
+} avs_report;
+
+/* ---- handle ---------------------------------------------------------------- */
+/* Replaces the implicit CUDA.jl context/stream of the reference. */
+int avs_create(avs_handle **h, int device);
+int avs_destroy(avs_handle *h);
+/* Pre-grow the workspace for (n, tile, precision) so that later calls allocate nothing. */
+int avs_reserve(avs_handle *h, int64_t n, int32_t tile, int32_t precision);
+const char *avs_strerror(int status);
+int avs_version(void);
+
+/* ---- entry point: my_CU_svdval ------------------------------------------------
+ * m x n column-major A (ld lda >= m), tile = block_size; sigma receives n
+ * values in descending order.  m != n, tile not a power of two, tile < 16 or
+ * n % tile != 0 return AVS_ERR_NOT_IMPLEMENTED (SVD_GPU.jl:261-262).
+ * opts and report may be NULL. */
+/* Host matrices: my_CU_svdval(::Matrix{Float32}, b), SVD_GPU.jl:257-270. */
+int avs_svdvals_s(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const float *A, float *sigma,
+                  const avs_opts *opts, avs_report *report);
+/* Float64 host matrices (the reference has no Float64 method; same contract). */
+int avs_svdvals_d(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const double *A, double *sigma,
+                  const avs_opts *opts, avs_report *report);
+/* Device matrices: my_CU_svdval(::CuMatrix{Float32}, b), SVD_GPU.jl:272-283. */
+int avs_svdvals_dev_s(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const float *dA,
+                      float *dsigma, const avs_opts *opts, avs_report *report);
+int avs_svdvals_dev_d(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const double *dA,
+                      double *dsigma, const avs_opts *opts, avs_report *report);
+
+/* ---- building blocks (device pointers) ----------------------------------------
+ * Blockbidiag! (KAbasedSVD/src/tiledalgos.jl:17-34) on a TiledMatrix
+ * (TiledMatrix.jl:41-67) in place: on return dA holds the upper band
+ * 0 <= j - i <= tile.  Entries outside the band hold Householder vectors
+ * (the reference zeroes them with triu!/tril!/.= 0, tiledalgos.jl:40,46,52,58);
+ * avs_extract_band_* reads only the band. */
+int avs_blockbidiag_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *dA, const avs_opts *opts,
+                          avs_report *report);
+int avs_blockbidiag_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *dA, const avs_opts *opts,
+                          avs_report *report);
+/* Copy the upper band 0 <= j - i <= bw of a dense n x n matrix into a dense
+ * FP64 n x n matrix with zeros elsewhere (the reference's banded array). */
+int avs_extract_band_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t bw, const float *dA, double *dB,
+                           int64_t ldb);
+int avs_extract_band_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t bw, const double *dA, double *dB,
+                           int64_t ldb);
+/* bidiagonalize(A, bw) (KAbasedSVD/src/bulgechasing.jl:33-42): upper band of
+ * width bw in a dense FP64 n x n matrix -> diagonal d (n) and superdiagonal e
+ * (n-1) of an upper bidiagonal with the same singular values (FP64 bulge chase). */
+int avs_band_to_bidiag_dev(avs_handle *h, int64_t n, int32_t bw, const double *dB, int64_t ldb, double *dd,
+                           double *de, avs_report *report);
+/* diag_lapack / LAPACK.bdsdc!('U','N',d,e) (bulgechasing.jl:50-53): singular
+ * values of the upper bidiagonal, descending, by FP64 bisection on the
+ * Golub-Kahan tridiagonal.  rel_tol as avs_opts.bisect_rel_tol. */
+int avs_bidiag_svals_dev(avs_handle *h, int64_t n, const double *dd, const double *de, double *dsigma,
+                         double rel_tol, avs_report *report);
+
+/* Tile kernels, one tile (b x b, column-major, ld b), device pointers.
+ * QR_unsafe_kernel! (QRkernels.jl:3-66): R above, unit-lower V below, tau[0..b-2]. */
+int avs_geqrt_tile_dev_s(avs_handle *h, int32_t b, float *dA, float *dtau);
+int avs_geqrt_tile_dev_d(avs_handle *h, int32_t b, double *dA, double *dtau);
+/* QR_unsafe_kernel2! (QRkernels.jl:71-129): R (upper triangle of dR) and the
+ * full bottom tile dB, which receives V; tau[0..b-1]. */
+int avs_tsqrt_tile_dev_s(avs_handle *h, int32_t b, float *dR, float *dB, float *dtau);
+int avs_tsqrt_tile_dev_d(avs_handle *h, int32_t b, double *dR, double *dB, double *dtau);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AVS_H */

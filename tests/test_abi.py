@@ -1,0 +1,70 @@
+"""CPU tests of the C ABI: the library builds for sm_103a, loads, and exports
+every function include/avs.h declares; host-side argument logic.  No compute
+call is made here (there is no GPU)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(REPO, "include", "avs.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(avs_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_declares_expected(avs_mod):
+    decl = declared_functions()
+    assert set(avs_mod.EXPORTED_SYMBOLS) == set(decl), set(decl) ^ set(avs_mod.EXPORTED_SYMBOLS)
+
+
+def test_library_exports_every_declared_symbol(avs_mod):
+    lib = avs_mod.lib()
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+        assert ctypes.cast(getattr(lib, name), ctypes.c_void_p).value
+
+
+def test_library_is_sm103a_and_has_no_torch(avs_mod):
+    path = avs_mod.library_path()
+    data = open(path, "rb").read()
+    assert b"sm_103a" in data or b"sm_103" in data
+    assert b"libtorch" not in data and b"libc10" not in data
+
+
+def test_strerror_and_version(avs_mod):
+    lib = avs_mod.lib()
+    assert lib.avs_strerror(avs_mod.NOT_IMPLEMENTED) == b"Not implemented"
+    assert lib.avs_strerror(0) == b"success"
+    assert lib.avs_version() >= 1
+
+
+def test_argument_checks_without_device(avs_mod):
+    """Invalid arguments are rejected before any device work (LAPACK info style)."""
+    lib = avs_mod.lib()
+    r = lib.avs_svdvals_s(None, 64, 64, 64, 16, None, None, None, None)
+    assert r == -1
+
+
+def test_create_without_gpu_reports_no_device(avs_mod):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    h = ctypes.c_void_p()
+    rc = avs_mod.lib().avs_create(ctypes.byref(h), 0)
+    assert rc == 5  # AVS_ERR_NO_DEVICE
+
+
+def test_workloads_are_seeded():
+    import numpy as np
+    from avs import workloads
+    a1 = workloads.gaussian(32, 4, 1 / np.sqrt(32))
+    a2 = workloads.gaussian(32, 4, 1 / np.sqrt(32))
+    assert np.array_equal(a1, a2) and a1.flags.f_contiguous
+    a, s = workloads.geometric_spectrum(64, 2, 3, 1e-6)
+    np.testing.assert_allclose(np.linalg.svd(a, compute_uv=False), s, rtol=1e-9, atol=1e-14)
+    sz = workloads.batch_sizes(4096, 5)
+    assert set(np.unique(sz)) <= {64, 128, 256, 512, 1024}

@@ -1,0 +1,145 @@
+"""CPU tests: the oracle (restatement of the reference path) against the
+reference's own known-answer relations (LAPACK) and the committed golden
+fixtures.  Mirrors KAbasedSVD/test/test_QR_kernels.jl, test_tiledalgo.jl and
+CUDAbasedSVD/test.jl, with seeded inputs."""
+import os
+
+import numpy as np
+import pytest
+import scipy.linalg as sl
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "golden.npz")
+
+
+def julia_approx(x, y, rtol):
+    """Julia's isapprox on arrays: norm(x - y) <= rtol * max(norm(x), norm(y))."""
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    return np.linalg.norm(x - y) <= rtol * max(np.linalg.norm(x), np.linalg.norm(y))
+
+
+RTOL = {np.float32: np.sqrt(np.finfo(np.float32).eps), np.float64: np.sqrt(np.finfo(np.float64).eps)}
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("b", [16, 32])
+def test_tile_kernels_vs_lapack(oracle_mod, dt, b):
+    O = oracle_mod
+    rng = np.random.default_rng(b)
+    a = rng.random((b, b)).astype(dt)
+    f, tau = O.geqrt(a)
+    # QR_unsafe_kernel! factors == LAPACK qr(a).factors (test_QR_kernels.jl:16)
+    assert julia_approx(f, sl.qr(a.astype(np.float64), mode="raw")[0][0], RTOL[dt])
+    q = sl.qr(a.astype(np.float64))[0]
+    bm = rng.random((b, 5 * b)).astype(dt)
+    assert julia_approx(O.apply1(bm, f, tau, True), q.T @ bm, RTOL[dt])   # :20-21, :76
+    assert julia_approx(O.apply1(bm, f, tau, False), q @ bm, RTOL[dt])    # :23-25
+    a2 = rng.random((2 * b, b)).astype(dt)
+    r, v, tau2 = O.tsqrt(a2[:b], a2[b:])
+    stacked = np.vstack([np.triu(a2[:b]), a2[b:]]).astype(np.float64)
+    # QR_unsafe_kernel2! == qr([triu R; B]).factors (:42)
+    assert julia_approx(np.vstack([np.triu(r), v]), sl.qr(stacked, mode="raw")[0][0], RTOL[dt])
+    # strictly-lower part of the top tile untouched (:41)
+    assert np.array_equal(np.tril(r, -1), np.tril(a2[:b], -1))
+    q2 = sl.qr(stacked)[0]
+    bb = rng.random((2 * b, 5 * b)).astype(dt)
+    o1, o2 = O.apply2(bb[:b], bb[b:], v, tau2, True)
+    assert julia_approx(np.vstack([o1, o2]), q2.T @ bb, RTOL[dt])          # :84-85
+    o1, o2 = O.apply2(bb[:b], bb[b:], v, tau2, False)
+    assert julia_approx(np.vstack([o1, o2]), q2 @ bb, RTOL[dt])            # :51-52
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("b,nt", [(16, 4), (16, 6), (32, 4)])
+def test_blockbidiag_preserves_svals(oracle_mod, dt, b, nt):
+    """Blockbidiag! keeps the singular values and leaves an upper band (test_tiledalgo.jl:28-32)."""
+    O = oracle_mod
+    n = b * nt
+    a = np.random.default_rng(nt * b).random((n, n)).astype(dt)
+    band = O.blockbidiag(a, b)
+    i, j = np.indices(band.shape)
+    assert np.all(band[(j - i < 0) | (j - i > b)] == 0)
+    assert julia_approx(sl.svdvals(band.astype(np.float64)), sl.svdvals(a.astype(np.float64)), RTOL[dt])
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+@pytest.mark.parametrize("n,bw", [(64, 16), (128, 32), (200, 16), (256, 64)])
+def test_bidiagonalize(oracle_mod, dt, n, bw):
+    """bidiagonalize gives an exact bidiagonal with the band's singular values
+    (the check of BRD/src/bulgechasing2.jl:101-116)."""
+    O = oracle_mod
+    rng = np.random.default_rng(n + bw)
+    band = np.triu(np.tril(rng.standard_normal((n, n)), bw)).astype(dt)
+    bd = O.bidiagonalize(band, bw)
+    off = bd.copy()
+    off[np.arange(n), np.arange(n)] = 0
+    off[np.arange(n - 1), np.arange(1, n)] = 0
+    assert np.all(off == 0)
+    d, e = O.extract_bidiag(bd)
+    assert julia_approx(O.bidiag_svals(d, e), sl.svdvals(band.astype(np.float64)), RTOL[dt])
+
+
+def test_bidiag_svals_vs_lapack(oracle_mod):
+    """Stage 3 (bdsdc('U','N')) restated as bisection equals LAPACK on the dense bidiagonal."""
+    rng = np.random.default_rng(7)
+    for n in (1, 2, 5, 64, 300):
+        d = rng.standard_normal(n)
+        e = rng.standard_normal(max(n - 1, 0))
+        B = np.diag(d) + (np.diag(e, 1) if n > 1 else 0)
+        ref = sl.svdvals(B)
+        got = oracle_mod.bidiag_svals(d, e)
+        assert np.all(np.diff(got) <= 0)
+        assert np.max(np.abs(got - ref)) <= 1e-13 * max(ref[0], 1)
+    # graded values keep high relative accuracy
+    d = 10.0 ** -np.arange(0, 12)
+    e = 1e-3 * d[:-1]
+    got = oracle_mod.bidiag_svals(d, e, rel_tol=1e-30)
+    ref = sl.svdvals(np.diag(d) + np.diag(e, 1))
+    assert np.max(np.abs(got - ref) / ref) < 1e-10
+
+
+@pytest.mark.parametrize("dt,b,nt", [(np.float32, 16, 4), (np.float32, 16, 7), (np.float64, 32, 4)])
+def test_end_to_end_vs_lapack(oracle_mod, dt, b, nt):
+    """my_CU_svdval restated ~= LAPACK svdvals (CUDAbasedSVD/test.jl:9-13, integer-valued input)."""
+    n = b * nt
+    a = np.random.default_rng(n).integers(1, 11, size=(n, n)).astype(dt)
+    got = oracle_mod.svdvals(a, b)
+    ref = sl.svdvals(a.astype(np.float64))
+    assert julia_approx(got, ref, RTOL[dt])
+
+
+def test_not_implemented_cases(oracle_mod):
+    a = np.ones((64, 64))
+    for b in (8, 24, 48):   # < 16, not a power of two, not dividing
+        with pytest.raises(NotImplementedError):
+            oracle_mod.svdvals(a, b)
+    with pytest.raises(NotImplementedError):
+        oracle_mod.svdvals(np.ones((64, 32)), 16)
+
+
+def test_golden_fixtures(oracle_mod):
+    """The oracle reproduces the committed fixtures (bitwise for the stage
+    outputs: same code, same inputs) and stays within tolerance of LAPACK."""
+    O = oracle_mod
+    g = np.load(GOLDEN)
+    for b, dt in ((16, "float64"), (32, "float32")):
+        key = "tile_b%d_%s" % (b, dt)
+        f, tau = O.geqrt(g[key + "_geqrt_in"])
+        np.testing.assert_array_equal(f, g[key + "_geqrt_factors"])
+        np.testing.assert_array_equal(tau, g[key + "_geqrt_tau"])
+        r, v, tau2 = O.tsqrt(g[key + "_tsqrt_in"][:b], g[key + "_tsqrt_in"][b:])
+        np.testing.assert_array_equal(v, g[key + "_tsqrt_v"])
+        np.testing.assert_array_equal(tau2, g[key + "_tsqrt_tau"])
+        rt = RTOL[np.dtype(dt).type]
+        assert julia_approx(g[key + "_geqrt_factors"], g[key + "_lapack_geqrt_factors"], rt)
+    names = sorted({k[: -len("_A")] for k in g.files if k.endswith("_A")})
+    assert len(names) == 5
+    for name in names:
+        a = g[name + "_A"]
+        b = int(g[name + "_tile"])
+        band = O.blockbidiag(a, b)
+        np.testing.assert_array_equal(O.extract_band(band, b), g[name + "_band"])
+        s = O.svdvals(a, b)
+        np.testing.assert_allclose(s, g[name + "_sigma_oracle"], rtol=0, atol=1e-14 * s[0])
+        rt = 1e-5 if a.dtype == np.float32 else 1e-12
+        assert np.max(np.abs(s - g[name + "_sigma_lapack"])) <= rt * s[0]
