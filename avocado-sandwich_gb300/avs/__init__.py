@@ -45,7 +45,7 @@ EXPORTED_SYMBOLS = [
     "avs_create", "avs_destroy", "avs_reserve", "avs_strerror", "avs_version",
     "avs_svdvals_s", "avs_svdvals_d", "avs_svdvals_dev_s", "avs_svdvals_dev_d",
     "avs_blockbidiag_dev_s", "avs_blockbidiag_dev_d", "avs_extract_band_dev_s", "avs_extract_band_dev_d",
-    "avs_band_to_bidiag_dev", "avs_bidiag_svals_dev",
+    "avs_band_to_bidiag_dev", "avs_bidiag_svals_dev", "avs_bidiag_svals_noalloc",
     "avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d", "avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d",
 ]
 
@@ -100,6 +100,7 @@ def lib():
             getattr(L, nm).argtypes = [P, I64, I64, I32, P, P, I64]
         L.avs_band_to_bidiag_dev.argtypes = [P, I64, I32, P, I64, P, P, RP]
         L.avs_bidiag_svals_dev.argtypes = [P, I64, P, P, P, ctypes.c_double, RP]
+        L.avs_bidiag_svals_noalloc.argtypes = [I64, P, P, P, ctypes.c_double, P]
         for nm in ("avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d"):
             getattr(L, nm).argtypes = [P, I32, P, P]
         for nm in ("avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d"):

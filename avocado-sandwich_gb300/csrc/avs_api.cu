@@ -281,6 +281,7 @@ const char *avs_strerror(int status) {
         case AVS_ERR_NO_DEVICE: return "no usable CUDA device";
         case AVS_ERR_UNSUPPORTED: return "valid request not provided by this build";
         case AVS_ERR_INTERNAL: return "internal error";
+        case AVS_ERR_TOO_LARGE: return "size exceeds the static scratch of the allocation-free entry point";
         default: return status < 0 ? "invalid argument" : "unknown error";
     }
 }
@@ -542,6 +543,11 @@ int avs_bidiag_svals_dev(avs_handle *h, int64_t n, const double *dd, const doubl
         rep->kernel_launches = launches;
     }
     return AVS_SUCCESS;
+}
+
+int avs_bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *dsigma, double rel_tol,
+                             void *stream) {
+    return bidiag_svals_noalloc(n, dd, de, dsigma, rel_tol, reinterpret_cast<cudaStream_t>(stream));
 }
 
 int avs_geqrt_tile_dev_s(avs_handle *h, int32_t b, float *dA, float *dtau) {

@@ -113,6 +113,8 @@ struct Stage2Work {
 int stage2_chase(double *dAB, int64_t n, int bw, int64_t ldab, double *dd, double *de, const Stage2Work &w,
                  cudaStream_t s, int num_sms, int64_t *launches);
 
+int bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *dsigma, double rel_tol,
+                         cudaStream_t s);
 int stage3_bisect(const double *dd, const double *de, int64_t n, double rel_tol, double *dsigma, double *dscratch,
                   cudaStream_t s, int64_t *launches);
 

@@ -120,6 +120,75 @@ int stage3_bisect(const double *dd, const double *de, int64_t n, double rel_tol,
     return AVS_SUCCESS;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the bisection (avs_bidiag_svals_noalloc).
+//
+// Some callers cannot call cudaMalloc at the moment they need singular values:
+// a host that has handed all device memory to its own pool allocator (Julia's
+// CUDA.jl, PyTorch's caching allocator) and forbids allocations behind the
+// pool's back, or a latency-critical loop that must not pay cudaMalloc's
+// implicit device synchronisation.  For them the scratch of the bisection --
+// the Gershgorin bound and pivot guard of TGK(B), and a zero-padded copy of the
+// superdiagonal -- lives in the file-scope device array below instead of a
+// workspace.  Every GPU that loads the library holds it (about 512 KiB) until
+// the process exits.  Every call shares it and it keeps the last call's
+// contents; calls that overlap on the GPU race on it.
+constexpr int64_t kNoAllocMaxN = 65536;
+constexpr int64_t kNoAllocHead = 8;  // [0] bound, [1] pivmin, rest unused
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocHead + kNoAllocMaxN + 1];
+
+}  // namespace avs
+
+#include <mutex>
+
+namespace avs {
+namespace {
+constexpr int kMaxDevices = 64;
+double *g_noalloc_ptr[kMaxDevices] = {};
+std::mutex g_noalloc_mu;
+}  // namespace
+
+// Device address of the static scratch for the current device.  Host code may
+// not use g_noalloc_scratch as a device pointer (it names a host-side shadow),
+// so the address is looked up once per device with that device current.
+static int noalloc_scratch(double **out) {
+    int dev = 0;
+    AVS_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return AVS_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        AVS_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = static_cast<double *>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return AVS_SUCCESS;
+}
+
+int bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *dsigma, double rel_tol,
+                         cudaStream_t s) {
+    if (n < 0) return -1;
+    if (n > kNoAllocMaxN) return AVS_ERR_TOO_LARGE;
+    if (n > 0 && !dd) return -2;
+    if (n > 1 && !de) return -3;
+    if (n > 0 && !dsigma) return -4;
+    if (n == 0) return AVS_SUCCESS;
+    double *scr = nullptr;
+    int rc = noalloc_scratch(&scr);
+    if (rc != AVS_SUCCESS) return rc;
+    double *te = scr + kNoAllocHead;
+    // the previous call's contents are still there: rewrite the whole padded copy
+    if (n > 1) AVS_CUDA_TRY(cudaMemcpyAsync(te, de, sizeof(double) * (size_t)(n - 1), cudaMemcpyDeviceToDevice, s));
+    AVS_CUDA_TRY(cudaMemsetAsync(te + (n - 1), 0, sizeof(double) * 2, s));
+    if (!(rel_tol > 0.0)) rel_tol = 2.0 * DBL_EPSILON;
+    tgk_bound_kernel<<<1, 1024, 0, s>>>(dd, te, n, scr);
+    AVS_CUDA_TRY(cudaGetLastError());
+    bisect_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(dd, te, n, rel_tol, scr, dsigma);
+    AVS_CUDA_TRY(cudaGetLastError());
+    AVS_CUDA_TRY(cudaStreamSynchronize(s));
+    return AVS_SUCCESS;
+}
+
 template <typename T>
 int cast_from_double(const double *src, T *dst, int64_t n, cudaStream_t s) {
     const int nb = (int)std::min<int64_t>((n + 255) / 256, 1024);

@@ -52,6 +52,7 @@ extern "C" {
 #define AVS_ERR_NO_DEVICE 5            /* no usable CUDA device */
 #define AVS_ERR_UNSUPPORTED 6          /* valid request this build does not provide */
 #define AVS_ERR_INTERNAL 7
+#define AVS_ERR_TOO_LARGE 8            /* n above the static scratch of avs_bidiag_svals_noalloc */
 
 /* ---- precision modes of the trailing WY updates (stage 1) ---------------- */
 /* Householder generation/scaling, bulge chase and bisection always run in FP64
@@ -139,6 +140,20 @@ int avs_band_to_bidiag_dev(avs_handle *h, int64_t n, int32_t bw, const double *d
  * Golub-Kahan tridiagonal.  rel_tol as avs_opts.bisect_rel_tol. */
 int avs_bidiag_svals_dev(avs_handle *h, int64_t n, const double *dd, const double *de, double *dsigma,
                          double rel_tol, avs_report *report);
+
+/* Allocation-free variant of avs_bidiag_svals_dev.  No counterpart in the
+ * reference.  For callers that cannot call cudaMalloc when they need the
+ * values -- a host whose device memory belongs to its own pool allocator
+ * (Julia's CUDA.jl, PyTorch's caching allocator), or a latency-critical loop
+ * that must not pay cudaMalloc's implicit synchronisation.  Needs no handle;
+ * runs on the current device and on `stream` (a cudaStream_t, NULL = legacy
+ * default stream) and returns when the values are in dsigma.  Its scratch is a
+ * static device array in the library (~512 KiB per GPU, held until exit), so
+ * n <= 65536; larger n returns AVS_ERR_TOO_LARGE.  The first call on a device
+ * looks the array's address up (call it once before any stream capture).
+ * Calls share the array: calls that overlap on the GPU race on it. */
+int avs_bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *dsigma, double rel_tol,
+                             void *stream);
 
 /* Tile kernels, one tile (b x b, column-major, ld b), device pointers.
  * QR_unsafe_kernel! (QRkernels.jl:3-66): R above, unit-lower V below, tau[0..b-2]. */
