@@ -36,7 +36,7 @@ inline bool is_pow2(int64_t x) { return x > 0 && (x & (x - 1)) == 0; }
 // Workspace carve-up for one call.
 struct Layout {
     size_t off_w, off_stage, off_tau, off_tblk, off_flags1, off_flags2, off_err, off_ab, off_d, off_e, off_sig,
-        off_scr, off_out, total;
+        off_scr, off_out, off_tfull, total;
     int64_t ldab;
 };
 
@@ -54,6 +54,8 @@ Layout make_layout(int64_t n, int b, size_t elem, size_t stage_elem) {
     o = align_up(o + elem * (size_t)(nt + 1) * (size_t)b);
     L.off_tblk = o;
     o = align_up(o + elem * (size_t)(nt + 1) * (size_t)(b / 16) * 256);
+    L.off_tfull = o;
+    o = align_up(o + (b >= 128 ? elem * (size_t)(nt + 1) * (size_t)b * (size_t)b : 0));
     L.off_flags1 = o;
     o = align_up(o + sizeof(int) * (size_t)(nt + 4));
     L.off_flags2 = o;
@@ -162,6 +164,7 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
     w1.tblk = ws_at(h, L.off_tblk);
     w1.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags1));
     w1.err = err;
+    w1.tfull = ws_at(h, L.off_tfull);
     if ((rc = stage1_ge2bnd<S>(W, n, n, b, w1, s, &launches)) != AVS_SUCCESS) return rc;
     AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
     double *AB = reinterpret_cast<double *>(ws_at(h, L.off_ab));
@@ -372,6 +375,7 @@ int blockbidiag_dev(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *dA, 
     w1.tblk = ws_at(h, L.off_tblk);
     w1.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags1));
     w1.err = err;
+    w1.tfull = ws_at(h, L.off_tfull);
     int64_t launches = 0;
     AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
     if ((rc = stage1_ge2bnd<T>(dA, n, lda, tile, w1, s, &launches)) != AVS_SUCCESS) return rc;
@@ -424,6 +428,7 @@ int tile_kernel(avs_handle *h, int32_t b, T *dA, T *dB, T *dtau, bool ts) {
     w1.tblk = ws_at(h, L.off_tblk);
     w1.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags1));
     w1.err = err;
+    w1.tfull = ws_at(h, L.off_tfull);
     if (!ts) {
         rc = stage1_geqrt_tile<T>(dA, b, dtau, w1, s);
     } else {

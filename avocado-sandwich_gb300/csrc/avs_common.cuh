@@ -89,7 +89,12 @@ struct Stage1Work {
     void *tblk;       // [nt][b/ib][ib*ib] of T
     int *flags;       // ticket (1) + progress (nt) + err (1), reset per launch
     int *err;         // device status word (shared with other stages)
+    void *tfull;      // [nt][b*b] of T: full compact-WY factors (tiles 128, 256)
 };
+
+template <typename T>
+int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const void *tblk,
+                       void *tfull, cudaStream_t s);
 
 template <typename T>
 int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cudaStream_t s, int64_t *launches);

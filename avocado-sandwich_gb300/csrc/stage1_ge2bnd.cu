@@ -172,10 +172,12 @@ __global__ void __launch_bounds__(kNT) panel_kernel(PanelArgs args) {
                     }
                 }
             }
-            if (jj != i) acc = (double)accT;
 #pragma unroll
-            for (int o = 8; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (g == 0 && jj >= i) dsum[jj] = acc;
+            for (int o = 8; o > 0; o >>= 1) {
+                accT += __shfl_xor_sync(0xffffffffu, accT, o);
+                acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            }
+            if (g == 0 && jj >= i) dsum[jj] = (jj == i) ? acc : (double)accT;
             __syncthreads();
             if (tid == 0) {
                 const double s = dsum[i];
@@ -190,11 +192,15 @@ __global__ void __launch_bounds__(kNT) panel_kernel(PanelArgs args) {
                 }
                 if (!isfinite(tv) || !isfinite(nu)) { atomicCAS(args.err, kDevOk, kDevNonfinite); tv = 0.0; }
                 scal[0] = nu;
+                scal[1] = (tv != 0.0) ? 1.0 / nu : 0.0;         // scaling of V
+                scal[2] = (tv != 0.0) ? (tv / nu) / nu : 0.0;   // taucorr / nu
                 stau[i] = tv;
             }
             __syncthreads();
             const double nu = scal[0];
             const double tv = stau[i];
+            const T inv_nu = (T)scal[1];
+            const T f_upd = (T)scal[2];
             if (tv == 0.0) {
                 // identity reflector: zero column (or the GEQRT tail) -> V column = 0
                 if (jj == i) {
@@ -210,18 +216,21 @@ __global__ void __launch_bounds__(kNT) panel_kernel(PanelArgs args) {
             if (jj >= i) {
                 const double w = nu * (double)rv + dsum[jj];
                 const T wT = (T)w;
-                for (int m = 0; m < rows_per_g; ++m) {
+                const T fw = f_upd * wT;  // (x_t / nu) * (tau / nu) * w_j = x_t * fw
+#pragma unroll
+                for (int m = 0; m < 16; ++m) {
+                    if (m >= rows_per_g) break;
                     const int t = g + 16 * m;
                     if (geqrt) {
                         if (t > c) {
-                            if (jj > i) X[t + jj * ldx] -= (T)(((double)xr[m] / nu) * tc) * wT;
-                            else X[t + i * ldx] = (T)((double)xr[m] / nu);
+                            if (jj > i) X[t + jj * ldx] -= xr[m] * fw;
+                            else X[t + i * ldx] = xr[m] * inv_nu;
                         } else if (t == c) {
                             X[c + jj * ldx] = (T)((double)rv - tc * w);
                         }
                     } else {
-                        if (jj > i) X[t + jj * ldx] -= (T)(((double)xr[m] / nu) * tc) * wT;
-                        else X[t + i * ldx] = (T)((double)xr[m] / nu);
+                        if (jj > i) X[t + jj * ldx] -= xr[m] * fw;
+                        else X[t + i * ldx] = xr[m] * inv_nu;
                     }
                 }
                 if (!geqrt && g == 0) Rt[i + (c0 + jj) * kIB] = (T)((double)rv - tc * w);
@@ -524,14 +533,22 @@ int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cud
         // QR half-step: GEQRT(k,k) + TSQRT(row,k), Q^T applied to the row panels.
         const int P = nt - k;
         if ((rc = launch_panel<T, 0>(dA, lda, b, k, k, P, 0, w, s)) != AVS_SUCCESS) return rc;
-        if ((rc = launch_update<T, 0>(dA, lda, n, b, k, k, P, w, s)) != AVS_SUCCESS) return rc;
-        if (launches) *launches += (k + 1 < nt) ? 2 : 1;
+        if (b >= 128 && w.tfull)
+            rc = stage1_update_full<T>(dA, lda, n, b, 0, k, k, P, w.tblk, w.tfull, s);
+        else
+            rc = launch_update<T, 0>(dA, lda, n, b, k, k, P, w, s);
+        if (rc != AVS_SUCCESS) return rc;
+        if (launches) *launches += (k + 1 < nt) ? ((b >= 128 && w.tfull) ? 3 : 2) : 1;
         if (k == nt - 1) break;
         // LQ half-step: the same on the transposed view, top tile (k, k+1).
         const int PL = nt - k - 1;
         if ((rc = launch_panel<T, 1>(dA, lda, b, k + 1, k, PL, 0, w, s)) != AVS_SUCCESS) return rc;
-        if ((rc = launch_update<T, 1>(dA, lda, n, b, k + 1, k, PL, w, s)) != AVS_SUCCESS) return rc;
-        if (launches) *launches += 2;
+        if (b >= 128 && w.tfull)
+            rc = stage1_update_full<T>(dA, lda, n, b, 1, k + 1, k, PL, w.tblk, w.tfull, s);
+        else
+            rc = launch_update<T, 1>(dA, lda, n, b, k + 1, k, PL, w, s);
+        if (rc != AVS_SUCCESS) return rc;
+        if (launches) *launches += (b >= 128 && w.tfull) ? 3 : 2;
     }
     return AVS_SUCCESS;
 }

@@ -1,0 +1,435 @@
+// Stage 1, trailing update with the full compact-WY factor of each tile
+// (tiles of 128 and 256).
+//
+// The reflectors a panel role generated for its tile (GEQRT: b - 1 of them,
+// TSQRT: b) are applied to the trailing columns as one block reflector
+// Q_p = I - Y_p T_p Y_p^T, in the reference's order (GEQRT first, then the
+// TSQRT tiles top to bottom, TiledMatrix.jl:107-113 / QRkernels.jl:131-197):
+//
+//   GEQRT tile:  Z = Y0^T Top,          W = T0^T Z,  Top -= Y0 W
+//   TSQRT tile:  Z = Top + V_p^T A_p,   W = T_p^T Z, Top -= W, A_p -= V_p W
+//
+// tbuild_kernel forms T_p (b x b, upper triangular) from the 16 x 16 diagonal
+// blocks the panel kernel produced and the Gram matrix G = Y_p^T Y_p:
+// T[0:c0, J] = -T[0:c0, 0:c0] G[0:c0, J] T_JJ for the column blocks J.
+//
+// update_full_kernel: one CTA per column strip keeps the strip of the top tile
+// row in shared memory for the whole half-step; each of the three products is
+// a register-blocked GEMM (8 rows x CB columns per thread, K = b streamed
+// through shared memory in chunks that the next chunk's loads overlap).
+#include <algorithm>
+
+#include "avs_common.cuh"
+
+namespace avs {
+namespace {
+
+constexpr int kWIB = 16;     // diagonal block size of T (the panel's compact-WY blocks)
+constexpr int kWNT = 256;    // threads per CTA
+
+template <typename T>
+struct WCfg {
+    static constexpr int W = sizeof(T) == 8 ? 32 : 64;   // strip width
+    static constexpr int KC = sizeof(T) == 8 ? 8 : 16;   // K chunk
+};
+
+struct TBuildArgs {
+    const void *a;
+    int64_t lda;
+    int b;
+    int pr, pc, P;
+    const void *tblk;  // [P][b/16][256]
+    void *tfull;       // [P][b*b], T(l, i) at l + i*b
+};
+
+// ---------------------------------------------------------------------------
+// T build.  One CTA per tile.
+template <typename T, int LAYOUT>
+__global__ void __launch_bounds__(kWNT) tbuild_kernel(TBuildArgs args) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int b = args.b;
+    const int nb = b / kWIB;
+    const int p = blockIdx.x;
+    const bool geqrt = (p == 0);
+    const int tid = threadIdx.x;
+    View<const T, LAYOUT> V{reinterpret_cast<const T *>(args.a), args.lda};
+    const int64_t row0 = (int64_t)(args.pr + p) * b;
+    const int64_t col0 = (int64_t)args.pc * b;
+    T *Tf = reinterpret_cast<T *>(args.tfull) + (size_t)p * b * b;
+    const T *tb = reinterpret_cast<const T *>(args.tblk) + (size_t)p * nb * kWIB * kWIB;
+
+    // ---- 1. G(l, i) = y_l^T y_i for l < i in different 16-blocks, into Tf
+    constexpr int KC = 32;
+    T *chunk = reinterpret_cast<T *>(smem_raw);  // KC x (b + 1)
+    const int ldc = b + 1;
+    // 4 x 4 micro-blocks (lb, ib) of G with block16(lb*4) < block16(ib*4)
+    const int nmb = b / 4;
+    int total = 0;
+    for (int ib = 0; ib < nmb; ++ib) total += (ib * 4 / kWIB) * (kWIB / 4);
+    for (int base = 0; base < total; base += kWNT) {
+        // locate this thread's micro-block (lb, ib)
+        int my = base + tid, lb = -1, ibk = -1;
+        if (my < total) {
+            int acc = 0;
+            for (int ib = 0; ib < nmb; ++ib) {
+                const int cnt = (ib * 4 / kWIB) * (kWIB / 4);
+                if (my < acc + cnt) { ibk = ib; lb = my - acc; break; }
+                acc += cnt;
+            }
+        }
+        T g[4][4];
+#pragma unroll
+        for (int x = 0; x < 4; ++x)
+#pragma unroll
+            for (int y = 0; y < 4; ++y) g[x][y] = T(0);
+        for (int k0 = 0; k0 < b; k0 += KC) {
+            __syncthreads();
+            for (int idx = tid; idx < KC * b; idx += kWNT) {
+                int k, m;
+                if (LAYOUT == 0) { k = idx % KC; m = idx / KC; } else { m = idx % b; k = idx / b; }
+                const int t = k0 + k;
+                T v = V(row0 + t, col0 + m);
+                if (geqrt) v = (t == m) ? T(1) : (t > m ? v : T(0));
+                chunk[k * ldc + m] = v;
+            }
+            __syncthreads();
+            if (lb >= 0) {
+                for (int k = 0; k < KC; ++k) {
+                    T a[4], c[4];
+#pragma unroll
+                    for (int x = 0; x < 4; ++x) a[x] = chunk[k * ldc + lb * 4 + x];
+#pragma unroll
+                    for (int y = 0; y < 4; ++y) c[y] = chunk[k * ldc + ibk * 4 + y];
+#pragma unroll
+                    for (int x = 0; x < 4; ++x)
+#pragma unroll
+                        for (int y = 0; y < 4; ++y) g[x][y] += a[x] * c[y];
+                }
+            }
+        }
+        if (lb >= 0) {
+#pragma unroll
+            for (int x = 0; x < 4; ++x)
+#pragma unroll
+                for (int y = 0; y < 4; ++y) Tf[(lb * 4 + x) + (size_t)(ibk * 4 + y) * b] = g[x][y];
+        }
+    }
+    __syncthreads();
+    // ---- 2. diagonal blocks and zeros below them; first column block
+    for (int idx = tid; idx < b * b; idx += kWNT) {
+        const int l = idx % b, i = idx / b;
+        const int bl = l / kWIB, bi = i / kWIB;
+        if (bl == bi) Tf[l + (size_t)i * b] = tb[(size_t)bi * kWIB * kWIB + (l % kWIB) + (i % kWIB) * kWIB];
+        else if (bl > bi) Tf[l + (size_t)i * b] = T(0);
+    }
+    __syncthreads();
+    // ---- 3. column blocks J = 1..nb-1: T[0:c0, J] = -T[0:c0,0:c0] G[0:c0, J] T_JJ
+    T *Y1 = chunk;  // (b) x kWIB
+    for (int J = 1; J < nb; ++J) {
+        const int c0 = J * kWIB;
+        for (int idx = tid; idx < c0 * kWIB; idx += kWNT) {
+            const int r = idx % c0, q = idx / c0;
+            T s = T(0);
+            for (int m = r; m < c0; ++m) s += Tf[r + (size_t)m * b] * Tf[m + (size_t)(c0 + q) * b];
+            Y1[r + q * b] = s;
+        }
+        __syncthreads();
+        for (int idx = tid; idx < c0 * kWIB; idx += kWNT) {
+            const int r = idx % c0, q = idx / c0;
+            T s = T(0);
+#pragma unroll
+            for (int qq = 0; qq < kWIB; ++qq)
+                s += Y1[r + qq * b] * tb[(size_t)J * kWIB * kWIB + qq + q * kWIB];
+            Tf[r + (size_t)(c0 + q) * b] = -s;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Trailing update with full T.
+struct UpdFullArgs {
+    void *a;
+    int64_t lda;
+    int64_t n;
+    int b;
+    int pr, pc, P;
+    const void *tfull;
+};
+
+// A-operand sources for the three products.
+enum ASrc { kVrows = 0, kTrows = 1, kVcols = 2 };
+
+template <typename T, int B>
+struct UCfg {
+    static constexpr int W = WCfg<T>::W;
+    static constexpr int KC = WCfg<T>::KC;
+    static constexpr int MB = 8;                  // rows per thread
+    static constexpr int TM = B / MB;             // threads along rows
+    static constexpr int TC = kWNT / TM;          // threads along columns
+    static constexpr int CB = W / TC;             // columns per thread
+    static constexpr int LDB = B + 4;             // leading dimension of strip buffers (rows)
+    static constexpr int LDC = B + 4;             // leading dimension of A chunks (m)
+    static constexpr int PER = KC * B / kWNT;     // chunk elements per thread
+    static_assert(CB >= 1 && PER >= 1, "update configuration");
+};
+
+template <typename T, int LAYOUT, int B>
+struct UpdCtx {
+    using C = UCfg<T, B>;
+    View<T, LAYOUT> V;
+    const T *Tf;      // T of the current tile, ld B
+    int64_t row0, col0;
+    bool geqrt;
+    // element (k, m) of the A operand for source s (chunk-relative k0 added by caller)
+    __device__ __forceinline__ T a_elem(int s, int k, int m) const {
+        if (s == kVrows) {  // V(k, m): Z = V^T ...
+            T v = V(row0 + k, col0 + m);
+            if (geqrt) v = (k == m) ? T(1) : (k > m ? v : T(0));
+            return v;
+        } else if (s == kTrows) {  // T(k, m)
+            return Tf[k + (size_t)m * B];
+        } else {  // V(m, k): ... -= V W
+            T v = V(row0 + m, col0 + k);
+            if (geqrt) v = (m == k) ? T(1) : (m > k ? v : T(0));
+            return v;
+        }
+    }
+    // chunk element index -> (k, m), coalesced for the source
+    __device__ __forceinline__ void map(int s, int idx, int &k, int &m) const {
+        const bool kfast = (s == kTrows) || (s == kVrows && LAYOUT == 0) || (s == kVcols && LAYOUT == 1);
+        if (kfast) { k = idx % C::KC; m = idx / C::KC; } else { m = idx % B; k = idx / B; }
+    }
+};
+
+// acc (+|-)= A(k, m)^T-view ... : acc[i][j] += sign * sum_k A(k, m0+i) * Bop(k, c0+j)
+template <typename T, int LAYOUT, int B>
+__device__ __forceinline__ void gemm(const UpdCtx<T, LAYOUT, B> &ctx, int src, T (&acc)[8][UCfg<T, B>::CB],
+                                     const T *Bop, T *chunk0, T *chunk1, bool neg) {
+    using C = UCfg<T, B>;
+    const int tid = threadIdx.x;
+    const int m0 = tid % C::TM;  // rows m0 + TM*i: consecutive lanes, consecutive rows
+    const int c0 = (tid / C::TM) * C::CB;
+    T pre[C::PER];
+    // prologue: chunk 0 into registers
+#pragma unroll
+    for (int e = 0; e < C::PER; ++e) {
+        int k, m;
+        ctx.map(src, tid + e * kWNT, k, m);
+        pre[e] = ctx.a_elem(src, k, m);
+    }
+    T *bufs[2] = {chunk0, chunk1};
+    const int nchunk = B / C::KC;
+    for (int ch = 0; ch < nchunk; ++ch) {
+        T *cur = bufs[ch & 1];
+#pragma unroll
+        for (int e = 0; e < C::PER; ++e) {
+            int k, m;
+            ctx.map(src, tid + e * kWNT, k, m);
+            cur[k * C::LDC + m] = pre[e];
+        }
+        __syncthreads();
+        if (ch + 1 < nchunk) {
+            const int k0n = (ch + 1) * C::KC;
+#pragma unroll
+            for (int e = 0; e < C::PER; ++e) {
+                int k, m;
+                ctx.map(src, tid + e * kWNT, k, m);
+                pre[e] = ctx.a_elem(src, k0n + k, m);
+            }
+        }
+        const int k0 = ch * C::KC;
+#pragma unroll 4
+        for (int k = 0; k < C::KC; ++k) {
+            T av[8], bv[C::CB];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) av[i] = cur[k * C::LDC + m0 + C::TM * i];
+#pragma unroll
+            for (int j = 0; j < C::CB; ++j) bv[j] = Bop[(k0 + k) + (c0 + j) * C::LDB];
+            if (neg) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+#pragma unroll
+                    for (int j = 0; j < C::CB; ++j) acc[i][j] -= av[i] * bv[j];
+            } else {
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+#pragma unroll
+                    for (int j = 0; j < C::CB; ++j) acc[i][j] += av[i] * bv[j];
+            }
+        }
+    }
+    __syncthreads();
+}
+
+template <typename T, int LAYOUT, int B>
+__global__ void __launch_bounds__(kWNT) update_full_kernel(UpdFullArgs args) {
+    using C = UCfg<T, B>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *Top = reinterpret_cast<T *>(smem_raw);      // LDB x W, column-major
+    T *Buf = Top + (size_t)C::LDB * C::W;          // LDB x W
+    T *ch0 = Buf + (size_t)C::LDB * C::W;          // KC x LDC
+    T *ch1 = ch0 + (size_t)C::KC * C::LDC;
+    const int tid = threadIdx.x;
+    const int64_t j0 = (int64_t)(args.pc + 1) * B + (int64_t)blockIdx.x * C::W;
+    const int wc = (int)min((int64_t)C::W, args.n - j0);
+    if (wc <= 0) return;
+    View<T, LAYOUT> V{reinterpret_cast<T *>(args.a), args.lda};
+    const int64_t top0 = (int64_t)args.pr * B;
+    const int m0 = tid % C::TM;
+    const int c0 = (tid / C::TM) * C::CB;
+
+    auto load_strip = [&](T *S, int64_t r0) {
+        for (int idx = tid; idx < B * C::W; idx += kWNT) {
+            int t, c;
+            if (LAYOUT == 0) { t = idx % B; c = idx / B; } else { c = idx % C::W; t = idx / C::W; }
+            S[t + c * C::LDB] = (c < wc) ? V(r0 + t, j0 + c) : T(0);
+        }
+    };
+    auto store_strip = [&](const T *S, int64_t r0) {
+        for (int idx = tid; idx < B * C::W; idx += kWNT) {
+            int t, c;
+            if (LAYOUT == 0) { t = idx % B; c = idx / B; } else { c = idx % C::W; t = idx / C::W; }
+            if (c < wc) V(r0 + t, j0 + c) = S[t + c * C::LDB];
+        }
+    };
+    auto get_blk = [&](const T *S, T (&r)[8][C::CB]) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < C::CB; ++j) r[i][j] = S[(m0 + C::TM * i) + (c0 + j) * C::LDB];
+    };
+    auto put_blk = [&](T *S, const T (&r)[8][C::CB]) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < C::CB; ++j) S[(m0 + C::TM * i) + (c0 + j) * C::LDB] = r[i][j];
+    };
+    auto zero = [&](T (&r)[8][C::CB]) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < C::CB; ++j) r[i][j] = T(0);
+    };
+
+    load_strip(Top, top0);
+    __syncthreads();
+    T acc[8][C::CB];
+    T apr[8][C::CB];
+    for (int p = 0; p < args.P; ++p) {
+        UpdCtx<T, LAYOUT, B> ctx;
+        ctx.V = V;
+        ctx.Tf = reinterpret_cast<const T *>(args.tfull) + (size_t)p * B * B;
+        ctx.row0 = (int64_t)(args.pr + p) * B;
+        ctx.col0 = (int64_t)args.pc * B;
+        ctx.geqrt = (p == 0);
+        if (p == 0) {
+            zero(acc);
+            gemm<T, LAYOUT, B>(ctx, kVrows, acc, Top, ch0, ch1, false);   // Z = Y0^T Top
+            put_blk(Buf, acc);
+            __syncthreads();
+            zero(acc);
+            gemm<T, LAYOUT, B>(ctx, kTrows, acc, Buf, ch0, ch1, false);   // W = T0^T Z
+            put_blk(Buf, acc);
+            __syncthreads();
+            get_blk(Top, acc);
+            gemm<T, LAYOUT, B>(ctx, kVcols, acc, Buf, ch0, ch1, true);    // Top -= Y0 W
+            put_blk(Top, acc);
+            __syncthreads();
+        } else {
+            load_strip(Buf, ctx.row0);
+            __syncthreads();
+            get_blk(Top, acc);
+            gemm<T, LAYOUT, B>(ctx, kVrows, acc, Buf, ch0, ch1, false);   // Z = Top + V^T A_p
+            get_blk(Buf, apr);
+            __syncthreads();
+            put_blk(Buf, acc);
+            __syncthreads();
+            zero(acc);
+            gemm<T, LAYOUT, B>(ctx, kTrows, acc, Buf, ch0, ch1, false);   // W = T^T Z
+            {
+                T tp[8][C::CB];
+                get_blk(Top, tp);
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+#pragma unroll
+                    for (int j = 0; j < C::CB; ++j) tp[i][j] -= acc[i][j];
+                put_blk(Top, tp);                                             // Top -= W
+            }
+            put_blk(Buf, acc);
+            __syncthreads();
+            gemm<T, LAYOUT, B>(ctx, kVcols, apr, Buf, ch0, ch1, true);    // A_p -= V W
+            put_blk(Buf, apr);
+            __syncthreads();
+            store_strip(Buf, ctx.row0);
+            __syncthreads();
+        }
+    }
+    store_strip(Top, top0);
+}
+
+template <typename T, int B>
+size_t upd_full_smem() {
+    using C = UCfg<T, B>;
+    return sizeof(T) * (2 * (size_t)C::LDB * C::W + 2 * (size_t)C::KC * C::LDC);
+}
+
+template <typename T, int LAYOUT, int B>
+int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const void *tfull, cudaStream_t s) {
+    using C = UCfg<T, B>;
+    static bool attr = false;
+    const size_t smem = upd_full_smem<T, B>();
+    if (!attr) {
+        AVS_CUDA_TRY(cudaFuncSetAttribute(update_full_kernel<T, LAYOUT, B>,
+                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = true;
+    }
+    const int64_t ncols = n - (int64_t)(pc + 1) * B;
+    if (ncols <= 0) return AVS_SUCCESS;
+    UpdFullArgs a{dA, lda, n, B, pr, pc, P, tfull};
+    update_full_kernel<T, LAYOUT, B><<<(unsigned)((ncols + C::W - 1) / C::W), kWNT, smem, s>>>(a);
+    AVS_CUDA_TRY(cudaGetLastError());
+    return AVS_SUCCESS;
+}
+
+template <typename T, int LAYOUT>
+int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const void *tblk, void *tfull,
+                  cudaStream_t s) {
+    static bool attr = false;
+    const size_t smem = sizeof(T) * (size_t)32 * (256 + 1) > sizeof(T) * (size_t)256 * 256 / 16
+                            ? sizeof(T) * (size_t)32 * (256 + 1)
+                            : sizeof(T) * (size_t)256 * 16;
+    if (!attr) {
+        AVS_CUDA_TRY(
+            cudaFuncSetAttribute(tbuild_kernel<T, LAYOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr = true;
+    }
+    TBuildArgs a{dA, lda, b, pr, pc, P, tblk, tfull};
+    tbuild_kernel<T, LAYOUT><<<P, kWNT, smem, s>>>(a);
+    AVS_CUDA_TRY(cudaGetLastError());
+    return AVS_SUCCESS;
+}
+
+}  // namespace
+
+// Full-T trailing update of one half-step (tiles 128 and 256).
+template <typename T>
+int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const void *tblk,
+                       void *tfull, cudaStream_t s) {
+    int rc;
+    if (layout == 0) {
+        if ((rc = launch_tbuild<T, 0>(dA, lda, b, pr, pc, P, tblk, tfull, s)) != AVS_SUCCESS) return rc;
+        return b == 256 ? launch_upd_full<T, 0, 256>(dA, lda, n, pr, pc, P, tfull, s)
+                        : launch_upd_full<T, 0, 128>(dA, lda, n, pr, pc, P, tfull, s);
+    }
+    if ((rc = launch_tbuild<T, 1>(dA, lda, b, pr, pc, P, tblk, tfull, s)) != AVS_SUCCESS) return rc;
+    return b == 256 ? launch_upd_full<T, 1, 256>(dA, lda, n, pr, pc, P, tfull, s)
+                    : launch_upd_full<T, 1, 128>(dA, lda, n, pr, pc, P, tfull, s);
+}
+
+template int stage1_update_full<float>(float *, int64_t, int64_t, int, int, int, int, int, const void *, void *,
+                                       cudaStream_t);
+template int stage1_update_full<double>(double *, int64_t, int64_t, int, int, int, int, int, const void *, void *,
+                                        cudaStream_t);
+
+}  // namespace avs

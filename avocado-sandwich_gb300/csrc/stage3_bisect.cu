@@ -47,6 +47,22 @@ __global__ void tgk_bound_kernel(const double *d, const double *e, int64_t n, do
     }
 }
 
+// Pivot recurrence q_i = -x - a_i / q_{i-1} (a_i = squared off-diagonal of
+// TGK), counting negative pivots.  The division is replaced by a reciprocal:
+// a single-precision estimate (hardware rcp) refined by one Newton-Raphson
+// step r' = r (2 - q r), which leaves a relative error near 2^-46; pivots
+// outside the single-precision range fall back to an FP64 division.  The
+// count is then exact for off-diagonals perturbed by ~1e-14 relatively.
+__device__ __forceinline__ double recip_nr(double q) {
+    const double aq = fabs(q);
+    if (aq > 1e-36 && aq < 1e36) {
+        const double r = (double)__frcp_rn((float)q);
+        const double e = fma(-q, r, 1.0);
+        return fma(r, e, r);
+    }
+    return 1.0 / q;
+}
+
 __device__ __forceinline__ int tgk_count(const double *__restrict__ d, const double *__restrict__ e, int64_t n,
                                          double x, double pivmin) {
     int cnt = 0;
@@ -55,14 +71,37 @@ __device__ __forceinline__ int tgk_count(const double *__restrict__ d, const dou
     cnt += (q < 0.0);
     for (int64_t i = 0; i < n; ++i) {
         const double di = __ldg(d + i);
-        q = -x - (di * di) / q;
+        q = fma(-(di * di), recip_nr(q), -x);
         if (fabs(q) < pivmin) q = -pivmin;
         cnt += (q < 0.0);
         if (i + 1 < n) {
             const double ei = __ldg(e + i);
-            q = -x - (ei * ei) / q;
+            q = fma(-(ei * ei), recip_nr(q), -x);
             if (fabs(q) < pivmin) q = -pivmin;
             cnt += (q < 0.0);
+        }
+    }
+    return cnt;
+}
+
+// The same count in FP32 (used only to narrow the bracket; every bracket it
+// produces is re-checked with FP64 counts before it is trusted).
+__device__ __forceinline__ int tgk_count_f32(const double *__restrict__ d, const double *__restrict__ e, int64_t n,
+                                             float x, float pivmin) {
+    int cnt = 0;
+    float q = -x;
+    if (fabsf(q) < pivmin) q = -pivmin;
+    cnt += (q < 0.0f);
+    for (int64_t i = 0; i < n; ++i) {
+        const float di = (float)__ldg(d + i);
+        q = -x - __fdividef(di * di, q);
+        if (fabsf(q) < pivmin || !isfinite(q)) q = -pivmin;
+        cnt += (q < 0.0f);
+        if (i + 1 < n) {
+            const float ei = (float)__ldg(e + i);
+            q = -x - __fdividef(ei * ei, q);
+            if (fabsf(q) < pivmin || !isfinite(q)) q = -pivmin;
+            cnt += (q < 0.0f);
         }
     }
     return cnt;
@@ -81,6 +120,25 @@ __global__ void bisect_kernel(const double *d, const double *e, int64_t n, doubl
     const double tol = rel_tol * bound;
     const int64_t target = 2 * n - 1 - k;  // TGK index (ascending) of the k-th largest sigma
     double lo = 0.0, hi = bound * (1.0 + 4.0 * DBL_EPSILON) + pivmin;
+    // phase 1: FP32 counts shrink the bracket to ~2^-18 of its width
+    if (bound < 1e30 && bound > 1e-30) {
+        float flo = 0.0f, fhi = (float)hi;
+        const float fpiv = fmaxf((float)pivmin, 1e-37f);
+        for (int it = 0; it < 18; ++it) {
+            const float mid = 0.5f * (flo + fhi);
+            if (mid <= flo || mid >= fhi) break;
+            if (tgk_count_f32(d, e, n, mid, fpiv) > target)
+                fhi = mid;
+            else
+                flo = mid;
+        }
+        // widen by a few FP32 ulps of the bracket and verify it in FP64
+        const double w = fmax((double)(fhi - flo), 1e-7 * bound);
+        const double tlo = fmax(0.0, (double)flo - w), thi = fmin(hi, (double)fhi + w);
+        if (tgk_count(d, e, n, tlo, pivmin) <= target) lo = tlo;
+        if (tgk_count(d, e, n, thi, pivmin) > target) hi = thi;
+    }
+    // phase 2: FP64 bisection to the requested width
     for (int it = 0; it < 128 && hi - lo > tol; ++it) {
         const double mid = 0.5 * (lo + hi);
         if (mid <= lo || mid >= hi) break;
@@ -105,6 +163,13 @@ __global__ void copy2d_kernel(const TI *src, int64_t lds, TO *dst, int64_t ldd, 
             dst[r + c * ldd] = (TO)src[r + c * lds];
 }
 
+// Threads per CTA: small enough that the values spread over every SM.
+inline int bisect_threads(int64_t n) {
+    int t = 128;
+    while (t > 32 && (n + t - 1) / t < 2 * 152) t >>= 1;
+    return t;
+}
+
 }  // namespace
 
 int stage3_bisect(const double *dd, const double *de, int64_t n, double rel_tol, double *dsigma, double *dscratch,
@@ -113,7 +178,7 @@ int stage3_bisect(const double *dd, const double *de, int64_t n, double rel_tol,
     if (!(rel_tol > 0.0)) rel_tol = 2.0 * DBL_EPSILON;
     tgk_bound_kernel<<<1, 1024, 0, s>>>(dd, de, n, dscratch);
     AVS_CUDA_TRY(cudaGetLastError());
-    const int threads = 128;
+    const int threads = bisect_threads(n);
     bisect_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, s>>>(dd, de, n, rel_tol, dscratch, dsigma);
     AVS_CUDA_TRY(cudaGetLastError());
     if (launches) *launches += 2;
@@ -183,7 +248,8 @@ int bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *
     if (!(rel_tol > 0.0)) rel_tol = 2.0 * DBL_EPSILON;
     tgk_bound_kernel<<<1, 1024, 0, s>>>(dd, te, n, scr);
     AVS_CUDA_TRY(cudaGetLastError());
-    bisect_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(dd, te, n, rel_tol, scr, dsigma);
+    const int threads = bisect_threads(n);
+    bisect_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, s>>>(dd, te, n, rel_tol, scr, dsigma);
     AVS_CUDA_TRY(cudaGetLastError());
     AVS_CUDA_TRY(cudaStreamSynchronize(s));
     return AVS_SUCCESS;
