@@ -176,7 +176,10 @@ def from_device(t):
     return t.detach().cpu().numpy().T.copy()
 
 
-def my_CU_svdval(A, block_size, precision=None, report=None, handle=None, rel_tol=0.0):
+STAGES = {"auto": 0, "fp64": 1, "df64": 2}
+
+
+def my_CU_svdval(A, block_size, precision=None, report=None, handle=None, rel_tol=0.0, stages="auto"):
     """Singular values (descending) of the square matrix A with tile ``block_size``.
 
     ``A`` is a numpy array (the ``Matrix{Float32}`` method, host copies inside

@@ -36,7 +36,7 @@ inline bool is_pow2(int64_t x) { return x > 0 && (x & (x - 1)) == 0; }
 // Workspace carve-up for one call.
 struct Layout {
     size_t off_w, off_stage, off_tau, off_tblk, off_flags1, off_flags2, off_err, off_ab, off_d, off_e, off_sig,
-        off_scr, off_out, off_tfull, total;
+        off_scr, off_out, off_tfull, off_pairs, total;
     int64_t ldab;
 };
 
@@ -73,6 +73,8 @@ Layout make_layout(int64_t n, int b, size_t elem, size_t stage_elem) {
     o = align_up(o + sizeof(double) * 8);
     L.off_out = o;
     o = align_up(o + sizeof(double) * (size_t)n);
+    L.off_pairs = o;
+    o = align_up(o + sizeof(float2) * (size_t)(2 * n + 1));
     L.total = o;
     return L;
 }
@@ -109,6 +111,19 @@ size_t storage_elem(int prec) {
         case AVS_PREC_FP32: return 4;
         default: return 0;
     }
+}
+
+// Arithmetic of stages 2 and 3: FP64 for the plain FP64 path (or on request),
+// double-float (two FP32, ~44-48 bits) for the FP32-class modes.
+bool fp64_stages(int prec, const avs_opts *opts) {
+    if (opts && (opts->flags & AVS_FLAG_FP64_STAGES)) return true;
+    if (opts && (opts->flags & AVS_FLAG_DF64_STAGES)) return false;
+    return prec == AVS_PREC_FP64;
+}
+
+double bisect_tol(bool f64, const avs_opts *opts) {
+    if (opts && opts->bisect_rel_tol > 0) return opts->bisect_rel_tol;
+    return f64 ? 2.0 * DBL_EPSILON : 4e-14;
 }
 
 int check_common(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const void *A, const void *sigma) {
@@ -150,7 +165,7 @@ float ev_ms(cudaEvent_t a, cudaEvent_t b) {
 // (type TI, leading dimension lds) on the device; sigma_out (type TO) on the device.
 template <typename S, typename TI, typename TO>
 int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src, int64_t lds, TO *sigma_out,
-                 double rel_tol, cudaStream_t s, avs_report *rep) {
+                 double rel_tol, bool fp64_stages, cudaStream_t s, avs_report *rep) {
     int rc;
     int64_t launches = 0;
     S *W = reinterpret_cast<S *>(ws_at(h, L.off_w));
@@ -170,17 +185,27 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
     double *AB = reinterpret_cast<double *>(ws_at(h, L.off_ab));
     double *dd = reinterpret_cast<double *>(ws_at(h, L.off_d));
     double *de = reinterpret_cast<double *>(ws_at(h, L.off_e));
-    if ((rc = extract_band_compact<S>(W, n, n, b, AB, L.ldab, s)) != AVS_SUCCESS) return rc;
-    ++launches;
     Stage2Work w2;
     w2.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags2));
     w2.err = err;
-    if ((rc = stage2_chase(AB, n, b, L.ldab, dd, de, w2, s, h->num_sms, &launches)) != AVS_SUCCESS) return rc;
+    if (fp64_stages) {
+        if ((rc = extract_band_compact<S>(W, n, n, b, AB, L.ldab, s)) != AVS_SUCCESS) return rc;
+        ++launches;
+        if ((rc = stage2_chase(AB, n, b, L.ldab, dd, de, w2, s, h->num_sms, &launches)) != AVS_SUCCESS) return rc;
+    } else {
+        // the FP64 band buffer holds the float2 band (same size)
+        if ((rc = stage2_chase_df<S>(W, n, n, b, reinterpret_cast<float2 *>(AB), L.ldab, dd, de, w2, s, h->num_sms,
+                                     &launches)) != AVS_SUCCESS)
+            return rc;
+    }
     AVS_CUDA_TRY(cudaEventRecord(h->ev[2], s));
     double *sig = reinterpret_cast<double *>(ws_at(h, L.off_sig));
-    if ((rc = stage3_bisect(dd, de, n, rel_tol, sig, reinterpret_cast<double *>(ws_at(h, L.off_scr)), s,
-                            &launches)) != AVS_SUCCESS)
-        return rc;
+    if (fp64_stages)
+        rc = stage3_bisect(dd, de, n, rel_tol, sig, reinterpret_cast<double *>(ws_at(h, L.off_scr)), s, &launches);
+    else
+        rc = stage3_bisect_df(dd, de, n, rel_tol, sig, reinterpret_cast<double *>(ws_at(h, L.off_scr)),
+                              reinterpret_cast<float2 *>(ws_at(h, L.off_pairs)), s, &launches);
+    if (rc != AVS_SUCCESS) return rc;
     if ((rc = cast_from_double<TO>(sig, sigma_out, n, s)) != AVS_SUCCESS) return rc;
     ++launches;
     AVS_CUDA_TRY(cudaEventRecord(h->ev[3], s));
@@ -215,9 +240,10 @@ int svdvals_dev(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, 
     AVS_CUDA_TRY(cudaSetDevice(h->device));
     const Layout L = make_layout(n, tile, elem, 0);
     if ((rc = ensure_ws(h, L.total)) != AVS_SUCCESS) return rc;
-    const double tol = (opts && opts->bisect_rel_tol > 0) ? opts->bisect_rel_tol : 2.0 * DBL_EPSILON;
-    if (elem == 8) return run_pipeline<double, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, s, rep);
-    return run_pipeline<float, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, s, rep);
+    const bool f64 = fp64_stages(prec, opts);
+    const double tol = bisect_tol(f64, opts);
+    if (elem == 8) return run_pipeline<double, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, s, rep);
+    return run_pipeline<float, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, s, rep);
 }
 
 template <typename T>
@@ -243,12 +269,13 @@ int svdvals_host(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile,
     avs_opts o2 = opts ? *opts : avs_opts{};
     o2.stream = s;
     avs_report r2{};
-    const double tol = (o2.bisect_rel_tol > 0) ? o2.bisect_rel_tol : 2.0 * DBL_EPSILON;
+    const bool f64 = fp64_stages(prec, opts);
+    const double tol = bisect_tol(f64, opts);
     T *dout = reinterpret_cast<T *>(ws_at(h, L.off_out));
     if (elem == 8)
-        rc = run_pipeline<double, T, T>(h, L, n, tile, stage, n, dout, tol, s, &r2);
+        rc = run_pipeline<double, T, T>(h, L, n, tile, stage, n, dout, tol, f64, s, &r2);
     else
-        rc = run_pipeline<float, T, T>(h, L, n, tile, stage, n, dout, tol, s, &r2);
+        rc = run_pipeline<float, T, T>(h, L, n, tile, stage, n, dout, tol, f64, s, &r2);
     if (rc == AVS_SUCCESS) {
         AVS_CUDA_TRY(cudaMemcpyAsync(sigma, dout, sizeof(T) * (size_t)n, cudaMemcpyDeviceToHost, s));
         AVS_CUDA_TRY(cudaEventRecord(h->ev[5], s));

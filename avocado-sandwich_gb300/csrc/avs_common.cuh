@@ -118,8 +118,13 @@ struct Stage2Work {
 int stage2_chase(double *dAB, int64_t n, int bw, int64_t ldab, double *dd, double *de, const Stage2Work &w,
                  cudaStream_t s, int num_sms, int64_t *launches);
 
+template <typename T>
+int stage2_chase_df(const T *dW, int64_t n, int64_t ldw, int bw, float2 *dAB, int64_t ldab, double *dd, double *de,
+                    const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
 int bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *dsigma, double rel_tol,
                          cudaStream_t s);
+int stage3_bisect_df(const double *dd, const double *de, int64_t n, double rel_tol, double *dsigma, double *dscratch,
+                     float2 *dpairs, cudaStream_t s, int64_t *launches);
 int stage3_bisect(const double *dd, const double *de, int64_t n, double rel_tol, double *dsigma, double *dscratch,
                   cudaStream_t s, int64_t *launches);
 

@@ -39,6 +39,7 @@
 #include <cmath>
 
 #include "avs_common.cuh"
+#include "df64.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -177,44 +178,144 @@ struct ChaseCfg {
     static_assert(CPG >= 1 && CPW >= 1, "chase configuration");
 };
 
-// Reflector of sv[0..L) (LAPACK convention, see make_reflector) computed by
-// every CTA of the cluster from the same global data.
-__device__ __forceinline__ void cluster_reflector(double *sv, int L, double *red, double *s_tau, double *s_beta) {
-    double part = 0.0;
-    for (int i = 1 + threadIdx.x; i < L; i += blockDim.x) part += sv[i] * sv[i];
-    const double s = block_sum(part, red);
-    const double alpha = sv[0];
-    double tau = 0.0, beta = alpha, scal = 0.0;
-    if (s > 0.0) {
-        const double nrm = sqrt(alpha * alpha + s);
-        beta = alpha >= 0.0 ? -nrm : nrm;
-        tau = (beta - alpha) / beta;
-        scal = 1.0 / (alpha - beta);
+// Scalar arithmetic of the chase: FP64, or double-float pairs stored as float2.
+template <typename S>
+struct ChaseAr;
+
+template <>
+struct ChaseAr<double> {
+    using V = double;   // register value
+    using St = double;  // storage element
+    static __device__ __forceinline__ V zero() { return 0.0; }
+    static __device__ __forceinline__ V one() { return 1.0; }
+    static __device__ __forceinline__ V ld(const St *p) { return __ldcg(p); }
+    static __device__ __forceinline__ void st(St *p, V v) { *p = v; }
+    static __device__ __forceinline__ V add(V a, V b) { return a + b; }
+    static __device__ __forceinline__ V sub(V a, V b) { return a - b; }
+    static __device__ __forceinline__ V mul(V a, V b) { return a * b; }
+    static __device__ __forceinline__ V fma(V a, V b, V c) { return ::fma(a, b, c); }
+    static __device__ __forceinline__ V neg(V a) { return -a; }
+    static __device__ __forceinline__ V div(V a, V b) { return a / b; }
+    static __device__ __forceinline__ V sqrt(V a) { return ::sqrt(a); }
+    static __device__ __forceinline__ bool ge0(V a) { return a >= 0.0; }
+    static __device__ __forceinline__ bool gt0(V a) { return a > 0.0; }
+    static __device__ __forceinline__ bool iszero(V a) { return a == 0.0; }
+    static __device__ __forceinline__ V shfl_xor(V a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
+    static __device__ __forceinline__ double to_double(V a) { return a; }
+    static __device__ __forceinline__ St from_double(double a) { return a; }
+};
+
+template <>
+struct ChaseAr<df64> {
+    using V = df64;
+    using St = float2;
+    static __device__ __forceinline__ V zero() { return df64{0.0f, 0.0f}; }
+    static __device__ __forceinline__ V one() { return df64{1.0f, 0.0f}; }
+    static __device__ __forceinline__ V ld(const St *p) {
+        const float2 v = __ldcg(p);
+        return df64{v.x, v.y};
+    }
+    static __device__ __forceinline__ void st(St *p, V v) { *p = make_float2(v.hi, v.lo); }
+    static __device__ __forceinline__ V add(V a, V b) { return df_add(a, b); }
+    static __device__ __forceinline__ V sub(V a, V b) { return df_sub(a, b); }
+    static __device__ __forceinline__ V mul(V a, V b) { return df_mul(a, b); }
+    static __device__ __forceinline__ V fma(V a, V b, V c) { return df_add(df_mul(a, b), c); }
+    static __device__ __forceinline__ V neg(V a) { return df_neg(a); }
+    static __device__ __forceinline__ V div(V a, V b) { return df_div(a, b); }
+    static __device__ __forceinline__ V sqrt(V a) { return df_sqrt(a); }
+    static __device__ __forceinline__ bool ge0(V a) { return !df_lt0(a); }
+    static __device__ __forceinline__ bool gt0(V a) { return a.hi > 0.0f || (a.hi == 0.0f && a.lo > 0.0f); }
+    static __device__ __forceinline__ bool iszero(V a) { return a.hi == 0.0f && a.lo == 0.0f; }
+    static __device__ __forceinline__ V shfl_xor(V a, int o) {
+        return df64{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
+    }
+    static __device__ __forceinline__ double to_double(V a) { return df_to_double(a); }
+    static __device__ __forceinline__ St from_double(double a) {
+        const df64 v = df_from_double(a);
+        return make_float2(v.hi, v.lo);
+    }
+};
+
+template <typename S>
+struct BandT {
+    using Ar = ChaseAr<S>;
+    typename Ar::St *ab;
+    int64_t ldab;
+    int ku;  // 2bw - 1
+    __device__ __forceinline__ typename Ar::St *at(int64_t r, int64_t c) const { return ab + (ku + r - c) + c * ldab; }
+};
+
+template <typename S>
+__device__ __forceinline__ typename ChaseAr<S>::V warp_sum_s(typename ChaseAr<S>::V v) {
+    using Ar = ChaseAr<S>;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = Ar::add(v, Ar::shfl_xor(v, o));
+    return v;
+}
+
+template <typename S>
+__device__ __forceinline__ typename ChaseAr<S>::V block_sum_s(typename ChaseAr<S>::V v,
+                                                              typename ChaseAr<S>::V *red) {
+    using Ar = ChaseAr<S>;
+    v = warp_sum_s<S>(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        typename Ar::V t = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : Ar::zero();
+        t = warp_sum_s<S>(t);
+        if (threadIdx.x == 0) red[0] = t;
+    }
+    __syncthreads();
+    return red[0];
+}
+
+// Reflector of sv[0..L) (LAPACK convention: beta = -sign(alpha) ||x||,
+// v = x / (alpha - beta), v0 = 1, tau = (beta - alpha) / beta; tau = 0 when
+// x[1..] == 0), computed by every CTA of the cluster from the same data.
+template <typename S>
+__device__ __forceinline__ void cluster_reflector(typename ChaseAr<S>::V *sv, int L, typename ChaseAr<S>::V *red,
+                                                  typename ChaseAr<S>::V *s_tau, typename ChaseAr<S>::V *s_beta) {
+    using Ar = ChaseAr<S>;
+    using V = typename Ar::V;
+    V part = Ar::zero();
+    for (int i = 1 + threadIdx.x; i < L; i += blockDim.x) part = Ar::fma(sv[i], sv[i], part);
+    const V s = block_sum_s<S>(part, red);
+    const V alpha = sv[0];
+    V tau = Ar::zero(), beta = alpha, scal = Ar::zero();
+    if (Ar::gt0(s)) {
+        const V nrm = Ar::sqrt(Ar::fma(alpha, alpha, s));
+        beta = Ar::ge0(alpha) ? Ar::neg(nrm) : nrm;
+        tau = Ar::div(Ar::sub(beta, alpha), beta);
+        scal = Ar::div(Ar::one(), Ar::sub(alpha, beta));
     }
     __syncthreads();  // every thread has read alpha = sv[0]
-    for (int i = 1 + threadIdx.x; i < L; i += blockDim.x) sv[i] *= scal;
+    for (int i = 1 + threadIdx.x; i < L; i += blockDim.x) sv[i] = Ar::mul(sv[i], scal);
     if (threadIdx.x == 0) {
-        sv[0] = 1.0;
+        sv[0] = Ar::one();
         *s_tau = tau;
         *s_beta = beta;
     }
     __syncthreads();
 }
 
-template <int BW>
-__global__ void __launch_bounds__(512) chase_cluster_kernel(double *ab, int64_t n, int64_t ldab, int *ticket,
-                                                            int *done, int *err) {
+template <int BW, typename S>
+__global__ void __launch_bounds__(512) chase_cluster_kernel(typename ChaseAr<S>::St *ab, int64_t n, int64_t ldab,
+                                                            int *ticket, int *done, int *err) {
     using Cfg = ChaseCfg<BW>;
+    using Ar = ChaseAr<S>;
+    using V = typename Ar::V;
     cg::cluster_group cluster = cg::this_cluster();
     const int q = (int)cluster.block_rank();
-    __shared__ double sv[BW];
-    __shared__ double red[32];
-    __shared__ double part[Cfg::G][Cfg::RPC];
-    __shared__ double wrow[Cfg::RPC];
-    __shared__ double s_tau, s_beta;
+    __shared__ V sv[BW];
+    __shared__ V red[32];
+    __shared__ V part[Cfg::G][Cfg::RPC];
+    __shared__ V wrow[Cfg::RPC];
+    __shared__ V s_tau, s_beta;
     __shared__ int s_j;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    Band A{ab, ldab, 2 * BW - 1};
+    BandT<S> A{ab, ldab, 2 * BW - 1};
 
     for (;;) {
         if (q == 0 && tid == 0) s_j = atomicAdd(ticket, 1);
@@ -232,43 +333,43 @@ __global__ void __launch_bounds__(512) chase_cluster_kernel(double *ab, int64_t 
             if (tid == 0 && j > 0) wait_geq(done + j - 1, min(2 * m + 4, ops_prev), err);
             __syncthreads();
             if (L >= 2) {
-                for (int i = tid; i < L; i += blockDim.x) sv[i] = __ldcg(A.at(rho, c0 + i));
+                for (int i = tid; i < L; i += blockDim.x) sv[i] = Ar::ld(A.at(rho, c0 + i));
                 __syncthreads();
-                cluster_reflector(sv, L, red, &s_tau, &s_beta);
-                const double tau = s_tau;
-                if (tau != 0.0) {
+                cluster_reflector<S>(sv, L, red, &s_tau, &s_beta);
+                const V tau = s_tau;
+                if (!Ar::iszero(tau)) {
                     const int rr = tid % Cfg::RPC, g = tid / Cfg::RPC;
                     const int64_t r = rho + 1 + (int64_t)q * Cfg::RPC + rr;
                     const bool rv = (r <= c1);
-                    double vals[Cfg::CPG];
-                    double acc = 0.0;
+                    V vals[Cfg::CPG];
+                    V acc = Ar::zero();
 #pragma unroll
                     for (int k = 0; k < Cfg::CPG; ++k) {
                         const int ci = g * Cfg::CPG + k;
-                        vals[k] = (rv && ci < L) ? __ldcg(A.at(r, c0 + ci)) : 0.0;
-                        acc += vals[k] * ((ci < L) ? sv[ci] : 0.0);
+                        vals[k] = (rv && ci < L) ? Ar::ld(A.at(r, c0 + ci)) : Ar::zero();
+                        if (ci < L) acc = Ar::fma(vals[k], sv[ci], acc);
                     }
                     part[g][rr] = acc;
                     __syncthreads();
                     if (g == 0) {
-                        double w = 0.0;
+                        V w = Ar::zero();
 #pragma unroll
-                        for (int gg = 0; gg < Cfg::G; ++gg) w += part[gg][rr];
-                        wrow[rr] = w * tau;
+                        for (int gg = 0; gg < Cfg::G; ++gg) w = Ar::add(w, part[gg][rr]);
+                        wrow[rr] = Ar::mul(w, tau);
                     }
                     __syncthreads();
-                    const double w = wrow[rr];
+                    const V w = wrow[rr];
                     if (rv) {
 #pragma unroll
                         for (int k = 0; k < Cfg::CPG; ++k) {
                             const int ci = g * Cfg::CPG + k;
-                            if (ci < L) *A.at(r, c0 + ci) = vals[k] - w * sv[ci];
+                            if (ci < L) Ar::st(A.at(r, c0 + ci), Ar::sub(vals[k], Ar::mul(w, sv[ci])));
                         }
                     }
                 }
                 if (q == 0) {
-                    if (tid == 0) *A.at(rho, c0) = s_beta;
-                    for (int i = 1 + tid; i < L; i += blockDim.x) *A.at(rho, c0 + i) = 0.0;
+                    if (tid == 0) Ar::st(A.at(rho, c0), s_beta);
+                    for (int i = 1 + tid; i < L; i += blockDim.x) Ar::st(A.at(rho, c0 + i), Ar::zero());
                 }
             }
             __threadfence();
@@ -278,45 +379,45 @@ __global__ void __launch_bounds__(512) chase_cluster_kernel(double *ab, int64_t 
             if (tid == 0 && j > 0) wait_geq(done + j - 1, min(2 * m + 5, ops_prev), err);
             __syncthreads();
             if (L >= 2) {
-                for (int i = tid; i < L; i += blockDim.x) sv[i] = __ldcg(A.at(c0 + i, c0));
+                for (int i = tid; i < L; i += blockDim.x) sv[i] = Ar::ld(A.at(c0 + i, c0));
                 __syncthreads();
-                cluster_reflector(sv, L, red, &s_tau, &s_beta);
-                const double tau = s_tau;
-                if (tau != 0.0) {
+                cluster_reflector<S>(sv, L, red, &s_tau, &s_beta);
+                const V tau = s_tau;
+                if (!Ar::iszero(tau)) {
                     const int64_t cend = min(c0 + 2 * (int64_t)BW - 1, n - 1);
                     const int64_t cbase = c0 + 1 + (int64_t)q * Cfg::CPC + (int64_t)wid * Cfg::CPW;
-                    double vals[Cfg::CPW][Cfg::RPL];
+                    V vals[Cfg::CPW][Cfg::RPL];
 #pragma unroll
                     for (int k = 0; k < Cfg::CPW; ++k) {
                         const int64_t c = cbase + k;
 #pragma unroll
                         for (int t = 0; t < Cfg::RPL; ++t) {
                             const int ri = lane + 32 * t;
-                            vals[k][t] = (c <= cend && ri < L) ? __ldcg(A.at(c0 + ri, c)) : 0.0;
+                            vals[k][t] = (c <= cend && ri < L) ? Ar::ld(A.at(c0 + ri, c)) : Ar::zero();
                         }
                     }
 #pragma unroll
                     for (int k = 0; k < Cfg::CPW; ++k) {
                         const int64_t c = cbase + k;
-                        double acc = 0.0;
+                        V acc = Ar::zero();
 #pragma unroll
                         for (int t = 0; t < Cfg::RPL; ++t) {
                             const int ri = lane + 32 * t;
-                            acc += (ri < L) ? sv[ri] * vals[k][t] : 0.0;
+                            if (ri < L) acc = Ar::fma(sv[ri], vals[k][t], acc);
                         }
-                        const double w = warp_sum(acc) * tau;
+                        const V w = Ar::mul(warp_sum_s<S>(acc), tau);
                         if (c <= cend) {
 #pragma unroll
                             for (int t = 0; t < Cfg::RPL; ++t) {
                                 const int ri = lane + 32 * t;
-                                if (ri < L) *A.at(c0 + ri, c) = vals[k][t] - w * sv[ri];
+                                if (ri < L) Ar::st(A.at(c0 + ri, c), Ar::sub(vals[k][t], Ar::mul(w, sv[ri])));
                             }
                         }
                     }
                 }
                 if (q == 0) {
-                    if (tid == 0) *A.at(c0, c0) = s_beta;
-                    for (int i = 1 + tid; i < L; i += blockDim.x) *A.at(c0 + i, c0) = 0.0;
+                    if (tid == 0) Ar::st(A.at(c0, c0), s_beta);
+                    for (int i = 1 + tid; i < L; i += blockDim.x) Ar::st(A.at(c0 + i, c0), Ar::zero());
                 }
             }
             __threadfence();
@@ -328,8 +429,9 @@ __global__ void __launch_bounds__(512) chase_cluster_kernel(double *ab, int64_t 
     }
 }
 
-template <int BW>
-int launch_chase_cluster(double *dAB, int64_t n, int64_t ldab, const Stage2Work &w, cudaStream_t s, int num_sms) {
+template <int BW, typename S>
+int launch_chase_cluster(typename ChaseAr<S>::St *dAB, int64_t n, int64_t ldab, const Stage2Work &w, cudaStream_t s,
+                         int num_sms) {
     using Cfg = ChaseCfg<BW>;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
@@ -344,7 +446,7 @@ int launch_chase_cluster(double *dAB, int64_t n, int64_t ldab, const Stage2Work 
     cfg.numAttrs = 1;
     int max_clusters = 0;
     cfg.gridDim = dim3(Cfg::C * 64);
-    if (cudaOccupancyMaxActiveClusters(&max_clusters, chase_cluster_kernel<BW>, &cfg) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveClusters(&max_clusters, chase_cluster_kernel<BW, S>, &cfg) != cudaSuccess ||
         max_clusters <= 0) {
         cudaGetLastError();
         max_clusters = std::max(1, num_sms / Cfg::C);
@@ -353,8 +455,48 @@ int launch_chase_cluster(double *dAB, int64_t n, int64_t ldab, const Stage2Work 
     const int64_t want = std::max<int64_t>(1, (n / BW) / 2 + 2);
     const int64_t clusters = std::min<int64_t>(std::min<int64_t>(want, max_clusters), n - 1);
     cfg.gridDim = dim3((unsigned)(clusters * Cfg::C));
-    AVS_CUDA_TRY(cudaLaunchKernelEx(&cfg, chase_cluster_kernel<BW>, dAB, n, ldab, w.flags, w.flags + 1, w.err));
+    AVS_CUDA_TRY(cudaLaunchKernelEx(&cfg, chase_cluster_kernel<BW, S>, dAB, n, ldab, w.flags, w.flags + 1, w.err));
     return AVS_SUCCESS;
+}
+
+template <typename S>
+int launch_chase_any(typename ChaseAr<S>::St *dAB, int64_t n, int bw, int64_t ldab, const Stage2Work &w,
+                     cudaStream_t s, int num_sms) {
+    switch (bw) {
+        case 16: return launch_chase_cluster<16, S>(dAB, n, ldab, w, s, num_sms);
+        case 32: return launch_chase_cluster<32, S>(dAB, n, ldab, w, s, num_sms);
+        case 64: return launch_chase_cluster<64, S>(dAB, n, ldab, w, s, num_sms);
+        case 128: return launch_chase_cluster<128, S>(dAB, n, ldab, w, s, num_sms);
+        case 256: return launch_chase_cluster<256, S>(dAB, n, ldab, w, s, num_sms);
+        default: return AVS_ERR_UNSUPPORTED;
+    }
+}
+
+// float2 band (double-float) <-> extraction
+template <typename T>
+__global__ void extract_band_df_kernel(const T *a, int64_t n, int64_t lda, int bw, float2 *ab, int64_t ldab) {
+    const int64_t c = blockIdx.x;
+    const int ku = 2 * bw - 1;
+    for (int i = threadIdx.x; i <= bw; i += blockDim.x) {
+        const int64_t r = c - bw + i;
+        if (r >= 0) {
+            const double v = (double)a[r + c * lda];
+            const float h = (float)v;
+            ab[(ku + r - c) + c * ldab] = make_float2(h, (float)(v - (double)h));
+        }
+    }
+}
+
+__global__ void bidiag_out_df_kernel(const float2 *ab, int64_t n, int bw, int64_t ldab, double *d, double *e) {
+    const int ku = 2 * bw - 1;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float2 x = ab[ku + i * ldab];
+        d[i] = (double)x.x + (double)x.y;
+        if (i + 1 < n) {
+            const float2 y = ab[(ku - 1) + (i + 1) * ldab];
+            e[i] = (double)y.x + (double)y.y;
+        }
+    }
 }
 
 template <typename T>
@@ -426,22 +568,16 @@ int stage2_chase(double *dAB, int64_t n, int bw, int64_t ldab, double *dd, doubl
                  cudaStream_t s, int num_sms, int64_t *launches) {
     if (n >= 2 && bw >= 2) {
         AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(n + 1), s));
-        int rc = AVS_SUCCESS;
-        switch (bw) {
-            case 16: rc = launch_chase_cluster<16>(dAB, n, ldab, w, s, num_sms); break;
-            case 32: rc = launch_chase_cluster<32>(dAB, n, ldab, w, s, num_sms); break;
-            case 64: rc = launch_chase_cluster<64>(dAB, n, ldab, w, s, num_sms); break;
-            case 128: rc = launch_chase_cluster<128>(dAB, n, ldab, w, s, num_sms); break;
-            case 256: rc = launch_chase_cluster<256>(dAB, n, ldab, w, s, num_sms); break;
-            default: {
-                // any other band width: one CTA per sweep, step-level lag 3
-                const int64_t sweeps = n - 1;
-                const int64_t want = std::max<int64_t>(1, (n / bw) / 3 + 4);
-                const int grid = (int)std::min<int64_t>(std::min<int64_t>(sweeps, want), (int64_t)num_sms * 2);
-                chase_kernel<<<grid, kChaseThreads, sizeof(double) * (size_t)bw, s>>>(dAB, n, bw, ldab, w.flags,
-                                                                                       w.flags + 1, w.err);
-                AVS_CUDA_TRY(cudaGetLastError());
-            }
+        int rc = launch_chase_any<double>(dAB, n, bw, ldab, w, s, num_sms);
+        if (rc == AVS_ERR_UNSUPPORTED) {
+            // any other band width: one CTA per sweep, step-level lag 3
+            const int64_t sweeps = n - 1;
+            const int64_t want = std::max<int64_t>(1, (n / bw) / 3 + 4);
+            const int grid = (int)std::min<int64_t>(std::min<int64_t>(sweeps, want), (int64_t)num_sms * 2);
+            chase_kernel<<<grid, kChaseThreads, sizeof(double) * (size_t)bw, s>>>(dAB, n, bw, ldab, w.flags,
+                                                                                   w.flags + 1, w.err);
+            AVS_CUDA_TRY(cudaGetLastError());
+            rc = AVS_SUCCESS;
         }
         if (rc != AVS_SUCCESS) return rc;
         if (launches) *launches += 1;
@@ -452,5 +588,28 @@ int stage2_chase(double *dAB, int64_t n, int bw, int64_t ldab, double *dd, doubl
     if (launches) *launches += 1;
     return AVS_SUCCESS;
 }
+
+// Double-float chase for the pipeline's FP32-class modes (tiles 16..256).
+template <typename T>
+int stage2_chase_df(const T *dW, int64_t n, int64_t ldw, int bw, float2 *dAB, int64_t ldab, double *dd, double *de,
+                    const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches) {
+    AVS_CUDA_TRY(cudaMemsetAsync(dAB, 0, sizeof(float2) * (size_t)ldab * (size_t)n, s));
+    extract_band_df_kernel<T><<<(unsigned)n, 128, 0, s>>>(dW, n, ldw, bw, dAB, ldab);
+    AVS_CUDA_TRY(cudaGetLastError());
+    if (n >= 2) {
+        AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(n + 1), s));
+        const int rc = launch_chase_any<df64>(dAB, n, bw, ldab, w, s, num_sms);
+        if (rc != AVS_SUCCESS) return rc;
+    }
+    const int nb = (int)std::min<int64_t>((n + 255) / 256, 4096);
+    bidiag_out_df_kernel<<<nb > 0 ? nb : 1, 256, 0, s>>>(dAB, n, bw, ldab, dd, de);
+    AVS_CUDA_TRY(cudaGetLastError());
+    if (launches) *launches += 3;
+    return AVS_SUCCESS;
+}
+template int stage2_chase_df<float>(const float *, int64_t, int64_t, int, float2 *, int64_t, double *, double *,
+                                    const Stage2Work &, cudaStream_t, int, int64_t *);
+template int stage2_chase_df<double>(const double *, int64_t, int64_t, int, float2 *, int64_t, double *, double *,
+                                     const Stage2Work &, cudaStream_t, int, int64_t *);
 
 }  // namespace avs

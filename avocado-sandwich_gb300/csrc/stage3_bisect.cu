@@ -12,6 +12,7 @@
 #include <cmath>
 
 #include "avs_common.cuh"
+#include "df64.cuh"
 
 namespace avs {
 namespace {
@@ -150,6 +151,97 @@ __global__ void bisect_kernel(const double *d, const double *e, int64_t n, doubl
     sigma[k] = 0.5 * (lo + hi);
 }
 
+// ---- double-float bisection (the pipeline's stage 3 for FP32-class modes) ----
+// B is scaled by 1/bound so every quantity stays inside FP32's exponent range;
+// the squared TGK off-diagonals a_i = (off_i / bound)^2 are formed once in FP64
+// and stored as df64 pairs.  A count costs ~60 FP32 instructions per pivot
+// instead of an FP64 division; relative errors of ~1e-14 per pivot keep the
+// count exact for a matrix within ~1e-14 of TGK(B) (the backward-stability
+// argument of the FP64 recurrence).
+__global__ void tgk_prep_df_kernel(const double *d, const double *e, int64_t n, const double *scratch, float2 *a) {
+    const double inv = scratch[0] > 0.0 ? 1.0 / scratch[0] : 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < 2 * n - 1;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double off = ((i & 1) ? e[i >> 1] : d[i >> 1]) * inv;
+        const double sq = off * off;
+        const float h = (float)sq;
+        a[i] = make_float2(h, (float)(sq - (double)h));
+    }
+}
+
+__device__ __forceinline__ int tgk_count_df(const float2 *__restrict__ a, int64_t m, df64 x, float pivmin) {
+    int cnt = 0;
+    const df64 nx = df_neg(x);
+    df64 q = nx;
+    if (fabsf(q.hi) < pivmin) q = df64{-pivmin, 0.0f};
+    cnt += df_lt0(q);
+    for (int64_t i = 0; i < m; ++i) {
+        const float2 ai = __ldg(a + i);
+        q = df_sub(nx, df_mul(df64{ai.x, ai.y}, df_rcp(q)));
+        if (fabsf(q.hi) < pivmin) q = df64{-pivmin, 0.0f};
+        cnt += df_lt0(q);
+    }
+    return cnt;
+}
+
+__device__ __forceinline__ int tgk_count_f(const float2 *__restrict__ a, int64_t m, float x, float pivmin) {
+    int cnt = 0;
+    float q = -x;
+    if (fabsf(q) < pivmin) q = -pivmin;
+    cnt += (q < 0.0f);
+    for (int64_t i = 0; i < m; ++i) {
+        q = -x - __fdividef(__ldg(a + i).x, q);
+        if (fabsf(q) < pivmin || !isfinite(q)) q = -pivmin;
+        cnt += (q < 0.0f);
+    }
+    return cnt;
+}
+
+__global__ void bisect_df_kernel(const float2 *a, int64_t n, double rel_tol, const double *scratch, double *sigma) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const double bound = scratch[0];
+    if (bound == 0.0) {
+        sigma[k] = 0.0;
+        return;
+    }
+    const int64_t m = 2 * n - 1;
+    const float pivmin = 1e-36f;
+    const int64_t target = 2 * n - 1 - k;
+    // FP32 phase on the scaled problem (all values in [0, 1])
+    float flo = 0.0f, fhi = 1.0f + 1e-6f;
+    for (int it = 0; it < 20; ++it) {
+        const float mid = 0.5f * (flo + fhi);
+        if (mid <= flo || mid >= fhi) break;
+        if (tgk_count_f(a, m, mid, pivmin) > target)
+            fhi = mid;
+        else
+            flo = mid;
+    }
+    df64 lo = df64{0.0f, 0.0f}, hi = df64{1.0f + 1e-6f, 0.0f};
+    {
+        const float w = fmaxf(fhi - flo, 4e-7f);
+        const df64 tlo = df64{fmaxf(0.0f, flo - w), 0.0f};
+        const df64 thi = df64{fminf(1.0f + 1e-6f, fhi + w), 0.0f};
+        if (tgk_count_df(a, m, tlo, pivmin) <= target) lo = tlo;
+        if (tgk_count_df(a, m, thi, pivmin) > target) hi = thi;
+    }
+    const float tol = (float)fmax(rel_tol, 1e-15);
+    for (int it = 0; it < 100; ++it) {
+        const df64 width = df_sub(hi, lo);
+        if (width.hi <= tol) break;
+        df64 mid = df_add(lo, hi);
+        mid.hi *= 0.5f;
+        mid.lo *= 0.5f;
+        if (tgk_count_df(a, m, mid, pivmin) > target)
+            hi = mid;
+        else
+            lo = mid;
+    }
+    const df64 c = df_add(lo, hi);
+    sigma[k] = bound * 0.5 * df_to_double(c);
+}
+
 template <typename T>
 __global__ void cast_kernel(const double *src, T *dst, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -252,6 +344,23 @@ int bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *
     bisect_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, s>>>(dd, te, n, rel_tol, scr, dsigma);
     AVS_CUDA_TRY(cudaGetLastError());
     AVS_CUDA_TRY(cudaStreamSynchronize(s));
+    return AVS_SUCCESS;
+}
+
+int stage3_bisect_df(const double *dd, const double *de, int64_t n, double rel_tol, double *dsigma, double *dscratch,
+                     float2 *dpairs, cudaStream_t s, int64_t *launches) {
+    if (n <= 0) return AVS_SUCCESS;
+    if (!(rel_tol > 0.0)) rel_tol = 1e-14;
+    tgk_bound_kernel<<<1, 1024, 0, s>>>(dd, de, n, dscratch);
+    AVS_CUDA_TRY(cudaGetLastError());
+    const int pb = (int)std::min<int64_t>((2 * n + 255) / 256, 1024);
+    tgk_prep_df_kernel<<<pb, 256, 0, s>>>(dd, de, n, dscratch, dpairs);
+    AVS_CUDA_TRY(cudaGetLastError());
+    const int threads = bisect_threads(n);
+    bisect_df_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, s>>>(dpairs, n, rel_tol, dscratch,
+                                                                                  dsigma);
+    AVS_CUDA_TRY(cudaGetLastError());
+    if (launches) *launches += 3;
     return AVS_SUCCESS;
 }
 

@@ -263,7 +263,7 @@ def main():
         t0 = time.perf_counter()
         s_host = avs.my_CU_svdval(a_cm, b, precision=args.precision, handle=h)
         e2e_times.append(time.perf_counter() - t0)
-    e2e = {"value": float(np.mean(e2e_times)), "unit": UNIT, "h2d_bytes_per_step": int(n * n * 4),
+    e2e = {"value": float(np.mean(e2e_times)) if e2e_times else None, "unit": UNIT, "h2d_bytes_per_step": int(n * n * 4),
            "d2h_bytes_per_step": int(n * 4), "steps": args.e2e_steps}
 
     # accuracy of this mode against the plain FP64 GPU path (whose parity with

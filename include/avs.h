@@ -66,12 +66,21 @@ extern "C" {
 #define AVS_PREC_BF16 5    /* FP32 tiles, BF16 tensor-core updates, FP32 accumulate */
 #define AVS_PREC_BF16X3 6  /* FP32 tiles, split BF16 (3 products) tensor-core updates */
 
+/* ---- avs_opts.flags ---------------------------------------------------------
+ * Stages 2 and 3 (bulge chase, bisection) run in FP64 for AVS_PREC_FP64 and in
+ * double-float arithmetic (pairs of FP32, ~44-48 significant bits; GB300 issues
+ * FP64 at 1/64 of the FP32 rate) for the FP32-class modes.  These flags
+ * override that choice. */
+#define AVS_FLAG_FP64_STAGES 1
+#define AVS_FLAG_DF64_STAGES 2
+
 typedef struct avs_handle avs_handle;
 
 typedef struct avs_opts {
     int32_t precision;      /* AVS_PREC_* (0 = default for the entry point's type) */
-    int32_t flags;          /* reserved, 0 */
-    double bisect_rel_tol;  /* bisection width relative to ||B|| (0 = 2 * DBL_EPSILON) */
+    int32_t flags;          /* AVS_FLAG_* (0 = defaults) */
+    double bisect_rel_tol;  /* bisection width relative to ||B|| (0 = 2 * DBL_EPSILON in FP64,
+                               4e-14 in double-float) */
     void *stream;           /* cudaStream_t for the _dev entry points (NULL = handle stream) */
 } avs_opts;
 

@@ -180,3 +180,21 @@ def test_zero_and_degenerate_inputs(avs_mod, torch_cuda):
     assert rel_err(s, ref) < 1e-12
     d = np.diag(np.arange(1, n + 1, dtype=np.float64))
     assert rel_err(avs_mod.my_CU_svdval(d, b), np.arange(n, 0, -1)) < 1e-14
+
+
+@pytest.mark.parametrize("n,b", [(512, 32), (1024, 64), (2048, 128), (2048, 256)])
+def test_double_float_stages_match_fp64_stages(avs_mod, torch_cuda, n, b):
+    """The bulge chase and bisection in double-float arithmetic (default for
+    FP32-class modes) agree with the FP64 stages; on FP64 tiles the
+    double-float stages stay within 1e-12 of the known spectrum."""
+    from avs import workloads
+    a, sig = workloads.geometric_spectrum(n, 21, 22, 1e-6)
+    s64 = avs_mod.my_CU_svdval(a, b, stages="fp64")
+    sdf = avs_mod.my_CU_svdval(a, b, stages="df64")
+    assert rel_err(s64, sig) < 1e-12
+    assert rel_err(sdf, sig) < 1e-12
+    a32 = a.astype(np.float32)
+    s32_64 = avs_mod.my_CU_svdval(a32, b, stages="fp64")
+    s32_df = avs_mod.my_CU_svdval(a32, b)
+    assert rel_err(s32_df, s32_64) < 1e-9
+    assert rel_err(s32_df, sig) < 1e-5
