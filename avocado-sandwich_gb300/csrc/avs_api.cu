@@ -36,11 +36,11 @@ inline bool is_pow2(int64_t x) { return x > 0 && (x & (x - 1)) == 0; }
 // Workspace carve-up for one call.
 struct Layout {
     size_t off_w, off_stage, off_tau, off_tblk, off_flags1, off_flags2, off_err, off_ab, off_d, off_e, off_sig,
-        off_scr, off_out, off_tfull, off_pairs, total;
+        off_scr, off_out, off_tfull, off_pairs, off_tcS, off_tcW, total;
     int64_t ldab;
 };
 
-Layout make_layout(int64_t n, int b, size_t elem, size_t stage_elem) {
+Layout make_layout(int64_t n, int b, size_t elem, size_t stage_elem, bool tc = false) {
     Layout L{};
     const int64_t nt = n / b;
     size_t o = 0;
@@ -75,6 +75,11 @@ Layout make_layout(int64_t n, int b, size_t elem, size_t stage_elem) {
     o = align_up(o + sizeof(double) * (size_t)n);
     L.off_pairs = o;
     o = align_up(o + sizeof(float2) * (size_t)(2 * n + 1));
+    const size_t tcb = tc ? sizeof(float) * (size_t)(nt + 1) * (size_t)b * (size_t)n : 0;
+    L.off_tcS = o;
+    o = align_up(o + tcb);
+    L.off_tcW = o;
+    o = align_up(o + tcb);
     L.total = o;
     return L;
 }
@@ -108,9 +113,20 @@ int resolve_precision(int32_t requested, bool input_double) {
 size_t storage_elem(int prec) {
     switch (prec) {
         case AVS_PREC_FP64: return 8;
-        case AVS_PREC_FP32: return 4;
+        case AVS_PREC_FP32:
+        case AVS_PREC_TF32:
+        case AVS_PREC_TF32X3: return 4;
         default: return 0;
     }
+}
+
+// Tensor-core split of a precision mode: 0 = SIMT update, 1 = TF32, 3 = split
+// TF32, -1 = not provided for this tile.  Tiles below 128 keep the 16-block
+// SIMT update (their updates are small).
+int tc_split_of(int prec, int tile) {
+    if (prec == AVS_PREC_TF32) return tile >= 128 ? 1 : 0;
+    if (prec == AVS_PREC_TF32X3) return tile >= 128 ? 3 : 0;
+    return 0;
 }
 
 // Arithmetic of stages 2 and 3: FP64 for the plain FP64 path (or on request),
@@ -165,7 +181,7 @@ float ev_ms(cudaEvent_t a, cudaEvent_t b) {
 // (type TI, leading dimension lds) on the device; sigma_out (type TO) on the device.
 template <typename S, typename TI, typename TO>
 int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src, int64_t lds, TO *sigma_out,
-                 double rel_tol, bool fp64_stages, cudaStream_t s, avs_report *rep) {
+                 double rel_tol, bool fp64_stages, int tc_split, cudaStream_t s, avs_report *rep) {
     int rc;
     int64_t launches = 0;
     S *W = reinterpret_cast<S *>(ws_at(h, L.off_w));
@@ -180,6 +196,9 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
     w1.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags1));
     w1.err = err;
     w1.tfull = ws_at(h, L.off_tfull);
+    w1.tc_split = tc_split;
+    w1.tc_S = reinterpret_cast<float *>(ws_at(h, L.off_tcS));
+    w1.tc_W = reinterpret_cast<float *>(ws_at(h, L.off_tcW));
     if ((rc = stage1_ge2bnd<S>(W, n, n, b, w1, s, &launches)) != AVS_SUCCESS) return rc;
     AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
     double *AB = reinterpret_cast<double *>(ws_at(h, L.off_ab));
@@ -238,12 +257,14 @@ int svdvals_dev(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, 
     if (rep) rep->precision = prec;
     cudaStream_t s = (opts && opts->stream) ? reinterpret_cast<cudaStream_t>(opts->stream) : h->stream;
     AVS_CUDA_TRY(cudaSetDevice(h->device));
-    const Layout L = make_layout(n, tile, elem, 0);
+    const int split = tc_split_of(prec, tile);
+    if (split < 0) return AVS_ERR_UNSUPPORTED;
+    const Layout L = make_layout(n, tile, elem, 0, split > 0);
     if ((rc = ensure_ws(h, L.total)) != AVS_SUCCESS) return rc;
     const bool f64 = fp64_stages(prec, opts);
     const double tol = bisect_tol(f64, opts);
-    if (elem == 8) return run_pipeline<double, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, s, rep);
-    return run_pipeline<float, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, s, rep);
+    if (elem == 8) return run_pipeline<double, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, 0, s, rep);
+    return run_pipeline<float, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, split, s, rep);
 }
 
 template <typename T>
@@ -259,7 +280,9 @@ int svdvals_host(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile,
     const size_t elem = storage_elem(prec);
     if (elem == 0) return AVS_ERR_UNSUPPORTED;
     AVS_CUDA_TRY(cudaSetDevice(h->device));
-    const Layout L = make_layout(n, tile, elem, sizeof(T));
+    const int split = tc_split_of(prec, tile);
+    if (split < 0) return AVS_ERR_UNSUPPORTED;
+    const Layout L = make_layout(n, tile, elem, sizeof(T), split > 0);
     if ((rc = ensure_ws(h, L.total)) != AVS_SUCCESS) return rc;
     cudaStream_t s = h->stream;
     T *stage = reinterpret_cast<T *>(ws_at(h, L.off_stage));
@@ -273,9 +296,9 @@ int svdvals_host(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile,
     const double tol = bisect_tol(f64, opts);
     T *dout = reinterpret_cast<T *>(ws_at(h, L.off_out));
     if (elem == 8)
-        rc = run_pipeline<double, T, T>(h, L, n, tile, stage, n, dout, tol, f64, s, &r2);
+        rc = run_pipeline<double, T, T>(h, L, n, tile, stage, n, dout, tol, f64, 0, s, &r2);
     else
-        rc = run_pipeline<float, T, T>(h, L, n, tile, stage, n, dout, tol, f64, s, &r2);
+        rc = run_pipeline<float, T, T>(h, L, n, tile, stage, n, dout, tol, f64, split, s, &r2);
     if (rc == AVS_SUCCESS) {
         AVS_CUDA_TRY(cudaMemcpyAsync(sigma, dout, sizeof(T) * (size_t)n, cudaMemcpyDeviceToHost, s));
         AVS_CUDA_TRY(cudaEventRecord(h->ev[5], s));
@@ -356,10 +379,11 @@ int avs_reserve(avs_handle *h, int64_t n, int32_t tile, int32_t precision) {
     if (n < 0) return -2;
     if (!is_pow2(tile) || tile < 16 || (n > 0 && n % tile != 0)) return AVS_ERR_NOT_IMPLEMENTED;
     if (tile > kMaxTile) return AVS_ERR_UNSUPPORTED;
-    const size_t elem = storage_elem(resolve_precision(precision, true));
+    const int prec = resolve_precision(precision, true);
+    const size_t elem = storage_elem(prec);
     if (elem == 0) return AVS_ERR_UNSUPPORTED;
     AVS_CUDA_TRY(cudaSetDevice(h->device));
-    return ensure_ws(h, make_layout(n, tile, elem, 8).total);
+    return ensure_ws(h, make_layout(n, tile, elem, 8, tc_split_of(prec, tile) > 0).total);
 }
 
 int avs_svdvals_s(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const float *A, float *sigma,

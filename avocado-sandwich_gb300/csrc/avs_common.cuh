@@ -90,7 +90,15 @@ struct Stage1Work {
     int *flags;       // ticket (1) + progress (nt) + err (1), reset per launch
     int *err;         // device status word (shared with other stages)
     void *tfull;      // [nt][b*b] of T: full compact-WY factors (tiles 128, 256)
+    float *tc_S = nullptr;  // tensor-core update scratch: [nt][b*n] each (FP32 tiles)
+    float *tc_W = nullptr;
+    int tc_split = 0;       // 0: SIMT update; 1: TF32; 3: split TF32
 };
+template <typename T>
+int stage1_tbuild(const T *dA, int64_t lda, int b, int layout, int pr, int pc, int P, const void *tblk, void *tfull,
+                  cudaStream_t s);
+int stage1_update_tc(float *a, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const float *tfull,
+                     float *S, float *Wb, int split, int *err, cudaStream_t s);
 
 template <typename T>
 int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const void *tblk,
@@ -121,6 +129,10 @@ int stage2_chase(double *dAB, int64_t n, int bw, int64_t ldab, double *dd, doubl
 template <typename T>
 int stage2_chase_df(const T *dW, int64_t n, int64_t ldw, int bw, float2 *dAB, int64_t ldab, double *dd, double *de,
                     const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
+namespace tc {
+struct GemmArgs;
+}
+int tc_gemm(const tc::GemmArgs &a, int batch, cudaStream_t s);
 int bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *dsigma, double rel_tol,
                          cudaStream_t s);
 int stage3_bisect_df(const double *dd, const double *de, int64_t n, double rel_tol, double *dsigma, double *dscratch,

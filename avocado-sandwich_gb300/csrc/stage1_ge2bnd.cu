@@ -39,6 +39,7 @@
 #include <cstdio>
 
 #include "avs_common.cuh"
+#include "df64.cuh"
 
 namespace avs {
 namespace {
@@ -350,6 +351,415 @@ __global__ void __launch_bounds__(kNT) panel_kernel(PanelArgs args) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Panel kernel, warp-synchronous reflector generation.
+//
+// Same roles, systolic schedule, outputs (V in place, tau, 16 x 16 T blocks)
+// and arithmetic as panel_kernel, restructured for latency: warp 0 generates
+// the 16 reflectors of a block with warp-level synchronisation only; the
+// reflector scalars use the closed forms of the reference's expressions
+// (n1 = ||x||, nu = alpha + sign(alpha) n1, tau = 2 nu^2 / (s + nu^2) = |nu| / n1,
+// tau / nu = sign(nu) / n1, tau / nu^2 = 1 / (n1 |nu|)) evaluated in FP64 for
+// FP64 tiles and in double-float for FP32 tiles (GB300 issues FP64 at 1/64 of
+// the FP32 rate); the block's Gram matrix uses the whole CTA; the apply to the
+// rest of the tile runs four threads per column with the column in registers.
+
+// Reflector scalars from s = sum of squares of the sub-column (as a pair) and
+// alpha.  Writes nu, tau, tau/nu, tau/nu^2, 1/nu, beta (the new diagonal).
+struct PScalars {
+    double nu, tau, tc, f, inv, beta;
+};
+
+__device__ __forceinline__ PScalars pscal_double(double s, double alpha) {
+    PScalars r;
+    const double n1 = sqrt(s + alpha * alpha);
+    const double sg = alpha < 0.0 ? -1.0 : 1.0;
+    r.nu = alpha + sg * n1;
+    if (r.nu == 0.0) {
+        r.tau = r.tc = r.f = r.inv = 0.0;
+        r.beta = alpha;
+        return r;
+    }
+    const double rn1 = 1.0 / n1;
+    const double anu = fabs(r.nu);
+    r.tau = anu * rn1;
+    r.tc = (r.nu < 0.0 ? -rn1 : rn1);
+    r.inv = 1.0 / r.nu;
+    r.f = rn1 * fabs(r.inv);
+    r.beta = -sg * n1;
+    return r;
+}
+
+// FP32 tiles: the same closed forms in double-float, rounded to FP32 at the
+// end -- no FP64 instruction (GB300 runs those at 1/64 of the FP32 rate).
+struct PScalarsF {
+    float nu, tau, tc, f, inv, beta;
+};
+
+__device__ __forceinline__ PScalarsF pscal_float(df64 s, float alpha) {
+    PScalarsF r;
+    const df64 a = df64{alpha, 0.0f};
+    const df64 n1 = df_sqrt(df_add(s, two_prod(alpha, alpha)));
+    const bool neg = alpha < 0.0f;
+    const df64 nu = neg ? df_sub(a, n1) : df_add(a, n1);
+    r.nu = nu.hi + nu.lo;
+    if (nu.hi == 0.0f) {
+        r.tau = r.tc = r.f = r.inv = 0.0f;
+        r.beta = alpha;
+        return r;
+    }
+    const df64 rn1 = df_rcp(n1);
+    const df64 anu = nu.hi < 0.0f ? df_neg(nu) : nu;
+    const df64 inv = df_rcp(nu);
+    const df64 tau = df_mul(anu, rn1);
+    const df64 f = df_mul(rn1, inv.hi < 0.0f ? df_neg(inv) : inv);
+    r.tau = tau.hi + tau.lo;
+    r.tc = nu.hi < 0.0f ? -(rn1.hi + rn1.lo) : (rn1.hi + rn1.lo);
+    r.inv = inv.hi + inv.lo;
+    r.f = f.hi + f.lo;
+    r.beta = neg ? (n1.hi + n1.lo) : -(n1.hi + n1.lo);
+    return r;
+}
+
+template <typename T>
+struct PScal;
+template <>
+struct PScal<double> {
+    using Acc = double;
+    static __device__ __forceinline__ Acc zero() { return 0.0; }
+    static __device__ __forceinline__ Acc sq(double x, Acc a) { return fma(x, x, a); }
+    static __device__ __forceinline__ Acc shfl_add(Acc a, int o) { return a + __shfl_xor_sync(0xffffffffu, a, o); }
+    static __device__ __forceinline__ void compute(Acc s, double alpha, double *out) {
+        const PScalars r = pscal_double(s, alpha);
+        out[0] = r.nu; out[1] = r.tc; out[2] = r.f; out[3] = r.inv; out[4] = r.beta; out[5] = r.tau;
+    }
+};
+template <>
+struct PScal<float> {
+    using Acc = df64;
+    static __device__ __forceinline__ Acc zero() { return df64{0.0f, 0.0f}; }
+    static __device__ __forceinline__ Acc sq(float x, Acc a) { return df_add(a, two_prod(x, x)); }
+    static __device__ __forceinline__ Acc shfl_add(Acc a, int o) {
+        return df_add(a, df64{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)});
+    }
+    static __device__ __forceinline__ void compute(Acc s, float alpha, float *out) {
+        const PScalarsF r = pscal_float(s, alpha);
+        out[0] = r.nu; out[1] = r.tc; out[2] = r.f; out[3] = r.inv; out[4] = r.beta; out[5] = r.tau;
+    }
+};
+
+__device__ __forceinline__ PScalars pscal_df(df64 s, float alpha) {
+    PScalars r;
+    const df64 a = df64{alpha, 0.0f};
+    const df64 n1 = df_sqrt(df_add(s, two_prod(alpha, alpha)));
+    const bool neg = alpha < 0.0f;
+    const df64 nu = neg ? df_sub(a, n1) : df_add(a, n1);
+    r.nu = df_to_double(nu);
+    if (nu.hi == 0.0f) {
+        r.tau = r.tc = r.f = r.inv = 0.0;
+        r.beta = alpha;
+        return r;
+    }
+    const df64 rn1 = df_rcp(n1);
+    const df64 anu = nu.hi < 0.0f ? df_neg(nu) : nu;
+    const df64 inv = df_rcp(nu);
+    r.tau = df_to_double(df_mul(anu, rn1));
+    r.tc = df_to_double(nu.hi < 0.0f ? df_neg(rn1) : rn1);
+    r.inv = df_to_double(inv);
+    r.f = df_to_double(df_mul(rn1, inv.hi < 0.0f ? df_neg(inv) : inv));
+    r.beta = df_to_double(neg ? n1 : df_neg(n1));
+    return r;
+}
+
+template <typename T>
+size_t panel2_smem_bytes(int b) {
+    return sizeof(T) * 32 /* tau, scalars */ +
+           sizeof(T) * ((size_t)ldpad(b) * kIB /* X */ + (size_t)kIB * b /* Rt */ + 2 * kIB * kIB /* Tm, G */ +
+                        (size_t)kIB * 33 /* red */ + 2 * kIB /* dsum, wbuf */);
+}
+
+template <typename T, int LAYOUT>
+__global__ void __launch_bounds__(kNT) panel2_kernel(PanelArgs args) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int b = args.b;
+    const int nb = b / kIB;
+    const int ldx = ldpad(b);
+    T *stau = reinterpret_cast<T *>(smem_raw);             // kIB
+    T *scal = stau + kIB;                                  // 16
+    T *X = scal + 16;                                      // ldx * kIB
+    T *Rt = X + (size_t)ldx * kIB;                         // kIB * b, Rt[l + j*kIB]
+    T *Tm = Rt + (size_t)kIB * b;                          // kIB * kIB, Tm[l + i*kIB]
+    T *G = Tm + kIB * kIB;                                 // kIB * kIB, G[l + i*kIB]
+    T *red = G + kIB * kIB;                                // kIB * 33
+    T *dsum = red + kIB * 33;                              // kIB
+    T *wbuf = dsum + kIB;                                  // kIB
+
+    __shared__ int s_role, s_ok;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) s_role = atomicAdd(args.ticket, 1) + args.first_role;
+    __syncthreads();
+    const int p = s_role;
+    if (p >= args.P) return;
+
+    View<T, LAYOUT> V{reinterpret_cast<T *>(args.a), args.lda};
+    const int64_t row0 = (int64_t)(args.pr + p) * b;
+    const int64_t top0 = (int64_t)args.pr * b;
+    const int64_t col0 = (int64_t)args.pc * b;
+    const bool geqrt = (p == 0);
+    T *tau_out = reinterpret_cast<T *>(args.tau) + (size_t)p * b;
+    T *tblk_out = reinterpret_cast<T *>(args.tblk) + (size_t)p * nb * kIB * kIB;
+    const int R = (b + 31) / 32;  // rows per lane in the reflector loop
+    const int RQ = b / 4;         // rows per thread in the apply
+
+    for (int cb = 0; cb < nb; ++cb) {
+        const int c0 = cb * kIB;
+        if (tid == 0) {
+            bool ok = true;
+            if (p > args.first_role) ok = wait_geq(args.progress + p - 1, cb + 1, args.err);
+            s_ok = ok;
+        }
+        __syncthreads();
+        if (!s_ok) return;
+        for (int idx = tid; idx < b * kIB; idx += kNT) {
+            int t, l;
+            if (LAYOUT == 0) { t = idx % b; l = idx / b; } else { l = idx % kIB; t = idx / kIB; }
+            X[t + l * ldx] = __ldcg(&V(row0 + t, col0 + c0 + l));
+        }
+        if (!geqrt) {
+            const int ncols = b - c0;
+            for (int idx = tid; idx < kIB * ncols; idx += kNT) {
+                int l, j;
+                if (LAYOUT == 0) { l = idx % kIB; j = idx / kIB; } else { j = idx % ncols; l = idx / ncols; }
+                Rt[l + (c0 + j) * kIB] = __ldcg(&V(top0 + c0 + l, col0 + c0 + j));
+            }
+        }
+        __syncthreads();
+
+        // ---- warp 0: the 16 reflectors of the block
+        if (wid == 0) {
+            for (int i = 0; i < kIB; ++i) {
+                const int c = c0 + i;
+                if (geqrt && c == b - 1) {  // the reference's GEQRT loops iter = 1:N-1
+                    if (lane == 0) stau[i] = T(0);
+                    __syncwarp();
+                    continue;
+                }
+                T xr[8];
+                T dp[kIB];
+#pragma unroll
+                for (int jj = 0; jj < kIB; ++jj) dp[jj] = T(0);
+                typename PScal<T>::Acc sq = PScal<T>::zero();
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    xr[r] = T(0);
+                    if (r < R) {
+                        const int t = lane + 32 * r;
+                        const bool live = (t < b) && (geqrt ? (t > c) : true);
+                        if (live) {
+                            const T x = X[t + i * ldx];
+                            xr[r] = x;
+                            sq = PScal<T>::sq(x, sq);
+#pragma unroll
+                            for (int jj = 0; jj < kIB; ++jj)
+                                if (jj > i) dp[jj] += x * X[t + jj * ldx];
+                        }
+                    }
+                }
+#pragma unroll
+                for (int jj = 0; jj < kIB; ++jj) red[jj * 33 + lane] = dp[jj];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) sq = PScal<T>::shfl_add(sq, o);
+                __syncwarp();
+                if (lane < kIB && lane > i) {
+                    T acc = T(0);
+#pragma unroll 8
+                    for (int q = 0; q < 32; ++q) acc += red[lane * 33 + q];
+                    dsum[lane] = acc;
+                }
+                if (lane == 0) {
+                    const T alpha = geqrt ? X[c + i * ldx] : Rt[i + c * kIB];
+                    T out[6];
+                    PScal<T>::compute(sq, alpha, out);
+                    if (!isfinite(out[5]) || !isfinite(out[0])) {
+                        atomicCAS(args.err, kDevOk, kDevNonfinite);
+                        out[5] = out[1] = out[2] = out[3] = T(0);
+                        out[4] = alpha;
+                    }
+                    stau[i] = out[5];
+                    scal[0] = out[0];
+                    scal[1] = out[1];
+                    scal[2] = out[2];
+                    scal[3] = out[3];
+                    scal[4] = out[4];
+                }
+                __syncwarp();
+                if (stau[i] == T(0)) {
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) {
+                        const int t = lane + 32 * r;
+                        if (r < R && t < b && (geqrt ? (t > c) : true)) X[t + i * ldx] = T(0);
+                    }
+                    __syncwarp();
+                    continue;
+                }
+                const T nu = scal[0], tc = scal[1], f = scal[2], inv = scal[3];
+                if (lane < kIB && lane > i) {
+                    const T rv = geqrt ? X[c + lane * ldx] : Rt[i + (c0 + lane) * kIB];
+                    const T w = nu * rv + dsum[lane];
+                    wbuf[lane] = w;
+                    if (geqrt) X[c + lane * ldx] = rv - tc * w;
+                    else Rt[i + (c0 + lane) * kIB] = rv - tc * w;
+                }
+                if (lane == 0) {
+                    if (geqrt) X[c + i * ldx] = scal[4];
+                    else Rt[i + c * kIB] = scal[4];
+                }
+                __syncwarp();
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const int t = lane + 32 * r;
+                    if (r < R && t < b && (geqrt ? (t > c) : true)) {
+                        const T x = xr[r];
+#pragma unroll
+                        for (int jj = 0; jj < kIB; ++jj)
+                            if (jj > i) X[t + jj * ldx] -= x * (f * wbuf[jj]);
+                        X[t + i * ldx] = x * inv;
+                    }
+                }
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+
+        // ---- Gram matrix of the block's reflectors (whole CTA), then T (warp 0)
+        {
+            const int pi = tid >> 1, h = tid & 1;
+            int l = -1, i = 0;
+            if (pi < kIB * (kIB - 1) / 2) {
+                int acc = 0;
+                for (int ii = 1; ii < kIB; ++ii) {
+                    if (pi < acc + ii) { i = ii; l = pi - acc; break; }
+                    acc += ii;
+                }
+            }
+            T part = T(0);
+            if (l >= 0) {
+                const int half = (b + 1) / 2;
+                const int tlo = h * half, thi = min(b, tlo + half);
+                for (int t = tlo; t < thi; ++t)
+                    if (geqrt ? (t > c0 + i) : true) part += X[t + l * ldx] * X[t + i * ldx];
+            }
+            part += __shfl_xor_sync(0xffffffffu, part, 1);
+            if (l >= 0 && h == 0) G[l + i * kIB] = part + (geqrt ? X[c0 + i + l * ldx] : T(0));
+        }
+        if (tid < kIB * kIB) Tm[tid] = T(0);
+        __syncthreads();
+        if (wid == 0) {
+            if (lane < kIB) Tm[lane + lane * kIB] = stau[lane];
+            __syncwarp();
+            for (int i = 1; i < kIB; ++i) {
+                if (lane < i) {
+                    T acc = T(0);
+                    for (int m = lane; m < i; ++m) acc += Tm[lane + m * kIB] * G[m + i * kIB];
+                    Tm[lane + i * kIB] = -stau[i] * acc;
+                }
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+
+        // ---- write V, tau, T
+        for (int idx = tid; idx < b * kIB; idx += kNT) {
+            int t, l;
+            if (LAYOUT == 0) { t = idx % b; l = idx / b; } else { l = idx % kIB; t = idx / kIB; }
+            if (!geqrt || t >= c0) V(row0 + t, col0 + c0 + l) = X[t + l * ldx];
+        }
+        if (tid < kIB) tau_out[c0 + tid] = stau[tid];
+        if (tid < kIB * kIB) tblk_out[(size_t)cb * kIB * kIB + tid] = Tm[tid];
+
+        // ---- apply the block to the rest of the tile: 4 threads per column
+        const int nrest = b - c0 - kIB;
+        const int quad = tid >> 2, qq = tid & 3;
+        for (int base = 0; base < nrest; base += kNT / 4) {
+            const int jrel = base + quad;
+            const bool cv = jrel < nrest;
+            const int j = c0 + kIB + (cv ? jrel : 0);
+            T cr[64];
+            T z[kIB];
+#pragma unroll
+            for (int l = 0; l < kIB; ++l) z[l] = T(0);
+#pragma unroll
+            for (int r = 0; r < 64; ++r) {
+                cr[r] = T(0);
+                if (r < RQ) {
+                    const int t = qq * RQ + r;
+                    if (cv && (!geqrt || t >= c0)) {
+                        const T cval = __ldcg(&V(row0 + t, col0 + j));
+                        cr[r] = cval;
+#pragma unroll
+                        for (int l = 0; l < kIB; ++l) {
+                            T y;
+                            if (geqrt) y = (t == c0 + l) ? T(1) : (t > c0 + l ? X[t + l * ldx] : T(0));
+                            else y = X[t + l * ldx];
+                            z[l] += y * cval;
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int l = 0; l < kIB; ++l) {
+                z[l] += __shfl_xor_sync(0xffffffffu, z[l], 1);
+                z[l] += __shfl_xor_sync(0xffffffffu, z[l], 2);
+                if (!geqrt && cv) z[l] += Rt[l + j * kIB];
+            }
+            T w[kIB];
+#pragma unroll
+            for (int l = 0; l < kIB; ++l) {
+                T acc = T(0);
+#pragma unroll
+                for (int m = 0; m <= l; ++m) acc += Tm[m + l * kIB] * z[m];
+                w[l] = acc;
+            }
+            if (!geqrt && cv) {
+#pragma unroll
+                for (int l = 0; l < kIB; ++l)
+                    if ((l >> 2) == qq) Rt[l + j * kIB] -= w[l];
+            }
+#pragma unroll
+            for (int r = 0; r < 64; ++r) {
+                if (r < RQ) {
+                    const int t = qq * RQ + r;
+                    if (cv && (!geqrt || t >= c0)) {
+                        T acc = cr[r];
+#pragma unroll
+                        for (int l = 0; l < kIB; ++l) {
+                            T y;
+                            if (geqrt) y = (t == c0 + l) ? T(1) : (t > c0 + l ? X[t + l * ldx] : T(0));
+                            else y = X[t + l * ldx];
+                            acc -= y * w[l];
+                        }
+                        V(row0 + t, col0 + j) = acc;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (!geqrt) {
+            const int ncols = b - c0;
+            for (int idx = tid; idx < kIB * ncols; idx += kNT) {
+                int l, jx;
+                if (LAYOUT == 0) { l = idx % kIB; jx = idx / kIB; } else { jx = idx % ncols; l = idx / ncols; }
+                V(top0 + c0 + l, col0 + c0 + jx) = Rt[l + (c0 + jx) * kIB];
+            }
+        }
+        __syncthreads();
+        if (tid == 0) {
+            __threadfence();
+            st_release(args.progress + p, cb + 1);
+        }
+    }
+}
+
 template <typename T>
 size_t update_smem_bytes(int b, int width) {
     return sizeof(T) * ((size_t)2 * ldpad(b) * width + (size_t)ldpad(b) * kIB + 2 * (size_t)kIB * width +
@@ -470,10 +880,10 @@ template <typename T, int LAYOUT>
 int launch_panel(T *dA, int64_t lda, int b, int pr, int pc, int P, int first_role, const Stage1Work &w,
                  cudaStream_t s) {
     static bool attr_set = false;
-    const size_t smem = panel_smem_bytes<T>(b);
+    const size_t smem = panel2_smem_bytes<T>(b);
     if (!attr_set) {
-        AVS_CUDA_TRY(cudaFuncSetAttribute(panel_kernel<T, LAYOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)panel_smem_bytes<T>(256)));
+        AVS_CUDA_TRY(cudaFuncSetAttribute(panel2_kernel<T, LAYOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)panel2_smem_bytes<T>(256)));
         attr_set = true;
     }
     AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(P + 1), s));
@@ -490,7 +900,7 @@ int launch_panel(T *dA, int64_t lda, int b, int pr, int pc, int P, int first_rol
     a.ticket = w.flags;
     a.progress = w.flags + 1;
     a.err = w.err;
-    panel_kernel<T, LAYOUT><<<P - first_role, kNT, smem, s>>>(a);
+    panel2_kernel<T, LAYOUT><<<P - first_role, kNT, smem, s>>>(a);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
 }
@@ -523,6 +933,21 @@ int launch_update(T *dA, int64_t lda, int64_t n, int b, int pr, int pc, int P, c
     return AVS_SUCCESS;
 }
 
+// Tensor-core trailing update: T build (shared with the SIMT path) + the
+// tcgen05 GEMM sequence.
+template <typename T>
+int update_tc_half(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const Stage1Work &w,
+                   cudaStream_t s) {
+    if constexpr (sizeof(T) != 4) {
+        return AVS_ERR_INTERNAL;
+    } else {
+        int rc = stage1_tbuild<T>(dA, lda, b, layout, pr, pc, P, w.tblk, w.tfull, s);
+        if (rc != AVS_SUCCESS) return rc;
+        return stage1_update_tc(reinterpret_cast<float *>(dA), lda, n, b, layout, pr, pc, P,
+                                reinterpret_cast<const float *>(w.tfull), w.tc_S, w.tc_W, w.tc_split, w.err, s);
+    }
+}
+
 }  // namespace
 
 template <typename T>
@@ -533,7 +958,9 @@ int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cud
         // QR half-step: GEQRT(k,k) + TSQRT(row,k), Q^T applied to the row panels.
         const int P = nt - k;
         if ((rc = launch_panel<T, 0>(dA, lda, b, k, k, P, 0, w, s)) != AVS_SUCCESS) return rc;
-        if (b >= 128 && w.tfull)
+        if (b >= 128 && w.tfull && w.tc_split && sizeof(T) == 4)
+            rc = update_tc_half<T>(dA, lda, n, b, 0, k, k, P, w, s);
+        else if (b >= 128 && w.tfull)
             rc = stage1_update_full<T>(dA, lda, n, b, 0, k, k, P, w.tblk, w.tfull, s);
         else
             rc = launch_update<T, 0>(dA, lda, n, b, k, k, P, w, s);
@@ -543,7 +970,9 @@ int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cud
         // LQ half-step: the same on the transposed view, top tile (k, k+1).
         const int PL = nt - k - 1;
         if ((rc = launch_panel<T, 1>(dA, lda, b, k + 1, k, PL, 0, w, s)) != AVS_SUCCESS) return rc;
-        if (b >= 128 && w.tfull)
+        if (b >= 128 && w.tfull && w.tc_split && sizeof(T) == 4)
+            rc = update_tc_half<T>(dA, lda, n, b, 1, k + 1, k, PL, w, s);
+        else if (b >= 128 && w.tfull)
             rc = stage1_update_full<T>(dA, lda, n, b, 1, k + 1, k, PL, w.tblk, w.tfull, s);
         else
             rc = launch_update<T, 1>(dA, lda, n, b, k + 1, k, PL, w, s);

@@ -412,6 +412,18 @@ int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const 
 
 }  // namespace
 
+// T build alone (for the tensor-core update path).
+template <typename T>
+int stage1_tbuild(const T *dA, int64_t lda, int b, int layout, int pr, int pc, int P, const void *tblk, void *tfull,
+                  cudaStream_t s) {
+    return layout == 0 ? launch_tbuild<T, 0>(dA, lda, b, pr, pc, P, tblk, tfull, s)
+                       : launch_tbuild<T, 1>(dA, lda, b, pr, pc, P, tblk, tfull, s);
+}
+template int stage1_tbuild<float>(const float *, int64_t, int, int, int, int, int, const void *, void *,
+                                  cudaStream_t);
+template int stage1_tbuild<double>(const double *, int64_t, int, int, int, int, int, const void *, void *,
+                                   cudaStream_t);
+
 // Full-T trailing update of one half-step (tiles 128 and 256).
 template <typename T>
 int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const void *tblk,

@@ -281,22 +281,24 @@ __device__ __forceinline__ void cluster_reflector(typename ChaseAr<S>::V *sv, in
     using V = typename Ar::V;
     V part = Ar::zero();
     for (int i = 1 + threadIdx.x; i < L; i += blockDim.x) part = Ar::fma(sv[i], sv[i], part);
-    const V s = block_sum_s<S>(part, red);
-    const V alpha = sv[0];
-    V tau = Ar::zero(), beta = alpha, scal = Ar::zero();
-    if (Ar::gt0(s)) {
-        const V nrm = Ar::sqrt(Ar::fma(alpha, alpha, s));
-        beta = Ar::ge0(alpha) ? Ar::neg(nrm) : nrm;
-        tau = Ar::div(Ar::sub(beta, alpha), beta);
-        scal = Ar::div(Ar::one(), Ar::sub(alpha, beta));
-    }
-    __syncthreads();  // every thread has read alpha = sv[0]
-    for (int i = 1 + threadIdx.x; i < L; i += blockDim.x) sv[i] = Ar::mul(sv[i], scal);
-    if (threadIdx.x == 0) {
-        sv[0] = Ar::one();
+    const V s = block_sum_s<S>(part, red);  // ends with a barrier; red[1] is free
+    if (threadIdx.x == 0) {  // one thread forms the scalars (sqrt and divisions are costly)
+        const V alpha = sv[0];
+        V tau = Ar::zero(), beta = alpha, scal = Ar::zero();
+        if (Ar::gt0(s)) {
+            const V nrm = Ar::sqrt(Ar::fma(alpha, alpha, s));
+            beta = Ar::ge0(alpha) ? Ar::neg(nrm) : nrm;
+            tau = Ar::div(Ar::sub(beta, alpha), beta);
+            scal = Ar::div(Ar::one(), Ar::sub(alpha, beta));
+        }
+        red[1] = scal;
         *s_tau = tau;
         *s_beta = beta;
+        sv[0] = Ar::one();
     }
+    __syncthreads();
+    const V scal = red[1];
+    for (int i = 1 + threadIdx.x; i < L; i += blockDim.x) sv[i] = Ar::mul(sv[i], scal);
     __syncthreads();
 }
 
@@ -330,12 +332,24 @@ __global__ void __launch_bounds__(512) chase_cluster_kernel(typename ChaseAr<S>:
             const int64_t c1 = min(c0 + BW - 1, n - 1);
             const int L = (int)(c1 - c0 + 1);
             // ================= R op (op 2m) =================
-            if (tid == 0 && j > 0) wait_geq(done + j - 1, min(2 * m + 4, ops_prev), err);
-            __syncthreads();
+            // The reflector's input (row rho, columns c0..c1) is final once this
+            // sweep's previous op and op 2m of sweep j-1 are done -- already
+            // waited for when m >= 1 -- so it is formed before the wait for the
+            // block (op 2m+3 of sweep j-1); for m == 0 the wait comes first.
+            if (m == 0) {
+                if (tid == 0 && j > 0) wait_geq(done + j - 1, min(4, ops_prev), err);
+                __syncthreads();
+            }
             if (L >= 2) {
                 for (int i = tid; i < L; i += blockDim.x) sv[i] = Ar::ld(A.at(rho, c0 + i));
                 __syncthreads();
                 cluster_reflector<S>(sv, L, red, &s_tau, &s_beta);
+            }
+            if (m > 0) {
+                if (tid == 0 && j > 0) wait_geq(done + j - 1, min(2 * m + 4, ops_prev), err);
+                __syncthreads();
+            }
+            if (L >= 2) {
                 const V tau = s_tau;
                 if (!Ar::iszero(tau)) {
                     const int rr = tid % Cfg::RPC, g = tid / Cfg::RPC;
@@ -376,12 +390,16 @@ __global__ void __launch_bounds__(512) chase_cluster_kernel(typename ChaseAr<S>:
             cluster.sync();
             if (q == 0 && tid == 0) st_release(done + j, 2 * m + 1);
             // ================= L op (op 2m+1) =================
-            if (tid == 0 && j > 0) wait_geq(done + j - 1, min(2 * m + 5, ops_prev), err);
-            __syncthreads();
+            // Column c0 (rows c0..c1) is final after this sweep's R op and op
+            // 2m+1 of sweep j-1 (covered by the R op's wait): reflector first.
             if (L >= 2) {
                 for (int i = tid; i < L; i += blockDim.x) sv[i] = Ar::ld(A.at(c0 + i, c0));
                 __syncthreads();
                 cluster_reflector<S>(sv, L, red, &s_tau, &s_beta);
+            }
+            if (tid == 0 && j > 0) wait_geq(done + j - 1, min(2 * m + 5, ops_prev), err);
+            __syncthreads();
+            if (L >= 2) {
                 const V tau = s_tau;
                 if (!Ar::iszero(tau)) {
                     const int64_t cend = min(c0 + 2 * (int64_t)BW - 1, n - 1);
@@ -480,9 +498,13 @@ __global__ void extract_band_df_kernel(const T *a, int64_t n, int64_t lda, int b
     for (int i = threadIdx.x; i <= bw; i += blockDim.x) {
         const int64_t r = c - bw + i;
         if (r >= 0) {
-            const double v = (double)a[r + c * lda];
-            const float h = (float)v;
-            ab[(ku + r - c) + c * ldab] = make_float2(h, (float)(v - (double)h));
+            if (sizeof(T) == 4) {
+                ab[(ku + r - c) + c * ldab] = make_float2((float)a[r + c * lda], 0.0f);  // exact
+            } else {
+                const double v = (double)a[r + c * lda];
+                const float h = (float)v;
+                ab[(ku + r - c) + c * ldab] = make_float2(h, (float)(v - (double)h));
+            }
         }
     }
 }

@@ -198,3 +198,21 @@ def test_double_float_stages_match_fp64_stages(avs_mod, torch_cuda, n, b):
     s32_df = avs_mod.my_CU_svdval(a32, b)
     assert rel_err(s32_df, s32_64) < 1e-9
     assert rel_err(s32_df, sig) < 1e-5
+
+
+@pytest.mark.parametrize("n,b", [(512, 128), (1024, 128), (1024, 256), (2048, 256)])
+def test_tensor_core_modes(avs_mod, torch_cuda, n, b):
+    """Trailing updates on tcgen05: split TF32 (3 products) keeps FP32-class
+    accuracy (<= 1e-5 of sigma_max against LAPACK); single-pass TF32 states
+    its larger error."""
+    from avs import workloads
+    a = workloads.gaussian(n, 31, 1.0 / np.sqrt(n), dtype=np.float32)
+    lap = sl.svdvals(a.astype(np.float64))
+    r = avs_mod.Report()
+    s3 = avs_mod.my_CU_svdval(a, b, precision="tf32x3", report=r)
+    assert r.precision == 4
+    assert rel_err(s3, lap) < 1e-5
+    s32 = avs_mod.my_CU_svdval(a, b, precision="fp32")
+    assert rel_err(s3, s32) < 1e-5
+    s1 = avs_mod.my_CU_svdval(a, b, precision="tf32")
+    assert rel_err(s1, lap) < 5e-3
