@@ -31,7 +31,7 @@ import numpy as np
 __all__ = [
     "AvsError", "Handle", "lib", "library_path", "my_CU_svdval", "svdvals", "Blockbidiag", "extract_band",
     "bidiagonalize", "diag_lapack", "geqrt_tile", "tsqrt_tile", "to_device", "from_device", "PREC",
-    "NOT_IMPLEMENTED", "EXPORTED_SYMBOLS", "Report",
+    "NOT_IMPLEMENTED", "EXPORTED_SYMBOLS", "Report", "svdvals_batched", "autotune_tile",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -47,6 +47,7 @@ EXPORTED_SYMBOLS = [
     "avs_blockbidiag_dev_s", "avs_blockbidiag_dev_d", "avs_extract_band_dev_s", "avs_extract_band_dev_d",
     "avs_band_to_bidiag_dev", "avs_bidiag_svals_dev", "avs_bidiag_svals_noalloc",
     "avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d", "avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d",
+    "avs_svdvals_batched_dev_s", "avs_autotune_tile",
 ]
 
 
@@ -101,6 +102,8 @@ def lib():
         L.avs_band_to_bidiag_dev.argtypes = [P, I64, I32, P, I64, P, P, RP]
         L.avs_bidiag_svals_dev.argtypes = [P, I64, P, P, P, ctypes.c_double, RP]
         L.avs_bidiag_svals_noalloc.argtypes = [I64, P, P, P, ctypes.c_double, P]
+        L.avs_svdvals_batched_dev_s.argtypes = [P, I32, P, P, P, P, P, OP, RP]
+        L.avs_autotune_tile.argtypes = [P, I64, I32, ctypes.POINTER(ctypes.c_int32)]
         for nm in ("avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d"):
             getattr(L, nm).argtypes = [P, I32, P, P]
         for nm in ("avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d"):
@@ -224,6 +227,62 @@ def my_CU_svdval(A, block_size, precision=None, report=None, handle=None, rel_to
 
 
 svdvals = my_CU_svdval
+
+
+def svdvals_batched(mats, tiles=None, report=None, handle=None, rel_tol=0.0):
+    """Singular values of many independent square float32 matrices in one call.
+
+    ``mats`` is a list of CUDA torch tensors, each holding an n_i x n_i matrix
+    column-major (see ``to_device``); orders may differ.  ``tiles`` is None (the
+    autotuner picks a tile per order), an int for all, or a list.  Returns a
+    list of CUDA float32 tensors of n_i values each (descending).  This is the
+    batching client of the many-small-SVDs workload (RMT/rmt.jl:9-36), which the
+    reference serves one LAPACK call at a time.
+    """
+    import torch
+    h = handle or default_handle()
+    cnt = len(mats)
+    if cnt == 0:
+        return []
+    if isinstance(tiles, int):
+        tiles = [tiles] * cnt
+    n = (ctypes.c_int64 * cnt)()
+    ld = (ctypes.c_int64 * cnt)()
+    tt = (ctypes.c_int32 * cnt)()
+    pa = (ctypes.c_void_p * cnt)()
+    ps = (ctypes.c_void_p * cnt)()
+    outs = []
+    dev = None
+    for i, A in enumerate(mats):
+        if not _is_torch_cuda(A) or A.dim() != 2 or A.dtype != torch.float32:
+            raise TypeError("svdvals_batched takes 2-D float32 CUDA tensors")
+        if A.shape[0] != A.shape[1]:
+            raise NotImplementedError("Not implemented")
+        if A.stride(1) != 1:
+            A = A.contiguous()
+            mats[i] = A
+        dev = A.device
+        n[i] = A.shape[0]
+        ld[i] = max(A.stride(0), 1)
+        tt[i] = 0 if tiles is None else int(tiles[i])
+        pa[i] = A.data_ptr()
+        o = torch.empty(A.shape[0], dtype=torch.float32, device=A.device)
+        ps[i] = o.data_ptr()
+        outs.append(o)
+    opt = Opts(0, 0, float(rel_tol), ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    r = report if report is not None else Report()
+    rc = lib().avs_svdvals_batched_dev_s(h.ptr, cnt, n, ld, None if tiles is None else tt, pa, ps,
+                                         ctypes.byref(opt), ctypes.byref(r))
+    _check(rc, "avs_svdvals_batched_dev_s")
+    return outs
+
+
+def autotune_tile(n, sample=16, handle=None):
+    """Tile the batched path uses for order n (timed on the device, cached on the handle)."""
+    h = handle or default_handle()
+    best = ctypes.c_int32(0)
+    _check(lib().avs_autotune_tile(h.ptr, int(n), int(sample), ctypes.byref(best)), "avs_autotune_tile")
+    return best.value
 
 
 def Blockbidiag(A, tile, handle=None):

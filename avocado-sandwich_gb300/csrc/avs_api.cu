@@ -4,7 +4,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <new>
+#include <tuple>
+#include <vector>
 
 #include "avs_common.cuh"
 
@@ -23,6 +26,15 @@ struct avs_handle {
     size_t ws_bytes = 0;
     cudaEvent_t ev[6] = {};
     int *h_err = nullptr;  // pinned status word
+    // batched path: its own grow-only workspace, pinned pointer tables,
+    // captured graphs per group shape, autotuned tiles per order n
+    void *bws = nullptr;
+    size_t bws_bytes = 0;
+    void *pinned = nullptr;
+    size_t pinned_bytes = 0;
+    std::map<std::tuple<int64_t, int, int>, cudaGraphExec_t> graphs;
+    std::map<std::tuple<int64_t, int, int>, int64_t> graph_launches;  // kernels per graph
+    std::map<int64_t, int> tuned;
 };
 
 namespace {
@@ -369,6 +381,9 @@ int avs_destroy(avs_handle *h) {
     for (auto &e : h->ev)
         if (e) cudaEventDestroy(e);
     if (h->h_err) cudaFreeHost(h->h_err);
+    for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    if (h->bws) cudaFree(h->bws);
+    if (h->pinned) cudaFreeHost(h->pinned);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return AVS_SUCCESS;
@@ -620,3 +635,321 @@ int avs_tsqrt_tile_dev_d(avs_handle *h, int32_t b, double *dR, double *dB, doubl
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Batched singular values (many independent matrices of mixed orders).
+namespace {
+
+struct BatchLayout {
+    size_t err, W, tau, tblk, tfull, f1, ab, f2, d, e, sig, scr, pairs, ptrs, total;
+};
+
+BatchLayout batch_layout(int64_t n, int b, int cnt) {
+    BatchLayout L{};
+    const int64_t nt = n / b;
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o = align_up(o + bytes);
+        return at;
+    };
+    L.err = take(64);
+    L.W = take(sizeof(float) * (size_t)cnt * n * n);
+    L.tau = take(sizeof(float) * (size_t)cnt * (nt + 1) * b);
+    L.tblk = take(sizeof(float) * (size_t)cnt * (nt + 1) * (b / 16) * 256);
+    L.tfull = take(b >= 128 ? sizeof(float) * (size_t)cnt * (nt + 1) * b * b : 0);
+    L.f1 = take(sizeof(int) * (size_t)cnt * (nt + 4));
+    L.ab = take(sizeof(float2) * (size_t)cnt * 3 * b * n);
+    L.f2 = take(sizeof(int) * ((size_t)cnt * (n + 1) + 4));
+    L.d = take(sizeof(double) * (size_t)cnt * n);
+    L.e = take(sizeof(double) * (size_t)cnt * n);
+    L.sig = take(sizeof(double) * (size_t)cnt * n);
+    L.scr = take(sizeof(double) * (size_t)cnt * 4);
+    L.pairs = take(sizeof(float2) * (size_t)cnt * 2 * n);
+    L.ptrs = take(sizeof(void *) * 3 * (size_t)cnt + 64);
+    L.total = o + 256;
+    return L;
+}
+
+__global__ void gather_kernel(const float *const *src, const int64_t *lds, float *dst, int64_t n) {
+    const int64_t zb = blockIdx.y;
+    const float *a = src[zb];
+    const int64_t ld = lds[zb];
+    float *w = dst + zb * n * n;
+    for (int64_t c = blockIdx.x; c < n; c += gridDim.x)
+        for (int64_t r = threadIdx.x; r < n; r += blockDim.x) w[r + c * n] = a[r + c * ld];
+}
+
+__global__ void scatter_kernel(const double *sig, float *const *dst, int64_t n, int cnt) {
+    const int64_t total = n * (int64_t)cnt;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x)
+        dst[g / n][g % n] = (float)sig[g];
+}
+
+int ensure_bws(avs_handle *h, size_t bytes) {
+    if (h->bws_bytes >= bytes) return AVS_SUCCESS;
+    cudaStreamSynchronize(h->stream);
+    for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second);  // graphs hold old pointers
+    h->graphs.clear();
+    h->graph_launches.clear();
+    if (h->bws) cudaFree(h->bws);
+    h->bws = nullptr;
+    h->bws_bytes = 0;
+    cudaError_t e = cudaMalloc(&h->bws, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return AVS_ERR_OOM;
+    }
+    h->bws_bytes = bytes;
+    return AVS_SUCCESS;
+}
+
+int ensure_pinned(avs_handle *h, size_t bytes) {
+    if (h->pinned_bytes >= bytes) return AVS_SUCCESS;
+    cudaStreamSynchronize(h->stream);
+    if (h->pinned) cudaFreeHost(h->pinned);
+    h->pinned = nullptr;
+    h->pinned_bytes = 0;
+    AVS_CUDA_TRY(cudaMallocHost(&h->pinned, bytes));
+    h->pinned_bytes = bytes;
+    return AVS_SUCCESS;
+}
+
+// The launches of one group (gather .. scatter), captured once per shape.
+int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cnt, double tol, cudaStream_t s,
+                   int64_t *launches) {
+    char *base = reinterpret_cast<char *>(h->bws);
+    float *W = reinterpret_cast<float *>(base + L.W);
+    const float *const *src = reinterpret_cast<const float *const *>(base + L.ptrs);
+    float *const *dst = reinterpret_cast<float *const *>(base + L.ptrs + sizeof(void *) * cnt);
+    const int64_t *lds = reinterpret_cast<const int64_t *>(base + L.ptrs + 2 * sizeof(void *) * cnt);
+    int *err = reinterpret_cast<int *>(base + L.err);
+    const int64_t nt = n / b;
+    AVS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+    gather_kernel<<<dim3((unsigned)std::min<int64_t>(n, 1024), (unsigned)cnt), 256, 0, s>>>(src, lds, W, n);
+    AVS_CUDA_TRY(cudaGetLastError());
+    Stage1Work w1;
+    w1.tau = base + L.tau;
+    w1.tblk = base + L.tblk;
+    w1.tfull = b >= 128 ? base + L.tfull : nullptr;
+    w1.flags = reinterpret_cast<int *>(base + L.f1);
+    w1.err = err;
+    w1.batch = cnt;
+    w1.sA = n * n;
+    w1.sTau = (nt + 1) * b;
+    w1.sTblk = (nt + 1) * (b / 16) * 256;
+    w1.sTfull = (nt + 1) * (int64_t)b * b;
+    w1.sFlags = nt + 4;
+    int rc = stage1_ge2bnd<float>(W, n, n, b, w1, s, launches);
+    if (rc != AVS_SUCCESS) return rc;
+    Stage2Work w2;
+    w2.flags = reinterpret_cast<int *>(base + L.f2);
+    w2.err = err;
+    double *dd = reinterpret_cast<double *>(base + L.d);
+    double *de = reinterpret_cast<double *>(base + L.e);
+    rc = stage2_chase_df_batched(W, n, b, cnt, reinterpret_cast<float2 *>(base + L.ab), 3 * (int64_t)b, dd, de, w2, s,
+                                 h->num_sms, launches);
+    if (rc != AVS_SUCCESS) return rc;
+    double *sig = reinterpret_cast<double *>(base + L.sig);
+    rc = stage3_bisect_df_batched(dd, de, n, cnt, tol, sig, reinterpret_cast<double *>(base + L.scr),
+                                  reinterpret_cast<float2 *>(base + L.pairs), s, launches);
+    if (rc != AVS_SUCCESS) return rc;
+    scatter_kernel<<<(unsigned)std::min<int64_t>((n * cnt + 255) / 256, 8192), 256, 0, s>>>(sig, dst, n, cnt);
+    AVS_CUDA_TRY(cudaGetLastError());
+    if (launches) *launches += 2;
+    return AVS_SUCCESS;
+}
+
+// Seeded N(0,1)-like fill for the autotuner's sample matrices (sum of four
+// uniforms from a 32-bit integer hash; the distribution only needs to be generic).
+__global__ void fill_sample_kernel(float *a, int64_t count, uint32_t seed) {
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < count; g += (int64_t)gridDim.x * blockDim.x) {
+        float acc = 0.f;
+        for (uint32_t k = 0; k < 4; ++k) {
+            uint32_t x = (uint32_t)g * 4u + k + seed * 0x9E3779B9u;
+            x ^= x >> 16;
+            x *= 0x7feb352dU;
+            x ^= x >> 15;
+            x *= 0x846ca68bU;
+            x ^= x >> 16;
+            acc += (float)(x >> 8) * (1.0f / 16777216.0f);
+        }
+        a[g] = (acc - 2.0f) * 1.7320508f;
+    }
+}
+
+bool valid_tile(int64_t n, int t) { return is_pow2(t) && t >= 16 && t <= kMaxTile && n % t == 0 && t <= n; }
+
+}  // namespace
+
+extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
+                                         const int32_t *tile, const float *const *dA, float *const *dsigma,
+                                         const avs_opts *opts, avs_report *rep) {
+    if (rep) std::memset(rep, 0, sizeof(*rep));
+    if (!h) return -1;
+    if (count < 0) return -2;
+    if (count == 0) return AVS_SUCCESS;
+    if (!n) return -3;
+    if (!lda) return -4;
+    if (!dA) return -6;
+    if (!dsigma) return -7;
+    std::vector<int> tiles(count);
+    for (int i = 0; i < count; ++i) {
+        if (n[i] < 0) return -3;
+        if (lda[i] < (n[i] > 1 ? n[i] : 1)) return -4;
+        const int t = tile ? tile[i] : 0;
+        if (t != 0 && !valid_tile(n[i], t)) return (t > kMaxTile && is_pow2(t)) ? AVS_ERR_UNSUPPORTED
+                                                                                : AVS_ERR_NOT_IMPLEMENTED;
+        if (n[i] > 0 && (!dA[i] || !dsigma[i])) return dA[i] ? -7 : -6;
+        tiles[i] = t;
+    }
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    // tiles left to the autotuner
+    for (int i = 0; i < count; ++i) {
+        if (tiles[i] != 0 || n[i] == 0) continue;
+        auto it = h->tuned.find(n[i]);
+        if (it == h->tuned.end()) {
+            int rc = avs_autotune_tile(h, n[i], 16, nullptr);
+            if (rc != AVS_SUCCESS) return rc;
+            it = h->tuned.find(n[i]);
+        }
+        tiles[i] = it->second;
+    }
+    // groups of equal (n, tile)
+    std::map<std::pair<int64_t, int>, std::vector<int>> groups;
+    for (int i = 0; i < count; ++i)
+        if (n[i] > 0) groups[{n[i], tiles[i]}].push_back(i);
+    size_t need = 0;
+    size_t pin_need = sizeof(int) * 16 * (groups.size() + 1);
+    for (auto &g : groups) {
+        need = std::max(need, batch_layout(g.first.first, g.first.second, (int)g.second.size()).total);
+        pin_need += sizeof(void *) * 3 * g.second.size();
+    }
+    int rc;
+    if ((rc = ensure_bws(h, need)) != AVS_SUCCESS) return rc;
+    if ((rc = ensure_pinned(h, pin_need)) != AVS_SUCCESS) return rc;
+    cudaStream_t s = h->stream;  // graphs are captured and replayed on the handle's stream
+    if (opts && opts->stream) {  // order after the caller's work on its stream
+        AVS_CUDA_TRY(cudaEventRecord(h->ev[4], reinterpret_cast<cudaStream_t>(opts->stream)));
+        AVS_CUDA_TRY(cudaStreamWaitEvent(s, h->ev[4], 0));
+    }
+    const double tol = bisect_tol(false, opts);
+    // pinned layout: one status word per group (16 ints apart), then the pointer tables
+    int *h_status = reinterpret_cast<int *>(h->pinned);
+    void **tab = reinterpret_cast<void **>(h_status + 16 * (groups.size() + 1));
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
+    int64_t launches = 0;
+    size_t gi = 0;
+    for (auto &g : groups) {
+        const int64_t gn = g.first.first;
+        const int gb = g.first.second;
+        const int cnt = (int)g.second.size();
+        const BatchLayout L = batch_layout(gn, gb, cnt);
+        // pointer tables: sources, destinations, leading dimensions
+        for (int q = 0; q < cnt; ++q) {
+            tab[q] = const_cast<float *>(dA[g.second[q]]);
+            tab[cnt + q] = dsigma[g.second[q]];
+            reinterpret_cast<int64_t *>(tab + 2 * cnt)[q] = lda[g.second[q]];
+        }
+        AVS_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(h->bws) + L.ptrs, tab, sizeof(void *) * 3 * cnt,
+                                     cudaMemcpyHostToDevice, s));
+        const auto key = std::make_tuple(gn, gb, cnt);
+        auto it = h->graphs.find(key);
+        if (it == h->graphs.end()) {
+            cudaGraph_t graph;
+            AVS_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            int64_t l = 0;
+            rc = group_launches(h, L, gn, gb, cnt, tol, s, &l);
+            h->graph_launches[key] = l;
+            cudaError_t ce = cudaStreamEndCapture(s, &graph);
+            if (rc != AVS_SUCCESS) return rc;
+            AVS_CUDA_TRY(ce);
+            cudaGraphExec_t exec;
+            ce = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            AVS_CUDA_TRY(ce);
+            it = h->graphs.emplace(key, exec).first;
+        }
+        AVS_CUDA_TRY(cudaGraphLaunch(it->second, s));
+        launches += h->graph_launches[key];
+        AVS_CUDA_TRY(cudaMemcpyAsync(h_status + 16 * gi, reinterpret_cast<char *>(h->bws) + L.err, sizeof(int),
+                                     cudaMemcpyDeviceToHost, s));
+        tab += 3 * cnt;
+        ++gi;
+    }
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
+    {
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_last_cuda_error(e);
+            return AVS_ERR_CUDA;
+        }
+    }
+    rc = AVS_SUCCESS;
+    for (size_t q = 0; q < gi && rc == AVS_SUCCESS; ++q) {
+        const int dev_err = h_status[16 * q];
+        if (dev_err == kDevTimeout) rc = AVS_ERR_TIMEOUT;
+        else if (dev_err == kDevNonfinite) rc = AVS_ERR_NONFINITE;
+        else if (dev_err != kDevOk) rc = AVS_ERR_INTERNAL;
+    }
+    if (rep) {
+        rep->t_total_ms = ev_ms(h->ev[0], h->ev[1]);
+        rep->kernel_launches = launches;
+        rep->workspace_bytes = (int64_t)h->bws_bytes;
+        rep->precision = AVS_PREC_FP32;
+        rep->status = rc;
+    }
+    return rc;
+}
+
+// Autotuner: time each valid tile in {32, 64, 128} on `sample` seeded random
+// matrices of order n through the batched path; keep the fastest.
+extern "C" int avs_autotune_tile(avs_handle *h, int64_t n, int32_t sample, int32_t *best) {
+    if (!h) return -1;
+    if (n <= 0) return -2;
+    if (sample <= 0) sample = 16;
+    const int cands[3] = {32, 64, 128};
+    std::vector<int> valid;
+    for (int t : cands)
+        if (valid_tile(n, t) && n / t >= 2) valid.push_back(t);
+    if (valid.empty())
+        for (int t : {16, 32, 64, 128, 256})
+            if (valid_tile(n, t)) { valid.push_back(t); break; }
+    if (valid.empty()) return AVS_ERR_NOT_IMPLEMENTED;
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    float *A = nullptr, *S = nullptr;
+    AVS_CUDA_TRY(cudaMalloc(&A, sizeof(float) * (size_t)sample * n * n));
+    if (cudaMalloc(&S, sizeof(float) * (size_t)sample * n) != cudaSuccess) {
+        cudaFree(A);
+        return AVS_ERR_OOM;
+    }
+    fill_sample_kernel<<<1024, 256, 0, h->stream>>>(A, (int64_t)sample * n * n, 7u);
+    std::vector<const float *> pa(sample);
+    std::vector<float *> ps(sample);
+    std::vector<int64_t> nn(sample, n), ll(sample, n);
+    for (int i = 0; i < sample; ++i) {
+        pa[i] = A + (size_t)i * n * n;
+        ps[i] = S + (size_t)i * n;
+    }
+    int bt = valid[0];
+    float bestms = 1e30f;
+    int rc = AVS_SUCCESS;
+    for (int t : valid) {
+        std::vector<int32_t> tt(sample, t);
+        avs_report r;
+        for (int rep = 0; rep < 2 && rc == AVS_SUCCESS; ++rep)  // first call captures the graph
+            rc = avs_svdvals_batched_dev_s(h, sample, nn.data(), ll.data(), tt.data(), pa.data(), ps.data(), nullptr,
+                                           &r);
+        if (rc != AVS_SUCCESS) break;
+        if (r.t_total_ms < bestms) {
+            bestms = (float)r.t_total_ms;
+            bt = t;
+        }
+    }
+    cudaFree(A);
+    cudaFree(S);
+    if (rc != AVS_SUCCESS) return rc;
+    h->tuned[n] = bt;
+    if (best) *best = bt;
+    return AVS_SUCCESS;
+}

@@ -93,16 +93,20 @@ struct Stage1Work {
     float *tc_S = nullptr;  // tensor-core update scratch: [nt][b*n] each (FP32 tiles)
     float *tc_W = nullptr;
     int tc_split = 0;       // 0: SIMT update; 1: TF32; 3: split TF32
+    // batched mode: `batch` matrices at dA + z*sA, each with its own tau / T
+    // blocks / full T / flag block at the given strides (elements, ints)
+    int batch = 1;
+    int64_t sA = 0, sTau = 0, sTblk = 0, sTfull = 0, sFlags = 0;
 };
 template <typename T>
-int stage1_tbuild(const T *dA, int64_t lda, int b, int layout, int pr, int pc, int P, const void *tblk, void *tfull,
+int stage1_tbuild(const T *dA, int64_t lda, int b, int layout, int pr, int pc, int P, const Stage1Work &w,
                   cudaStream_t s);
 int stage1_update_tc(float *a, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const float *tfull,
                      float *S, float *Wb, int split, int *err, cudaStream_t s);
 
 template <typename T>
-int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const void *tblk,
-                       void *tfull, cudaStream_t s);
+int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const Stage1Work &w,
+                       cudaStream_t s);
 
 template <typename T>
 int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cudaStream_t s, int64_t *launches);
@@ -133,6 +137,10 @@ namespace tc {
 struct GemmArgs;
 }
 int tc_gemm(const tc::GemmArgs &a, int batch, cudaStream_t s);
+int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
+                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
+int stage3_bisect_df_batched(const double *dd, const double *de, int64_t n, int batch, double rel_tol,
+                             double *dsigma, double *dscratch, float2 *dpairs, cudaStream_t s, int64_t *launches);
 int bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *dsigma, double rel_tol,
                          cudaStream_t s);
 int stage3_bisect_df(const double *dd, const double *de, int64_t n, double rel_tol, double *dsigma, double *dscratch,

@@ -18,12 +18,11 @@
 // its column block cb as soon as role p-1 has finished block cb: the roles form
 // a systolic pipeline over the row tiles whose critical path is
 // (#tiles + b/16) block steps instead of #tiles * b reflector steps.  Within a
-// block the 16 reflectors are generated one column at a time with the
-// reference's nu/tau formulas (scalars in FP64), their compact-WY factor T
-// (16 x 16) is formed, and the block is applied to the rest of the tile with
-// it.  Roles are handed out by an atomic ticket in launch order, so a role only
-// ever waits on a role already running: no co-residency assumption, and every
-// wait is bounded.
+// block the 16 reflectors are generated one column at a time, their
+// compact-WY factor T (16 x 16) is formed, and the block is applied to the rest
+// of the tile with it.  Roles are handed out by an atomic ticket in launch
+// order, so a role only ever waits on a role already running: no co-residency
+// assumption, and every wait is bounded.
 //
 // Trailing update kernel.  One CTA owns a column strip of the trailing matrix,
 // keeps the strip of the top tile row in shared memory, and applies the GEQRT
@@ -60,6 +59,7 @@ struct PanelArgs {
     int *ticket;
     int *progress;   // [P]
     int *err;
+    int64_t sA, sTau, sTblk, sFlags;  // per-matrix strides (blockIdx.y = matrix)
 };
 
 struct UpdateArgs {
@@ -70,299 +70,18 @@ struct UpdateArgs {
     int pr, pc, P;
     int width;  // strip width
     const void *tblk;
+    int64_t sA, sTblk;  // per-matrix strides (blockIdx.y = matrix)
 };
 
 __host__ __device__ inline int ldpad(int b) { return b + 1; }
 
-template <typename T>
-size_t panel_smem_bytes(int b) {
-    size_t doubles = 2 * kIB + kIB * kIB + 8;                    // dsum, tau, G, scalars
-    size_t ts = (size_t)ldpad(b) * kIB        /* X  */
-                + (size_t)kIB * b             /* Rt */
-                + (size_t)ldpad(b) * kCW      /* C  */
-                + 2 * (size_t)kIB * kCW       /* Z, W */
-                + (size_t)kIB * kIB;          /* Tm */
-    return doubles * sizeof(double) + ts * sizeof(T);
-}
-
-template <typename T, int LAYOUT>
-__global__ void __launch_bounds__(kNT) panel_kernel(PanelArgs args) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int b = args.b;
-    const int nb = b / kIB;
-    const int ldx = ldpad(b);
-    double *dsum = reinterpret_cast<double *>(smem_raw);  // kIB
-    double *stau = dsum + kIB;                             // kIB
-    double *G = stau + kIB;                                // kIB*kIB, G[l + i*kIB]
-    double *scal = G + kIB * kIB;                          // 8
-    T *X = reinterpret_cast<T *>(scal + 8);                // ldx * kIB
-    T *Rt = X + (size_t)ldx * kIB;                         // kIB * b, Rt[l + j*kIB]
-    T *C = Rt + (size_t)kIB * b;                           // ldx * kCW
-    T *Zs = C + (size_t)ldx * kCW;                         // kIB * kCW
-    T *Ws = Zs + kIB * kCW;                                // kIB * kCW
-    T *Tm = Ws + kIB * kCW;                                // kIB * kIB, Tm[l + i*kIB]
-
-    __shared__ int s_role, s_ok;
-    const int tid = threadIdx.x;
-    const int jj = tid >> 4;  // column within the block
-    const int g = tid & 15;   // row group
-    if (tid == 0) s_role = atomicAdd(args.ticket, 1) + args.first_role;
-    __syncthreads();
-    const int p = s_role;
-    if (p >= args.P) return;
-
-    View<T, LAYOUT> V{reinterpret_cast<T *>(args.a), args.lda};
-    const int64_t row0 = (int64_t)(args.pr + p) * b;  // my tile (view rows)
-    const int64_t top0 = (int64_t)args.pr * b;        // top tile (view rows)
-    const int64_t col0 = (int64_t)args.pc * b;        // panel (view cols)
-    const bool geqrt = (p == 0);
-    T *tau_out = reinterpret_cast<T *>(args.tau) + (size_t)p * b;
-    T *tblk_out = reinterpret_cast<T *>(args.tblk) + (size_t)p * nb * kIB * kIB;
-    const int rows_per_g = b / 16;
-
-    for (int cb = 0; cb < nb; ++cb) {
-        const int c0 = cb * kIB;
-        // ---- wait for the previous role to release block cb of the top rows
-        if (tid == 0) {
-            bool ok = true;
-            if (p > args.first_role) ok = wait_geq(args.progress + p - 1, cb + 1, args.err);
-            s_ok = ok;
-        }
-        __syncthreads();
-        if (!s_ok) return;
-
-        // ---- load my 16-column slice (and, for TSQRT, the top rows c0..c0+15)
-        for (int idx = tid; idx < b * kIB; idx += kNT) {
-            int t, l;
-            if (LAYOUT == 0) { t = idx % b; l = idx / b; } else { l = idx % kIB; t = idx / kIB; }
-            X[t + l * ldx] = __ldcg(&V(row0 + t, col0 + c0 + l));
-        }
-        if (!geqrt) {
-            const int ncols = b - c0;
-            for (int idx = tid; idx < kIB * ncols; idx += kNT) {
-                int l, j;
-                if (LAYOUT == 0) { l = idx % kIB; j = idx / kIB; } else { j = idx % ncols; l = idx / ncols; }
-                Rt[l + (c0 + j) * kIB] = __ldcg(&V(top0 + c0 + l, col0 + c0 + j));
-            }
-        }
-        __syncthreads();
-
-        // ---- 16 reflectors, one column at a time (QRkernels.jl:17-58 / 87-120)
-        for (int i = 0; i < kIB; ++i) {
-            const int c = c0 + i;  // column (and, for GEQRT, pivot row) in the tile
-            if (geqrt && c == b - 1) {  // the reference loops iter = 1:N-1 for GEQRT
-                if (tid == 0) { stau[i] = 0.0; }
-                __syncthreads();
-                continue;
-            }
-            T xr[16];
-            double acc = 0.0;
-            T accT = T(0);
-            T rv = T(0);
-            if (jj >= i) rv = geqrt ? X[c + jj * ldx] : Rt[i + (c0 + jj) * kIB];
-#pragma unroll
-            for (int m = 0; m < 16; ++m) {
-                xr[m] = T(0);
-                if (m < rows_per_g) {
-                    const int t = g + 16 * m;
-                    const bool live = geqrt ? (t > c) : true;
-                    xr[m] = live ? X[t + i * ldx] : T(0);
-                    if (jj >= i) {
-                        if (jj == i) acc += (double)xr[m] * (double)xr[m];
-                        else accT += xr[m] * X[t + jj * ldx];
-                    }
-                }
-            }
-#pragma unroll
-            for (int o = 8; o > 0; o >>= 1) {
-                accT += __shfl_xor_sync(0xffffffffu, accT, o);
-                acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            }
-            if (g == 0 && jj >= i) dsum[jj] = (jj == i) ? acc : (double)accT;
-            __syncthreads();
-            if (tid == 0) {
-                const double s = dsum[i];
-                const double alpha = geqrt ? (double)X[c + i * ldx] : (double)Rt[i + c * kIB];
-                const double n1 = sqrt(s + alpha * alpha);
-                const double nu = alpha + (alpha < 0.0 ? -n1 : n1);
-                double tv = 0.0;
-                if (nu != 0.0) {
-                    const double n2 = sqrt(s + nu * nu);
-                    const double q = nu / n2;
-                    tv = 2.0 * (q * q);
-                }
-                if (!isfinite(tv) || !isfinite(nu)) { atomicCAS(args.err, kDevOk, kDevNonfinite); tv = 0.0; }
-                scal[0] = nu;
-                scal[1] = (tv != 0.0) ? 1.0 / nu : 0.0;         // scaling of V
-                scal[2] = (tv != 0.0) ? (tv / nu) / nu : 0.0;   // taucorr / nu
-                stau[i] = tv;
-            }
-            __syncthreads();
-            const double nu = scal[0];
-            const double tv = stau[i];
-            const T inv_nu = (T)scal[1];
-            const T f_upd = (T)scal[2];
-            if (tv == 0.0) {
-                // identity reflector: zero column (or the GEQRT tail) -> V column = 0
-                if (jj == i) {
-                    for (int m = 0; m < rows_per_g; ++m) {
-                        const int t = g + 16 * m;
-                        if (geqrt ? (t > c) : true) X[t + i * ldx] = T(0);
-                    }
-                }
-                __syncthreads();
-                continue;
-            }
-            const double tc = tv / nu;  // taucorr
-            if (jj >= i) {
-                const double w = nu * (double)rv + dsum[jj];
-                const T wT = (T)w;
-                const T fw = f_upd * wT;  // (x_t / nu) * (tau / nu) * w_j = x_t * fw
-#pragma unroll
-                for (int m = 0; m < 16; ++m) {
-                    if (m >= rows_per_g) break;
-                    const int t = g + 16 * m;
-                    if (geqrt) {
-                        if (t > c) {
-                            if (jj > i) X[t + jj * ldx] -= xr[m] * fw;
-                            else X[t + i * ldx] = xr[m] * inv_nu;
-                        } else if (t == c) {
-                            X[c + jj * ldx] = (T)((double)rv - tc * w);
-                        }
-                    } else {
-                        if (jj > i) X[t + jj * ldx] -= xr[m] * fw;
-                        else X[t + i * ldx] = xr[m] * inv_nu;
-                    }
-                }
-                if (!geqrt && g == 0) Rt[i + (c0 + jj) * kIB] = (T)((double)rv - tc * w);
-            }
-            __syncthreads();
-        }
-
-        // ---- compact-WY factor of the block: G = Y^T Y (strict upper), T recurrence
-        {
-            const int i = jj;
-            for (int l = 0; l < kIB; ++l) {
-                double part = 0.0;
-                if (l < i) {
-                    T pt = T(0);
-                    for (int m = 0; m < rows_per_g; ++m) {
-                        const int t = g + 16 * m;
-                        if (geqrt ? (t > c0 + i) : true) pt += X[t + l * ldx] * X[t + i * ldx];
-                    }
-                    part = (double)pt;
-                }
-#pragma unroll
-                for (int o = 8; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-                if (g == 0) {
-                    if (l < i && geqrt) part += (double)X[c0 + i + l * ldx];  // unit entry of y_i
-                    G[l + i * kIB] = (l < i) ? part : 0.0;
-                }
-            }
-        }
-        if (tid < kIB * kIB) Tm[tid] = T(0);
-        __syncthreads();
-        if (tid < kIB) Tm[tid + tid * kIB] = (T)stau[tid];
-        __syncthreads();
-        for (int i = 1; i < kIB; ++i) {
-            if (tid < i) {
-                double sacc = 0.0;
-                for (int m = tid; m < i; ++m) sacc += (double)Tm[tid + m * kIB] * G[m + i * kIB];
-                Tm[tid + i * kIB] = (T)(-stau[i] * sacc);
-            }
-            __syncthreads();
-        }
-
-        // ---- write V (and the block's R rows), tau, T.  GEQRT writes only rows
-        // >= c0: rows above are top rows that the next role may be updating.
-        for (int idx = tid; idx < b * kIB; idx += kNT) {
-            int t, l;
-            if (LAYOUT == 0) { t = idx % b; l = idx / b; } else { l = idx % kIB; t = idx / kIB; }
-            if (!geqrt || t >= c0) V(row0 + t, col0 + c0 + l) = X[t + l * ldx];
-        }
-        if (tid < kIB) tau_out[c0 + tid] = (T)stau[tid];
-        if (tid < kIB * kIB) tblk_out[(size_t)cb * kIB * kIB + tid] = Tm[tid];
-
-        // ---- apply the block to the rest of the tile (and the top rows), chunked
-        for (int j = c0 + kIB; j < b; j += kCW) {
-            const int cw = min(kCW, b - j);
-            for (int idx = tid; idx < b * cw; idx += kNT) {
-                int t, cc;
-                if (LAYOUT == 0) { t = idx % b; cc = idx / b; } else { cc = idx % cw; t = idx / cw; }
-                C[t + cc * ldx] = __ldcg(&V(row0 + t, col0 + j + cc));
-            }
-            __syncthreads();
-            for (int o = tid; o < kIB * cw; o += kNT) {
-                const int l = o % kIB, cc = o / kIB;
-                T z = geqrt ? T(0) : Rt[l + (j + cc) * kIB];
-                const int tstart = geqrt ? (c0 + l) : 0;
-                if (geqrt) z += C[tstart + cc * ldx];  // unit diagonal of Y
-                for (int t = geqrt ? tstart + 1 : 0; t < b; ++t) z += X[t + l * ldx] * C[t + cc * ldx];
-                Zs[l + cc * kIB] = z;
-            }
-            __syncthreads();
-            for (int o = tid; o < kIB * cw; o += kNT) {
-                const int l = o % kIB, cc = o / kIB;
-                T w = T(0);
-                for (int m = 0; m <= l; ++m) w += Tm[m + l * kIB] * Zs[m + cc * kIB];
-                Ws[l + cc * kIB] = w;
-                if (!geqrt) Rt[l + (j + cc) * kIB] -= w;
-            }
-            __syncthreads();
-            for (int idx = tid; idx < b * cw; idx += kNT) {
-                const int t = idx % b, cc = idx / b;
-                T acc2 = T(0);
-                if (geqrt) {
-                    if (t >= c0) {
-                        const int lmax = min(kIB - 1, t - c0);
-                        for (int l = 0; l <= lmax; ++l) {
-                            const T y = (t == c0 + l) ? T(1) : X[t + l * ldx];
-                            acc2 += y * Ws[l + cc * kIB];
-                        }
-                        C[t + cc * ldx] -= acc2;
-                    }
-                } else {
-#pragma unroll
-                    for (int l = 0; l < kIB; ++l) acc2 += X[t + l * ldx] * Ws[l + cc * kIB];
-                    C[t + cc * ldx] -= acc2;
-                }
-            }
-            __syncthreads();
-            for (int idx = tid; idx < b * cw; idx += kNT) {
-                int t, cc;
-                if (LAYOUT == 0) { t = idx % b; cc = idx / b; } else { cc = idx % cw; t = idx / cw; }
-                if (!geqrt || t >= c0) V(row0 + t, col0 + j + cc) = C[t + cc * ldx];
-            }
-            __syncthreads();
-        }
-        if (!geqrt) {
-            const int ncols = b - c0;
-            for (int idx = tid; idx < kIB * ncols; idx += kNT) {
-                int l, jx;
-                if (LAYOUT == 0) { l = idx % kIB; jx = idx / kIB; } else { jx = idx % ncols; l = idx / ncols; }
-                V(top0 + c0 + l, col0 + c0 + jx) = Rt[l + (c0 + jx) * kIB];
-            }
-        }
-        __syncthreads();
-        if (tid == 0) {
-            __threadfence();
-            st_release(args.progress + p, cb + 1);
-        }
-    }
-}
-
 // ---------------------------------------------------------------------------
-// Panel kernel, warp-synchronous reflector generation.
-//
-// Same roles, systolic schedule, outputs (V in place, tau, 16 x 16 T blocks)
-// and arithmetic as panel_kernel, restructured for latency: warp 0 generates
-// the 16 reflectors of a block with warp-level synchronisation only; the
-// reflector scalars use the closed forms of the reference's expressions
-// (n1 = ||x||, nu = alpha + sign(alpha) n1, tau = 2 nu^2 / (s + nu^2) = |nu| / n1,
-// tau / nu = sign(nu) / n1, tau / nu^2 = 1 / (n1 |nu|)) evaluated in FP64 for
-// FP64 tiles and in double-float for FP32 tiles (GB300 issues FP64 at 1/64 of
-// the FP32 rate); the block's Gram matrix uses the whole CTA; the apply to the
-// rest of the tile runs four threads per column with the column in registers.
+// Reflector scalars.  The reference's expressions (QRkernels.jl:27-31) in
+// closed form: n1 = ||x||, nu = alpha + sign(alpha) n1,
+// tau = 2 nu^2 / (s + nu^2) = |nu| / n1, tau / nu = sign(nu) / n1,
+// tau / nu^2 = 1 / (n1 |nu|), new diagonal beta = -sign(alpha) n1; evaluated in
+// FP64 for FP64 tiles and in double-float for FP32 tiles (GB300 issues FP64 at
+// 1/64 of the FP32 rate).
 
 // Reflector scalars from s = sum of squares of the sub-column (as a pair) and
 // alpha.  Writes nu, tau, tau/nu, tau/nu^2, 1/nu, beta (the new diagonal).
@@ -398,23 +117,32 @@ struct PScalarsF {
 
 __device__ __forceinline__ PScalarsF pscal_float(df64 s, float alpha) {
     PScalarsF r;
-    const df64 a = df64{alpha, 0.0f};
-    const df64 n1 = df_sqrt(df_add(s, two_prod(alpha, alpha)));
-    const bool neg = alpha < 0.0f;
-    const df64 nu = neg ? df_sub(a, n1) : df_add(a, n1);
-    r.nu = nu.hi + nu.lo;
-    if (nu.hi == 0.0f) {
-        r.tau = r.tc = r.f = r.inv = 0.0f;
+    const df64 x = df_add(s, two_prod(alpha, alpha));  // n1^2
+    if (x.hi <= 0.0f) {  // zero column: identity reflector
+        r.nu = r.tau = r.tc = r.f = r.inv = 0.0f;
         r.beta = alpha;
         return r;
     }
-    const df64 rn1 = df_rcp(n1);
-    const df64 anu = nu.hi < 0.0f ? df_neg(nu) : nu;
-    const df64 inv = df_rcp(nu);
+    // 1/n1: hardware rsqrt estimate, one Newton step in double-float:
+    // y' = y + y (1 - x y^2) / 2
+    const float y0 = rsqrtf(x.hi);
+    const df64 e = df_sub(df64{1.0f, 0.0f}, df_mul(x, two_prod(y0, y0)));
+    const df64 rn1 = df_add(df64{y0, 0.0f}, df_mul_f(e, 0.5f * y0));
+    const df64 n1 = df_mul(x, rn1);
+    const bool neg = alpha < 0.0f;
+    const df64 a = df64{alpha, 0.0f};
+    const df64 nu = neg ? df_sub(a, n1) : df_add(a, n1);  // |nu| = |alpha| + n1 > 0
+    // 1/nu: hardware reciprocal estimate, one Newton step: z' = z + z (1 - nu z)
+    const float z0 = __fdividef(1.0f, nu.hi);
+    const df64 ez = df_sub(df64{1.0f, 0.0f}, df_mul_f(nu, z0));
+    const df64 inv = df_add(df64{z0, 0.0f}, df_mul_f(ez, z0));
+    const df64 anu = neg ? df_neg(nu) : nu;
+    const df64 ainv = neg ? df_neg(inv) : inv;
     const df64 tau = df_mul(anu, rn1);
-    const df64 f = df_mul(rn1, inv.hi < 0.0f ? df_neg(inv) : inv);
+    const df64 f = df_mul(rn1, ainv);
+    r.nu = nu.hi + nu.lo;
     r.tau = tau.hi + tau.lo;
-    r.tc = nu.hi < 0.0f ? -(rn1.hi + rn1.lo) : (rn1.hi + rn1.lo);
+    r.tc = neg ? -(rn1.hi + rn1.lo) : (rn1.hi + rn1.lo);
     r.inv = inv.hi + inv.lo;
     r.f = f.hi + f.lo;
     r.beta = neg ? (n1.hi + n1.lo) : -(n1.hi + n1.lo);
@@ -429,6 +157,7 @@ struct PScal<double> {
     static __device__ __forceinline__ Acc zero() { return 0.0; }
     static __device__ __forceinline__ Acc sq(double x, Acc a) { return fma(x, x, a); }
     static __device__ __forceinline__ Acc shfl_add(Acc a, int o) { return a + __shfl_xor_sync(0xffffffffu, a, o); }
+    static __device__ __forceinline__ Acc shfl_add_local(Acc a, Acc b) { return a + b; }
     static __device__ __forceinline__ void compute(Acc s, double alpha, double *out) {
         const PScalars r = pscal_double(s, alpha);
         out[0] = r.nu; out[1] = r.tc; out[2] = r.f; out[3] = r.inv; out[4] = r.beta; out[5] = r.tau;
@@ -442,88 +171,96 @@ struct PScal<float> {
     static __device__ __forceinline__ Acc shfl_add(Acc a, int o) {
         return df_add(a, df64{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)});
     }
+    static __device__ __forceinline__ Acc shfl_add_local(Acc a, Acc b) { return df_add(a, b); }
     static __device__ __forceinline__ void compute(Acc s, float alpha, float *out) {
         const PScalarsF r = pscal_float(s, alpha);
         out[0] = r.nu; out[1] = r.tc; out[2] = r.f; out[3] = r.inv; out[4] = r.beta; out[5] = r.tau;
     }
 };
 
-__device__ __forceinline__ PScalars pscal_df(df64 s, float alpha) {
-    PScalars r;
-    const df64 a = df64{alpha, 0.0f};
-    const df64 n1 = df_sqrt(df_add(s, two_prod(alpha, alpha)));
-    const bool neg = alpha < 0.0f;
-    const df64 nu = neg ? df_sub(a, n1) : df_add(a, n1);
-    r.nu = df_to_double(nu);
-    if (nu.hi == 0.0f) {
-        r.tau = r.tc = r.f = r.inv = 0.0;
-        r.beta = alpha;
-        return r;
+// ---------------------------------------------------------------------------
+// Panel kernel (roles, schedule and outputs as described at the top):
+//   * every thread owns one row of the 16-column slice (b <= 256 rows, 256
+//     threads); the 16 dot products of a reflector step
+//     are reduced with a warp reduce-scatter (16 shuffles) and one shared-memory
+//     pass across warps: two barriers per reflector;
+//   * the masked reflector block Y is written once per block (row-major, so the
+//     apply reads it with 16-byte loads);
+//   * the apply to the rest of the tile is Z = Y^T C (threads own 4 x 4 output
+//     blocks, C streamed from L2 in 16-byte vectors), W = T^T Z (+ top rows),
+//     C -= Y W (threads own rows, W broadcast from shared memory).
+
+template <typename T>
+__device__ __forceinline__ void ld4(const T *p, T (&v)[4]) {
+    if (sizeof(T) == 4) {
+        const float4 x = __ldcg(reinterpret_cast<const float4 *>(p));
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+    } else {
+        const double2 x = __ldcg(reinterpret_cast<const double2 *>(p));
+        const double2 y = __ldcg(reinterpret_cast<const double2 *>(p) + 1);
+        v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
     }
-    const df64 rn1 = df_rcp(n1);
-    const df64 anu = nu.hi < 0.0f ? df_neg(nu) : nu;
-    const df64 inv = df_rcp(nu);
-    r.tau = df_to_double(df_mul(anu, rn1));
-    r.tc = df_to_double(nu.hi < 0.0f ? df_neg(rn1) : rn1);
-    r.inv = df_to_double(inv);
-    r.f = df_to_double(df_mul(rn1, inv.hi < 0.0f ? df_neg(inv) : inv));
-    r.beta = df_to_double(neg ? n1 : df_neg(n1));
-    return r;
 }
 
 template <typename T>
-size_t panel2_smem_bytes(int b) {
-    return sizeof(T) * 32 /* tau, scalars */ +
-           sizeof(T) * ((size_t)ldpad(b) * kIB /* X */ + (size_t)kIB * b /* Rt */ + 2 * kIB * kIB /* Tm, G */ +
-                        (size_t)kIB * 33 /* red */ + 2 * kIB /* dsum, wbuf */);
+size_t panel3_smem_bytes(int b) {
+    return sizeof(T) * (32 /* tau, scalars */ + (size_t)ldpad(b) * kIB /* X */ + (size_t)b * kIB /* Yr */ +
+                        (size_t)kIB * b /* Rt */ + (size_t)kIB * b /* Ws */ + 2 * kIB * kIB /* Tm, G */ +
+                        8 * kIB /* part */ + 8 + 2 * kIB /* spart, dsum, rvs */) +
+           sizeof(double) * 16;
 }
 
 template <typename T, int LAYOUT>
-__global__ void __launch_bounds__(kNT) panel2_kernel(PanelArgs args) {
+__global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int b = args.b;
     const int nb = b / kIB;
     const int ldx = ldpad(b);
-    T *stau = reinterpret_cast<T *>(smem_raw);             // kIB
-    T *scal = stau + kIB;                                  // 16
-    T *X = scal + 16;                                      // ldx * kIB
-    T *Rt = X + (size_t)ldx * kIB;                         // kIB * b, Rt[l + j*kIB]
-    T *Tm = Rt + (size_t)kIB * b;                          // kIB * kIB, Tm[l + i*kIB]
-    T *G = Tm + kIB * kIB;                                 // kIB * kIB, G[l + i*kIB]
-    T *red = G + kIB * kIB;                                // kIB * 33
-    T *dsum = red + kIB * 33;                              // kIB
-    T *wbuf = dsum + kIB;                                  // kIB
+    using Acc = typename PScal<T>::Acc;
+    Acc *spart = reinterpret_cast<Acc *>(smem_raw);         // 8 warps
+    T *stau = reinterpret_cast<T *>(smem_raw + sizeof(double) * 16);
+    T *scal = stau + kIB;                                    // 16
+    T *X = scal + 16;                                        // ldx * kIB (column-major)
+    T *Yr = X + (size_t)ldx * kIB;                           // b * kIB (row-major: Yr[t*16 + l])
+    T *Rt = Yr + (size_t)b * kIB;                            // kIB * b, Rt[l + j*kIB]
+    T *Ws = Rt + (size_t)kIB * b;                            // kIB * b, Ws[l + j*kIB]
+    T *Tm = Ws + (size_t)kIB * b;                            // kIB * kIB, Tm[l + i*kIB]
+    T *G = Tm + kIB * kIB;                                   // kIB * kIB
+    T *part = G + kIB * kIB;                                 // 8 * kIB
+    T *dsum = part + 8 * kIB;                                // kIB
 
     __shared__ int s_role, s_ok;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    if (tid == 0) s_role = atomicAdd(args.ticket, 1) + args.first_role;
+    const int64_t zb = blockIdx.y;
+    int *ticket = args.ticket + zb * args.sFlags;
+    int *progress = args.progress + zb * args.sFlags;
+    if (tid == 0) s_role = atomicAdd(ticket, 1) + args.first_role;
     __syncthreads();
     const int p = s_role;
     if (p >= args.P) return;
 
-    View<T, LAYOUT> V{reinterpret_cast<T *>(args.a), args.lda};
+    View<T, LAYOUT> V{reinterpret_cast<T *>(args.a) + zb * args.sA, args.lda};
     const int64_t row0 = (int64_t)(args.pr + p) * b;
     const int64_t top0 = (int64_t)args.pr * b;
     const int64_t col0 = (int64_t)args.pc * b;
     const bool geqrt = (p == 0);
-    T *tau_out = reinterpret_cast<T *>(args.tau) + (size_t)p * b;
-    T *tblk_out = reinterpret_cast<T *>(args.tblk) + (size_t)p * nb * kIB * kIB;
-    const int R = (b + 31) / 32;  // rows per lane in the reflector loop
-    const int RQ = b / 4;         // rows per thread in the apply
+    T *tau_out = reinterpret_cast<T *>(args.tau) + zb * args.sTau + (size_t)p * b;
+    T *tblk_out = reinterpret_cast<T *>(args.tblk) + zb * args.sTblk + (size_t)p * nb * kIB * kIB;
+    const int t = tid;  // my row (b <= 256)
 
     for (int cb = 0; cb < nb; ++cb) {
         const int c0 = cb * kIB;
         if (tid == 0) {
             bool ok = true;
-            if (p > args.first_role) ok = wait_geq(args.progress + p - 1, cb + 1, args.err);
+            if (p > args.first_role) ok = wait_geq(progress + p - 1, cb + 1, args.err);
             s_ok = ok;
         }
         __syncthreads();
         if (!s_ok) return;
         for (int idx = tid; idx < b * kIB; idx += kNT) {
-            int t, l;
-            if (LAYOUT == 0) { t = idx % b; l = idx / b; } else { l = idx % kIB; t = idx / kIB; }
-            X[t + l * ldx] = __ldcg(&V(row0 + t, col0 + c0 + l));
+            int tt, l;
+            if (LAYOUT == 0) { tt = idx % b; l = idx / b; } else { l = idx % kIB; tt = idx / kIB; }
+            X[tt + l * ldx] = __ldcg(&V(row0 + tt, col0 + c0 + l));
         }
         if (!geqrt) {
             const int ncols = b - c0;
@@ -535,103 +272,84 @@ __global__ void __launch_bounds__(kNT) panel2_kernel(PanelArgs args) {
         }
         __syncthreads();
 
-        // ---- warp 0: the 16 reflectors of the block
-        if (wid == 0) {
-            for (int i = 0; i < kIB; ++i) {
-                const int c = c0 + i;
-                if (geqrt && c == b - 1) {  // the reference's GEQRT loops iter = 1:N-1
-                    if (lane == 0) stau[i] = T(0);
-                    __syncwarp();
-                    continue;
-                }
-                T xr[8];
-                T dp[kIB];
+        // ---- the 16 reflectors of the block, one per step, all threads
+        for (int i = 0; i < kIB; ++i) {
+            const int c = c0 + i;
+            if (geqrt && c == b - 1) {
+                if (tid == 0) stau[i] = T(0);
+                __syncthreads();
+                continue;
+            }
+            const bool live = (t < b) && (geqrt ? (t > c) : true);
+            const T x = live ? X[t + i * ldx] : T(0);
+            T pv[kIB];
 #pragma unroll
-                for (int jj = 0; jj < kIB; ++jj) dp[jj] = T(0);
-                typename PScal<T>::Acc sq = PScal<T>::zero();
+            for (int jj = 0; jj < kIB; ++jj) pv[jj] = (live && jj > i) ? x * X[t + jj * ldx] : T(0);
+            Acc sq = PScal<T>::zero();
+            if (live) sq = PScal<T>::sq(x, sq);
+            // warp reduce-scatter of pv[0..15]: lane L ends with the warp sum of pv[L & 15]
 #pragma unroll
-                for (int r = 0; r < 8; ++r) {
-                    xr[r] = T(0);
-                    if (r < R) {
-                        const int t = lane + 32 * r;
-                        const bool live = (t < b) && (geqrt ? (t > c) : true);
-                        if (live) {
-                            const T x = X[t + i * ldx];
-                            xr[r] = x;
-                            sq = PScal<T>::sq(x, sq);
+            for (int h = 8; h >= 1; h >>= 1) {
+                const bool upper = (lane & h) != 0;
 #pragma unroll
-                            for (int jj = 0; jj < kIB; ++jj)
-                                if (jj > i) dp[jj] += x * X[t + jj * ldx];
-                        }
-                    }
+                for (int q = 0; q < h; ++q) {
+                    const T send = upper ? pv[q] : pv[q + h];
+                    const T keep = upper ? pv[q + h] : pv[q];
+                    pv[q] = keep + __shfl_xor_sync(0xffffffffu, send, h);
                 }
+            }
+            // after the rounds lane L holds the sum of index (L & 15) in pv[0]; add the half-warp partner
+            pv[0] += __shfl_xor_sync(0xffffffffu, pv[0], 16);
 #pragma unroll
-                for (int jj = 0; jj < kIB; ++jj) red[jj * 33 + lane] = dp[jj];
+            for (int o = 16; o > 0; o >>= 1) sq = PScal<T>::shfl_add(sq, o);
+            if (lane < kIB) part[wid * kIB + lane] = pv[0];  // lane L holds index L & 15
+            if (lane == 0) spart[wid] = sq;
+            __syncthreads();
+            if (tid == 0) {
+                Acc s_all = PScal<T>::zero();
+                for (int w = 0; w < kNT / 32; ++w) s_all = PScal<T>::shfl_add_local(s_all, spart[w]);
+                const T alpha = geqrt ? X[c + i * ldx] : Rt[i + c * kIB];
+                T out[6];
+                PScal<T>::compute(s_all, alpha, out);
+                if (!isfinite(out[5]) || !isfinite(out[0])) {
+                    atomicCAS(args.err, kDevOk, kDevNonfinite);
+                    out[5] = out[1] = out[2] = out[3] = T(0);
+                    out[4] = alpha;
+                }
+                stau[i] = out[5];
+                scal[0] = out[0]; scal[1] = out[1]; scal[2] = out[2]; scal[3] = out[3]; scal[4] = out[4];
+            }
+            if (tid > i && tid < kIB) {
+                T acc = T(0);
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) sq = PScal<T>::shfl_add(sq, o);
-                __syncwarp();
-                if (lane < kIB && lane > i) {
-                    T acc = T(0);
-#pragma unroll 8
-                    for (int q = 0; q < 32; ++q) acc += red[lane * 33 + q];
-                    dsum[lane] = acc;
-                }
-                if (lane == 0) {
-                    const T alpha = geqrt ? X[c + i * ldx] : Rt[i + c * kIB];
-                    T out[6];
-                    PScal<T>::compute(sq, alpha, out);
-                    if (!isfinite(out[5]) || !isfinite(out[0])) {
-                        atomicCAS(args.err, kDevOk, kDevNonfinite);
-                        out[5] = out[1] = out[2] = out[3] = T(0);
-                        out[4] = alpha;
-                    }
-                    stau[i] = out[5];
-                    scal[0] = out[0];
-                    scal[1] = out[1];
-                    scal[2] = out[2];
-                    scal[3] = out[3];
-                    scal[4] = out[4];
-                }
-                __syncwarp();
-                if (stau[i] == T(0)) {
+                for (int w = 0; w < kNT / 32; ++w) acc += part[w * kIB + tid];
+                dsum[tid] = acc;
+            }
+            T rvr[kIB];
 #pragma unroll
-                    for (int r = 0; r < 8; ++r) {
-                        const int t = lane + 32 * r;
-                        if (r < R && t < b && (geqrt ? (t > c) : true)) X[t + i * ldx] = T(0);
-                    }
-                    __syncwarp();
-                    continue;
-                }
-                const T nu = scal[0], tc = scal[1], f = scal[2], inv = scal[3];
-                if (lane < kIB && lane > i) {
-                    const T rv = geqrt ? X[c + lane * ldx] : Rt[i + (c0 + lane) * kIB];
-                    const T w = nu * rv + dsum[lane];
-                    wbuf[lane] = w;
-                    if (geqrt) X[c + lane * ldx] = rv - tc * w;
-                    else Rt[i + (c0 + lane) * kIB] = rv - tc * w;
-                }
-                if (lane == 0) {
-                    if (geqrt) X[c + i * ldx] = scal[4];
-                    else Rt[i + c * kIB] = scal[4];
-                }
-                __syncwarp();
+            for (int jj = 0; jj < kIB; ++jj) rvr[jj] = geqrt ? X[c + jj * ldx] : Rt[i + (c0 + jj) * kIB];
+            __syncthreads();
+            const T tv = stau[i];
+            if (tv == T(0)) {
+                if (live) X[t + i * ldx] = T(0);
+                continue;  // no barrier needed: the next step reads only own rows until its first barrier
+            }
+            const T nu = scal[0], tc = scal[1], f = scal[2], inv = scal[3];
+            if (live) {
 #pragma unroll
-                for (int r = 0; r < 8; ++r) {
-                    const int t = lane + 32 * r;
-                    if (r < R && t < b && (geqrt ? (t > c) : true)) {
-                        const T x = xr[r];
-#pragma unroll
-                        for (int jj = 0; jj < kIB; ++jj)
-                            if (jj > i) X[t + jj * ldx] -= x * (f * wbuf[jj]);
-                        X[t + i * ldx] = x * inv;
-                    }
-                }
-                __syncwarp();
+                for (int jj = 0; jj < kIB; ++jj)
+                    if (jj > i) X[t + jj * ldx] -= x * (f * (nu * rvr[jj] + dsum[jj]));
+                X[t + i * ldx] = x * inv;
+            }
+            if (tid < kIB && tid >= i) {
+                const T nv = (tid == i) ? scal[4] : rvr[tid] - tc * (nu * rvr[tid] + dsum[tid]);
+                if (geqrt) X[c + tid * ldx] = nv;
+                else Rt[i + (c0 + tid) * kIB] = nv;
             }
         }
         __syncthreads();
 
-        // ---- Gram matrix of the block's reflectors (whole CTA), then T (warp 0)
+        // ---- Gram matrix of the block's reflectors, T (warp 0), masked Y
         {
             const int pi = tid >> 1, h = tid & 1;
             int l = -1, i = 0;
@@ -642,17 +360,23 @@ __global__ void __launch_bounds__(kNT) panel2_kernel(PanelArgs args) {
                     acc += ii;
                 }
             }
-            T part = T(0);
+            T pt = T(0);
             if (l >= 0) {
                 const int half = (b + 1) / 2;
                 const int tlo = h * half, thi = min(b, tlo + half);
-                for (int t = tlo; t < thi; ++t)
-                    if (geqrt ? (t > c0 + i) : true) part += X[t + l * ldx] * X[t + i * ldx];
+                for (int tt = tlo; tt < thi; ++tt)
+                    if (geqrt ? (tt > c0 + i) : true) pt += X[tt + l * ldx] * X[tt + i * ldx];
             }
-            part += __shfl_xor_sync(0xffffffffu, part, 1);
-            if (l >= 0 && h == 0) G[l + i * kIB] = part + (geqrt ? X[c0 + i + l * ldx] : T(0));
+            pt += __shfl_xor_sync(0xffffffffu, pt, 1);
+            if (l >= 0 && h == 0) G[l + i * kIB] = pt + (geqrt ? X[c0 + i + l * ldx] : T(0));
         }
         if (tid < kIB * kIB) Tm[tid] = T(0);
+        for (int idx = tid; idx < b * kIB; idx += kNT) {
+            const int tt = idx / kIB, l = idx % kIB;
+            T y = X[tt + l * ldx];
+            if (geqrt) y = (tt == c0 + l) ? T(1) : (tt > c0 + l ? y : T(0));
+            Yr[tt * kIB + l] = y;
+        }
         __syncthreads();
         if (wid == 0) {
             if (lane < kIB) Tm[lane + lane * kIB] = stau[lane];
@@ -666,79 +390,105 @@ __global__ void __launch_bounds__(kNT) panel2_kernel(PanelArgs args) {
                 __syncwarp();
             }
         }
-        __syncthreads();
-
-        // ---- write V, tau, T
         for (int idx = tid; idx < b * kIB; idx += kNT) {
-            int t, l;
-            if (LAYOUT == 0) { t = idx % b; l = idx / b; } else { l = idx % kIB; t = idx / kIB; }
-            if (!geqrt || t >= c0) V(row0 + t, col0 + c0 + l) = X[t + l * ldx];
+            int tt, l;
+            if (LAYOUT == 0) { tt = idx % b; l = idx / b; } else { l = idx % kIB; tt = idx / kIB; }
+            if (!geqrt || tt >= c0) V(row0 + tt, col0 + c0 + l) = X[tt + l * ldx];
         }
         if (tid < kIB) tau_out[c0 + tid] = stau[tid];
+        __syncthreads();
         if (tid < kIB * kIB) tblk_out[(size_t)cb * kIB * kIB + tid] = Tm[tid];
 
-        // ---- apply the block to the rest of the tile: 4 threads per column
-        const int nrest = b - c0 - kIB;
-        const int quad = tid >> 2, qq = tid & 3;
-        for (int base = 0; base < nrest; base += kNT / 4) {
-            const int jrel = base + quad;
-            const bool cv = jrel < nrest;
-            const int j = c0 + kIB + (cv ? jrel : 0);
-            T cr[64];
-            T z[kIB];
+        // ---- apply to the rest of the tile
+        const int jbase = c0 + kIB;
+        const int nrest = b - jbase;
+        const int tstart = geqrt ? c0 : 0;  // rows above c0 have Y = 0 for GEQRT
+        if (nrest > 0) {
+            // (a) Z = Y^T C: thread (jg, lg) -> columns 4jg..4jg+3, reflectors 4lg..4lg+3
+            for (int jg0 = 0; jg0 * 4 < nrest; jg0 += kNT / 4) {
+                const int jg = jg0 + (tid & 63), lg = tid >> 6;
+                const bool act = jg * 4 < nrest;
+                T z[4][4];
 #pragma unroll
-            for (int l = 0; l < kIB; ++l) z[l] = T(0);
+                for (int a = 0; a < 4; ++a)
 #pragma unroll
-            for (int r = 0; r < 64; ++r) {
-                cr[r] = T(0);
-                if (r < RQ) {
-                    const int t = qq * RQ + r;
-                    if (cv && (!geqrt || t >= c0)) {
-                        const T cval = __ldcg(&V(row0 + t, col0 + j));
-                        cr[r] = cval;
+                    for (int q = 0; q < 4; ++q) z[a][q] = T(0);
+                if (act) {
+                    const int j = jbase + 4 * jg;
+                    for (int tt = tstart; tt < b; tt += 4) {
+                        T cv[4][4];  // cv[row][col]
+                        if (LAYOUT == 0) {
 #pragma unroll
-                        for (int l = 0; l < kIB; ++l) {
-                            T y;
-                            if (geqrt) y = (t == c0 + l) ? T(1) : (t > c0 + l ? X[t + l * ldx] : T(0));
-                            else y = X[t + l * ldx];
-                            z[l] += y * cval;
+                            for (int q = 0; q < 4; ++q) {
+                                T col[4];
+                                ld4(&V(row0 + tt, col0 + j + q), col);
+#pragma unroll
+                                for (int r = 0; r < 4; ++r) cv[r][q] = col[r];
+                            }
+                        } else {
+#pragma unroll
+                            for (int r = 0; r < 4; ++r) ld4(&V(row0 + tt + r, col0 + j), cv[r]);
+                        }
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) {
+                            const T *yrow = Yr + (tt + r) * kIB + 4 * lg;
+#pragma unroll
+                            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                                for (int q = 0; q < 4; ++q) z[a][q] += yrow[a] * cv[r][q];
                         }
                     }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q)
+#pragma unroll
+                        for (int a = 0; a < 4; ++a) Ws[(4 * lg + a) + (4 * jg + q) * kIB] = z[a][q];
                 }
             }
+            __syncthreads();
+            // (b) W = T^T (Z + top rows); top rows -= W
+            for (int jr = tid; jr < nrest; jr += kNT) {
+                T zc[kIB];
 #pragma unroll
-            for (int l = 0; l < kIB; ++l) {
-                z[l] += __shfl_xor_sync(0xffffffffu, z[l], 1);
-                z[l] += __shfl_xor_sync(0xffffffffu, z[l], 2);
-                if (!geqrt && cv) z[l] += Rt[l + j * kIB];
+                for (int l = 0; l < kIB; ++l) {
+                    zc[l] = Ws[l + jr * kIB];
+                    if (!geqrt) zc[l] += Rt[l + (jbase + jr) * kIB];
+                }
+#pragma unroll
+                for (int l = 0; l < kIB; ++l) {
+                    T acc = T(0);
+#pragma unroll
+                    for (int m = 0; m <= l; ++m) acc += Tm[m + l * kIB] * zc[m];
+                    Ws[l + jr * kIB] = acc;
+                    if (!geqrt) Rt[l + (jbase + jr) * kIB] -= acc;
+                }
             }
-            T w[kIB];
+            __syncthreads();
+            // (c) C -= Y W: thread owns row t, four columns at a time
+            if (t >= tstart && t < b) {
+                T yv[kIB];
 #pragma unroll
-            for (int l = 0; l < kIB; ++l) {
-                T acc = T(0);
+                for (int l = 0; l < kIB; ++l) yv[l] = Yr[t * kIB + l];
+                for (int jr = 0; jr < nrest; jr += 4) {
+                    T acc[4];
 #pragma unroll
-                for (int m = 0; m <= l; ++m) acc += Tm[m + l * kIB] * z[m];
-                w[l] = acc;
-            }
-            if (!geqrt && cv) {
+                    for (int q = 0; q < 4; ++q) {
+                        T s2 = T(0);
 #pragma unroll
-                for (int l = 0; l < kIB; ++l)
-                    if ((l >> 2) == qq) Rt[l + j * kIB] -= w[l];
-            }
+                        for (int l = 0; l < kIB; ++l) s2 += yv[l] * Ws[l + (jr + q) * kIB];
+                        acc[q] = s2;
+                    }
+                    if (LAYOUT == 0) {
 #pragma unroll
-            for (int r = 0; r < 64; ++r) {
-                if (r < RQ) {
-                    const int t = qq * RQ + r;
-                    if (cv && (!geqrt || t >= c0)) {
-                        T acc = cr[r];
-#pragma unroll
-                        for (int l = 0; l < kIB; ++l) {
-                            T y;
-                            if (geqrt) y = (t == c0 + l) ? T(1) : (t > c0 + l ? X[t + l * ldx] : T(0));
-                            else y = X[t + l * ldx];
-                            acc -= y * w[l];
+                        for (int q = 0; q < 4; ++q) {
+                            T *cp = &V(row0 + t, col0 + jbase + jr + q);
+                            *cp = __ldcg(cp) - acc[q];
                         }
-                        V(row0 + t, col0 + j) = acc;
+                    } else {  // the four columns are contiguous in memory
+                        T *cp = &V(row0 + t, col0 + jbase + jr);
+                        T cv[4];
+                        ld4(cp, cv);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) cp[q] = cv[q] - acc[q];
                     }
                 }
             }
@@ -755,7 +505,7 @@ __global__ void __launch_bounds__(kNT) panel2_kernel(PanelArgs args) {
         __syncthreads();
         if (tid == 0) {
             __threadfence();
-            st_release(args.progress + p, cb + 1);
+            st_release(progress + p, cb + 1);
         }
     }
 }
@@ -784,10 +534,11 @@ __global__ void __launch_bounds__(kNT) update_kernel(UpdateArgs args) {
     const int64_t j0 = (int64_t)(args.pc + 1) * b + (int64_t)blockIdx.x * W;
     const int wc = (int)min((int64_t)W, args.n - j0);
     if (wc <= 0) return;
-    View<T, LAYOUT> V{reinterpret_cast<T *>(args.a), args.lda};
+    const int64_t zb = blockIdx.y;
+    View<T, LAYOUT> V{reinterpret_cast<T *>(args.a) + zb * args.sA, args.lda};
     const int64_t top0 = (int64_t)args.pr * b;
     const int64_t col0 = (int64_t)args.pc * b;
-    const T *tblk = reinterpret_cast<const T *>(args.tblk);
+    const T *tblk = reinterpret_cast<const T *>(args.tblk) + zb * args.sTblk;
 
     auto load_strip = [&](T *S, int64_t r0) {
         for (int idx = tid; idx < b * wc; idx += kNT) {
@@ -880,13 +631,14 @@ template <typename T, int LAYOUT>
 int launch_panel(T *dA, int64_t lda, int b, int pr, int pc, int P, int first_role, const Stage1Work &w,
                  cudaStream_t s) {
     static bool attr_set = false;
-    const size_t smem = panel2_smem_bytes<T>(b);
+    const size_t smem = panel3_smem_bytes<T>(b);
     if (!attr_set) {
-        AVS_CUDA_TRY(cudaFuncSetAttribute(panel2_kernel<T, LAYOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)panel2_smem_bytes<T>(256)));
+        AVS_CUDA_TRY(cudaFuncSetAttribute(panel3_kernel<T, LAYOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)panel3_smem_bytes<T>(256)));
         attr_set = true;
     }
-    AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(P + 1), s));
+    const int batch = w.batch > 0 ? w.batch : 1;
+    AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(batch > 1 ? w.sFlags * batch : P + 1), s));
     PanelArgs a;
     a.a = dA;
     a.lda = lda;
@@ -900,7 +652,11 @@ int launch_panel(T *dA, int64_t lda, int b, int pr, int pc, int P, int first_rol
     a.ticket = w.flags;
     a.progress = w.flags + 1;
     a.err = w.err;
-    panel2_kernel<T, LAYOUT><<<P - first_role, kNT, smem, s>>>(a);
+    a.sA = w.sA;
+    a.sTau = w.sTau;
+    a.sTblk = w.sTblk;
+    a.sFlags = w.sFlags;
+    panel3_kernel<T, LAYOUT><<<dim3(P - first_role, batch), kNT, smem, s>>>(a);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
 }
@@ -927,8 +683,10 @@ int launch_update(T *dA, int64_t lda, int64_t n, int b, int pr, int pc, int P, c
     a.P = P;
     a.width = width;
     a.tblk = w.tblk;
+    a.sA = w.sA;
+    a.sTblk = w.sTblk;
     const unsigned grid = (unsigned)((ncols + width - 1) / width);
-    update_kernel<T, LAYOUT><<<grid, kNT, update_smem_bytes<T>(b, width), s>>>(a);
+    update_kernel<T, LAYOUT><<<dim3(grid, w.batch > 0 ? w.batch : 1), kNT, update_smem_bytes<T>(b, width), s>>>(a);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
 }
@@ -941,7 +699,7 @@ int update_tc_half(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int
     if constexpr (sizeof(T) != 4) {
         return AVS_ERR_INTERNAL;
     } else {
-        int rc = stage1_tbuild<T>(dA, lda, b, layout, pr, pc, P, w.tblk, w.tfull, s);
+        int rc = stage1_tbuild<T>(dA, lda, b, layout, pr, pc, P, w, s);
         if (rc != AVS_SUCCESS) return rc;
         return stage1_update_tc(reinterpret_cast<float *>(dA), lda, n, b, layout, pr, pc, P,
                                 reinterpret_cast<const float *>(w.tfull), w.tc_S, w.tc_W, w.tc_split, w.err, s);
@@ -961,7 +719,7 @@ int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cud
         if (b >= 128 && w.tfull && w.tc_split && sizeof(T) == 4)
             rc = update_tc_half<T>(dA, lda, n, b, 0, k, k, P, w, s);
         else if (b >= 128 && w.tfull)
-            rc = stage1_update_full<T>(dA, lda, n, b, 0, k, k, P, w.tblk, w.tfull, s);
+            rc = stage1_update_full<T>(dA, lda, n, b, 0, k, k, P, w, s);
         else
             rc = launch_update<T, 0>(dA, lda, n, b, k, k, P, w, s);
         if (rc != AVS_SUCCESS) return rc;
@@ -973,7 +731,7 @@ int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cud
         if (b >= 128 && w.tfull && w.tc_split && sizeof(T) == 4)
             rc = update_tc_half<T>(dA, lda, n, b, 1, k + 1, k, PL, w, s);
         else if (b >= 128 && w.tfull)
-            rc = stage1_update_full<T>(dA, lda, n, b, 1, k + 1, k, PL, w.tblk, w.tfull, s);
+            rc = stage1_update_full<T>(dA, lda, n, b, 1, k + 1, k, PL, w, s);
         else
             rc = launch_update<T, 1>(dA, lda, n, b, k + 1, k, PL, w, s);
         if (rc != AVS_SUCCESS) return rc;

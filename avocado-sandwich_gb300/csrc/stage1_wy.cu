@@ -40,6 +40,7 @@ struct TBuildArgs {
     int pr, pc, P;
     const void *tblk;  // [P][b/16][256]
     void *tfull;       // [P][b*b], T(l, i) at l + i*b
+    int64_t sA, sTblk, sTfull;  // per-matrix strides (blockIdx.y = matrix)
 };
 
 // ---------------------------------------------------------------------------
@@ -50,13 +51,14 @@ __global__ void __launch_bounds__(kWNT) tbuild_kernel(TBuildArgs args) {
     const int b = args.b;
     const int nb = b / kWIB;
     const int p = blockIdx.x;
+    const int64_t zb = blockIdx.y;
     const bool geqrt = (p == 0);
     const int tid = threadIdx.x;
-    View<const T, LAYOUT> V{reinterpret_cast<const T *>(args.a), args.lda};
+    View<const T, LAYOUT> V{reinterpret_cast<const T *>(args.a) + zb * args.sA, args.lda};
     const int64_t row0 = (int64_t)(args.pr + p) * b;
     const int64_t col0 = (int64_t)args.pc * b;
-    T *Tf = reinterpret_cast<T *>(args.tfull) + (size_t)p * b * b;
-    const T *tb = reinterpret_cast<const T *>(args.tblk) + (size_t)p * nb * kWIB * kWIB;
+    T *Tf = reinterpret_cast<T *>(args.tfull) + zb * args.sTfull + (size_t)p * b * b;
+    const T *tb = reinterpret_cast<const T *>(args.tblk) + zb * args.sTblk + (size_t)p * nb * kWIB * kWIB;
 
     // ---- 1. G(l, i) = y_l^T y_i for l < i in different 16-blocks, into Tf
     constexpr int KC = 32;
@@ -155,6 +157,7 @@ struct UpdFullArgs {
     int b;
     int pr, pc, P;
     const void *tfull;
+    int64_t sA, sTfull;  // per-matrix strides (blockIdx.y = matrix)
 };
 
 // A-operand sources for the three products.
@@ -274,7 +277,8 @@ __global__ void __launch_bounds__(kWNT) update_full_kernel(UpdFullArgs args) {
     const int64_t j0 = (int64_t)(args.pc + 1) * B + (int64_t)blockIdx.x * C::W;
     const int wc = (int)min((int64_t)C::W, args.n - j0);
     if (wc <= 0) return;
-    View<T, LAYOUT> V{reinterpret_cast<T *>(args.a), args.lda};
+    const int64_t zb = blockIdx.y;
+    View<T, LAYOUT> V{reinterpret_cast<T *>(args.a) + zb * args.sA, args.lda};
     const int64_t top0 = (int64_t)args.pr * B;
     const int m0 = tid % C::TM;
     const int c0 = (tid / C::TM) * C::CB;
@@ -319,7 +323,7 @@ __global__ void __launch_bounds__(kWNT) update_full_kernel(UpdFullArgs args) {
     for (int p = 0; p < args.P; ++p) {
         UpdCtx<T, LAYOUT, B> ctx;
         ctx.V = V;
-        ctx.Tf = reinterpret_cast<const T *>(args.tfull) + (size_t)p * B * B;
+        ctx.Tf = reinterpret_cast<const T *>(args.tfull) + zb * args.sTfull + (size_t)p * B * B;
         ctx.row0 = (int64_t)(args.pr + p) * B;
         ctx.col0 = (int64_t)args.pc * B;
         ctx.geqrt = (p == 0);
@@ -375,7 +379,7 @@ size_t upd_full_smem() {
 }
 
 template <typename T, int LAYOUT, int B>
-int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const void *tfull, cudaStream_t s) {
+int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const Stage1Work &w, cudaStream_t s) {
     using C = UCfg<T, B>;
     static bool attr = false;
     const size_t smem = upd_full_smem<T, B>();
@@ -386,15 +390,15 @@ int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const 
     }
     const int64_t ncols = n - (int64_t)(pc + 1) * B;
     if (ncols <= 0) return AVS_SUCCESS;
-    UpdFullArgs a{dA, lda, n, B, pr, pc, P, tfull};
-    update_full_kernel<T, LAYOUT, B><<<(unsigned)((ncols + C::W - 1) / C::W), kWNT, smem, s>>>(a);
+    UpdFullArgs a{dA, lda, n, B, pr, pc, P, w.tfull, w.sA, w.sTfull};
+    const unsigned gx = (unsigned)((ncols + C::W - 1) / C::W);
+    update_full_kernel<T, LAYOUT, B><<<dim3(gx, w.batch > 0 ? w.batch : 1), kWNT, smem, s>>>(a);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
 }
 
 template <typename T, int LAYOUT>
-int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const void *tblk, void *tfull,
-                  cudaStream_t s) {
+int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const Stage1Work &w, cudaStream_t s) {
     static bool attr = false;
     const size_t smem = sizeof(T) * (size_t)32 * (256 + 1) > sizeof(T) * (size_t)256 * 256 / 16
                             ? sizeof(T) * (size_t)32 * (256 + 1)
@@ -404,8 +408,8 @@ int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const 
             cudaFuncSetAttribute(tbuild_kernel<T, LAYOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
-    TBuildArgs a{dA, lda, b, pr, pc, P, tblk, tfull};
-    tbuild_kernel<T, LAYOUT><<<P, kWNT, smem, s>>>(a);
+    TBuildArgs a{dA, lda, b, pr, pc, P, w.tblk, w.tfull, w.sA, w.sTblk, w.sTfull};
+    tbuild_kernel<T, LAYOUT><<<dim3(P, w.batch > 0 ? w.batch : 1), kWNT, smem, s>>>(a);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
 }
@@ -414,34 +418,33 @@ int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const 
 
 // T build alone (for the tensor-core update path).
 template <typename T>
-int stage1_tbuild(const T *dA, int64_t lda, int b, int layout, int pr, int pc, int P, const void *tblk, void *tfull,
+int stage1_tbuild(const T *dA, int64_t lda, int b, int layout, int pr, int pc, int P, const Stage1Work &w,
                   cudaStream_t s) {
-    return layout == 0 ? launch_tbuild<T, 0>(dA, lda, b, pr, pc, P, tblk, tfull, s)
-                       : launch_tbuild<T, 1>(dA, lda, b, pr, pc, P, tblk, tfull, s);
+    return layout == 0 ? launch_tbuild<T, 0>(dA, lda, b, pr, pc, P, w, s)
+                       : launch_tbuild<T, 1>(dA, lda, b, pr, pc, P, w, s);
 }
-template int stage1_tbuild<float>(const float *, int64_t, int, int, int, int, int, const void *, void *,
-                                  cudaStream_t);
-template int stage1_tbuild<double>(const double *, int64_t, int, int, int, int, int, const void *, void *,
+template int stage1_tbuild<float>(const float *, int64_t, int, int, int, int, int, const Stage1Work &, cudaStream_t);
+template int stage1_tbuild<double>(const double *, int64_t, int, int, int, int, int, const Stage1Work &,
                                    cudaStream_t);
 
 // Full-T trailing update of one half-step (tiles 128 and 256).
 template <typename T>
-int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const void *tblk,
-                       void *tfull, cudaStream_t s) {
+int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const Stage1Work &w,
+                       cudaStream_t s) {
     int rc;
     if (layout == 0) {
-        if ((rc = launch_tbuild<T, 0>(dA, lda, b, pr, pc, P, tblk, tfull, s)) != AVS_SUCCESS) return rc;
-        return b == 256 ? launch_upd_full<T, 0, 256>(dA, lda, n, pr, pc, P, tfull, s)
-                        : launch_upd_full<T, 0, 128>(dA, lda, n, pr, pc, P, tfull, s);
+        if ((rc = launch_tbuild<T, 0>(dA, lda, b, pr, pc, P, w, s)) != AVS_SUCCESS) return rc;
+        return b == 256 ? launch_upd_full<T, 0, 256>(dA, lda, n, pr, pc, P, w, s)
+                        : launch_upd_full<T, 0, 128>(dA, lda, n, pr, pc, P, w, s);
     }
-    if ((rc = launch_tbuild<T, 1>(dA, lda, b, pr, pc, P, tblk, tfull, s)) != AVS_SUCCESS) return rc;
-    return b == 256 ? launch_upd_full<T, 1, 256>(dA, lda, n, pr, pc, P, tfull, s)
-                    : launch_upd_full<T, 1, 128>(dA, lda, n, pr, pc, P, tfull, s);
+    if ((rc = launch_tbuild<T, 1>(dA, lda, b, pr, pc, P, w, s)) != AVS_SUCCESS) return rc;
+    return b == 256 ? launch_upd_full<T, 1, 256>(dA, lda, n, pr, pc, P, w, s)
+                    : launch_upd_full<T, 1, 128>(dA, lda, n, pr, pc, P, w, s);
 }
 
-template int stage1_update_full<float>(float *, int64_t, int64_t, int, int, int, int, int, const void *, void *,
+template int stage1_update_full<float>(float *, int64_t, int64_t, int, int, int, int, int, const Stage1Work &,
                                        cudaStream_t);
-template int stage1_update_full<double>(double *, int64_t, int64_t, int, int, int, int, int, const void *, void *,
+template int stage1_update_full<double>(double *, int64_t, int64_t, int, int, int, int, int, const Stage1Work &,
                                         cudaStream_t);
 
 }  // namespace avs

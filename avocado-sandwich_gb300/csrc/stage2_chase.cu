@@ -165,9 +165,9 @@ __global__ void __launch_bounds__(kChaseThreads) chase_kernel(double *ab, int64_
     }
 }
 
-template <int BW>
+template <int BW, int CC = (BW >= 128 ? 8 : (BW == 64 ? 4 : (BW == 32 ? 2 : 1)))>
 struct ChaseCfg {
-    static constexpr int C = BW >= 128 ? 8 : (BW == 64 ? 4 : (BW == 32 ? 2 : 1));  // CTAs per cluster
+    static constexpr int C = CC;  // CTAs per cluster (one sweep per cluster)
     static constexpr int NT = 512;
     static constexpr int RPC = 2 * BW / C;          // R op: rows per CTA (64 or 32)
     static constexpr int G = NT / RPC;              // R op: column groups
@@ -302,10 +302,11 @@ __device__ __forceinline__ void cluster_reflector(typename ChaseAr<S>::V *sv, in
     __syncthreads();
 }
 
-template <int BW, typename S>
-__global__ void __launch_bounds__(512) chase_cluster_kernel(typename ChaseAr<S>::St *ab, int64_t n, int64_t ldab,
-                                                            int *ticket, int *done, int *err) {
-    using Cfg = ChaseCfg<BW>;
+template <int BW, typename S, int CC>
+__global__ void __launch_bounds__(512) chase_cluster_kernel(typename ChaseAr<S>::St *ab_base, int64_t n, int64_t ldab,
+                                                            int *ticket, int *done_base, int *err, int batch,
+                                                            int64_t sAB, int64_t sDone) {
+    using Cfg = ChaseCfg<BW, CC>;
     using Ar = ChaseAr<S>;
     using V = typename Ar::V;
     cg::cluster_group cluster = cg::this_cluster();
@@ -317,14 +318,17 @@ __global__ void __launch_bounds__(512) chase_cluster_kernel(typename ChaseAr<S>:
     __shared__ V s_tau, s_beta;
     __shared__ int s_j;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    BandT<S> A{ab, ldab, 2 * BW - 1};
 
     for (;;) {
         if (q == 0 && tid == 0) s_j = atomicAdd(ticket, 1);
         cluster.sync();
-        const int64_t j = *cluster.map_shared_rank(&s_j, 0);
+        const int64_t tk = *cluster.map_shared_rank(&s_j, 0);
         cluster.sync();
+        // tickets are sweep-major over the batch: every matrix advances its own wavefront
+        const int64_t j = tk / batch, zb = tk % batch;
         if (j >= n - 1) return;
+        BandT<S> A{ab_base + zb * sAB, ldab, 2 * BW - 1};
+        int *done = done_base + zb * sDone;
         const int nsteps = (int)((n - j - 2) / BW) + 1;
         const int ops_prev = (j > 0) ? 2 * ((int)((n - j - 1) / BW) + 1) : 0;
         int64_t rho = j, c0 = j + 1;
@@ -447,10 +451,10 @@ __global__ void __launch_bounds__(512) chase_cluster_kernel(typename ChaseAr<S>:
     }
 }
 
-template <int BW, typename S>
+template <int BW, typename S, int CC = ChaseCfg<BW>::C>
 int launch_chase_cluster(typename ChaseAr<S>::St *dAB, int64_t n, int64_t ldab, const Stage2Work &w, cudaStream_t s,
-                         int num_sms) {
-    using Cfg = ChaseCfg<BW>;
+                         int num_sms, int batch = 1, int64_t sAB = 0, int64_t sDone = 0) {
+    using Cfg = ChaseCfg<BW, CC>;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -464,16 +468,17 @@ int launch_chase_cluster(typename ChaseAr<S>::St *dAB, int64_t n, int64_t ldab, 
     cfg.numAttrs = 1;
     int max_clusters = 0;
     cfg.gridDim = dim3(Cfg::C * 64);
-    if (cudaOccupancyMaxActiveClusters(&max_clusters, chase_cluster_kernel<BW, S>, &cfg) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveClusters(&max_clusters, chase_cluster_kernel<BW, S, CC>, &cfg) != cudaSuccess ||
         max_clusters <= 0) {
         cudaGetLastError();
         max_clusters = std::max(1, num_sms / Cfg::C);
     }
-    // Sweeps in flight are bounded by the wavefront: about (n / bw) / 2.
-    const int64_t want = std::max<int64_t>(1, (n / BW) / 2 + 2);
-    const int64_t clusters = std::min<int64_t>(std::min<int64_t>(want, max_clusters), n - 1);
+    // Sweeps in flight are bounded by the wavefront: about (n / bw) / 2 per matrix.
+    const int64_t want = std::max<int64_t>(1, ((n / BW) / 2 + 2) * (int64_t)batch);
+    const int64_t clusters = std::min<int64_t>(std::min<int64_t>(want, max_clusters), (n - 1) * (int64_t)batch);
     cfg.gridDim = dim3((unsigned)(clusters * Cfg::C));
-    AVS_CUDA_TRY(cudaLaunchKernelEx(&cfg, chase_cluster_kernel<BW, S>, dAB, n, ldab, w.flags, w.flags + 1, w.err));
+    AVS_CUDA_TRY(cudaLaunchKernelEx(&cfg, chase_cluster_kernel<BW, S, CC>, dAB, n, ldab, w.flags, w.flags + 1, w.err,
+                                    batch, sAB, sDone));
     return AVS_SUCCESS;
 }
 
@@ -633,5 +638,65 @@ template int stage2_chase_df<float>(const float *, int64_t, int64_t, int, float2
                                     const Stage2Work &, cudaStream_t, int, int64_t *);
 template int stage2_chase_df<double>(const double *, int64_t, int64_t, int, float2 *, int64_t, double *, double *,
                                      const Stage2Work &, cudaStream_t, int, int64_t *);
+
+// ---------------------------------------------------------------------------
+// Batched chase (double-float): `batch` matrices of the same order n and band
+// width bw, stacked at stride n*n (tiles) / ldab*n (band) / n+1 (flags) / n (d, e).
+namespace {
+template <typename T>
+__global__ void extract_band_df_batched(const T *a, int64_t n, int bw, float2 *ab, int64_t ldab) {
+    const int64_t c = blockIdx.x, zb = blockIdx.y;
+    const int ku = 2 * bw - 1;
+    const T *az = a + zb * n * n;
+    float2 *abz = ab + zb * ldab * n;
+    for (int i = threadIdx.x; i <= bw; i += blockDim.x) {
+        const int64_t r = c - bw + i;
+        if (r >= 0) abz[(ku + r - c) + c * ldab] = make_float2((float)az[r + c * n], 0.0f);
+    }
+}
+__global__ void bidiag_out_df_batched(const float2 *ab, int64_t n, int bw, int64_t ldab, double *d, double *e,
+                                      int batch) {
+    const int ku = 2 * bw - 1;
+    const int64_t total = n * (int64_t)batch;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t zb = g / n, i = g % n;
+        const float2 *abz = ab + zb * ldab * n;
+        const float2 x = abz[ku + i * ldab];
+        d[zb * n + i] = (double)x.x + (double)x.y;
+        if (i + 1 < n) {
+            const float2 y = abz[(ku - 1) + (i + 1) * ldab];
+            e[zb * n + i] = (double)y.x + (double)y.y;
+        } else {
+            e[zb * n + i] = 0.0;
+        }
+    }
+}
+}  // namespace
+
+int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
+                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches) {
+    AVS_CUDA_TRY(cudaMemsetAsync(dAB, 0, sizeof(float2) * (size_t)ldab * (size_t)n * batch, s));
+    extract_band_df_batched<float><<<dim3((unsigned)n, (unsigned)batch), 128, 0, s>>>(dW, n, bw, dAB, ldab);
+    AVS_CUDA_TRY(cudaGetLastError());
+    if (n >= 2) {
+        AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)((n + 1) * (int64_t)batch + 1), s));
+        int rc;
+        // small bands: one CTA per sweep (the batch supplies the parallelism)
+        switch (bw) {
+            case 16: rc = launch_chase_cluster<16, df64, 1>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
+            case 32: rc = launch_chase_cluster<32, df64, 1>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
+            case 64: rc = launch_chase_cluster<64, df64, 1>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
+            case 128: rc = launch_chase_cluster<128, df64, 2>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
+            case 256: rc = launch_chase_cluster<256, df64, 8>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
+            default: rc = AVS_ERR_UNSUPPORTED;
+        }
+        if (rc != AVS_SUCCESS) return rc;
+    }
+    const int nb = (int)std::min<int64_t>((n * batch + 255) / 256, 8192);
+    bidiag_out_df_batched<<<nb > 0 ? nb : 1, 256, 0, s>>>(dAB, n, bw, ldab, dd, de, batch);
+    AVS_CUDA_TRY(cudaGetLastError());
+    if (launches) *launches += 3;
+    return AVS_SUCCESS;
+}
 
 }  // namespace avs

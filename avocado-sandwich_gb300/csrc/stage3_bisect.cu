@@ -17,8 +17,8 @@
 namespace avs {
 namespace {
 
-// scratch[0] = Gershgorin bound of TGK, scratch[1] = pivmin
-__global__ void tgk_bound_kernel(const double *d, const double *e, int64_t n, double *scratch) {
+// scratch[0] = Gershgorin bound of TGK, scratch[1] = pivmin (one block).
+__device__ void tgk_bound_body(const double *d, const double *e, int64_t n, double *scratch) {
     __shared__ double sb[32], sm[32];
     double bound = 0.0, maxsq = 0.0;
     for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
@@ -46,6 +46,10 @@ __global__ void tgk_bound_kernel(const double *d, const double *e, int64_t n, do
         scratch[0] = b2;
         scratch[1] = DBL_MIN * fmax(m2, 1.0);
     }
+}
+
+__global__ void tgk_bound_kernel(const double *d, const double *e, int64_t n, double *scratch) {
+    tgk_bound_body(d, e, n, scratch);
 }
 
 // Pivot recurrence q_i = -x - a_i / q_{i-1} (a_i = squared off-diagonal of
@@ -197,14 +201,10 @@ __device__ __forceinline__ int tgk_count_f(const float2 *__restrict__ a, int64_t
     return cnt;
 }
 
-__global__ void bisect_df_kernel(const float2 *a, int64_t n, double rel_tol, const double *scratch, double *sigma) {
-    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    const double bound = scratch[0];
-    if (bound == 0.0) {
-        sigma[k] = 0.0;
-        return;
-    }
+// k-th largest singular value of the scaled problem (a = squared scaled
+// off-diagonals, bound = the scale), returned unscaled.
+__device__ double bisect_df_one(const float2 *a, int64_t n, int64_t k, double rel_tol, double bound) {
+    if (bound == 0.0) return 0.0;
     const int64_t m = 2 * n - 1;
     const float pivmin = 1e-36f;
     const int64_t target = 2 * n - 1 - k;
@@ -239,7 +239,13 @@ __global__ void bisect_df_kernel(const float2 *a, int64_t n, double rel_tol, con
             lo = mid;
     }
     const df64 c = df_add(lo, hi);
-    sigma[k] = bound * 0.5 * df_to_double(c);
+    return bound * 0.5 * df_to_double(c);
+}
+
+__global__ void bisect_df_kernel(const float2 *a, int64_t n, double rel_tol, const double *scratch, double *sigma) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    sigma[k] = bisect_df_one(a, n, k, rel_tol, scratch[0]);
 }
 
 template <typename T>
@@ -388,5 +394,55 @@ template int copy_convert_2d<float, double>(const float *, int64_t, double *, in
                                             cudaStream_t);
 template int copy_convert_2d<double, float>(const double *, int64_t, float *, int64_t, int64_t, int64_t,
                                             cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// Batched double-float bisection: `batch` bidiagonals of order n stacked at
+// stride n (d, e), singular values to dsigma (stride n).
+namespace {
+__global__ void tgk_bound_batched(const double *d, const double *e, int64_t n, double *scratch) {
+    const int64_t zb = blockIdx.x;
+    tgk_bound_body(d + zb * n, e + zb * n, n, scratch + zb * 4);
+}
+__global__ void tgk_prep_df_batched(const double *d, const double *e, int64_t n, int batch, const double *scratch,
+                                    float2 *a) {
+    const int64_t m = 2 * n - 1;
+    const int64_t total = m * (int64_t)batch;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t zb = g / m, i = g % m;
+        const double bnd = scratch[zb * 4];
+        const double inv = bnd > 0.0 ? 1.0 / bnd : 0.0;
+        const double off = ((i & 1) ? e[zb * n + (i >> 1)] : d[zb * n + (i >> 1)]) * inv;
+        const double sq = off * off;
+        const float h = (float)sq;
+        a[zb * (2 * n) + i] = make_float2(h, (float)(sq - (double)h));
+    }
+}
+__global__ void bisect_df_batched(const float2 *a, int64_t n, int batch, double rel_tol, const double *scratch,
+                                  double *sigma) {
+    const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (g >= n * (int64_t)batch) return;
+    const int64_t zb = g / n, k = g % n;
+    sigma[g] = bisect_df_one(a + zb * (2 * n), n, k, rel_tol, scratch[zb * 4]);
+}
+}  // namespace
+
+int stage3_bisect_df_batched(const double *dd, const double *de, int64_t n, int batch, double rel_tol,
+                             double *dsigma, double *dscratch, float2 *dpairs, cudaStream_t s, int64_t *launches) {
+    if (n <= 0 || batch <= 0) return AVS_SUCCESS;
+    if (!(rel_tol > 0.0)) rel_tol = 4e-14;
+    tgk_bound_batched<<<batch, 256, 0, s>>>(dd, de, n, dscratch);
+    AVS_CUDA_TRY(cudaGetLastError());
+    const int64_t total = (2 * n - 1) * (int64_t)batch;
+    tgk_prep_df_batched<<<(unsigned)std::min<int64_t>((total + 255) / 256, 8192), 256, 0, s>>>(dd, de, n, batch,
+                                                                                              dscratch, dpairs);
+    AVS_CUDA_TRY(cudaGetLastError());
+    const int64_t nv = n * (int64_t)batch;
+    const int threads = bisect_threads(nv);
+    bisect_df_batched<<<(unsigned)((nv + threads - 1) / threads), threads, 0, s>>>(dpairs, n, batch, rel_tol,
+                                                                                   dscratch, dsigma);
+    AVS_CUDA_TRY(cudaGetLastError());
+    if (launches) *launches += 3;
+    return AVS_SUCCESS;
+}
 
 }  // namespace avs

@@ -164,6 +164,32 @@ int avs_bidiag_svals_dev(avs_handle *h, int64_t n, const double *dd, const doubl
 int avs_bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *dsigma, double rel_tol,
                              void *stream);
 
+/* Batched singular values of `count` independent square FP32 matrices of mixed
+ * orders, all on the device (the many-small-matrices workload of RMT/rmt.jl:9-36,
+ * which calls LAPACK once per matrix).  Matrix i is n[i] x n[i], column-major
+ * with leading dimension lda[i], at dA[i]; its n[i] values go to dsigma[i]
+ * (descending, FP32).  tile[i] = 0 (or tile == NULL) lets the autotuner choose
+ * the tile for that order; otherwise the same "Not implemented" rules as
+ * avs_svdvals_dev_s apply per matrix.  Matrices of equal (n, tile) run as one
+ * group: stage-1 launches cover the whole group, one cluster chase kernel runs
+ * all the group's sweeps, one bisection kernel all its values.  Each group's
+ * launch sequence is captured once in a CUDA graph (kept per (n, tile, group
+ * size) on the handle) and replayed.  Results of a matrix do not depend on the
+ * other matrices of the call.  Precision: FP32 tiles with double-float stages
+ * 2 and 3 (the `precision` field of opts is ignored; bisect_rel_tol is used).
+ * The pointer arrays are host arrays.  The work runs on the handle's stream,
+ * after the work queued so far on opts->stream (when given); the call blocks
+ * until all values are written.  report->t_total_ms covers all groups. */
+int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
+                              const int32_t *tile, const float *const *dA, float *const *dsigma,
+                              const avs_opts *opts, avs_report *report);
+
+/* Autotuner of the batched path: times tiles 32, 64 and 128 (those that divide
+ * n with at least two tiles) on `sample` seeded random matrices of order n,
+ * stores the fastest on the handle (used for tile 0 in the batched call) and
+ * returns it in *best (may be NULL).  sample <= 0 means 16. */
+int avs_autotune_tile(avs_handle *h, int64_t n, int32_t sample, int32_t *best);
+
 /* Tile kernels, one tile (b x b, column-major, ld b), device pointers.
  * QR_unsafe_kernel! (QRkernels.jl:3-66): R above, unit-lower V below, tau[0..b-2]. */
 int avs_geqrt_tile_dev_s(avs_handle *h, int32_t b, float *dA, float *dtau);

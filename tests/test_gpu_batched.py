@@ -1,0 +1,109 @@
+"""GPU tests of the batched path (many independent matrices of mixed orders in
+one call): every matrix's values equal those of the single-matrix call on the
+same input (same kernels, batch-invariant arithmetic), agree with LAPACK
+within the FP32 tolerance, and do not depend on the other matrices of the
+call.  The workload shape follows the many-small-SVDs client of the reference
+(RMT/rmt.jl:9-36)."""
+import numpy as np
+import pytest
+import scipy.linalg as sl
+
+pytestmark = pytest.mark.gpu
+
+TOL32 = 1e-5
+
+
+def rel_err(got, ref):
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    return float(np.max(np.abs(got - ref)) / max(np.max(np.abs(ref)), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _mats(avs_mod, sizes, seed):
+    rng = np.random.default_rng(seed)
+    hosts = [(rng.standard_normal((n, n)) / np.sqrt(n)).astype(np.float32) for n in sizes]
+    return hosts, [avs_mod.to_device(a) for a in hosts]
+
+
+@pytest.mark.parametrize("tile", [16, 32, 64])
+def test_batched_equals_single(avs_mod, torch_cuda, tile):
+    sizes = [64, 128, 64, 256, 128, 64, 192, 256]
+    sizes = [n for n in sizes if n % tile == 0]
+    hosts, devs = _mats(avs_mod, sizes, 11 + tile)
+    outs = avs_mod.svdvals_batched(devs, tiles=tile)
+    for a, d, o in zip(hosts, devs, outs):
+        single = avs_mod.my_CU_svdval(d, tile).cpu().numpy()
+        got = o.cpu().numpy()
+        assert np.array_equal(got, single), rel_err(got, single)
+        ref = sl.svdvals(a.astype(np.float64))
+        assert rel_err(got, ref) < TOL32
+        assert np.all(np.diff(got) <= 0)
+
+
+def test_batched_tile128(avs_mod, torch_cuda):
+    """Tiles >= 128 take the full compact-WY update in the batch too."""
+    sizes = [256, 512, 256]
+    hosts, devs = _mats(avs_mod, sizes, 77)
+    outs = avs_mod.svdvals_batched(devs, tiles=128)
+    for a, d, o in zip(hosts, devs, outs):
+        got = o.cpu().numpy()
+        assert np.array_equal(got, avs_mod.my_CU_svdval(d, 128).cpu().numpy())
+        assert rel_err(got, sl.svdvals(a.astype(np.float64))) < TOL32
+
+
+def test_batched_solo_vs_mix(avs_mod, torch_cuda):
+    """A matrix gives bit-identical values alone and inside a mixed batch."""
+    hosts, devs = _mats(avs_mod, [128, 64, 128, 256, 128, 64], 5)
+    mix = avs_mod.svdvals_batched(devs, tiles=[32, 32, 64, 32, 32, 16])
+    for i, d in enumerate(devs):
+        tile = [32, 32, 64, 32, 32, 16][i]
+        solo = avs_mod.svdvals_batched([d], tiles=tile)[0]
+        assert torch_cuda.equal(solo, mix[i])
+
+
+def test_batched_autotune(avs_mod, torch_cuda):
+    h = avs_mod.Handle()
+    try:
+        t = avs_mod.autotune_tile(256, sample=8, handle=h)
+        assert t in (32, 64, 128)
+        hosts, devs = _mats(avs_mod, [256, 128, 256], 9)
+        outs = avs_mod.svdvals_batched(devs, tiles=None, handle=h)
+        for a, o in zip(hosts, outs):
+            assert rel_err(o.cpu().numpy(), sl.svdvals(a.astype(np.float64))) < TOL32
+    finally:
+        h.close()
+
+
+def test_batched_graph_replay_and_report(avs_mod, torch_cuda):
+    """Repeated calls replay the captured graphs and give the same values; the
+    report counts the kernels of every group."""
+    hosts, devs = _mats(avs_mod, [64, 128, 64], 3)
+    r = avs_mod.Report()
+    first = avs_mod.svdvals_batched(devs, tiles=32, report=r)
+    assert r.kernel_launches > 0 and r.t_total_ms > 0
+    second = avs_mod.svdvals_batched(devs, tiles=32)
+    for x, y in zip(first, second):
+        assert torch_cuda.equal(x, y)
+
+
+def test_batched_edge_cases(avs_mod, torch_cuda):
+    assert avs_mod.svdvals_batched([]) == []
+    _, devs = _mats(avs_mod, [96], 1)
+    with pytest.raises(NotImplementedError):
+        avs_mod.svdvals_batched(devs, tiles=64)  # 64 does not divide 96
+    with pytest.raises(NotImplementedError):
+        avs_mod.svdvals_batched(devs, tiles=24)  # not a power of two
+    rect = torch_cuda.zeros((64, 32), device="cuda", dtype=torch_cuda.float32)
+    with pytest.raises(NotImplementedError):
+        avs_mod.svdvals_batched([rect], tiles=16)
+    z = torch_cuda.zeros((64, 64), device="cuda", dtype=torch_cuda.float32)
+    out = avs_mod.svdvals_batched([z], tiles=16)[0]
+    assert torch_cuda.count_nonzero(out).item() == 0
