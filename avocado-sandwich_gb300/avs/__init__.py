@@ -31,7 +31,8 @@ import numpy as np
 __all__ = [
     "AvsError", "Handle", "lib", "library_path", "my_CU_svdval", "svdvals", "Blockbidiag", "extract_band",
     "bidiagonalize", "diag_lapack", "geqrt_tile", "tsqrt_tile", "to_device", "from_device", "PREC",
-    "NOT_IMPLEMENTED", "EXPORTED_SYMBOLS", "Report", "svdvals_batched", "autotune_tile",
+    "NOT_IMPLEMENTED", "EXPORTED_SYMBOLS", "Report", "svdvals_batched", "autotune_tile", "Server",
+    "estimate_bytes",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -47,7 +48,8 @@ EXPORTED_SYMBOLS = [
     "avs_blockbidiag_dev_s", "avs_blockbidiag_dev_d", "avs_extract_band_dev_s", "avs_extract_band_dev_d",
     "avs_band_to_bidiag_dev", "avs_bidiag_svals_dev", "avs_bidiag_svals_noalloc",
     "avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d", "avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d",
-    "avs_svdvals_batched_dev_s", "avs_autotune_tile",
+    "avs_svdvals_batched_dev_s", "avs_autotune_tile", "avs_trim", "avs_workspace_bytes", "avs_estimate_bytes",
+    "avs_serve_create", "avs_serve_submit", "avs_serve_wait", "avs_serve_stats_get", "avs_serve_destroy",
 ]
 
 
@@ -61,6 +63,22 @@ class Report(ctypes.Structure):
                 ("t_stage3_ms", ctypes.c_double), ("t_h2d_ms", ctypes.c_double), ("t_d2h_ms", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int64), ("workspace_bytes", ctypes.c_int64),
                 ("precision", ctypes.c_int32), ("status", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("workers", ctypes.c_int32), ("max_batch", ctypes.c_int32),
+                ("autotune", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_int64)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("failed", ctypes.c_int64),
+                ("queued", ctypes.c_int64), ("batches", ctypes.c_int64), ("p50_ms", ctypes.c_double),
+                ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
+                ("throughput_rps", ctypes.c_double), ("mean_batch", ctypes.c_double),
+                ("peak_bytes", ctypes.c_int64), ("budget_bytes", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -104,6 +122,14 @@ def lib():
         L.avs_bidiag_svals_noalloc.argtypes = [I64, P, P, P, ctypes.c_double, P]
         L.avs_svdvals_batched_dev_s.argtypes = [P, I32, P, P, P, P, P, OP, RP]
         L.avs_autotune_tile.argtypes = [P, I64, I32, ctypes.POINTER(ctypes.c_int32)]
+        L.avs_trim.argtypes = [P]
+        L.avs_workspace_bytes.argtypes = [P, ctypes.POINTER(I64), ctypes.POINTER(I64)]
+        L.avs_estimate_bytes.argtypes = [I64, I32, I32, I32, ctypes.POINTER(I64)]
+        L.avs_serve_create.argtypes = [ctypes.POINTER(P), ctypes.POINTER(ServeConfig)]
+        L.avs_serve_submit.argtypes = [P, I64, I64, I32, I32, P, P, ctypes.POINTER(I64)]
+        L.avs_serve_wait.argtypes = [P, I64, ctypes.c_double, ctypes.POINTER(I32), ctypes.POINTER(ctypes.c_double)]
+        L.avs_serve_stats_get.argtypes = [P, ctypes.POINTER(ServeStats)]
+        L.avs_serve_destroy.argtypes = [P]
         for nm in ("avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d"):
             getattr(L, nm).argtypes = [P, I32, P, P]
         for nm in ("avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d"):
@@ -363,3 +389,77 @@ def tsqrt_tile(r, bt, handle=None):
     _check(fn(h.ptr, b, ctypes.c_void_p(tr.data_ptr()), ctypes.c_void_p(tb.data_ptr()),
               ctypes.c_void_p(tau.data_ptr())), "avs_tsqrt_tile_dev")
     return from_device(tr), from_device(tb), tau.cpu().numpy()
+
+
+def estimate_bytes(n, tile, precision="fp32", count=0):
+    """Device workspace of one call (count 0) or of one batched FP32 group of ``count``."""
+    b = ctypes.c_int64(0)
+    _check(lib().avs_estimate_bytes(int(n), int(tile), _prec(precision), int(count), ctypes.byref(b)),
+           "avs_estimate_bytes")
+    return b.value
+
+
+class Server:
+    """SVD request server with continuous batching (``avs_serve_*`` in avs.h).
+
+    ``submit(A)`` queues a host matrix (numpy float32 / float64, square) and
+    returns a request id; ``wait(id)`` blocks until its values are ready and
+    returns ``(sigma, latency_ms)``.  Several execution slots run groups
+    concurrently on the GPU; FP32 requests of the same order that are queued
+    together run as one batched call.  ``stats()`` gives p50/p99 latency,
+    throughput and the device memory held against the admission budget.
+    """
+
+    def __init__(self, device=0, workers=4, max_batch=512, autotune=False, hbm_budget_bytes=0):
+        cfg = ServeConfig(device, workers, max_batch, 1 if autotune else 0, int(hbm_budget_bytes))
+        p = ctypes.c_void_p()
+        _check(lib().avs_serve_create(ctypes.byref(p), ctypes.byref(cfg)), "avs_serve_create")
+        self.ptr = p
+        self._live = {}
+
+    def submit(self, A, tile=0):
+        a = np.asfortranarray(A)
+        if a.ndim != 2 or a.shape[0] != a.shape[1]:
+            raise NotImplementedError("Not implemented")
+        if a.dtype not in (np.float32, np.float64):
+            raise TypeError("float32 / float64 only")
+        out = np.empty(a.shape[0], dtype=a.dtype)
+        rid = ctypes.c_int64(0)
+        dt = 1 if a.dtype == np.float64 else 0
+        rc = lib().avs_serve_submit(self.ptr, a.shape[0], max(a.shape[0], 1), dt, int(tile),
+                                    ctypes.c_void_p(a.ctypes.data), ctypes.c_void_p(out.ctypes.data),
+                                    ctypes.byref(rid))
+        _check(rc, "avs_serve_submit")
+        self._live[rid.value] = (a, out)
+        return rid.value
+
+    def wait(self, rid, timeout_ms=-1.0):
+        st = ctypes.c_int32(0)
+        lat = ctypes.c_double(0.0)
+        rc = lib().avs_serve_wait(self.ptr, int(rid), float(timeout_ms), ctypes.byref(st), ctypes.byref(lat))
+        a, out = self._live.pop(rid, (None, None)) if rc != 3 else self._live.get(rid, (None, None))
+        _check(rc, "avs_serve_wait")
+        return out, lat.value
+
+    def stats(self):
+        s = ServeStats()
+        _check(lib().avs_serve_stats_get(self.ptr, ctypes.byref(s)), "avs_serve_stats_get")
+        return s.as_dict()
+
+    def close(self):
+        if self.ptr:
+            lib().avs_serve_destroy(self.ptr)
+            self.ptr = None
+            self._live.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

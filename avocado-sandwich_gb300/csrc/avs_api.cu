@@ -32,8 +32,20 @@ struct avs_handle {
     size_t bws_bytes = 0;
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
-    std::map<std::tuple<int64_t, int, int>, cudaGraphExec_t> graphs;
-    std::map<std::tuple<int64_t, int, int>, int64_t> graph_launches;  // kernels per graph
+    struct Graph {
+        cudaGraphExec_t exec = nullptr;
+        int64_t kernels = 0;
+        cudaEvent_t ev[4] = {};  // recorded inside the graph: start, after stage 1, 2, 3
+    };
+    std::map<std::tuple<int64_t, int, int>, Graph> graphs;
+    void drop_graphs() {
+        for (auto &kv : graphs) {
+            cudaGraphExecDestroy(kv.second.exec);
+            for (cudaEvent_t e : kv.second.ev)
+                if (e) cudaEventDestroy(e);
+        }
+        graphs.clear();
+    }
     std::map<int64_t, int> tuned;
 };
 
@@ -381,7 +393,7 @@ int avs_destroy(avs_handle *h) {
     for (auto &e : h->ev)
         if (e) cudaEventDestroy(e);
     if (h->h_err) cudaFreeHost(h->h_err);
-    for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second);
+    h->drop_graphs();
     if (h->bws) cudaFree(h->bws);
     if (h->pinned) cudaFreeHost(h->pinned);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -689,9 +701,7 @@ __global__ void scatter_kernel(const double *sig, float *const *dst, int64_t n, 
 int ensure_bws(avs_handle *h, size_t bytes) {
     if (h->bws_bytes >= bytes) return AVS_SUCCESS;
     cudaStreamSynchronize(h->stream);
-    for (auto &kv : h->graphs) cudaGraphExecDestroy(kv.second);  // graphs hold old pointers
-    h->graphs.clear();
-    h->graph_launches.clear();
+    h->drop_graphs();  // graphs hold pointers into the old workspace
     if (h->bws) cudaFree(h->bws);
     h->bws = nullptr;
     h->bws_bytes = 0;
@@ -717,7 +727,7 @@ int ensure_pinned(avs_handle *h, size_t bytes) {
 
 // The launches of one group (gather .. scatter), captured once per shape.
 int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cnt, double tol, cudaStream_t s,
-                   int64_t *launches) {
+                   const cudaEvent_t *ev, int64_t *launches) {
     char *base = reinterpret_cast<char *>(h->bws);
     float *W = reinterpret_cast<float *>(base + L.W);
     const float *const *src = reinterpret_cast<const float *const *>(base + L.ptrs);
@@ -725,6 +735,7 @@ int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cn
     const int64_t *lds = reinterpret_cast<const int64_t *>(base + L.ptrs + 2 * sizeof(void *) * cnt);
     int *err = reinterpret_cast<int *>(base + L.err);
     const int64_t nt = n / b;
+    AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[0], s, cudaEventRecordExternal));
     AVS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
     gather_kernel<<<dim3((unsigned)std::min<int64_t>(n, 1024), (unsigned)cnt), 256, 0, s>>>(src, lds, W, n);
     AVS_CUDA_TRY(cudaGetLastError());
@@ -742,6 +753,7 @@ int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cn
     w1.sFlags = nt + 4;
     int rc = stage1_ge2bnd<float>(W, n, n, b, w1, s, launches);
     if (rc != AVS_SUCCESS) return rc;
+    AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[1], s, cudaEventRecordExternal));
     Stage2Work w2;
     w2.flags = reinterpret_cast<int *>(base + L.f2);
     w2.err = err;
@@ -750,12 +762,14 @@ int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cn
     rc = stage2_chase_df_batched(W, n, b, cnt, reinterpret_cast<float2 *>(base + L.ab), 3 * (int64_t)b, dd, de, w2, s,
                                  h->num_sms, launches);
     if (rc != AVS_SUCCESS) return rc;
+    AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal));
     double *sig = reinterpret_cast<double *>(base + L.sig);
     rc = stage3_bisect_df_batched(dd, de, n, cnt, tol, sig, reinterpret_cast<double *>(base + L.scr),
                                   reinterpret_cast<float2 *>(base + L.pairs), s, launches);
     if (rc != AVS_SUCCESS) return rc;
     scatter_kernel<<<(unsigned)std::min<int64_t>((n * cnt + 255) / 256, 8192), 256, 0, s>>>(sig, dst, n, cnt);
     AVS_CUDA_TRY(cudaGetLastError());
+    AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal));
     if (launches) *launches += 2;
     return AVS_SUCCESS;
 }
@@ -828,6 +842,7 @@ extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int
     int rc;
     if ((rc = ensure_bws(h, need)) != AVS_SUCCESS) return rc;
     if ((rc = ensure_pinned(h, pin_need)) != AVS_SUCCESS) return rc;
+    if (h->graphs.size() > 256) h->drop_graphs();  // bound the cache of group shapes
     cudaStream_t s = h->stream;  // graphs are captured and replayed on the handle's stream
     if (opts && opts->stream) {  // order after the caller's work on its stream
         AVS_CUDA_TRY(cudaEventRecord(h->ev[4], reinterpret_cast<cudaStream_t>(opts->stream)));
@@ -840,6 +855,7 @@ extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int
     AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
     int64_t launches = 0;
     size_t gi = 0;
+    std::vector<const avs_handle::Graph *> ran;
     for (auto &g : groups) {
         const int64_t gn = g.first.first;
         const int gb = g.first.second;
@@ -856,22 +872,26 @@ extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int
         const auto key = std::make_tuple(gn, gb, cnt);
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
+            avs_handle::Graph gr;
+            for (cudaEvent_t &e : gr.ev) AVS_CUDA_TRY(cudaEventCreate(&e));
             cudaGraph_t graph;
             AVS_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            int64_t l = 0;
-            rc = group_launches(h, L, gn, gb, cnt, tol, s, &l);
-            h->graph_launches[key] = l;
+            rc = group_launches(h, L, gn, gb, cnt, tol, s, gr.ev, &gr.kernels);
             cudaError_t ce = cudaStreamEndCapture(s, &graph);
-            if (rc != AVS_SUCCESS) return rc;
-            AVS_CUDA_TRY(ce);
-            cudaGraphExec_t exec;
-            ce = cudaGraphInstantiate(&exec, graph, 0);
-            cudaGraphDestroy(graph);
-            AVS_CUDA_TRY(ce);
-            it = h->graphs.emplace(key, exec).first;
+            if (rc == AVS_SUCCESS && ce == cudaSuccess) {
+                ce = cudaGraphInstantiate(&gr.exec, graph, 0);
+                cudaGraphDestroy(graph);
+            }
+            if (rc != AVS_SUCCESS || ce != cudaSuccess) {
+                for (cudaEvent_t e : gr.ev) cudaEventDestroy(e);
+                if (rc != AVS_SUCCESS) return rc;
+                AVS_CUDA_TRY(ce);
+            }
+            it = h->graphs.emplace(key, gr).first;
         }
-        AVS_CUDA_TRY(cudaGraphLaunch(it->second, s));
-        launches += h->graph_launches[key];
+        AVS_CUDA_TRY(cudaGraphLaunch(it->second.exec, s));
+        launches += it->second.kernels;
+        ran.push_back(&it->second);
         AVS_CUDA_TRY(cudaMemcpyAsync(h_status + 16 * gi, reinterpret_cast<char *>(h->bws) + L.err, sizeof(int),
                                      cudaMemcpyDeviceToHost, s));
         tab += 3 * cnt;
@@ -894,6 +914,11 @@ extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int
     }
     if (rep) {
         rep->t_total_ms = ev_ms(h->ev[0], h->ev[1]);
+        for (const avs_handle::Graph *g : ran) {
+            rep->t_stage1_ms += ev_ms(g->ev[0], g->ev[1]);
+            rep->t_stage2_ms += ev_ms(g->ev[1], g->ev[2]);
+            rep->t_stage3_ms += ev_ms(g->ev[2], g->ev[3]);
+        }
         rep->kernel_launches = launches;
         rep->workspace_bytes = (int64_t)h->bws_bytes;
         rep->precision = AVS_PREC_FP32;
@@ -951,5 +976,44 @@ extern "C" int avs_autotune_tile(avs_handle *h, int64_t n, int32_t sample, int32
     if (rc != AVS_SUCCESS) return rc;
     h->tuned[n] = bt;
     if (best) *best = bt;
+    return AVS_SUCCESS;
+}
+
+// ===========================================================================
+// Memory accounting helpers (used by admission control of the serving loop).
+extern "C" int avs_trim(avs_handle *h) {
+    if (!h) return -1;
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    AVS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    h->drop_graphs();
+    if (h->ws) cudaFree(h->ws);
+    if (h->bws) cudaFree(h->bws);
+    if (h->pinned) cudaFreeHost(h->pinned);
+    h->ws = h->bws = h->pinned = nullptr;
+    h->ws_bytes = h->bws_bytes = h->pinned_bytes = 0;
+    return AVS_SUCCESS;
+}
+
+extern "C" int avs_workspace_bytes(avs_handle *h, int64_t *single_bytes, int64_t *batched_bytes) {
+    if (!h) return -1;
+    if (single_bytes) *single_bytes = (int64_t)h->ws_bytes;
+    if (batched_bytes) *batched_bytes = (int64_t)h->bws_bytes;
+    return AVS_SUCCESS;
+}
+
+extern "C" int avs_estimate_bytes(int64_t n, int32_t tile, int32_t precision, int32_t count, int64_t *bytes) {
+    if (n < 0) return -1;
+    if (!is_pow2(tile) || tile < 16 || (n > 0 && n % tile != 0) || tile > n) return AVS_ERR_NOT_IMPLEMENTED;
+    if (tile > kMaxTile) return AVS_ERR_UNSUPPORTED;
+    if (count < 0) return -4;
+    if (!bytes) return -5;
+    if (count >= 1) {  // batched FP32 group
+        *bytes = (int64_t)batch_layout(n, tile, count).total;
+        return AVS_SUCCESS;
+    }
+    const int prec = resolve_precision(precision, true);
+    const size_t elem = storage_elem(prec);
+    if (elem == 0) return AVS_ERR_UNSUPPORTED;
+    *bytes = (int64_t)make_layout(n, tile, elem, elem, tc_split_of(prec, tile) > 0).total;
     return AVS_SUCCESS;
 }

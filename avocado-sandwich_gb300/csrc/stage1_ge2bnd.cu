@@ -630,7 +630,7 @@ __global__ void __launch_bounds__(kNT) update_kernel(UpdateArgs args) {
 template <typename T, int LAYOUT>
 int launch_panel(T *dA, int64_t lda, int b, int pr, int pc, int P, int first_role, const Stage1Work &w,
                  cudaStream_t s) {
-    static bool attr_set = false;
+    static std::atomic<bool> attr_set{false};
     const size_t smem = panel3_smem_bytes<T>(b);
     if (!attr_set) {
         AVS_CUDA_TRY(cudaFuncSetAttribute(panel3_kernel<T, LAYOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -665,7 +665,7 @@ template <typename T, int LAYOUT>
 int launch_update(T *dA, int64_t lda, int64_t n, int b, int pr, int pc, int P, const Stage1Work &w,
                   cudaStream_t s) {
     const int width = sizeof(T) == 8 ? 32 : 64;
-    static bool attr_set = false;
+    static std::atomic<bool> attr_set{false};
     if (!attr_set) {
         AVS_CUDA_TRY(cudaFuncSetAttribute(update_kernel<T, LAYOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)update_smem_bytes<T>(256, width)));

@@ -381,7 +381,7 @@ size_t upd_full_smem() {
 template <typename T, int LAYOUT, int B>
 int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const Stage1Work &w, cudaStream_t s) {
     using C = UCfg<T, B>;
-    static bool attr = false;
+    static std::atomic<bool> attr{false};
     const size_t smem = upd_full_smem<T, B>();
     if (!attr) {
         AVS_CUDA_TRY(cudaFuncSetAttribute(update_full_kernel<T, LAYOUT, B>,
@@ -399,7 +399,7 @@ int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const 
 
 template <typename T, int LAYOUT>
 int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const Stage1Work &w, cudaStream_t s) {
-    static bool attr = false;
+    static std::atomic<bool> attr{false};
     const size_t smem = sizeof(T) * (size_t)32 * (256 + 1) > sizeof(T) * (size_t)256 * 256 / 16
                             ? sizeof(T) * (size_t)32 * (256 + 1)
                             : sizeof(T) * (size_t)256 * 16;

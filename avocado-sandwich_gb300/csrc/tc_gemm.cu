@@ -291,7 +291,7 @@ __global__ void __launch_bounds__(NT) tc_gemm_kernel(GemmArgs g) {
 int tc_gemm(const tc::GemmArgs &a, int batch, cudaStream_t s) {
     if (a.M % tc::BM || a.N % tc::BN || a.K % tc::BK || batch <= 0) return AVS_ERR_INTERNAL;
     const int smem = (a.split == 3 ? 4 : 2) * tc::TILE_BYTES * tc::STAGES + 1024 + tc::SMEM_PAD;
-    static bool attr = false;
+    static std::atomic<bool> attr{false};
     if (!attr) {
         AVS_CUDA_TRY(cudaFuncSetAttribute(tc::tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           4 * tc::TILE_BYTES * tc::STAGES + 1024 + tc::SMEM_PAD));

@@ -190,6 +190,65 @@ int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, co
  * returns it in *best (may be NULL).  sample <= 0 means 16. */
 int avs_autotune_tile(avs_handle *h, int64_t n, int32_t sample, int32_t *best);
 
+/* Release the handle's cached device workspace, pinned tables and captured
+ * graphs (the handle stays usable; the next call allocates again). */
+int avs_trim(avs_handle *h);
+/* Device bytes the handle currently holds: the workspace of the single-matrix
+ * entry points and that of the batched entry point (either pointer may be NULL). */
+int avs_workspace_bytes(avs_handle *h, int64_t *single_bytes, int64_t *batched_bytes);
+/* Device workspace one call needs: count == 0 -> one avs_svdvals_{s,d} call of
+ * order n with this tile and precision; count >= 1 -> one batched FP32 group of
+ * `count` matrices of order n (the caller's inputs and outputs not included). */
+int avs_estimate_bytes(int64_t n, int32_t tile, int32_t precision, int32_t count, int64_t *bytes);
+
+/* ---- serving loop ---------------------------------------------------------------
+ * An SVD request server with continuous batching (no counterpart in the
+ * reference, whose entry point is one blocking call).  Requests (host matrices,
+ * FP32 or FP64, any supported order) are queued by avs_serve_submit and run by
+ * `workers` execution slots, each with its own handle and CUDA stream, so the
+ * work of several requests overlaps on the GPU.  A free slot takes the oldest
+ * queued request and, for FP32, every other queued FP32 request of the same
+ * order (up to max_batch) into one batched call.  Admission is by device
+ * memory: a slot starts a group only while the bytes held by all slots stay
+ * within hbm_budget_bytes; otherwise it shrinks the group, releases its own
+ * cached workspace, or waits until others finish.  Each result equals the
+ * result of the same request served alone (the batched kernels are
+ * batch-invariant).  Latency = completion - submission (host steady clock). */
+typedef struct avs_server avs_server;
+
+#define AVS_DTYPE_F32 0
+#define AVS_DTYPE_F64 1
+
+typedef struct avs_serve_config {
+    int32_t device;
+    int32_t workers;          /* execution slots (0 = 4) */
+    int32_t max_batch;        /* requests per batched group (0 = 512) */
+    int32_t autotune;         /* 1 = autotune FP32 tiles per order, 0 = fixed rule */
+    int64_t hbm_budget_bytes; /* 0 = 80% of the device memory free at creation */
+} avs_serve_config;
+
+typedef struct avs_serve_stats {
+    int64_t submitted, completed, failed, queued, batches;
+    double p50_ms, p99_ms, mean_ms, max_ms; /* latency of completed requests */
+    double throughput_rps;                  /* completed / (last completion - first submission) */
+    double mean_batch;                      /* requests per group */
+    int64_t peak_bytes;                     /* peak device bytes held by the slots */
+    int64_t budget_bytes;
+} avs_serve_stats;
+
+int avs_serve_create(avs_server **srv, const avs_serve_config *cfg);
+/* Queue one request: n x n column-major A (ld lda) of type dtype in host memory,
+ * n values to sigma (same type).  Both buffers must stay valid until the request
+ * completes.  tile = 0 picks the tile.  Returns its id in *id. */
+int avs_serve_submit(avs_server *srv, int64_t n, int64_t lda, int32_t dtype, int32_t tile, const void *A, void *sigma,
+                     int64_t *id);
+/* Block until request id completes; its status and latency (ms) are returned.
+ * timeout_ms < 0 waits forever; a timeout returns AVS_ERR_TIMEOUT. */
+int avs_serve_wait(avs_server *srv, int64_t id, double timeout_ms, int32_t *status, double *latency_ms);
+int avs_serve_stats_get(avs_server *srv, avs_serve_stats *out);
+/* Drain the queue, stop the slots and free everything. */
+int avs_serve_destroy(avs_server *srv);
+
 /* Tile kernels, one tile (b x b, column-major, ld b), device pointers.
  * QR_unsafe_kernel! (QRkernels.jl:3-66): R above, unit-lower V below, tau[0..b-2]. */
 int avs_geqrt_tile_dev_s(avs_handle *h, int32_t b, float *dA, float *dtau);

@@ -68,3 +68,32 @@ def test_workloads_are_seeded():
     np.testing.assert_allclose(np.linalg.svd(a, compute_uv=False), s, rtol=1e-9, atol=1e-14)
     sz = workloads.batch_sizes(4096, 5)
     assert set(np.unique(sz)) <= {64, 128, 256, 512, 1024}
+
+
+def test_estimate_bytes_host_logic(avs_mod):
+    """Workspace estimates are pure host arithmetic: monotone in n and in the
+    group size, and the reference's "Not implemented" rules apply."""
+    e1 = avs_mod.estimate_bytes(1024, 64, "fp32", 0)
+    e2 = avs_mod.estimate_bytes(2048, 64, "fp32", 0)
+    assert 0 < e1 < e2
+    g1 = avs_mod.estimate_bytes(256, 32, "fp32", 1)
+    g8 = avs_mod.estimate_bytes(256, 32, "fp32", 8)
+    assert 0 < g1 < g8 and g8 >= 8 * 256 * 256 * 4
+    assert avs_mod.estimate_bytes(1024, 64, "fp64", 0) > e1
+    with pytest.raises(NotImplementedError):
+        avs_mod.estimate_bytes(96, 64, "fp32", 0)
+    with pytest.raises(NotImplementedError):
+        avs_mod.estimate_bytes(96, 24, "fp32", 0)
+
+
+def test_serve_and_batched_without_gpu(avs_mod):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    lib = avs_mod.lib()
+    p = ctypes.c_void_p()
+    assert lib.avs_serve_create(ctypes.byref(p), None) == 5  # AVS_ERR_NO_DEVICE
+    assert lib.avs_serve_submit(None, 64, 64, 0, 0, None, None, None) == -1
+    assert lib.avs_svdvals_batched_dev_s(None, 1, None, None, None, None, None, None, None) == -1
+    with pytest.raises(avs_mod.AvsError):
+        avs_mod.Server()

@@ -1,0 +1,97 @@
+"""GPU tests of the serving loop (avs_serve_* in avs.h): mixed FP32/FP64
+requests of several orders submitted together are batched and overlapped, and
+every result is bit-identical to the same request served alone and to the
+single-matrix entry point; admission keeps the held device memory within the
+budget and fails a request that can never fit."""
+import numpy as np
+import pytest
+import scipy.linalg as sl
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def rule_tile(n):
+    t = 32 if n <= 256 else (64 if n <= 1024 else 128)
+    while t > 16 and (n % t or t > n):
+        t //= 2
+    return t
+
+
+def _requests(seed):
+    rng = np.random.default_rng(seed)
+    spec = [(128, np.float32), (256, np.float64), (128, np.float32), (512, np.float32), (256, np.float32),
+            (128, np.float64), (128, np.float32), (512, np.float64), (256, np.float32), (1024, np.float32)]
+    return [(rng.standard_normal((n, n)) / np.sqrt(n)).astype(dt) for n, dt in spec]
+
+
+def test_serving_mix_equals_solo(avs_mod, torch_cuda):
+    mats = _requests(1)
+    with avs_mod.Server(workers=3) as srv:
+        ids = [srv.submit(a) for a in mats]
+        outs = [srv.wait(i) for i in ids]
+        st = srv.stats()
+    assert st["completed"] == len(mats) and st["failed"] == 0
+    assert st["batches"] <= len(mats) and 0 < st["p50_ms"] <= st["p99_ms"] <= st["max_ms"]
+    for a, (sig, lat) in zip(mats, outs):
+        assert lat > 0
+        single = avs_mod.my_CU_svdval(a, rule_tile(a.shape[0]))
+        assert np.array_equal(sig, single)
+        tol = 1e-12 if a.dtype == np.float64 else 1e-5
+        ref = sl.svdvals(a.astype(np.float64))
+        assert np.max(np.abs(sig - ref)) / ref[0] < tol
+    # each request alone in a fresh server
+    with avs_mod.Server(workers=1) as srv:
+        for a, (sig, _) in zip(mats, outs):
+            solo, _ = srv.wait(srv.submit(a))
+            assert np.array_equal(solo, sig)
+
+
+def test_serving_groups_same_order(avs_mod, torch_cuda):
+    """Requests of one order queued together run as few groups."""
+    rng = np.random.default_rng(3)
+    mats = [(rng.standard_normal((128, 128)) / np.sqrt(128)).astype(np.float32) for _ in range(64)]
+    with avs_mod.Server(workers=1) as srv:
+        ids = [srv.submit(a) for a in mats]
+        outs = [srv.wait(i)[0] for i in ids]
+        st = srv.stats()
+    assert st["completed"] == 64 and st["mean_batch"] > 2
+    for a, s in zip(mats, outs):
+        assert np.array_equal(s, avs_mod.my_CU_svdval(a, 32))
+
+
+def test_serving_admission_budget(avs_mod, torch_cuda):
+    n = 256
+    budget = avs_mod.estimate_bytes(n, 32, "fp32", 4) + 4 * (n * n + n) * 4 + 4096
+    rng = np.random.default_rng(4)
+    mats = [(rng.standard_normal((n, n)) / np.sqrt(n)).astype(np.float32) for _ in range(16)]
+    big = rng.standard_normal((2048, 2048)).astype(np.float32)
+    with avs_mod.Server(workers=2, hbm_budget_bytes=budget) as srv:
+        ids = [srv.submit(a) for a in mats]
+        for i, a in zip(ids, mats):
+            s, _ = srv.wait(i)
+            assert np.array_equal(s, avs_mod.my_CU_svdval(a, 32))
+        bid = srv.submit(big)
+        with pytest.raises(avs_mod.AvsError) as ei:
+            srv.wait(bid)
+        assert ei.value.status == 2  # AVS_ERR_OOM: larger than the whole budget
+        st = srv.stats()
+    assert st["peak_bytes"] <= budget
+    assert st["completed"] == 16 and st["failed"] == 1
+
+
+def test_serving_rejects_invalid(avs_mod, torch_cuda):
+    with avs_mod.Server(workers=1) as srv:
+        with pytest.raises(NotImplementedError):
+            srv.submit(np.zeros((96, 96), np.float32), tile=64)
+        with pytest.raises(NotImplementedError):
+            srv.submit(np.zeros((64, 32), np.float32))
+        z, _ = srv.wait(srv.submit(np.zeros((64, 64), np.float32)))
+        assert not np.any(z)
