@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "avs_common.cuh"
+#include "tc_gemm.cuh"
 
 namespace avs {
 static thread_local cudaError_t g_last_cuda = cudaSuccess;
@@ -60,11 +61,11 @@ inline bool is_pow2(int64_t x) { return x > 0 && (x & (x - 1)) == 0; }
 // Workspace carve-up for one call.
 struct Layout {
     size_t off_w, off_stage, off_tau, off_tblk, off_flags1, off_flags2, off_err, off_ab, off_d, off_e, off_sig,
-        off_scr, off_out, off_tfull, off_pairs, off_tcS, off_tcW, total;
+        off_scr, off_out, off_tfull, off_pairs, off_tc, total;
     int64_t ldab;
 };
 
-Layout make_layout(int64_t n, int b, size_t elem, size_t stage_elem, bool tc = false) {
+Layout make_layout(int64_t n, int b, size_t elem, size_t stage_elem, int tc_fmt = 0) {
     Layout L{};
     const int64_t nt = n / b;
     size_t o = 0;
@@ -99,11 +100,8 @@ Layout make_layout(int64_t n, int b, size_t elem, size_t stage_elem, bool tc = f
     o = align_up(o + sizeof(double) * (size_t)n);
     L.off_pairs = o;
     o = align_up(o + sizeof(float2) * (size_t)(2 * n + 1));
-    const size_t tcb = tc ? sizeof(float) * (size_t)(nt + 1) * (size_t)b * (size_t)n : 0;
-    L.off_tcS = o;
-    o = align_up(o + tcb);
-    L.off_tcW = o;
-    o = align_up(o + tcb);
+    L.off_tc = o;
+    o = align_up(o + (tc_fmt ? stage1_tc_bytes(n, b, tc_fmt) : 0));
     L.total = o;
     return L;
 }
@@ -139,18 +137,25 @@ size_t storage_elem(int prec) {
         case AVS_PREC_FP64: return 8;
         case AVS_PREC_FP32:
         case AVS_PREC_TF32:
-        case AVS_PREC_TF32X3: return 4;
+        case AVS_PREC_TF32X3:
+        case AVS_PREC_BF16:
+        case AVS_PREC_BF16X3: return 4;
         default: return 0;
     }
 }
 
-// Tensor-core split of a precision mode: 0 = SIMT update, 1 = TF32, 3 = split
-// TF32, -1 = not provided for this tile.  Tiles below 128 keep the 16-block
-// SIMT update (their updates are small).
+// Operand format of the tensor-core trailing update for a precision mode
+// (tc::Fmt: 1 TF32, 3 split TF32, 4 BF16, 5 split BF16); 0 = SIMT update.
+// Tiles below 128 keep the 16-block SIMT update (their updates are small).
 int tc_split_of(int prec, int tile) {
-    if (prec == AVS_PREC_TF32) return tile >= 128 ? 1 : 0;
-    if (prec == AVS_PREC_TF32X3) return tile >= 128 ? 3 : 0;
-    return 0;
+    if (tile < 128) return 0;
+    switch (prec) {
+        case AVS_PREC_TF32: return tc::kTF32;
+        case AVS_PREC_TF32X3: return tc::kTF32X3;
+        case AVS_PREC_BF16: return tc::kBF16;
+        case AVS_PREC_BF16X3: return tc::kBF16X3;
+        default: return 0;
+    }
 }
 
 // Arithmetic of stages 2 and 3: FP64 for the plain FP64 path (or on request),
@@ -221,8 +226,7 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
     w1.err = err;
     w1.tfull = ws_at(h, L.off_tfull);
     w1.tc_split = tc_split;
-    w1.tc_S = reinterpret_cast<float *>(ws_at(h, L.off_tcS));
-    w1.tc_W = reinterpret_cast<float *>(ws_at(h, L.off_tcW));
+    w1.tc_ws = tc_split ? ws_at(h, L.off_tc) : nullptr;
     if ((rc = stage1_ge2bnd<S>(W, n, n, b, w1, s, &launches)) != AVS_SUCCESS) return rc;
     AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
     double *AB = reinterpret_cast<double *>(ws_at(h, L.off_ab));
@@ -283,7 +287,7 @@ int svdvals_dev(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, 
     AVS_CUDA_TRY(cudaSetDevice(h->device));
     const int split = tc_split_of(prec, tile);
     if (split < 0) return AVS_ERR_UNSUPPORTED;
-    const Layout L = make_layout(n, tile, elem, 0, split > 0);
+    const Layout L = make_layout(n, tile, elem, 0, split);
     if ((rc = ensure_ws(h, L.total)) != AVS_SUCCESS) return rc;
     const bool f64 = fp64_stages(prec, opts);
     const double tol = bisect_tol(f64, opts);
@@ -306,7 +310,7 @@ int svdvals_host(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile,
     AVS_CUDA_TRY(cudaSetDevice(h->device));
     const int split = tc_split_of(prec, tile);
     if (split < 0) return AVS_ERR_UNSUPPORTED;
-    const Layout L = make_layout(n, tile, elem, sizeof(T), split > 0);
+    const Layout L = make_layout(n, tile, elem, sizeof(T), split);
     if ((rc = ensure_ws(h, L.total)) != AVS_SUCCESS) return rc;
     cudaStream_t s = h->stream;
     T *stage = reinterpret_cast<T *>(ws_at(h, L.off_stage));
@@ -410,7 +414,7 @@ int avs_reserve(avs_handle *h, int64_t n, int32_t tile, int32_t precision) {
     const size_t elem = storage_elem(prec);
     if (elem == 0) return AVS_ERR_UNSUPPORTED;
     AVS_CUDA_TRY(cudaSetDevice(h->device));
-    return ensure_ws(h, make_layout(n, tile, elem, 8, tc_split_of(prec, tile) > 0).total);
+    return ensure_ws(h, make_layout(n, tile, elem, 8, tc_split_of(prec, tile)).total);
 }
 
 int avs_svdvals_s(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const float *A, float *sigma,
@@ -1014,6 +1018,6 @@ extern "C" int avs_estimate_bytes(int64_t n, int32_t tile, int32_t precision, in
     const int prec = resolve_precision(precision, true);
     const size_t elem = storage_elem(prec);
     if (elem == 0) return AVS_ERR_UNSUPPORTED;
-    *bytes = (int64_t)make_layout(n, tile, elem, elem, tc_split_of(prec, tile) > 0).total;
+    *bytes = (int64_t)make_layout(n, tile, elem, elem, tc_split_of(prec, tile)).total;
     return AVS_SUCCESS;
 }

@@ -91,9 +91,8 @@ struct Stage1Work {
     int *flags;       // ticket (1) + progress (nt) + err (1), reset per launch
     int *err;         // device status word (shared with other stages)
     void *tfull;      // [nt][b*b] of T: full compact-WY factors (tiles 128, 256)
-    float *tc_S = nullptr;  // tensor-core update scratch: [nt][b*n] each (FP32 tiles)
-    float *tc_W = nullptr;
-    int tc_split = 0;       // 0: SIMT update; 1: TF32; 3: split TF32
+    void *tc_ws = nullptr;  // tensor-core update buffers (stage1_tc_bytes), FP32 tiles
+    int tc_split = 0;       // operand format of the tensor-core update (tc::Fmt); 0: SIMT update
     // batched mode: `batch` matrices at dA + z*sA, each with its own tau / T
     // blocks / full T / flag block at the given strides (elements, ints)
     int batch = 1;
@@ -102,8 +101,26 @@ struct Stage1Work {
 template <typename T>
 int stage1_tbuild(const T *dA, int64_t lda, int b, int layout, int pr, int pc, int P, const Stage1Work &w,
                   cudaStream_t s);
-int stage1_update_tc(float *a, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const float *tfull,
-                     float *S, float *Wb, int split, int *err, cudaStream_t s);
+
+// Tensor-core update buffers (carved from Stage1Work::tc_ws).
+struct TcBufs {
+    float *xt;        // n x n: the transposed working matrix
+    void *ph, *pl;    // n x n operand planes of the trailing block
+    void *ych, *ycl;  // [nt][b][b] Y^T planes (GEMM 1)
+    void *yrh, *yrl;  // [nt][b][b] Y planes (GEMM 2)
+    float *S;         // [nt][n][b] S_p = Y_p^T A_p
+    void *wh, *wl;    // [nt][n][b] W_p planes
+    size_t bytes;
+};
+TcBufs stage1_tc_carve(void *ws, int64_t n, int b, int fmt);
+size_t stage1_tc_bytes(int64_t n, int b, int fmt);
+int stage1_tc_planes(const float *x, int64_t n, int fmt, const TcBufs &tb, cudaStream_t s);
+int stage1_tc_transpose(const float *src, float *dst, int64_t n, int64_t i0, int64_t j0, int fmt, const TcBufs &tb,
+                        cudaStream_t s);
+int stage1_tc_update(float *x, int64_t n, int b, int pr, int pc, int P, const Stage1Work &w, const TcBufs &tb,
+                     cudaStream_t s, int64_t *launches);
+int stage1_chain_tc(float *x, int64_t ldx, int64_t n, int b, int pr, int pc, int P, const float *tfull,
+                    const float *S, int64_t ntr, void *w_hi, void *w_lo, int fmt, cudaStream_t s);
 
 template <typename T>
 int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const Stage1Work &w,
@@ -134,10 +151,6 @@ int stage2_chase(double *dAB, int64_t n, int bw, int64_t ldab, double *dd, doubl
 template <typename T>
 int stage2_chase_df(const T *dW, int64_t n, int64_t ldw, int bw, float2 *dAB, int64_t ldab, double *dd, double *de,
                     const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
-namespace tc {
-struct GemmArgs;
-}
-int tc_gemm(const tc::GemmArgs &a, int batch, cudaStream_t s);
 int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
                             double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
 int stage3_bisect_df_batched(const double *dd, const double *de, int64_t n, int batch, double rel_tol,

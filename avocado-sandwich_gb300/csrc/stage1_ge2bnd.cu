@@ -691,34 +691,52 @@ int launch_update(T *dA, int64_t lda, int64_t n, int b, int pr, int pc, int P, c
     return AVS_SUCCESS;
 }
 
-// Tensor-core trailing update: T build (shared with the SIMT path) + the
-// tcgen05 GEMM sequence.
-template <typename T>
-int update_tc_half(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const Stage1Work &w,
-                   cudaStream_t s) {
-    if constexpr (sizeof(T) != 4) {
-        return AVS_ERR_INTERNAL;
-    } else {
-        int rc = stage1_tbuild<T>(dA, lda, b, layout, pr, pc, P, w, s);
-        if (rc != AVS_SUCCESS) return rc;
-        return stage1_update_tc(reinterpret_cast<float *>(dA), lda, n, b, layout, pr, pc, P,
-                                reinterpret_cast<const float *>(w.tfull), w.tc_S, w.tc_W, w.tc_split, w.err, s);
-    }
-}
-
 }  // namespace
+
+// GE2BND with tensor-core trailing updates (FP32 tiles, b = 128 or 256, one
+// matrix, lda = n): QR half-steps on X, LQ half-steps as QR half-steps on the
+// transposed trailing block in tb.xt.
+int stage1_ge2bnd_tc(float *X, int64_t n, int b, const Stage1Work &w, cudaStream_t s, int64_t *launches) {
+    const int nt = (int)(n / b);
+    const int fmt = w.tc_split;
+    const TcBufs tb = stage1_tc_carve(w.tc_ws, n, b, fmt);
+    float *XT = tb.xt;
+    int rc;
+    if ((rc = stage1_tc_planes(X, n, fmt, tb, s)) != AVS_SUCCESS) return rc;
+    for (int k = 0; k < nt; ++k) {
+        const int64_t kb = (int64_t)k * b, k1b = (int64_t)(k + 1) * b;
+        const int P = nt - k;
+        if ((rc = launch_panel<float, 0>(X, n, b, k, k, P, 0, w, s)) != AVS_SUCCESS) return rc;
+        if ((rc = stage1_tbuild<float>(X, n, b, 0, k, k, P, w, s)) != AVS_SUCCESS) return rc;
+        if ((rc = stage1_tc_update(X, n, b, k, k, P, w, tb, s, launches)) != AVS_SUCCESS) return rc;
+        if (launches) *launches += 2;
+        if (k == nt - 1) break;
+        // X rows kb.., columns k1b.. -> XT rows k1b.., columns kb..
+        if ((rc = stage1_tc_transpose(X, XT, n, kb, k1b, fmt, tb, s)) != AVS_SUCCESS) return rc;
+        const int PL = nt - k - 1;
+        if ((rc = launch_panel<float, 0>(XT, n, b, k + 1, k, PL, 0, w, s)) != AVS_SUCCESS) return rc;
+        if ((rc = stage1_tbuild<float>(XT, n, b, 0, k + 1, k, PL, w, s)) != AVS_SUCCESS) return rc;
+        if ((rc = stage1_tc_update(XT, n, b, k + 1, k, PL, w, tb, s, launches)) != AVS_SUCCESS) return rc;
+        // and back: XT rows k1b.., columns kb.. -> X rows kb.., columns k1b..
+        if ((rc = stage1_tc_transpose(XT, X, n, k1b, kb, fmt, tb, s)) != AVS_SUCCESS) return rc;
+        if (launches) *launches += 4;
+    }
+    return AVS_SUCCESS;
+}
 
 template <typename T>
 int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cudaStream_t s, int64_t *launches) {
     const int nt = (int)(n / b);
     int rc;
+    if constexpr (sizeof(T) == 4) {
+        if (w.tc_split && w.tc_ws && b >= 128 && lda == n && (w.batch <= 1))
+            return stage1_ge2bnd_tc(reinterpret_cast<float *>(dA), n, b, w, s, launches);
+    }
     for (int k = 0; k < nt; ++k) {
         // QR half-step: GEQRT(k,k) + TSQRT(row,k), Q^T applied to the row panels.
         const int P = nt - k;
         if ((rc = launch_panel<T, 0>(dA, lda, b, k, k, P, 0, w, s)) != AVS_SUCCESS) return rc;
-        if (b >= 128 && w.tfull && w.tc_split && sizeof(T) == 4)
-            rc = update_tc_half<T>(dA, lda, n, b, 0, k, k, P, w, s);
-        else if (b >= 128 && w.tfull)
+        if (b >= 128 && w.tfull)
             rc = stage1_update_full<T>(dA, lda, n, b, 0, k, k, P, w, s);
         else
             rc = launch_update<T, 0>(dA, lda, n, b, k, k, P, w, s);
@@ -728,9 +746,7 @@ int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cud
         // LQ half-step: the same on the transposed view, top tile (k, k+1).
         const int PL = nt - k - 1;
         if ((rc = launch_panel<T, 1>(dA, lda, b, k + 1, k, PL, 0, w, s)) != AVS_SUCCESS) return rc;
-        if (b >= 128 && w.tfull && w.tc_split && sizeof(T) == 4)
-            rc = update_tc_half<T>(dA, lda, n, b, 1, k + 1, k, PL, w, s);
-        else if (b >= 128 && w.tfull)
+        if (b >= 128 && w.tfull)
             rc = stage1_update_full<T>(dA, lda, n, b, 1, k + 1, k, PL, w, s);
         else
             rc = launch_update<T, 1>(dA, lda, n, b, k + 1, k, PL, w, s);

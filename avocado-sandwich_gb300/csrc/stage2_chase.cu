@@ -201,8 +201,15 @@ struct ChaseAr<double> {
     static __device__ __forceinline__ bool gt0(V a) { return a > 0.0; }
     static __device__ __forceinline__ bool iszero(V a) { return a == 0.0; }
     static __device__ __forceinline__ V shfl_xor(V a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
+    static __device__ __forceinline__ V shfl(V a, int src) { return __shfl_sync(0xffffffffu, a, src); }
+    static __device__ __forceinline__ V rcp(V a) { return 1.0 / a; }
     static __device__ __forceinline__ double to_double(V a) { return a; }
     static __device__ __forceinline__ St from_double(double a) { return a; }
+    // dot-product accumulator: plain FMA chain
+    using Acc = double;
+    static __device__ __forceinline__ Acc acc_zero() { return 0.0; }
+    static __device__ __forceinline__ void acc_add(Acc &a, V x, V y) { a = ::fma(x, y, a); }
+    static __device__ __forceinline__ V acc_value(Acc a) { return a; }
 };
 
 template <>
@@ -229,7 +236,31 @@ struct ChaseAr<df64> {
     static __device__ __forceinline__ V shfl_xor(V a, int o) {
         return df64{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
     }
+    static __device__ __forceinline__ V shfl(V a, int src) {
+        return df64{__shfl_sync(0xffffffffu, a.hi, src), __shfl_sync(0xffffffffu, a.lo, src)};
+    }
+    static __device__ __forceinline__ V rcp(V a) { return df_rcp(a); }
     static __device__ __forceinline__ double to_double(V a) { return df_to_double(a); }
+    // Dot-product accumulator in compensated FP32 (Ogita, Rump & Oishi,
+    // "Accurate sum and dot product", SIAM J. Sci. Comput. 26 (2005), Dot2):
+    // s carries the running FP32 sum, c the exact rounding errors of the sums
+    // and of the double-float products; the loop-carried chain is one add.
+    struct Acc {
+        float s, c;
+    };
+    static __device__ __forceinline__ Acc acc_zero() { return Acc{0.0f, 0.0f}; }
+    static __device__ __forceinline__ void acc_add(Acc &a, V x, V y) {
+        const float p = __fmul_rn(x.hi, y.hi);
+        float ep = __fmaf_rn(x.hi, y.hi, -p);
+        ep = __fmaf_rn(x.hi, y.lo, ep);
+        ep = __fmaf_rn(x.lo, y.hi, ep);
+        const float t = __fadd_rn(a.s, p);
+        const float z = __fsub_rn(t, a.s);
+        const float es = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, z)), __fsub_rn(p, z));
+        a.s = t;
+        a.c = __fadd_rn(a.c, __fadd_rn(es, ep));
+    }
+    static __device__ __forceinline__ V acc_value(Acc a) { return two_sum(a.s, a.c); }
     static __device__ __forceinline__ St from_double(double a) {
         const df64 v = df_from_double(a);
         return make_float2(v.hi, v.lo);
@@ -253,53 +284,51 @@ __device__ __forceinline__ typename ChaseAr<S>::V warp_sum_s(typename ChaseAr<S>
     return v;
 }
 
-template <typename S>
-__device__ __forceinline__ typename ChaseAr<S>::V block_sum_s(typename ChaseAr<S>::V v,
-                                                              typename ChaseAr<S>::V *red) {
-    using Ar = ChaseAr<S>;
-    v = warp_sum_s<S>(v);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) red[wid] = v;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        typename Ar::V t = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : Ar::zero();
-        t = warp_sum_s<S>(t);
-        if (threadIdx.x == 0) red[0] = t;
-    }
-    __syncthreads();
-    return red[0];
-}
-
-// Reflector of sv[0..L) (LAPACK convention: beta = -sign(alpha) ||x||,
-// v = x / (alpha - beta), v0 = 1, tau = (beta - alpha) / beta; tau = 0 when
-// x[1..] == 0), computed by every CTA of the cluster from the same data.
-template <typename S>
-__device__ __forceinline__ void cluster_reflector(typename ChaseAr<S>::V *sv, int L, typename ChaseAr<S>::V *red,
-                                                  typename ChaseAr<S>::V *s_tau, typename ChaseAr<S>::V *s_beta) {
+// Reflector of x[0..L) read straight from the band by one warp (lane l holds
+// x[l + 32 t]): LAPACK convention, beta = -sign(alpha) ||x||, v = x / (alpha -
+// beta), v0 = 1, tau = (beta - alpha) / beta; tau = 0 when x[1..] == 0.  Every
+// lane forms the scalars (no broadcast); v goes to sv, tau and beta to
+// s_tau / s_beta.  Every CTA of the cluster computes the same reflector from
+// the same data.  row: x[i] = A(fixed, start + i); else x[i] = A(start + i, fixed).
+template <typename S, int BW>
+__device__ __forceinline__ void warp_reflector(const BandT<S> &A, bool row, int64_t fixed, int64_t start, int L,
+                                               typename ChaseAr<S>::V *sv, typename ChaseAr<S>::V *s_tau,
+                                               typename ChaseAr<S>::V *s_beta) {
     using Ar = ChaseAr<S>;
     using V = typename Ar::V;
-    V part = Ar::zero();
-    for (int i = 1 + threadIdx.x; i < L; i += blockDim.x) part = Ar::fma(sv[i], sv[i], part);
-    const V s = block_sum_s<S>(part, red);  // ends with a barrier; red[1] is free
-    if (threadIdx.x == 0) {  // one thread forms the scalars (sqrt and divisions are costly)
-        const V alpha = sv[0];
-        V tau = Ar::zero(), beta = alpha, scal = Ar::zero();
-        if (Ar::gt0(s)) {
-            const V nrm = Ar::sqrt(Ar::fma(alpha, alpha, s));
-            beta = Ar::ge0(alpha) ? Ar::neg(nrm) : nrm;
-            tau = Ar::div(Ar::sub(beta, alpha), beta);
-            scal = Ar::div(Ar::one(), Ar::sub(alpha, beta));
-        }
-        red[1] = scal;
+    constexpr int PER = (BW + 31) / 32;
+    const int lane = threadIdx.x & 31;
+    V x[PER];
+#pragma unroll
+    for (int t = 0; t < PER; ++t) {  // all loads in flight before the first use
+        const int i = lane + 32 * t;
+        x[t] = Ar::zero();
+        if (i < L) x[t] = Ar::ld(row ? A.at(fixed, start + i) : A.at(start + i, fixed));
+    }
+    typename Ar::Acc acc = Ar::acc_zero();
+#pragma unroll
+    for (int t = 0; t < PER; ++t) {
+        const int i = lane + 32 * t;
+        if (i >= 1 && i < L) Ar::acc_add(acc, x[t], x[t]);
+    }
+    const V s = warp_sum_s<S>(Ar::acc_value(acc));
+    const V alpha = Ar::shfl(x[0], 0);
+    V tau = Ar::zero(), beta = alpha, scal = Ar::zero();
+    if (Ar::gt0(s)) {
+        const V nrm = Ar::sqrt(Ar::fma(alpha, alpha, s));
+        beta = Ar::ge0(alpha) ? Ar::neg(nrm) : nrm;
+        tau = Ar::mul(Ar::sub(beta, alpha), Ar::rcp(beta));
+        scal = Ar::rcp(Ar::sub(alpha, beta));
+    }
+#pragma unroll
+    for (int t = 0; t < PER; ++t) {
+        const int i = lane + 32 * t;
+        if (i < L) sv[i] = (i == 0) ? Ar::one() : Ar::mul(x[t], scal);
+    }
+    if (lane == 0) {
         *s_tau = tau;
         *s_beta = beta;
-        sv[0] = Ar::one();
     }
-    __syncthreads();
-    const V scal = red[1];
-    for (int i = 1 + threadIdx.x; i < L; i += blockDim.x) sv[i] = Ar::mul(sv[i], scal);
-    __syncthreads();
 }
 
 template <int BW, typename S, int CC>
@@ -312,7 +341,6 @@ __global__ void __launch_bounds__(512) chase_cluster_kernel(typename ChaseAr<S>:
     cg::cluster_group cluster = cg::this_cluster();
     const int q = (int)cluster.block_rank();
     __shared__ V sv[BW];
-    __shared__ V red[32];
     __shared__ V part[Cfg::G][Cfg::RPC];
     __shared__ V wrow[Cfg::RPC];
     __shared__ V s_tau, s_beta;
@@ -345,9 +373,8 @@ __global__ void __launch_bounds__(512) chase_cluster_kernel(typename ChaseAr<S>:
                 __syncthreads();
             }
             if (L >= 2) {
-                for (int i = tid; i < L; i += blockDim.x) sv[i] = Ar::ld(A.at(rho, c0 + i));
+                if (wid == 0) warp_reflector<S, BW>(A, true, rho, c0, L, sv, &s_tau, &s_beta);
                 __syncthreads();
-                cluster_reflector<S>(sv, L, red, &s_tau, &s_beta);
             }
             if (m > 0) {
                 if (tid == 0 && j > 0) wait_geq(done + j - 1, min(2 * m + 4, ops_prev), err);
@@ -360,14 +387,18 @@ __global__ void __launch_bounds__(512) chase_cluster_kernel(typename ChaseAr<S>:
                     const int64_t r = rho + 1 + (int64_t)q * Cfg::RPC + rr;
                     const bool rv = (r <= c1);
                     V vals[Cfg::CPG];
-                    V acc = Ar::zero();
+                    typename Ar::Acc a0 = Ar::acc_zero(), a1 = Ar::acc_zero();
 #pragma unroll
                     for (int k = 0; k < Cfg::CPG; ++k) {
                         const int ci = g * Cfg::CPG + k;
                         vals[k] = (rv && ci < L) ? Ar::ld(A.at(r, c0 + ci)) : Ar::zero();
-                        if (ci < L) acc = Ar::fma(vals[k], sv[ci], acc);
                     }
-                    part[g][rr] = acc;
+#pragma unroll
+                    for (int k = 0; k < Cfg::CPG; ++k) {
+                        const int ci = g * Cfg::CPG + k;
+                        if (ci < L) Ar::acc_add((k & 1) ? a1 : a0, vals[k], sv[ci]);
+                    }
+                    part[g][rr] = Ar::add(Ar::acc_value(a0), Ar::acc_value(a1));
                     __syncthreads();
                     if (g == 0) {
                         V w = Ar::zero();
@@ -397,9 +428,8 @@ __global__ void __launch_bounds__(512) chase_cluster_kernel(typename ChaseAr<S>:
             // Column c0 (rows c0..c1) is final after this sweep's R op and op
             // 2m+1 of sweep j-1 (covered by the R op's wait): reflector first.
             if (L >= 2) {
-                for (int i = tid; i < L; i += blockDim.x) sv[i] = Ar::ld(A.at(c0 + i, c0));
+                if (wid == 0) warp_reflector<S, BW>(A, false, c0, c0, L, sv, &s_tau, &s_beta);
                 __syncthreads();
-                cluster_reflector<S>(sv, L, red, &s_tau, &s_beta);
             }
             if (tid == 0 && j > 0) wait_geq(done + j - 1, min(2 * m + 5, ops_prev), err);
             __syncthreads();
@@ -421,13 +451,13 @@ __global__ void __launch_bounds__(512) chase_cluster_kernel(typename ChaseAr<S>:
 #pragma unroll
                     for (int k = 0; k < Cfg::CPW; ++k) {
                         const int64_t c = cbase + k;
-                        V acc = Ar::zero();
+                        typename Ar::Acc acc = Ar::acc_zero();
 #pragma unroll
                         for (int t = 0; t < Cfg::RPL; ++t) {
                             const int ri = lane + 32 * t;
-                            if (ri < L) acc = Ar::fma(sv[ri], vals[k][t], acc);
+                            if (ri < L) Ar::acc_add(acc, sv[ri], vals[k][t]);
                         }
-                        const V w = Ar::mul(warp_sum_s<S>(acc), tau);
+                        const V w = Ar::mul(warp_sum_s<S>(Ar::acc_value(acc)), tau);
                         if (c <= cend) {
 #pragma unroll
                             for (int t = 0; t < Cfg::RPL; ++t) {

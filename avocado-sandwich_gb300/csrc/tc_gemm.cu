@@ -1,74 +1,62 @@
-// tcgen05 GEMM for the tensor-core trailing updates (TF32 and split TF32).
+// tcgen05 GEMM for the tensor-core trailing updates (TF32, split TF32, BF16,
+// split BF16), fed by TMA.
 //
-// D[M x N] = A[M x K] * B[K x N] for a batch of problems, FP32 in global
-// memory, TF32 tensor-core products accumulated in FP32 in tensor memory.
-// One CTA (4 warps) computes a 128 x 128 tile of D:
-//   * all threads stream A and B in 32-wide K blocks from global memory
-//     (either major order), round each value to TF32 (and, for the split
-//     mode, also the TF32 residual x - hi), and store them into shared memory
-//     in the canonical K-major 128-byte-swizzled layout (8-row atoms of
-//     1024 B; the 16-byte chunk c of row r sits at chunk c ^ (r & 7));
-//   * one thread issues tcgen05.mma (kind::tf32, M = 128, N = 128, K = 8) on
-//     shared-memory descriptors -- per K step hi*hi, or hi*hi + hi*lo + lo*hi
-//     for the split mode (FP32-class products) -- and commits them to an
-//     mbarrier that frees the shared-memory stage (two stages, so the loads of
-//     block k+1 overlap the products of block k);
-//   * the epilogue reads the accumulator with tcgen05.ld (warp w owns TMEM
-//     lanes 32w..32w+31, i.e. rows of D) and applies one of the fused updates
-//     the compact-WY trailing update needs.
-// Every wait is bounded; a timeout sets the device status word.
+// D[M x N] = A[M x K] * B[K x N] for a batch of problems p, FP32 accumulation
+// in tensor memory.  Both operands are K-major in global memory (row m of A /
+// row n of B holds K contiguous values) in one of four operand formats:
+//   kTF32    fp32 planes holding rna_tf32(x) (1 product);
+//   kTF32X3  two fp32 planes hi = rna_tf32(x), lo = rna_tf32(x - hi): the
+//            products lo*hi + hi*lo + hi*hi give FP32-class accuracy;
+//   kBF16    one bf16 plane (1 product);
+//   kBF16X3  two bf16 planes hi = bf16(x), lo = bf16(x - hi) (3 products).
+// The planes are produced by the kernels that write the operands (panel
+// copies, transposes, the chain kernel), so the GEMM itself only moves bytes.
+//
+// One CTA (4 warps) computes a 128 x BN tile of D:
+//   * warp 0, lane 0 issues cp.async.bulk.tensor loads of the K blocks (128
+//     bytes of K per row, 128-byte swizzle -- the canonical K-major layout of
+//     the tcgen05 shared-memory descriptors) into a ring of stages, each stage
+//     completing on its "full" mbarrier by transaction count;
+//   * warp 1, lane 0 issues tcgen05.mma (M = 128, N = BN, K = 8 for TF32 or
+//     16 for BF16 per instruction) and commits each stage to its "empty"
+//     mbarrier, which hands the stage back to the loader;
+//   * after the last commit all four warps read the accumulator with
+//     tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = rows of D) and either
+//     store D or subtract it from the output (the trailing-matrix update).
+// Every wait is bounded in time; a timeout sets the device status word and
+// the CTA skips its stores.
+#include <cuda.h>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "avs_common.cuh"
+#include "tc_gemm.cuh"
 
 namespace avs {
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 32;
+namespace {
+
+constexpr int BM = 128;
 constexpr int NT = 128;
-constexpr int STAGES = 2;
-constexpr int TILE_BYTES = BM * BK * 4;  // 16 KB: 128 rows x 128 B
-constexpr int TMEM_COLS = 256;           // accumulator uses BN = 128 of them
-constexpr int SMEM_PAD = 32 * 1024;      // slack after the last stage
-
-enum Epi : int {
-    kStore = 0,     // C = D
-    kSub = 1,       // C -= D
-    kTopUpdate = 2  // C -= D (C is the top rows), W = D, Z += C_new (if Z)
-};
-enum AMask : int { kNoMask = 0, kUnitLowerT = 1, kUnitLower = 2 };
-
-struct GemmArgs {
-    const float *A;
-    int64_t lda, strideA;
-    int a_kmajor, a_mask;
-    const float *B;
-    int64_t ldb, strideB;
-    int b_kmajor;
-    float *C;
-    int64_t ldc, strideC;
-    int c_colmajor;
-    float *W;
-    int64_t ldw, strideW;
-    float *Z;
-    int64_t ldz;
-    int M, N, K;
-    int epi, split;
-    int *err;
-};
+constexpr int kSmemStages = 200 * 1024;      // bytes of the stage ring
+constexpr long long kWaitNs = 2000000000ll;  // 2 s per wait
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ uint32_t to_tf32(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return r;
+__device__ __forceinline__ unsigned long long gtimer() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
 }
 
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms
-// 1024 B apart (SBO), leading offset unused for this layout (1), version 1.
+// 1024 B apart (stride byte offset), leading byte offset unused for this
+// layout (1), descriptor version 1 (bits 46-47), swizzle mode 2 (bits 61-63).
 __device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
     uint64_t d = 0;
     d |= (uint64_t)((addr >> 4) & 0x3FFFu);
@@ -79,18 +67,31 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
     return d;
 }
 
-// Instruction descriptor, kind::tf32: D FP32, A/B TF32, both K-major, M x N.
-__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+// Instruction descriptors: D FP32 (bits 4-5 = 1), A/B format (bits 7-9,
+// 10-12: TF32 = 2 for kind::tf32, BF16 = 1 for kind::f16), both operands
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc(int M, int N, bool bf16) {
+    return (1u << 4) | ((bf16 ? 1u : 2u) << 7) | ((bf16 ? 1u : 2u) << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
-        :
-        : "r"(d_tmem), "l"(a), "l"(b), "r"(idesc), "r"(acc));
+template <bool BF16>
+__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
+    if constexpr (BF16) {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+            :
+            : "r"(d_tmem), "l"(a), "l"(b), "r"(id), "r"(acc));
+    } else {
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
+            :
+            : "r"(d_tmem), "l"(a), "l"(b), "r"(id), "r"(acc));
+    }
 }
 
 __device__ __forceinline__ void mma_commit(uint32_t mbar) {
@@ -102,9 +103,14 @@ __device__ __forceinline__ void mbar_init(uint32_t mbar, int count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
 }
 
-// Bounded wait for the completion of phase `parity` of an mbarrier.
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+// Bounded wait for the completion of phase `parity` of an mbarrier (2 s).
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, int *err) {
-    for (long long it = 0; it < kSpinLimit; ++it) {
+    const unsigned long long t0 = gtimer();
+    for (long long it = 0;; ++it) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -114,14 +120,22 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, int *e
             : "r"(mbar), "r"(parity)
             : "memory");
         if (done) return true;
-        if ((it & 1023) == 1023 && ld_acquire(err) != kDevOk) return false;
+        if ((it & 255) == 255) {
+            if (ld_acquire(err) != kDevOk) return false;
+            if ((long long)(gtimer() - t0) > kWaitNs) {
+                atomicCAS(err, kDevOk, kDevTimeout);
+                return false;
+            }
+        }
     }
-    atomicCAS(err, kDevOk, kDevTimeout);
-    return false;
 }
 
-__device__ __forceinline__ uint32_t swz(int r, int k) {
-    return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((((k >> 2) ^ (r & 7)) << 4) | ((k & 3) << 2)));
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(mbar)
+        : "memory");
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
@@ -136,265 +150,218 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Store one value of a tile: (r, k) of the tile, split into hi (and lo).
-__device__ __forceinline__ void put(uint8_t *hi, uint8_t *lo, int r, int k, float x, bool split) {
-    const uint32_t off = swz(r, k);
-    const uint32_t h = to_tf32(x);
-    *reinterpret_cast<uint32_t *>(hi + off) = h;
-    if (split) *reinterpret_cast<uint32_t *>(lo + off) = to_tf32(x - __uint_as_float(h));
-}
+template <int BN, bool SPLIT, bool BF16>
+struct KCfg {
+    static constexpr int PLANES = SPLIT ? 2 : 1;
+    static constexpr int A_BYTES = BM * 128;  // 128 rows x 128 B of K
+    static constexpr int B_BYTES = BN * 128;
+    static constexpr int STAGE = (A_BYTES + B_BYTES) * PLANES;
+    static constexpr int STAGES = kSmemStages / STAGE > 6 ? 6 : kSmemStages / STAGE;
+    static constexpr int SMEM = STAGE * STAGES + 1024;
+    static constexpr int KSTEPS = 4;           // MMAs per 128-byte K block (32 B of K each)
+    static constexpr int BK = BF16 ? 64 : 32;  // K elements per block
+    static_assert(STAGES >= 2, "stage ring");
+};
 
-__device__ __forceinline__ void put4(uint8_t *hi, uint8_t *lo, int r, int k, float4 x, bool split) {
-    const uint32_t off = swz(r, k);  // k % 4 == 0: one 16-byte chunk
-    uint4 h = make_uint4(to_tf32(x.x), to_tf32(x.y), to_tf32(x.z), to_tf32(x.w));
-    *reinterpret_cast<uint4 *>(hi + off) = h;
-    if (split) {
-        uint4 l = make_uint4(to_tf32(x.x - __uint_as_float(h.x)), to_tf32(x.y - __uint_as_float(h.y)),
-                             to_tf32(x.z - __uint_as_float(h.z)), to_tf32(x.w - __uint_as_float(h.w)));
-        *reinterpret_cast<uint4 *>(lo + off) = l;
-    }
-}
-
-__device__ __forceinline__ float amask(int mask, int64_t m, int64_t k, float v) {
-    if (mask == kUnitLowerT) return (k == m) ? 1.0f : (k > m ? v : 0.0f);
-    if (mask == kUnitLower) return (m == k) ? 1.0f : (m > k ? v : 0.0f);
-    return v;
-}
-
-// Load the 128 x 32 block (rows r0.., k0..) of an operand into (hi, lo).
-// kmajor: element (row, k) at p[k + row * ld]; else at p[row + k * ld].
-__device__ __forceinline__ void load_tile(const float *p, int64_t ld, int kmajor, int mask, int64_t r0, int64_t k0,
-                                          uint8_t *hi, uint8_t *lo, bool split) {
-    const int tid = threadIdx.x;
-    if (kmajor) {
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int idx = tid + NT * i;
-            const int r = idx >> 3, c4 = idx & 7;
-            float4 v = __ldg(reinterpret_cast<const float4 *>(p + (k0 + 4 * c4) + (r0 + r) * ld));
-            if (mask) {
-                v.x = amask(mask, r0 + r, k0 + 4 * c4 + 0, v.x);
-                v.y = amask(mask, r0 + r, k0 + 4 * c4 + 1, v.y);
-                v.z = amask(mask, r0 + r, k0 + 4 * c4 + 2, v.z);
-                v.w = amask(mask, r0 + r, k0 + 4 * c4 + 3, v.w);
-            }
-            put4(hi, lo, r, 4 * c4, v, split);
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            const int idx = tid + NT * i;
-            const int kk = idx >> 5, m4 = idx & 31;
-            const float4 v = __ldg(reinterpret_cast<const float4 *>(p + (r0 + 4 * m4) + (k0 + kk) * ld));
-            const float e[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-                put(hi, lo, 4 * m4 + q, kk, mask ? amask(mask, r0 + 4 * m4 + q, k0 + kk, e[q]) : e[q], split);
-        }
-    }
-}
-
-__global__ void __launch_bounds__(NT) tc_gemm_kernel(GemmArgs g) {
+template <int BN, bool SPLIT, bool BF16>
+__global__ void __launch_bounds__(NT, 1)
+    gemm_kernel(const __grid_constant__ CUtensorMap ta_hi, const __grid_constant__ CUtensorMap ta_lo,
+                const __grid_constant__ CUtensorMap tb_hi, const __grid_constant__ CUtensorMap tb_lo, GemmDesc g) {
+    using C = KCfg<BN, SPLIT, BF16>;
     extern __shared__ uint8_t smem_dyn[];
-    __shared__ uint64_t mbar[STAGES];
+    __shared__ uint64_t full[C::STAGES], empty[C::STAGES], done;
     __shared__ uint32_t tmem_base;
-    const bool split = g.split == 3;
-    // 1024-byte aligned tiles: per stage A_hi, B_hi (, A_lo, B_lo)
+    __shared__ int s_fail;
     uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
-    const int per_stage = (split ? 4 : 2) * TILE_BYTES;
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
-    const int64_t z = blockIdx.z;
-    const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
-    const float *A = g.A + z * g.strideA;
-    const float *B = g.B + z * g.strideB;
+    const int p = (int)blockIdx.z + g.p0;
+    const int m0 = (int)blockIdx.y * BM, n0 = (int)blockIdx.x * BN;
 
     if (tid == 0) {
-        for (int s = 0; s < STAGES; ++s) mbar_init(smem_u32(&mbar[s]), 1);
+        for (int s = 0; s < C::STAGES; ++s) {
+            mbar_init(smem_u32(&full[s]), 1);
+            mbar_init(smem_u32(&empty[s]), 1);
+        }
+        mbar_init(smem_u32(&done), 1);
+        s_fail = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&ta_hi)) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&tb_hi)) : "memory");
     }
     if (wid == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
-                     "r"(TMEM_COLS));
+                     "r"(BN));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base;
-    const uint32_t idesc = idesc_tf32(BM, BN);
-    const int nkb = g.K / BK;
-    bool ok = true;
+    // stage s: A hi | B hi | A lo | B lo
+    auto stage_ptr = [&](int s, int which) -> uint32_t {
+        const uint32_t st = smem_u32(base) + (uint32_t)(s * C::STAGE);
+        switch (which) {
+            case 0: return st;
+            case 1: return st + C::A_BYTES;
+            case 2: return st + C::A_BYTES + C::B_BYTES;
+            default: return st + 2 * C::A_BYTES + C::B_BYTES;
+        }
+    };
 
-    for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % STAGES;
-        uint8_t *st = base + s * per_stage;
-        uint8_t *a_hi = st, *b_hi = st + TILE_BYTES;
-        uint8_t *a_lo = st + 2 * TILE_BYTES, *b_lo = st + 3 * TILE_BYTES;
-        if (kb >= STAGES) ok = mbar_wait(smem_u32(&mbar[s]), (uint32_t)((kb / STAGES - 1) & 1), g.err) && ok;
-        load_tile(A, g.lda, g.a_kmajor, g.a_mask, m0, (int64_t)kb * BK, a_hi, a_lo, split);
-        load_tile(B, g.ldb, g.b_kmajor, kNoMask, n0, (int64_t)kb * BK, b_hi, b_lo, split);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
+    if (wid == 0 && lane == 0) {
+        // ---- loader
+        for (int kb = 0; kb < g.nkb; ++kb) {
+            const int s = kb % C::STAGES;
+            if (kb >= C::STAGES && !mbar_wait(smem_u32(&empty[s]), (uint32_t)((kb / C::STAGES - 1) & 1), g.err)) {
+                s_fail = 1;
+                break;
+            }
+            const uint32_t fb = smem_u32(&full[s]);
+            mbar_expect_tx(fb, (uint32_t)C::STAGE);
+            const int ax = kb * C::BK, ay = g.a_y0 + p * g.a_yp + m0;
+            const int bx = g.b_x0 + p * g.b_xp + kb * C::BK, by = g.b_y0 + p * g.b_yp + n0;
+            tma_load_2d(stage_ptr(s, 0), &ta_hi, ax, ay, fb);
+            tma_load_2d(stage_ptr(s, 1), &tb_hi, bx, by, fb);
+            if constexpr (SPLIT) {
+                tma_load_2d(stage_ptr(s, 2), &ta_lo, ax, ay, fb);
+                tma_load_2d(stage_ptr(s, 3), &tb_lo, bx, by, fb);
+            }
+        }
+    } else if (wid == 1 && lane == 0) {
+        // ---- MMA issue
+        const uint32_t id = idesc(BM, BN, BF16);
+        for (int kb = 0; kb < g.nkb; ++kb) {
+            const int s = kb % C::STAGES;
+            if (!mbar_wait(smem_u32(&full[s]), (uint32_t)((kb / C::STAGES) & 1), g.err)) {
+                s_fail = 1;
+                break;
+            }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t ah = stage_ptr(s, 0), bh = stage_ptr(s, 1);
 #pragma unroll
-            for (int ks = 0; ks < BK / 8; ++ks) {
-                const uint32_t koff = ks * 32;  // 8 TF32 values = 32 bytes along K
-                const uint64_t ah = desc_sw128(smem_u32(a_hi) + koff), bh = desc_sw128(smem_u32(b_hi) + koff);
-                mma_tf32(tmem, ah, bh, idesc, (kb > 0 || ks > 0) ? 1u : 0u);
-                if (split) {
-                    const uint64_t al = desc_sw128(smem_u32(a_lo) + koff), bl = desc_sw128(smem_u32(b_lo) + koff);
-                    mma_tf32(tmem, ah, bl, idesc, 1u);
-                    mma_tf32(tmem, al, bh, idesc, 1u);
+            for (int ks = 0; ks < C::KSTEPS; ++ks) {
+                const uint32_t ko = ks * 32;
+                const uint64_t da = desc_sw128(ah + ko), db = desc_sw128(bh + ko);
+                if constexpr (SPLIT) {
+                    const uint32_t al = stage_ptr(s, 2), bl = stage_ptr(s, 3);
+                    mma<BF16>(tmem, desc_sw128(al + ko), db, id, (kb > 0 || ks > 0) ? 1u : 0u);
+                    mma<BF16>(tmem, da, desc_sw128(bl + ko), id, 1u);
+                    mma<BF16>(tmem, da, db, id, 1u);
+                } else {
+                    mma<BF16>(tmem, da, db, id, (kb > 0 || ks > 0) ? 1u : 0u);
                 }
             }
-            mma_commit(smem_u32(&mbar[s]));
+            mma_commit(smem_u32(&empty[s]));
         }
-        __syncthreads();
+        mma_commit(smem_u32(&done));
     }
-    {
-        const int s = (nkb - 1) % STAGES;
-        ok = mbar_wait(smem_u32(&mbar[s]), (uint32_t)(((nkb - 1) / STAGES) & 1), g.err) && ok;
-    }
+    __syncwarp();
+    const bool ok = mbar_wait(smem_u32(&done), 0u, g.err) && !*(volatile int *)&s_fail;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 
     // ---- epilogue: warp w owns rows m0 + 32w + lane
-    const int64_t m = m0 + 32 * wid + lane;
-    float *C = g.C + z * g.strideC;
+    const int64_t row = g.o_row0 + (int64_t)p * g.o_rowp + m0 + 32 * wid + lane;
+    const int64_t col0 = g.o_col0 + (int64_t)p * g.o_colp + n0;
     for (int c16 = 0; c16 < BN / 16; ++c16) {
         float v[16];
         tmem_ld16(tmem + ((uint32_t)(32 * wid) << 16) + (uint32_t)(c16 * 16), v);
         if (!ok) continue;
+        float *o = g.out + row + (col0 + c16 * 16) * g.ld_out;
+        if (g.epi == kEpiStore) {
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            const int64_t nn = n0 + c16 * 16 + q;
-            float *cp = g.c_colmajor ? (C + m + nn * g.ldc) : (C + nn + m * g.ldc);
-            if (g.epi == kStore) {
-                *cp = v[q];
-            } else if (g.epi == kSub) {
-                *cp = *cp - v[q];
-            } else {
-                const float cn = *cp - v[q];
-                *cp = cn;
-                if (g.W) g.W[z * g.strideW + m + nn * g.ldw] = v[q];
-                if (g.Z) g.Z[m + nn * g.ldz] += cn;
-            }
+            for (int q = 0; q < 16; ++q) o[q * g.ld_out] = v[q];
+        } else {
+            float cur[16];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) cur[q] = o[q * g.ld_out];
+#pragma unroll
+            for (int q = 0; q < 16; ++q) o[q * g.ld_out] = cur[q] - v[q];
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (wid == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    if (wid == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
 }
 
-}  // namespace tc
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// dependency on libcuda).
+using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                              const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-int tc_gemm(const tc::GemmArgs &a, int batch, cudaStream_t s) {
-    if (a.M % tc::BM || a.N % tc::BN || a.K % tc::BK || batch <= 0) return AVS_ERR_INTERNAL;
-    const int smem = (a.split == 3 ? 4 : 2) * tc::TILE_BYTES * tc::STAGES + 1024 + tc::SMEM_PAD;
+EncodeFn encode_fn() {
+    static EncodeFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeFn>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+template <int BN, bool SPLIT, bool BF16>
+int launch(const Operand &A, const Operand &B, const GemmDesc &g, int mtiles, int ntiles, int batch, cudaStream_t s) {
+    using C = KCfg<BN, SPLIT, BF16>;
     static std::atomic<bool> attr{false};
     if (!attr) {
-        AVS_CUDA_TRY(cudaFuncSetAttribute(tc::tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          4 * tc::TILE_BYTES * tc::STAGES + 1024 + tc::SMEM_PAD));
+        AVS_CUDA_TRY(cudaFuncSetAttribute(gemm_kernel<BN, SPLIT, BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          C::SMEM));
         attr = true;
     }
-    dim3 grid((unsigned)(a.N / tc::BN), (unsigned)(a.M / tc::BM), (unsigned)batch);
-    tc::tc_gemm_kernel<<<grid, tc::NT, smem, s>>>(a);
+    EncodeFn enc = encode_fn();
+    if (!enc) return AVS_ERR_UNSUPPORTED;
+    const CUtensorMapDataType dt = BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const int esz = BF16 ? 2 : 4;
+    CUtensorMap m[4];
+    auto make = [&](CUtensorMap *map, const Operand &op, const void *ptr, int box_rows) -> bool {
+        if (!ptr) ptr = op.hi;  // unused lo plane: any valid map
+        const cuuint64_t dims[2] = {(cuuint64_t)op.k_extent, (cuuint64_t)op.rows};
+        const cuuint64_t strides[1] = {(cuuint64_t)op.ld * esz};
+        const cuuint32_t box[2] = {(cuuint32_t)(128 / esz), (cuuint32_t)box_rows};
+        const cuuint32_t es[2] = {1, 1};
+        return enc(map, dt, 2, const_cast<void *>(ptr), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+    };
+    if (!make(&m[0], A, A.hi, BM) || !make(&m[1], A, A.lo, BM) || !make(&m[2], B, B.hi, BN) ||
+        !make(&m[3], B, B.lo, BN))
+        return AVS_ERR_INTERNAL;
+    gemm_kernel<BN, SPLIT, BF16><<<dim3((unsigned)ntiles, (unsigned)mtiles, (unsigned)batch), NT, C::SMEM, s>>>(
+        m[0], m[1], m[2], m[3], g);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
 }
 
-// ---------------------------------------------------------------------------
-// Trailing update of one half-step on the tensor cores (FP32 tiles, tile 128
-// or 256).  View element (i, j) is a[i + j*lda] (layout 0) or a[j + i*lda]
-// (layout 1); the panel occupies view rows pr*b.., columns pc*b..pc*b+b-1; the
-// trailing columns start at j0 = (pc+1)*b.  T_p comes from tbuild (tfull,
-// column-major b x b per tile); S and Wb hold P slots of b x N (ld b).
-int stage1_update_tc(float *a, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const float *tfull,
-                     float *S, float *Wb, int split, int *err, cudaStream_t s) {
-    const int64_t j0 = (int64_t)(pc + 1) * b;
-    const int64_t N = n - j0;
-    if (N <= 0) return AVS_SUCCESS;
-    const int64_t top0 = (int64_t)pr * b, col0 = (int64_t)pc * b;
-    auto vptr = [&](int64_t i, int64_t j) { return layout == 0 ? a + i + j * lda : a + j + i * lda; };
-    const int64_t tile_step = layout == 0 ? (int64_t)b : (int64_t)b * lda;  // view row tile -> next
-    const int64_t slot = (int64_t)b * N;
-    int rc;
-    tc::GemmArgs g;
-    auto base = [&]() {
-        tc::GemmArgs x = {};
-        x.M = b; x.N = (int)N; x.K = b; x.split = split; x.err = err;
-        return x;
-    };
-    // Y^T operand (m = l, k = t) of the tile whose view rows start at r0
-    auto set_yt = [&](tc::GemmArgs &x, int64_t r0) {
-        x.A = vptr(r0, col0); x.lda = lda; x.a_kmajor = layout == 0 ? 1 : 0;
-    };
-    // Y operand (m = t, k = l)
-    auto set_y = [&](tc::GemmArgs &x, int64_t r0) {
-        x.A = vptr(r0, col0); x.lda = lda; x.a_kmajor = layout == 0 ? 0 : 1;
-    };
-    // view rows r0.., trailing columns as B (k = t, n = c) or as C (m = t, n = c)
-    auto set_b_rows = [&](tc::GemmArgs &x, int64_t r0) {
-        x.B = vptr(r0, j0); x.ldb = lda; x.b_kmajor = layout == 0 ? 1 : 0;
-    };
-    auto set_c_rows = [&](tc::GemmArgs &x, int64_t r0) {
-        x.C = vptr(r0, j0); x.ldc = lda; x.c_colmajor = layout == 0 ? 1 : 0;
-    };
-    // 1. S_p = Y_p^T A_p for p = 1..P-1 (independent of one another)
-    if (P > 1) {
-        g = base();
-        set_yt(g, top0 + b); g.strideA = tile_step;
-        set_b_rows(g, top0 + b); g.strideB = tile_step;
-        g.C = S + slot; g.ldc = b; g.strideC = slot; g.c_colmajor = 1;
-        g.epi = tc::kStore;
-        if ((rc = tc_gemm(g, P - 1, s)) != AVS_SUCCESS) return rc;
+}  // namespace
+
+int gemm(int fmt, const Operand &A, const Operand &B, const GemmDesc &g, int M, int N, int batch, cudaStream_t s) {
+    if (M % BM || batch <= 0 || N % 128) return AVS_ERR_INTERNAL;
+    const bool wide = (N % 256 == 0);
+    switch (fmt) {
+        case kTF32:
+            return wide ? launch<256, false, false>(A, B, g, M / BM, N / 256, batch, s)
+                        : launch<128, false, false>(A, B, g, M / BM, N / 128, batch, s);
+        case kTF32X3: return launch<128, true, false>(A, B, g, M / BM, N / 128, batch, s);
+        case kBF16:
+            return wide ? launch<256, false, true>(A, B, g, M / BM, N / 256, batch, s)
+                        : launch<128, false, true>(A, B, g, M / BM, N / 128, batch, s);
+        case kBF16X3: return launch<128, true, true>(A, B, g, M / BM, N / 128, batch, s);
+        default: return AVS_ERR_UNSUPPORTED;
     }
-    // 2. S_0 = Y0^T Top (unit lower Y0 from the GEQRT tile)
-    g = base();
-    set_yt(g, top0); g.a_mask = tc::kUnitLowerT;
-    set_b_rows(g, top0);
-    g.C = S; g.ldc = b; g.c_colmajor = 1; g.epi = tc::kStore;
-    if ((rc = tc_gemm(g, 1, s)) != AVS_SUCCESS) return rc;
-    // 3. W_0 = T_0^T S_0
-    g = base();
-    g.A = tfull; g.lda = b; g.a_kmajor = 1;
-    g.B = S; g.ldb = b; g.b_kmajor = 1;
-    g.C = Wb; g.ldc = b; g.c_colmajor = 1; g.epi = tc::kStore;
-    if ((rc = tc_gemm(g, 1, s)) != AVS_SUCCESS) return rc;
-    // 4. Top -= Y0 W_0, and Z_1 = Top + S_1
-    g = base();
-    set_y(g, top0); g.a_mask = tc::kUnitLower;
-    g.B = Wb; g.ldb = b; g.b_kmajor = 1;
-    set_c_rows(g, top0);
-    g.epi = tc::kTopUpdate; g.W = nullptr;
-    g.Z = P > 1 ? S + slot : nullptr; g.ldz = b;
-    if ((rc = tc_gemm(g, 1, s)) != AVS_SUCCESS) return rc;
-    // 5. for each TSQRT tile in order: W_p = T_p^T Z_p, Top -= W_p, Z_{p+1} = Top + S_{p+1}
-    for (int p = 1; p < P; ++p) {
-        g = base();
-        g.A = tfull + (size_t)p * b * b; g.lda = b; g.a_kmajor = 1;
-        g.B = S + p * slot; g.ldb = b; g.b_kmajor = 1;
-        set_c_rows(g, top0);
-        g.epi = tc::kTopUpdate;
-        g.W = Wb + p * slot; g.ldw = b;
-        g.Z = (p + 1 < P) ? S + (p + 1) * slot : nullptr; g.ldz = b;
-        if ((rc = tc_gemm(g, 1, s)) != AVS_SUCCESS) return rc;
-    }
-    // 6. A_p -= Y_p W_p for p = 1..P-1
-    if (P > 1) {
-        g = base();
-        set_y(g, top0 + b); g.strideA = tile_step;
-        g.B = Wb + slot; g.ldb = b; g.b_kmajor = 1; g.strideB = slot;
-        set_c_rows(g, top0 + b); g.strideC = tile_step;
-        g.epi = tc::kSub;
-        if ((rc = tc_gemm(g, P - 1, s)) != AVS_SUCCESS) return rc;
-    }
-    return AVS_SUCCESS;
 }
 
+}  // namespace tc
+
 // ---------------------------------------------------------------------------
-// Self-test of the tensor-core GEMM against an FP64 SIMT product on the same
-// device data (used by the GPU tests; allocates its own buffers).
+// Self-test of the tensor-core GEMM against an FP64 product of the same data
+// (used by the GPU tests; allocates its own buffers).  A is M x K, B is N x K
+// (both K-major), C = A B^T is stored column-major (ld M).
 namespace {
 __global__ void fill_kernel(float *p, int64_t n, uint32_t seed) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -405,16 +372,15 @@ __global__ void fill_kernel(float *p, int64_t n, uint32_t seed) {
         p[i] = ((float)(h & 0xFFFFFF) / 16777216.0f) * 2.0f - 1.0f;
     }
 }
-__global__ void ref_kernel(const float *A, int64_t lda, int akm, const float *B, int64_t ldb, int bkm, double *D,
-                           int M, int N, int K) {
+__global__ void planes_kernel(const float *x, int64_t n, int fmt, void *hi, void *lo) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        tc::put_operand(fmt, hi, lo, i, x[i]);
+}
+__global__ void ref_kernel(const float *A, const float *B, double *D, int M, int N, int K) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x, n = blockIdx.y;
     if (m >= M) return;
     double acc = 0.0;
-    for (int k = 0; k < K; ++k) {
-        const double a = akm ? A[k + (int64_t)m * lda] : A[m + (int64_t)k * lda];
-        const double b = bkm ? B[k + (int64_t)n * ldb] : B[n + (int64_t)k * ldb];
-        acc += a * b;
-    }
+    for (int k = 0; k < K; ++k) acc += (double)A[k + (int64_t)m * K] * (double)B[k + (int64_t)n * K];
     D[m + (int64_t)n * M] = acc;
 }
 __global__ void cmp_kernel(const float *C, const double *D, int64_t n, float *out) {
@@ -439,30 +405,41 @@ __global__ void cmp_kernel(const float *C, const double *D, int64_t n, float *ou
 
 }  // namespace avs
 
-extern "C" int avsx_tc_gemm_selftest(int M, int N, int K, int a_kmajor, int b_kmajor, int split, float *relerr) {
+extern "C" int avsx_tc_gemm_selftest(int M, int N, int K, int fmt, float *relerr) {
     using namespace avs;
+    if (M <= 0 || N <= 0 || K <= 0 || M % 128 || N % 128 || K % 64) return AVS_ERR_INTERNAL;
+    if (fmt != tc::kTF32 && fmt != tc::kTF32X3 && fmt != tc::kBF16 && fmt != tc::kBF16X3) return AVS_ERR_UNSUPPORTED;
     float *A = nullptr, *B = nullptr, *C = nullptr, *out = nullptr;
+    void *ah = nullptr, *al = nullptr, *bh = nullptr, *bl = nullptr;
     double *D = nullptr;
     int *err = nullptr;
     int rc = AVS_SUCCESS;
-    const int64_t lda = a_kmajor ? K : M, ldb = b_kmajor ? K : N;
+    const size_t esz = (fmt == tc::kBF16 || fmt == tc::kBF16X3) ? 2 : 4;
     if (cudaMalloc(&A, sizeof(float) * (size_t)M * K) != cudaSuccess ||
         cudaMalloc(&B, sizeof(float) * (size_t)K * N) != cudaSuccess ||
         cudaMalloc(&C, sizeof(float) * (size_t)M * N) != cudaSuccess ||
         cudaMalloc(&D, sizeof(double) * (size_t)M * N) != cudaSuccess || cudaMalloc(&out, sizeof(float)) != cudaSuccess ||
-        cudaMalloc(&err, sizeof(int)) != cudaSuccess) {
+        cudaMalloc(&err, sizeof(int)) != cudaSuccess || cudaMalloc(&ah, esz * (size_t)M * K) != cudaSuccess ||
+        cudaMalloc(&al, esz * (size_t)M * K) != cudaSuccess || cudaMalloc(&bh, esz * (size_t)N * K) != cudaSuccess ||
+        cudaMalloc(&bl, esz * (size_t)N * K) != cudaSuccess) {
+        cudaGetLastError();
         rc = AVS_ERR_OOM;
     } else {
         cudaMemset(err, 0, sizeof(int));
         fill_kernel<<<256, 256>>>(A, (int64_t)M * K, 17u);
         fill_kernel<<<256, 256>>>(B, (int64_t)K * N, 91u);
-        ref_kernel<<<dim3((M + 127) / 128, N), 128>>>(A, lda, a_kmajor, B, ldb, b_kmajor, D, M, N, K);
-        tc::GemmArgs g = {};
-        g.A = A; g.lda = lda; g.a_kmajor = a_kmajor; g.a_mask = tc::kNoMask;
-        g.B = B; g.ldb = ldb; g.b_kmajor = b_kmajor;
-        g.C = C; g.ldc = M; g.c_colmajor = 1;
-        g.M = M; g.N = N; g.K = K; g.epi = tc::kStore; g.split = split; g.err = err;
-        rc = tc_gemm(g, 1, 0);
+        planes_kernel<<<256, 256>>>(A, (int64_t)M * K, fmt, ah, al);
+        planes_kernel<<<256, 256>>>(B, (int64_t)N * K, fmt, bh, bl);
+        ref_kernel<<<dim3((M + 127) / 128, N), 128>>>(A, B, D, M, N, K);
+        tc::Operand oa{ah, al, (int64_t)K, (int64_t)M, (int64_t)K};
+        tc::Operand ob{bh, bl, (int64_t)K, (int64_t)N, (int64_t)K};
+        tc::GemmDesc g = {};
+        g.nkb = (int)((size_t)K * esz / 128);
+        g.epi = tc::kEpiStore;
+        g.out = C;
+        g.ld_out = M;
+        g.err = err;
+        rc = tc::gemm(fmt, oa, ob, g, M, N, 1, 0);
         if (rc == AVS_SUCCESS) {
             cmp_kernel<<<1, 1024>>>(C, D, (int64_t)M * N, out);
             int herr = 0;
@@ -474,5 +451,6 @@ extern "C" int avsx_tc_gemm_selftest(int M, int N, int K, int a_kmajor, int b_km
         }
     }
     cudaFree(A); cudaFree(B); cudaFree(C); cudaFree(D); cudaFree(out); cudaFree(err);
+    cudaFree(ah); cudaFree(al); cudaFree(bh); cudaFree(bl);
     return rc;
 }
