@@ -707,10 +707,11 @@ int stage1_ge2bnd_tc(float *X, int64_t n, int b, const Stage1Work &w, cudaStream
         const int64_t kb = (int64_t)k * b, k1b = (int64_t)(k + 1) * b;
         const int P = nt - k;
         if ((rc = launch_panel<float, 0>(X, n, b, k, k, P, 0, w, s)) != AVS_SUCCESS) return rc;
+        if (launches) *launches += 1;
+        if (k == nt - 1) break;  // no trailing columns left
         if ((rc = stage1_tbuild<float>(X, n, b, 0, k, k, P, w, s)) != AVS_SUCCESS) return rc;
         if ((rc = stage1_tc_update(X, n, b, k, k, P, w, tb, s, launches)) != AVS_SUCCESS) return rc;
-        if (launches) *launches += 2;
-        if (k == nt - 1) break;
+        if (launches) *launches += 1;
         // X rows kb.., columns k1b.. -> XT rows k1b.., columns kb..
         if ((rc = stage1_tc_transpose(X, XT, n, kb, k1b, fmt, tb, s)) != AVS_SUCCESS) return rc;
         const int PL = nt - k - 1;

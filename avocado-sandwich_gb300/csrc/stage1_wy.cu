@@ -164,9 +164,9 @@ struct UpdFullArgs {
 // A-operand sources for the three products.
 enum ASrc { kVrows = 0, kTrows = 1, kVcols = 2 };
 
-template <typename T, int B>
+template <typename T, int B, int WW = WCfg<T>::W>
 struct UCfg {
-    static constexpr int W = WCfg<T>::W;
+    static constexpr int W = WW;
     static constexpr int KC = WCfg<T>::KC;
     static constexpr int MB = 8;                  // rows per thread
     static constexpr int TM = B / MB;             // threads along rows
@@ -178,9 +178,9 @@ struct UCfg {
     static_assert(CB >= 1 && PER >= 1, "update configuration");
 };
 
-template <typename T, int LAYOUT, int B>
+template <typename T, int LAYOUT, int B, int WW = WCfg<T>::W>
 struct UpdCtx {
-    using C = UCfg<T, B>;
+    using C = UCfg<T, B, WW>;
     View<T, LAYOUT> V;
     const T *Tf;      // T of the current tile, ld B
     int64_t row0, col0;
@@ -207,10 +207,10 @@ struct UpdCtx {
 };
 
 // acc (+|-)= A(k, m)^T-view ... : acc[i][j] += sign * sum_k A(k, m0+i) * Bop(k, c0+j)
-template <typename T, int LAYOUT, int B>
-__device__ __forceinline__ void gemm(const UpdCtx<T, LAYOUT, B> &ctx, int src, T (&acc)[8][UCfg<T, B>::CB],
+template <typename T, int LAYOUT, int B, int WW = WCfg<T>::W>
+__device__ __forceinline__ void gemm(const UpdCtx<T, LAYOUT, B, WW> &ctx, int src, T (&acc)[8][UCfg<T, B, WW>::CB],
                                      const T *Bop, T *chunk0, T *chunk1, bool neg) {
-    using C = UCfg<T, B>;
+    using C = UCfg<T, B, WW>;
     const int tid = threadIdx.x;
     const int m0 = tid % C::TM;  // rows m0 + TM*i: consecutive lanes, consecutive rows
     const int c0 = (tid / C::TM) * C::CB;
@@ -393,10 +393,12 @@ struct ChainArgs {
     int fmt;
 };
 
+constexpr int kChainW = 32;  // strip width: two CTAs per SM
+
 template <int B>
-__global__ void __launch_bounds__(kWNT) chain_kernel(ChainArgs args) {
+__global__ void __launch_bounds__(kWNT, 2) chain_kernel(ChainArgs args) {
     using T = float;
-    using C = UCfg<T, B>;
+    using C = UCfg<T, B, kChainW>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *Top = reinterpret_cast<T *>(smem_raw);  // LDB x W, column-major
     T *Buf = Top + (size_t)C::LDB * C::W;      // LDB x W
@@ -419,7 +421,7 @@ __global__ void __launch_bounds__(kWNT) chain_kernel(ChainArgs args) {
     __syncthreads();
     T acc[8][C::CB];
     for (int p = 0; p < args.P; ++p) {
-        UpdCtx<T, 0, B> ctx;
+        UpdCtx<T, 0, B, kChainW> ctx;
         ctx.V = V;
         ctx.Tf = args.tfull + (size_t)p * B * B;
         ctx.row0 = (int64_t)(args.pr + p) * B;
@@ -437,7 +439,7 @@ __global__ void __launch_bounds__(kWNT) chain_kernel(ChainArgs args) {
         for (int i = 0; i < 8; ++i)
 #pragma unroll
             for (int j = 0; j < C::CB; ++j) acc[i][j] = T(0);
-        gemm<T, 0, B>(ctx, kTrows, acc, Buf, ch0, ch1, false);  // W = T_p^T Z
+        gemm<T, 0, B, kChainW>(ctx, kTrows, acc, Buf, ch0, ch1, false);  // W = T_p^T Z
         if (p == 0) {
 #pragma unroll
             for (int i = 0; i < 8; ++i)
@@ -448,7 +450,7 @@ __global__ void __launch_bounds__(kWNT) chain_kernel(ChainArgs args) {
             for (int i = 0; i < 8; ++i)
 #pragma unroll
                 for (int j = 0; j < C::CB; ++j) acc[i][j] = Top[(m0 + C::TM * i) + (c0 + j) * C::LDB];
-            gemm<T, 0, B>(ctx, kVcols, acc, Buf, ch0, ch1, true);  // Top -= Y0 W
+            gemm<T, 0, B, kChainW>(ctx, kVcols, acc, Buf, ch0, ch1, true);  // Top -= Y0 W
 #pragma unroll
             for (int i = 0; i < 8; ++i)
 #pragma unroll
@@ -475,9 +477,9 @@ __global__ void __launch_bounds__(kWNT) chain_kernel(ChainArgs args) {
     }
 }
 
-template <typename T, int B>
+template <typename T, int B, int WW = WCfg<T>::W>
 size_t upd_full_smem() {
-    using C = UCfg<T, B>;
+    using C = UCfg<T, B, WW>;
     return sizeof(T) * (2 * (size_t)C::LDB * C::W + 2 * (size_t)C::KC * C::LDC);
 }
 
@@ -519,9 +521,9 @@ int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const 
 
 template <int B>
 int launch_chain(const ChainArgs &a, cudaStream_t s) {
-    using C = UCfg<float, B>;
+    using C = UCfg<float, B, kChainW>;
     static std::atomic<bool> attr{false};
-    const size_t smem = upd_full_smem<float, B>();
+    const size_t smem = upd_full_smem<float, B, kChainW>();
     if (!attr) {
         AVS_CUDA_TRY(cudaFuncSetAttribute(chain_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;

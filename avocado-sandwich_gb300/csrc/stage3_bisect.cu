@@ -173,70 +173,121 @@ __global__ void tgk_prep_df_kernel(const double *d, const double *e, int64_t n, 
     }
 }
 
-__device__ __forceinline__ int tgk_count_df(const float2 *__restrict__ a, int64_t m, df64 x, float pivmin) {
-    int cnt = 0;
-    const df64 nx = df_neg(x);
-    df64 q = nx;
-    if (fabsf(q.hi) < pivmin) q = df64{-pivmin, 0.0f};
-    cnt += df_lt0(q);
-    for (int64_t i = 0; i < m; ++i) {
-        const float2 ai = __ldg(a + i);
-        q = df_sub(nx, df_mul(df64{ai.x, ai.y}, df_rcp(q)));
-        if (fabsf(q.hi) < pivmin) q = df64{-pivmin, 0.0f};
-        cnt += df_lt0(q);
-    }
-    return cnt;
+// 1 / q in double-float: hardware reciprocal estimate of q.hi (relative error
+// ~2^-23) refined by one Newton-Raphson step r' = r + r (1 - q r) in df64.
+__device__ __forceinline__ df64 df_rcp_fast(df64 q) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(q.hi));
+    const df64 e = df_sub(df64{1.0f, 0.0f}, df_mul_f(q, r));
+    return df_add(df64{r, 0.0f}, df_mul_f(e, r));
 }
 
-__device__ __forceinline__ int tgk_count_f(const float2 *__restrict__ a, int64_t m, float x, float pivmin) {
-    int cnt = 0;
-    float q = -x;
-    if (fabsf(q) < pivmin) q = -pivmin;
-    cnt += (q < 0.0f);
-    for (int64_t i = 0; i < m; ++i) {
-        q = -x - __fdividef(__ldg(a + i).x, q);
-        if (fabsf(q) < pivmin || !isfinite(q)) q = -pivmin;
-        cnt += (q < 0.0f);
+// Sturm counts of TGK at K shifts at once (one pass over a, K independent
+// recurrences interleaved for instruction-level parallelism).
+template <int K>
+__device__ __forceinline__ void tgk_count_df_k(const float2 *__restrict__ a, int64_t m, const df64 (&x)[K],
+                                               float pivmin, int (&cnt)[K]) {
+    df64 nx[K], q[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        nx[j] = df_neg(x[j]);
+        q[j] = nx[j];
+        if (fabsf(q[j].hi) < pivmin) q[j] = df64{-pivmin, 0.0f};
+        cnt[j] = df_lt0(q[j]);
     }
-    return cnt;
+    for (int64_t i = 0; i < m; ++i) {
+        const float2 ai = __ldg(a + i);
+        const df64 av{ai.x, ai.y};
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            q[j] = df_sub(nx[j], df_mul(av, df_rcp_fast(q[j])));
+            if (fabsf(q[j].hi) < pivmin) q[j] = df64{-pivmin, 0.0f};
+            cnt[j] += df_lt0(q[j]);
+        }
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void tgk_count_f_k(const float2 *__restrict__ a, int64_t m, const float (&x)[K],
+                                              float pivmin, int (&cnt)[K]) {
+    float q[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        q[j] = -x[j];
+        if (fabsf(q[j]) < pivmin) q[j] = -pivmin;
+        cnt[j] = (q[j] < 0.0f);
+    }
+    for (int64_t i = 0; i < m; ++i) {
+        const float ai = __ldg(a + i).x;
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            q[j] = -x[j] - __fdividef(ai, q[j]);
+            if (fabsf(q[j]) < pivmin || !isfinite(q[j])) q[j] = -pivmin;
+            cnt[j] += (q[j] < 0.0f);
+        }
+    }
 }
 
 // k-th largest singular value of the scaled problem (a = squared scaled
-// off-diagonals, bound = the scale), returned unscaled.
+// off-diagonals, bound = the scale), returned unscaled.  Multisection: three
+// interior shifts per pass split the bracket in four (two bits per pass).
 __device__ double bisect_df_one(const float2 *a, int64_t n, int64_t k, double rel_tol, double bound) {
     if (bound == 0.0) return 0.0;
     const int64_t m = 2 * n - 1;
     const float pivmin = 1e-36f;
     const int64_t target = 2 * n - 1 - k;
-    // FP32 phase on the scaled problem (all values in [0, 1])
+    // FP32 phase on the scaled problem (all values in [0, 1]); count(x) > target <=> x > sigma_k
     float flo = 0.0f, fhi = 1.0f + 1e-6f;
-    for (int it = 0; it < 20; ++it) {
-        const float mid = 0.5f * (flo + fhi);
-        if (mid <= flo || mid >= fhi) break;
-        if (tgk_count_f(a, m, mid, pivmin) > target)
-            fhi = mid;
-        else
-            flo = mid;
+    for (int it = 0; it < 10; ++it) {
+        const float w = fhi - flo;
+        float x[3] = {flo + 0.25f * w, flo + 0.5f * w, flo + 0.75f * w};
+        if (!(x[0] > flo && x[2] < fhi && x[0] < x[1] && x[1] < x[2])) break;
+        int c[3];
+        tgk_count_f_k<3>(a, m, x, pivmin, c);
+        if (c[0] > target) {
+            fhi = x[0];
+        } else if (c[1] > target) {
+            flo = x[0];
+            fhi = x[1];
+        } else if (c[2] > target) {
+            flo = x[1];
+            fhi = x[2];
+        } else {
+            flo = x[2];
+        }
     }
+    // verified bracket in double-float
     df64 lo = df64{0.0f, 0.0f}, hi = df64{1.0f + 1e-6f, 0.0f};
     {
         const float w = fmaxf(fhi - flo, 4e-7f);
-        const df64 tlo = df64{fmaxf(0.0f, flo - w), 0.0f};
-        const df64 thi = df64{fminf(1.0f + 1e-6f, fhi + w), 0.0f};
-        if (tgk_count_df(a, m, tlo, pivmin) <= target) lo = tlo;
-        if (tgk_count_df(a, m, thi, pivmin) > target) hi = thi;
+        df64 t[2] = {df64{fmaxf(0.0f, flo - w), 0.0f}, df64{fminf(1.0f + 1e-6f, fhi + w), 0.0f}};
+        int c[2];
+        tgk_count_df_k<2>(a, m, t, pivmin, c);
+        if (c[0] <= target) lo = t[0];
+        if (c[1] > target) hi = t[1];
     }
     const float tol = (float)fmax(rel_tol, 1e-15);
-    for (int it = 0; it < 100; ++it) {
+    for (int it = 0; it < 60; ++it) {
         const df64 width = df_sub(hi, lo);
         if (width.hi <= tol) break;
-        df64 mid = df_add(lo, hi);
-        mid.hi *= 0.5f;
-        mid.lo *= 0.5f;
-        if (tgk_count_df(a, m, mid, pivmin) > target)
-            hi = mid;
-        else
-            lo = mid;
+        const df64 q4 = df64{0.25f * width.hi, 0.25f * width.lo};
+        df64 x[3];
+        x[0] = df_add(lo, q4);
+        x[1] = df_add(x[0], q4);
+        x[2] = df_add(x[1], q4);
+        int c[3];
+        tgk_count_df_k<3>(a, m, x, pivmin, c);
+        if (c[0] > target) {
+            hi = x[0];
+        } else if (c[1] > target) {
+            lo = x[0];
+            hi = x[1];
+        } else if (c[2] > target) {
+            lo = x[1];
+            hi = x[2];
+        } else {
+            lo = x[2];
+        }
     }
     const df64 c = df_add(lo, hi);
     return bound * 0.5 * df_to_double(c);
