@@ -460,7 +460,19 @@ int blockbidiag_dev(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *dA, 
     w1.tfull = ws_at(h, L.off_tfull);
     int64_t launches = 0;
     AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
-    if ((rc = stage1_ge2bnd<T>(dA, n, lda, tile, w1, s, &launches)) != AVS_SUCCESS) return rc;
+    // the stage-1 kernels move 16-byte vectors: a matrix that is not 16-byte
+    // aligned (pointer or leading dimension) runs on an aligned copy
+    const bool aligned = (reinterpret_cast<uintptr_t>(dA) % 16 == 0) && ((size_t)lda * sizeof(T)) % 16 == 0;
+    if (aligned) {
+        if ((rc = stage1_ge2bnd<T>(dA, n, lda, tile, w1, s, &launches)) != AVS_SUCCESS) return rc;
+    } else {
+        T *W = reinterpret_cast<T *>(ws_at(h, L.off_w));
+        AVS_CUDA_TRY(cudaMemcpy2DAsync(W, sizeof(T) * n, dA, sizeof(T) * lda, sizeof(T) * n, n,
+                                       cudaMemcpyDeviceToDevice, s));
+        if ((rc = stage1_ge2bnd<T>(W, n, n, tile, w1, s, &launches)) != AVS_SUCCESS) return rc;
+        AVS_CUDA_TRY(cudaMemcpy2DAsync(dA, sizeof(T) * lda, W, sizeof(T) * n, sizeof(T) * n, n,
+                                       cudaMemcpyDeviceToDevice, s));
+    }
     AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
     AVS_CUDA_TRY(cudaMemcpyAsync(h->h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     rc = finish_status(h, s);
@@ -512,7 +524,15 @@ int tile_kernel(avs_handle *h, int32_t b, T *dA, T *dB, T *dtau, bool ts) {
     w1.err = err;
     w1.tfull = ws_at(h, L.off_tfull);
     if (!ts) {
-        rc = stage1_geqrt_tile<T>(dA, b, dtau, w1, s);
+        if (reinterpret_cast<uintptr_t>(dA) % 16 == 0) {
+            rc = stage1_geqrt_tile<T>(dA, b, dtau, w1, s);
+        } else {  // 16-byte vectors in the kernel: run on an aligned copy
+            T *cp = reinterpret_cast<T *>(ws_at(h, L.off_w));
+            AVS_CUDA_TRY(cudaMemcpyAsync(cp, dA, sizeof(T) * (size_t)b * b, cudaMemcpyDeviceToDevice, s));
+            rc = stage1_geqrt_tile<T>(cp, b, dtau, w1, s);
+            if (rc == AVS_SUCCESS)
+                AVS_CUDA_TRY(cudaMemcpyAsync(dA, cp, sizeof(T) * (size_t)b * b, cudaMemcpyDeviceToDevice, s));
+        }
     } else {
         T *pair = reinterpret_cast<T *>(ws_at(h, L.off_w));  // 2b x b, ld 2b
         AVS_CUDA_TRY(cudaMemcpy2DAsync(pair, sizeof(T) * 2 * b, dA, sizeof(T) * b, sizeof(T) * b, b,

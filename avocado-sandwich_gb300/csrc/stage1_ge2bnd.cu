@@ -202,12 +202,37 @@ __device__ __forceinline__ void ld4(const T *p, T (&v)[4]) {
     }
 }
 
+// Rows of the trailing tile staged per chunk in the apply's first product
+// (two chunks in flight), and the padded leading dimension of a chunk.
+template <typename T>
+__host__ __device__ constexpr int chunk_rows() { return sizeof(T) == 8 ? 16 : 32; }
+template <typename T, int LAYOUT>
+__host__ __device__ inline int chunk_ld(int b) { return LAYOUT == 0 ? chunk_rows<T>() + 4 : b + 4; }
+template <typename T>
+__host__ __device__ inline size_t chunk_elems(int b) {
+    // the larger of the two layouts: [b][CR + 4] or [CR][b + 4]
+    const size_t a0 = (size_t)b * (chunk_rows<T>() + 4), a1 = (size_t)chunk_rows<T>() * (b + 4);
+    return a0 > a1 ? a0 : a1;
+}
+
 template <typename T>
 size_t panel3_smem_bytes(int b) {
     return sizeof(T) * (32 /* tau, scalars */ + (size_t)ldpad(b) * kIB /* X */ + (size_t)b * kIB /* Yr */ +
                         (size_t)kIB * b /* Rt */ + (size_t)kIB * b /* Ws */ + 2 * kIB * kIB /* Tm, G */ +
-                        8 * kIB /* part */ + 8 + 2 * kIB /* spart, dsum, rvs */) +
+                        8 * kIB /* part */ + 8 + 2 * kIB /* spart, dsum, rvs */ + 4 /* align */ +
+                        2 * chunk_elems<T>(b) /* C chunks */) +
            sizeof(double) * 16;
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+                 "l"(gmem)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 template <typename T, int LAYOUT>
@@ -228,6 +253,9 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
     T *G = Tm + kIB * kIB;                                   // kIB * kIB
     T *part = G + kIB * kIB;                                 // 8 * kIB
     T *dsum = part + 8 * kIB;                                // kIB
+    // C chunks (16-byte aligned): LAYOUT 0 [column][row], LAYOUT 1 [row][column]
+    T *cbuf0 = reinterpret_cast<T *>((reinterpret_cast<uintptr_t>(dsum + 2 * kIB + 8) + 15) & ~(uintptr_t)15);
+    T *cbuf1 = cbuf0 + chunk_elems<T>(b);
 
     __shared__ int s_role, s_ok;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -404,44 +432,61 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
         const int nrest = b - jbase;
         const int tstart = geqrt ? c0 : 0;  // rows above c0 have Y = 0 for GEQRT
         if (nrest > 0) {
-            // (a) Z = Y^T C: thread (jg, lg) -> columns 4jg..4jg+3, reflectors 4lg..4lg+3
-            for (int jg0 = 0; jg0 * 4 < nrest; jg0 += kNT / 4) {
-                const int jg = jg0 + (tid & 63), lg = tid >> 6;
-                const bool act = jg * 4 < nrest;
-                T z[4][4];
-#pragma unroll
-                for (int a = 0; a < 4; ++a)
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) z[a][q] = T(0);
-                if (act) {
-                    const int j = jbase + 4 * jg;
-                    for (int tt = tstart; tt < b; tt += 4) {
-                        T cv[4][4];  // cv[row][col]
-                        if (LAYOUT == 0) {
-#pragma unroll
-                            for (int q = 0; q < 4; ++q) {
-                                T col[4];
-                                ld4(&V(row0 + tt, col0 + j + q), col);
-#pragma unroll
-                                for (int r = 0; r < 4; ++r) cv[r][q] = col[r];
-                            }
-                        } else {
-#pragma unroll
-                            for (int r = 0; r < 4; ++r) ld4(&V(row0 + tt + r, col0 + j), cv[r]);
+            // (a) Z = Y^T C: the rows tstart..b-1 of C stream through shared
+            // memory in chunks of CR rows (cp.async, two chunks in flight);
+            // thread j owns column j and all 16 reflectors (Y rows broadcast).
+            {
+                constexpr int CR = chunk_rows<T>();
+                constexpr int VEC = 16 / (int)sizeof(T);  // elements per 16-byte copy
+                const int cld = chunk_ld<T, LAYOUT>(b);
+                const int nch = (b - tstart + CR - 1) / CR;
+                auto issue = [&](int ch, T *buf) {
+                    const int t0 = tstart + ch * CR;
+                    const int rows = min(CR, b - t0);
+                    if (LAYOUT == 0) {  // column j: rows t0.. contiguous
+                        const int per = rows / VEC;
+                        for (int idx = tid; idx < nrest * per; idx += kNT) {
+                            const int j = idx / per, r = (idx % per) * VEC;
+                            cp_async16(buf + j * cld + r, &V(row0 + t0 + r, col0 + jbase + j));
                         }
-#pragma unroll
-                        for (int r = 0; r < 4; ++r) {
-                            const T *yrow = Yr + (tt + r) * kIB + 4 * lg;
-#pragma unroll
-                            for (int a = 0; a < 4; ++a)
-#pragma unroll
-                                for (int q = 0; q < 4; ++q) z[a][q] += yrow[a] * cv[r][q];
+                    } else {  // row t: columns contiguous
+                        const int per = nrest / VEC;
+                        for (int idx = tid; idx < rows * per; idx += kNT) {
+                            const int r = idx / per, j = (idx % per) * VEC;
+                            cp_async16(buf + r * cld + j, &V(row0 + t0 + r, col0 + jbase + j));
                         }
                     }
+                    cp_async_commit();
+                };
+                T z[kIB];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q)
+                for (int l = 0; l < kIB; ++l) z[l] = T(0);
+                issue(0, cbuf0);
+                for (int ch = 0; ch < nch; ++ch) {
+                    if (ch + 1 < nch) {
+                        issue(ch + 1, (ch & 1) ? cbuf0 : cbuf1);
+                        cp_async_wait<1>();
+                    } else {
+                        cp_async_wait<0>();
+                    }
+                    __syncthreads();
+                    const T *buf = (ch & 1) ? cbuf1 : cbuf0;
+                    const int t0 = tstart + ch * CR;
+                    const int rows = min(CR, b - t0);
+                    const int j = tid;
+                    if (j < nrest) {
+                        for (int r = 0; r < rows; ++r) {
+                            const T cv = LAYOUT == 0 ? buf[j * cld + r] : buf[r * cld + j];
+                            const T *yrow = Yr + (t0 + r) * kIB;
 #pragma unroll
-                        for (int a = 0; a < 4; ++a) Ws[(4 * lg + a) + (4 * jg + q) * kIB] = z[a][q];
+                            for (int l = 0; l < kIB; ++l) z[l] += yrow[l] * cv;
+                        }
+                    }
+                    __syncthreads();
+                }
+                if (tid < nrest) {
+#pragma unroll
+                    for (int l = 0; l < kIB; ++l) Ws[l + tid * kIB] = z[l];
                 }
             }
             __syncthreads();
@@ -463,47 +508,79 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                 }
             }
             __syncthreads();
-            // (c) C -= Y W: thread owns row t, four columns at a time
+            // The top rows are final for this block: a TSQRT role hands the
+            // block to the next role now, before updating its own tile (c).
+            if (!geqrt) {
+                const int ncols = b - c0;
+                for (int idx = tid; idx < kIB * ncols; idx += kNT) {
+                    int l, jx;
+                    if (LAYOUT == 0) { l = idx % kIB; jx = idx / kIB; } else { jx = idx % ncols; l = idx / ncols; }
+                    V(top0 + c0 + l, col0 + c0 + jx) = Rt[l + (c0 + jx) * kIB];
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    __threadfence();
+                    st_release(progress + p, cb + 1);
+                }
+            }
+            // (c) C -= Y W: thread owns row t; 16 columns per group, the next
+            // group's loads issued before the current group's arithmetic
             if (t >= tstart && t < b) {
                 T yv[kIB];
 #pragma unroll
                 for (int l = 0; l < kIB; ++l) yv[l] = Yr[t * kIB + l];
-                for (int jr = 0; jr < nrest; jr += 4) {
-                    T acc[4];
+                T cur[16], nxt[16];
+                auto load16 = [&](int jr, T (&v)[16]) {
+                    if (LAYOUT == 0) {
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) {
+                        for (int q = 0; q < 16; ++q) v[q] = __ldcg(&V(row0 + t, col0 + jbase + jr + q));
+                    } else {
+#pragma unroll
+                        for (int q4 = 0; q4 < 4; ++q4) {
+                            T w4[4];
+                            ld4(&V(row0 + t, col0 + jbase + jr + 4 * q4), w4);
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) v[4 * q4 + q] = w4[q];
+                        }
+                    }
+                };
+                load16(0, cur);
+                for (int jr = 0; jr < nrest; jr += 16) {
+                    if (jr + 16 < nrest) load16(jr + 16, nxt);
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
                         T s2 = T(0);
 #pragma unroll
                         for (int l = 0; l < kIB; ++l) s2 += yv[l] * Ws[l + (jr + q) * kIB];
-                        acc[q] = s2;
+                        cur[q] -= s2;
                     }
                     if (LAYOUT == 0) {
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            T *cp = &V(row0 + t, col0 + jbase + jr + q);
-                            *cp = __ldcg(cp) - acc[q];
-                        }
-                    } else {  // the four columns are contiguous in memory
-                        T *cp = &V(row0 + t, col0 + jbase + jr);
-                        T cv[4];
-                        ld4(cp, cv);
+                        for (int q = 0; q < 16; ++q) V(row0 + t, col0 + jbase + jr + q) = cur[q];
+                    } else {
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) cp[q] = cv[q] - acc[q];
+                        for (int q = 0; q < 16; ++q) V(row0 + t, col0 + jbase + jr + q) = cur[q];
                     }
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) cur[q] = nxt[q];
                 }
             }
-        }
-        __syncthreads();
-        if (!geqrt) {
+        } else if (!geqrt) {
+            // no columns right of the block: the top rows of the block are final
             const int ncols = b - c0;
             for (int idx = tid; idx < kIB * ncols; idx += kNT) {
                 int l, jx;
                 if (LAYOUT == 0) { l = idx % kIB; jx = idx / kIB; } else { jx = idx % ncols; l = idx / ncols; }
                 V(top0 + c0 + l, col0 + c0 + jx) = Rt[l + (c0 + jx) * kIB];
             }
+            __syncthreads();
+            if (tid == 0) {
+                __threadfence();
+                st_release(progress + p, cb + 1);
+            }
         }
         __syncthreads();
-        if (tid == 0) {
+        if (geqrt && tid == 0) {
             __threadfence();
             st_release(progress + p, cb + 1);
         }
