@@ -110,6 +110,7 @@ struct TcBufs {
     void *yrh, *yrl;  // [nt][b][b] Y planes (GEMM 2)
     float *S;         // [nt][n][b] S_p = Y_p^T A_p
     void *wh, *wl;    // [nt][n][b] W_p planes
+    void *th, *tl;    // [nt][b][b] T_p planes
     size_t bytes;
 };
 TcBufs stage1_tc_carve(void *ws, int64_t n, int b, int fmt);
@@ -119,8 +120,9 @@ int stage1_tc_transpose(const float *src, float *dst, int64_t n, int64_t i0, int
                         cudaStream_t s);
 int stage1_tc_update(float *x, int64_t n, int b, int pr, int pc, int P, const Stage1Work &w, const TcBufs &tb,
                      cudaStream_t s, int64_t *launches);
-int stage1_chain_tc(float *x, int64_t ldx, int64_t n, int b, int pr, int pc, int P, const float *tfull,
-                    const float *S, int64_t ntr, void *w_hi, void *w_lo, int fmt, cudaStream_t s);
+int stage1_chain_tc2(float *x, int64_t n, int b, int pr, int pc, int P, const float *tfull, void *t_hi, void *t_lo,
+                     const void *y_hi, const void *y_lo, const float *S, int64_t ntr, void *w_hi, void *w_lo, int fmt,
+                     int *err, cudaStream_t s);
 
 template <typename T>
 int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const Stage1Work &w,

@@ -92,6 +92,8 @@ TcBufs stage1_tc_carve(void *ws, int64_t n, int b, int fmt) {
     t.S = static_cast<float *>(take(sizeof(float) * (size_t)nt * b * n));
     t.wh = take(e * (size_t)nt * b * n);
     t.wl = take(two ? e * (size_t)nt * b * n : 0);
+    t.th = take(e * (size_t)nt * b * b);
+    t.tl = take(two ? e * (size_t)nt * b * b : 0);
     t.bytes = o;
     return t;
 }
@@ -150,8 +152,8 @@ int stage1_tc_update(float *x, int64_t n, int b, int pr, int pc, int P, const St
         if ((rc = tc::gemm(fmt, A, B, g, b, (int)ntr, P, s)) != AVS_SUCCESS) return rc;
     }
     // chain along the tiles (top tile row, W_p)
-    if ((rc = stage1_chain_tc(x, n, n, b, pr, pc, P, static_cast<const float *>(w.tfull), tb.S, ntr, tb.wh, tb.wl,
-                              fmt, s)) != AVS_SUCCESS)
+    if ((rc = stage1_chain_tc2(x, n, b, pr, pc, P, static_cast<const float *>(w.tfull), tb.th, tb.tl, tb.yrh, tb.yrl,
+                               tb.S, ntr, tb.wh, tb.wl, fmt, w.err, s)) != AVS_SUCCESS)
         return rc;
     // A_p -= Y_p W_p, p = 1..P-1
     if (P > 1) {
@@ -176,7 +178,7 @@ int stage1_tc_update(float *x, int64_t n, int b, int pr, int pc, int P, const St
         g.err = w.err;
         if ((rc = tc::gemm(fmt, A, B, g, b, (int)ntr, P - 1, s)) != AVS_SUCCESS) return rc;
     }
-    if (launches) *launches += (P > 1) ? 4 : 3;
+    if (launches) *launches += (P > 1) ? 5 : 4;
     return AVS_SUCCESS;
 }
 

@@ -20,7 +20,6 @@
 #include <algorithm>
 
 #include "avs_common.cuh"
-#include "tc_gemm.cuh"
 
 namespace avs {
 namespace {
@@ -373,110 +372,6 @@ __global__ void __launch_bounds__(kWNT) update_full_kernel(UpdFullArgs args) {
     store_strip(Top, top0);
 }
 
-// ---------------------------------------------------------------------------
-// Chain of the tensor-core update (FP32 tiles, layout 0).  The two large
-// products of every tile, S_p = Y_p^T A_p and A_p -= Y_p W_p, run on the
-// tensor cores; what is left is the sequential part along the tiles of the
-// panel, per column strip of the top tile row:
-//   p = 0 (GEQRT):  W = T0^T S_0,        Top -= Y0 W
-//   p >= 1 (TSQRT): W = T_p^T (Top + S_p), Top -= W, W_p = W (operand planes)
-// S is [P][ntr][B] (l fastest), W_p is written as [P][ntr][B] in the GEMM
-// operand format.
-struct ChainArgs {
-    float *x;
-    int64_t ldx, n;
-    int pr, pc, P;
-    const float *tfull;  // [P][B*B]
-    const float *S;      // [P][ntr][B]
-    int64_t ntr;
-    void *w_hi, *w_lo;   // [P][ntr][B]
-    int fmt;
-};
-
-constexpr int kChainW = 32;  // strip width: two CTAs per SM
-
-template <int B>
-__global__ void __launch_bounds__(kWNT, 2) chain_kernel(ChainArgs args) {
-    using T = float;
-    using C = UCfg<T, B, kChainW>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *Top = reinterpret_cast<T *>(smem_raw);  // LDB x W, column-major
-    T *Buf = Top + (size_t)C::LDB * C::W;      // LDB x W
-    T *ch0 = Buf + (size_t)C::LDB * C::W;      // KC x LDC
-    T *ch1 = ch0 + (size_t)C::KC * C::LDC;
-    const int tid = threadIdx.x;
-    const int64_t js = (int64_t)blockIdx.x * C::W;  // strip offset within the trailing columns
-    const int64_t j0 = (int64_t)(args.pc + 1) * B + js;
-    const int wc = (int)min((int64_t)C::W, args.ntr - js);
-    if (wc <= 0) return;
-    View<T, 0> V{args.x, args.ldx};
-    const int64_t top0 = (int64_t)args.pr * B;
-    const int m0 = tid % C::TM;
-    const int c0 = (tid / C::TM) * C::CB;
-
-    for (int idx = tid; idx < B * C::W; idx += kWNT) {
-        const int t = idx % B, c = idx / B;
-        Top[t + c * C::LDB] = (c < wc) ? V(top0 + t, j0 + c) : T(0);
-    }
-    __syncthreads();
-    T acc[8][C::CB];
-    for (int p = 0; p < args.P; ++p) {
-        UpdCtx<T, 0, B, kChainW> ctx;
-        ctx.V = V;
-        ctx.Tf = args.tfull + (size_t)p * B * B;
-        ctx.row0 = (int64_t)(args.pr + p) * B;
-        ctx.col0 = (int64_t)args.pc * B;
-        ctx.geqrt = (p == 0);
-        const T *Sp = args.S + ((size_t)p * args.ntr + js) * B;
-        for (int idx = tid; idx < B * C::W; idx += kWNT) {
-            const int t = idx % B, c = idx / B;
-            T z = T(0);
-            if (c < wc) z = Sp[t + (size_t)c * B] + (p > 0 ? Top[t + c * C::LDB] : T(0));
-            Buf[t + c * C::LDB] = z;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int i = 0; i < 8; ++i)
-#pragma unroll
-            for (int j = 0; j < C::CB; ++j) acc[i][j] = T(0);
-        gemm<T, 0, B, kChainW>(ctx, kTrows, acc, Buf, ch0, ch1, false);  // W = T_p^T Z
-        if (p == 0) {
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-#pragma unroll
-                for (int j = 0; j < C::CB; ++j) Buf[(m0 + C::TM * i) + (c0 + j) * C::LDB] = acc[i][j];
-            __syncthreads();
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-#pragma unroll
-                for (int j = 0; j < C::CB; ++j) acc[i][j] = Top[(m0 + C::TM * i) + (c0 + j) * C::LDB];
-            gemm<T, 0, B, kChainW>(ctx, kVcols, acc, Buf, ch0, ch1, true);  // Top -= Y0 W
-#pragma unroll
-            for (int i = 0; i < 8; ++i)
-#pragma unroll
-                for (int j = 0; j < C::CB; ++j) Top[(m0 + C::TM * i) + (c0 + j) * C::LDB] = acc[i][j];
-        } else {
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int l = m0 + C::TM * i;
-#pragma unroll
-                for (int j = 0; j < C::CB; ++j) {
-                    const int c = c0 + j;
-                    Top[l + c * C::LDB] -= acc[i][j];
-                    if (c < wc)
-                        tc::put_operand(args.fmt, args.w_hi, args.w_lo, ((int64_t)p * args.ntr + js + c) * B + l,
-                                        acc[i][j]);
-                }
-            }
-        }
-        __syncthreads();
-    }
-    for (int idx = tid; idx < B * C::W; idx += kWNT) {
-        const int t = idx % B, c = idx / B;
-        if (c < wc) V(top0 + t, j0 + c) = Top[t + c * C::LDB];
-    }
-}
-
 template <typename T, int B, int WW = WCfg<T>::W>
 size_t upd_full_smem() {
     using C = UCfg<T, B, WW>;
@@ -519,21 +414,6 @@ int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const 
     return AVS_SUCCESS;
 }
 
-template <int B>
-int launch_chain(const ChainArgs &a, cudaStream_t s) {
-    using C = UCfg<float, B, kChainW>;
-    static std::atomic<bool> attr{false};
-    const size_t smem = upd_full_smem<float, B, kChainW>();
-    if (!attr) {
-        AVS_CUDA_TRY(cudaFuncSetAttribute(chain_kernel<B>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        attr = true;
-    }
-    const unsigned gx = (unsigned)((a.ntr + C::W - 1) / C::W);
-    chain_kernel<B><<<gx, kWNT, smem, s>>>(a);
-    AVS_CUDA_TRY(cudaGetLastError());
-    return AVS_SUCCESS;
-}
-
 }  // namespace
 
 // T build alone (for the tensor-core update path).
@@ -565,15 +445,6 @@ int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr,
 template int stage1_update_full<float>(float *, int64_t, int64_t, int, int, int, int, int, const Stage1Work &,
                                        cudaStream_t);
 
-// Chain part of the tensor-core update of one half-step (layout 0, b = 128 or 256).
-int stage1_chain_tc(float *x, int64_t ldx, int64_t n, int b, int pr, int pc, int P, const float *tfull,
-                    const float *S, int64_t ntr, void *w_hi, void *w_lo, int fmt, cudaStream_t s) {
-    if (ntr <= 0) return AVS_SUCCESS;
-    ChainArgs a{x, ldx, n, pr, pc, P, tfull, S, ntr, w_hi, w_lo, fmt};
-    if (b == 256) return launch_chain<256>(a, s);
-    if (b == 128) return launch_chain<128>(a, s);
-    return AVS_ERR_INTERNAL;
-}
 template int stage1_update_full<double>(double *, int64_t, int64_t, int, int, int, int, int, const Stage1Work &,
                                         cudaStream_t);
 

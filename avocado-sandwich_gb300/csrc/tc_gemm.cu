@@ -41,114 +41,7 @@ namespace {
 
 constexpr int BM = 128;
 constexpr int NT = 128;
-constexpr int kSmemStages = 200 * 1024;      // bytes of the stage ring
-constexpr long long kWaitNs = 2000000000ll;  // 2 s per wait
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ unsigned long long gtimer() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row atoms
-// 1024 B apart (stride byte offset), leading byte offset unused for this
-// layout (1), descriptor version 1 (bits 46-47), swizzle mode 2 (bits 61-63).
-__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((addr >> 4) & 0x3FFFu);
-    d |= (uint64_t)1u << 16;
-    d |= (uint64_t)(1024u >> 4) << 32;
-    d |= (uint64_t)1u << 46;
-    d |= (uint64_t)2u << 61;
-    return d;
-}
-
-// Instruction descriptors: D FP32 (bits 4-5 = 1), A/B format (bits 7-9,
-// 10-12: TF32 = 2 for kind::tf32, BF16 = 1 for kind::f16), both operands
-// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
-__host__ __device__ constexpr uint32_t idesc(int M, int N, bool bf16) {
-    return (1u << 4) | ((bf16 ? 1u : 2u) << 7) | ((bf16 ? 1u : 2u) << 10) | ((uint32_t)(N >> 3) << 17) |
-           ((uint32_t)(M >> 4) << 24);
-}
-
-template <bool BF16>
-__device__ __forceinline__ void mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t id, uint32_t acc) {
-    if constexpr (BF16) {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "setp.ne.b32 p, %4, 0;\n\t"
-            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
-            :
-            : "r"(d_tmem), "l"(a), "l"(b), "r"(id), "r"(acc));
-    } else {
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "setp.ne.b32 p, %4, 0;\n\t"
-            "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n"
-            :
-            : "r"(d_tmem), "l"(a), "l"(b), "r"(id), "r"(acc));
-    }
-}
-
-__device__ __forceinline__ void mma_commit(uint32_t mbar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t mbar, int count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
-}
-
-// Bounded wait for the completion of phase `parity` of an mbarrier (2 s).
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, int *err) {
-    const unsigned long long t0 = gtimer();
-    for (long long it = 0;; ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.b32 %0, 1, 0, p;\n\t}\n"
-            : "=r"(done)
-            : "r"(mbar), "r"(parity)
-            : "memory");
-        if (done) return true;
-        if ((it & 255) == 255) {
-            if (ld_acquire(err) != kDevOk) return false;
-            if ((long long)(gtimer() - t0) > kWaitNs) {
-                atomicCAS(err, kDevOk, kDevTimeout);
-                return false;
-            }
-        }
-    }
-}
-
-__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t mbar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
-        "[%4];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(mbar)
-        : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
+constexpr int kSmemStages = 200 * 1024;  // bytes of the stage ring
 
 template <int BN, bool SPLIT, bool BF16>
 struct KCfg {
@@ -314,23 +207,10 @@ int launch(const Operand &A, const Operand &B, const GemmDesc &g, int mtiles, in
                                           C::SMEM));
         attr = true;
     }
-    EncodeFn enc = encode_fn();
-    if (!enc) return AVS_ERR_UNSUPPORTED;
-    const CUtensorMapDataType dt = BF16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-    const int esz = BF16 ? 2 : 4;
+    if (!encode_fn()) return AVS_ERR_UNSUPPORTED;
     CUtensorMap m[4];
-    auto make = [&](CUtensorMap *map, const Operand &op, const void *ptr, int box_rows) -> bool {
-        if (!ptr) ptr = op.hi;  // unused lo plane: any valid map
-        const cuuint64_t dims[2] = {(cuuint64_t)op.k_extent, (cuuint64_t)op.rows};
-        const cuuint64_t strides[1] = {(cuuint64_t)op.ld * esz};
-        const cuuint32_t box[2] = {(cuuint32_t)(128 / esz), (cuuint32_t)box_rows};
-        const cuuint32_t es[2] = {1, 1};
-        return enc(map, dt, 2, const_cast<void *>(ptr), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-    };
-    if (!make(&m[0], A, A.hi, BM) || !make(&m[1], A, A.lo, BM) || !make(&m[2], B, B.hi, BN) ||
-        !make(&m[3], B, B.lo, BN))
+    if (!make_tmap(&m[0], A, A.hi, BM, BF16) || !make_tmap(&m[1], A, A.lo, BM, BF16) ||
+        !make_tmap(&m[2], B, B.hi, BN, BF16) || !make_tmap(&m[3], B, B.lo, BN, BF16))
         return AVS_ERR_INTERNAL;
     gemm_kernel<BN, SPLIT, BF16><<<dim3((unsigned)ntiles, (unsigned)mtiles, (unsigned)batch), NT, C::SMEM, s>>>(
         m[0], m[1], m[2], m[3], g);
@@ -339,6 +219,23 @@ int launch(const Operand &A, const Operand &B, const GemmDesc &g, int mtiles, in
 }
 
 }  // namespace
+
+// 2-D tensor map of a K-major operand plane: box of 128 bytes of K x box_rows
+// rows, 128-byte swizzle.  A null plane (unused lo) maps the hi plane.
+bool make_tmap(CUtensorMap *map, const Operand &op, const void *ptr, int box_rows, bool bf16) {
+    EncodeFn enc = encode_fn();
+    if (!enc) return false;
+    if (!ptr) ptr = op.hi;
+    const int esz = bf16 ? 2 : 4;
+    const cuuint64_t dims[2] = {(cuuint64_t)op.k_extent, (cuuint64_t)op.rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)op.ld * esz};
+    const cuuint32_t box[2] = {(cuuint32_t)(128 / esz), (cuuint32_t)box_rows};
+    const cuuint32_t es[2] = {1, 1};
+    return enc(map, bf16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+               const_cast<void *>(ptr), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 int gemm(int fmt, const Operand &A, const Operand &B, const GemmDesc &g, int M, int N, int batch, cudaStream_t s) {
     if (M % BM || batch <= 0 || N % 128) return AVS_ERR_INTERNAL;
