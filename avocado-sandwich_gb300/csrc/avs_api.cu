@@ -33,6 +33,7 @@ struct avs_handle {
     size_t bws_bytes = 0;
     void *pinned = nullptr;
     size_t pinned_bytes = 0;
+    std::vector<cudaEvent_t> upd_ev;  // event pairs timing the tensor-core updates
     struct Graph {
         cudaGraphExec_t exec = nullptr;
         int64_t kernels = 0;
@@ -227,6 +228,18 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
     w1.tfull = ws_at(h, L.off_tfull);
     w1.tc_split = tc_split;
     w1.tc_ws = tc_split ? ws_at(h, L.off_tc) : nullptr;
+    int upd_used = 0;
+    if (tc_split && rep) {
+        const int pairs = (int)(2 * (n / b));
+        while ((int)h->upd_ev.size() < 2 * pairs) {
+            cudaEvent_t e;
+            AVS_CUDA_TRY(cudaEventCreate(&e));
+            h->upd_ev.push_back(e);
+        }
+        w1.ev_pairs = h->upd_ev.data();
+        w1.ev_cap = pairs;
+        w1.ev_used = &upd_used;
+    }
     if ((rc = stage1_ge2bnd<S>(W, n, n, b, w1, s, &launches)) != AVS_SUCCESS) return rc;
     AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
     double *AB = reinterpret_cast<double *>(ws_at(h, L.off_ab));
@@ -263,6 +276,8 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
         rep->t_stage2_ms = ev_ms(h->ev[1], h->ev[2]);
         rep->t_stage3_ms = ev_ms(h->ev[2], h->ev[3]);
         rep->t_total_ms = ev_ms(h->ev[0], h->ev[3]);
+        rep->t_update_ms = 0.0;
+        for (int q = 0; q < upd_used; ++q) rep->t_update_ms += ev_ms(h->upd_ev[2 * q], h->upd_ev[2 * q + 1]);
         rep->kernel_launches = launches;
         rep->workspace_bytes = (int64_t)h->ws_bytes;
         rep->status = rc;
@@ -400,6 +415,7 @@ int avs_destroy(avs_handle *h) {
     h->drop_graphs();
     if (h->bws) cudaFree(h->bws);
     if (h->pinned) cudaFreeHost(h->pinned);
+    for (cudaEvent_t e : h->upd_ev) cudaEventDestroy(e);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return AVS_SUCCESS;

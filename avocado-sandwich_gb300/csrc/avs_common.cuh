@@ -93,6 +93,11 @@ struct Stage1Work {
     void *tfull;      // [nt][b*b] of T: full compact-WY factors (tiles 128, 256)
     void *tc_ws = nullptr;  // tensor-core update buffers (stage1_tc_bytes), FP32 tiles
     int tc_split = 0;       // operand format of the tensor-core update (tc::Fmt); 0: SIMT update
+    // optional timing of the tensor-core updates: event pairs (start, end) per
+    // half-step, at most ev_cap pairs; *ev_used counts the pairs recorded
+    cudaEvent_t *ev_pairs = nullptr;
+    int ev_cap = 0;
+    int *ev_used = nullptr;
     // batched mode: `batch` matrices at dA + z*sA, each with its own tau / T
     // blocks / full T / flag block at the given strides (elements, ints)
     int batch = 1;

@@ -770,6 +770,21 @@ int launch_update(T *dA, int64_t lda, int64_t n, int b, int pr, int pc, int P, c
 
 }  // namespace
 
+// Tensor-core trailing update of one half-step, bracketed by a pair of the
+// caller's events when it asked for timing.
+int timed_update(float *X, int64_t n, int b, int pr, int pc, int P, const Stage1Work &w, const TcBufs &tb,
+                 cudaStream_t s, int64_t *launches) {
+    const bool timed = w.ev_pairs && w.ev_used && *w.ev_used < w.ev_cap;
+    if (timed) AVS_CUDA_TRY(cudaEventRecord(w.ev_pairs[2 * *w.ev_used], s));
+    const int rc = stage1_tc_update(X, n, b, pr, pc, P, w, tb, s, launches);
+    if (rc != AVS_SUCCESS) return rc;
+    if (timed) {
+        AVS_CUDA_TRY(cudaEventRecord(w.ev_pairs[2 * *w.ev_used + 1], s));
+        ++*w.ev_used;
+    }
+    return AVS_SUCCESS;
+}
+
 // GE2BND with tensor-core trailing updates (FP32 tiles, b = 128 or 256, one
 // matrix, lda = n): QR half-steps on X, LQ half-steps as QR half-steps on the
 // transposed trailing block in tb.xt.
@@ -787,14 +802,14 @@ int stage1_ge2bnd_tc(float *X, int64_t n, int b, const Stage1Work &w, cudaStream
         if (launches) *launches += 1;
         if (k == nt - 1) break;  // no trailing columns left
         if ((rc = stage1_tbuild<float>(X, n, b, 0, k, k, P, w, s)) != AVS_SUCCESS) return rc;
-        if ((rc = stage1_tc_update(X, n, b, k, k, P, w, tb, s, launches)) != AVS_SUCCESS) return rc;
+        if ((rc = timed_update(X, n, b, k, k, P, w, tb, s, launches)) != AVS_SUCCESS) return rc;
         if (launches) *launches += 1;
         // X rows kb.., columns k1b.. -> XT rows k1b.., columns kb..
         if ((rc = stage1_tc_transpose(X, XT, n, kb, k1b, fmt, tb, s)) != AVS_SUCCESS) return rc;
         const int PL = nt - k - 1;
         if ((rc = launch_panel<float, 0>(XT, n, b, k + 1, k, PL, 0, w, s)) != AVS_SUCCESS) return rc;
         if ((rc = stage1_tbuild<float>(XT, n, b, 0, k + 1, k, PL, w, s)) != AVS_SUCCESS) return rc;
-        if ((rc = stage1_tc_update(XT, n, b, k + 1, k, PL, w, tb, s, launches)) != AVS_SUCCESS) return rc;
+        if ((rc = timed_update(XT, n, b, k + 1, k, PL, w, tb, s, launches)) != AVS_SUCCESS) return rc;
         // and back: XT rows k1b.., columns kb.. -> X rows kb.., columns k1b..
         if ((rc = stage1_tc_transpose(XT, X, n, k1b, kb, fmt, tb, s)) != AVS_SUCCESS) return rc;
         if (launches) *launches += 4;

@@ -1,18 +1,27 @@
 """Benchmark: seconds per singular-value decomposition of one n x n matrix.
 
-Workload (default): n = 16384, tile 256, i.i.d. N(0, 1/n) entries from a
-seeded PCG64 generator (the precision configuration of the tiled SVD), FP32
-tiles with the fastest precision mode that meets FP32-class accuracy.  Every
-timed step runs the whole path -- copy of the input into the workspace,
-GE2BND, bulge chase, bisection -- on an input already resident in HBM (1 GiB,
-larger than L2).  ``e2e`` times the same call through the host C-ABI entry
-point (avs_svdvals_s: host matrix in, host singular values out, copies inside
-the timed region).
+Headline workload (the precision configuration of the tiled SVD): n = 16384,
+tile 256, i.i.d. N(0, 1/n) entries from a seeded generator, FP32 tiles with
+the trailing compact-WY updates on the tensor cores in split TF32 (three TF32
+products per product, FP32 accumulation: FP32-class accuracy, stated against
+the plain FP64 GPU path).  Every timed step runs the whole path -- copy of the
+input into the workspace, GE2BND, bulge chase, bisection -- on an input
+already resident in HBM (1 GiB per matrix, larger than L2).  ``e2e`` times the
+same call through the host C-ABI entry point (avs_svdvals_s: host matrix in,
+host singular values out, copies inside the timed region).
+
+Also reported (single GPU): ``modes`` -- the other precision modes (TF32,
+split BF16, BF16, FP32 SIMT) with their singular-value errors; ``plain_fp64``
+-- the plain FP64 GPU path on the same matrix; ``batched`` -- 4096 FP32
+matrices of orders drawn from {64..1024} in one batched call against one call
+per matrix; ``serving`` -- a bounded Poisson request stream through the
+serving loop (avs.Server) with p50/p99 latency; ``cpu_baseline`` -- the oracle
+(a C restatement of the reference's CPU path) on a bounded sample.
 
 ``--impl reference`` times the reference's path on the host CPU instead: the
-oracle (a C restatement of the reference's Blockbidiag! + bidiagonalize + the
-bidiagonal singular values, OpenMP on all host threads) on a bounded sample
-of the same workload (n = 2048, same tile), scaled to n by n^3.
+oracle (Blockbidiag! + bidiagonalize + the bidiagonal singular values, OpenMP
+on all host threads) on a bounded sample of the same workload (n = 2048, same
+tile), scaled to n by n^3.
 
 One JSON line is printed by rank 0.  Several GPUs: one process per GPU, each
 running independent SVDs (the path does not shard: replicas only).
@@ -43,9 +52,15 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=16384)
     p.add_argument("--tile", type=int, default=256)
-    p.add_argument("--precision", default="fp32")
+    p.add_argument("--precision", default="tf32x3")
     p.add_argument("--e2e-steps", type=int, default=1)
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
+    p.add_argument("--no-modes", action="store_true", help="skip the other precision modes")
+    p.add_argument("--no-batched", action="store_true")
+    p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--batch-count", type=int, default=4096)
+    p.add_argument("--serve-requests", type=int, default=40)
+    p.add_argument("--serve-rate", type=float, default=6.0)
     p.add_argument("--cpu-sample-n", type=int, default=2048)
     p.add_argument("--no-cpu", action="store_true")
     return p.parse_args()
@@ -157,34 +172,65 @@ def load_traffic():
     return {}
 
 
-def roofline(args, stage_ms):
-    """Roofline of the dominant kernel of the step (stage times are CUDA-event
-    durations on the launching stream, averaged over the timed steps)."""
+def update_flops(n, b):
+    """Flops of the tensor-core trailing updates of one GE2BND (all half-steps):
+    S_p = Y_p^T A_p and A_p -= Y_p W_p (2 b^2 ntr each per tile), the chain
+    products T_p^T Z (b^2 ntr, triangular) and Y0 W0 (b^2 ntr, triangular)."""
+    nt = n // b
+    total = 0
+    for k in range(nt - 1):
+        ntr = n - (k + 1) * b
+        for P in (nt - k, nt - k - 1):  # QR half-step k, LQ half-step k
+            total += 2 * b * b * ntr * P + 2 * b * b * ntr * (P - 1) + b * b * ntr * (P + 1)
+    return float(total)
+
+
+def roofline(args, stage_ms, update_ms):
+    """Roofline of the dominant kernel of the step.  Stage times are CUDA-event
+    durations on the launching stream, averaged over the timed steps: stage 2
+    is one launch of the bulge-chase kernel (plus two copy kernels under 0.5%
+    of it), stage 3 one bisection launch, stage 1 the GE2BND launch sequence."""
     n, b = args.n, args.tile
     hbm, bf16, src = load_peaks()
     traffic = load_traffic()
     dom = max(stage_ms, key=stage_ms.get)
     t = stage_ms[dom] / 1e3
     if dom == "stage1":
-        # GE2BND: (8/3) n^3 flops; the trailing compact-WY updates are the tensor-shaped work
         flops = 8.0 / 3.0 * n ** 3
         ach = flops / t / 1e12
-        return {"bound": "tensor", "kernel": "ge2bnd (panel + trailing WY update)", "achieved": ach,
+        return {"bound": "tensor", "kernel": "ge2bnd (panels + trailing WY updates)", "achieved": ach,
                 "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16, "traffic": traffic.get("stage1"),
-                "algorithmic": "(8/3) n^3 flops per SVD", "peak_source": src + " bf16 dense"}
+                "algorithmic": "(8/3) n^3 flops per SVD", "peak_source": src + " bf16 dense (burst), of measured"}
     if dom == "stage2":
-        # bulge chase: the band (n x (b+1) FP64) read once and the bidiagonal written once
         byts = n * (b + 1) * 8.0 + 2 * n * 8.0
         ach = byts / t / 1e9
-        return {"bound": "hbm", "kernel": "chase_kernel (band -> bidiagonal, FP64)", "achieved": ach, "peak": hbm,
-                "unit": "GB/s", "frac": ach / hbm, "traffic": traffic.get("stage2"),
-                "algorithmic": "n(b+1)*8 + 16n bytes per SVD", "peak_source": src + " HBM copy",
-                "note": "the chase is bound by FP64 issue and the sweep wavefront, not by bytes"}
+        return {"bound": "hbm", "kernel": "chase_cluster_kernel (band -> bidiagonal, double-float)",
+                "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "traffic": traffic.get("stage2"),
+                "algorithmic": "n(b+1)*8 band bytes read + 16n bidiagonal bytes written per launch (one launch "
+                               "per SVD)", "peak_source": src + " HBM copy, of measured",
+                "note": "the chase is latency-bound (sweep wavefront, dependent reflector steps); its band "
+                        "(n*3b*8 bytes) stays in L2"}
     byts = 2 * n * 8.0
     ach = byts / t / 1e9
-    return {"bound": "hbm", "kernel": "bisect_kernel (FP64 Sturm counts)", "achieved": ach, "peak": hbm,
+    return {"bound": "hbm", "kernel": "bisect_df_kernel (Sturm counts)", "achieved": ach, "peak": hbm,
             "unit": "GB/s", "frac": ach / hbm, "traffic": traffic.get("stage3"),
-            "algorithmic": "2n*8 bytes per SVD", "peak_source": src + " HBM copy"}
+            "algorithmic": "2n*8 bytes per launch", "peak_source": src + " HBM copy, of measured"}
+
+
+def tensor_roofline(args, update_ms):
+    """Achieved rate of the tensor-core trailing updates (TMA-fed tcgen05 GEMMs
+    + chain) against the measured dense bf16 peak; split modes run three
+    products per product, so their tensor work is 3x the algorithmic flops."""
+    if not update_ms:
+        return None
+    hbm, bf16, src = load_peaks()
+    flops = update_flops(args.n, args.tile)
+    mult = 3.0 if args.precision in ("tf32x3", "bf16x3") else 1.0
+    ach = flops / (update_ms / 1e3) / 1e12
+    return {"kernels": "ycopy + gemm_kernel (S = Y^T A) + chain_tc_kernel + gemm_kernel (A -= Y W), per half-step",
+            "algorithmic_tflop": flops / 1e12, "ms": update_ms, "achieved": ach, "tensor_products": mult,
+            "tensor_rate": ach * mult, "peak": bf16, "unit": "TFLOP/s", "frac": ach * mult / bf16,
+            "peak_source": src + " bf16 dense (burst), of measured; TF32 runs at half the bf16 rate"}
 
 
 def run_reference(args):
@@ -203,6 +249,89 @@ def run_reference(args):
             "config": workload_desc(args), "impl": "reference", "cpu_baseline": cb,
             "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def run_modes(args, A, h, s64):
+    """The other precision modes on the same matrix: one warm-up, one timed call."""
+    import avs
+    out = {}
+    for p in ("tf32", "bf16x3", "bf16", "fp32"):
+        if p == args.precision:
+            continue
+        r = avs.Report()
+        avs.my_CU_svdval(A, args.tile, precision=p, report=r, handle=h)
+        s = avs.my_CU_svdval(A, args.tile, precision=p, report=r, handle=h).double().cpu().numpy()
+        d = {"s_per_svd": r.t_total_ms / 1e3,
+             "stage_ms": {"stage1": r.t_stage1_ms, "stage2": r.t_stage2_ms, "stage3": r.t_stage3_ms}}
+        if s64 is not None:
+            d["max_abs_err_over_sigma_max_vs_fp64"] = float(np.max(np.abs(s - s64)) / s64[0])
+        out[p] = d
+    return out
+
+
+def run_batched(args, h):
+    """Many-matrices workload: `count` FP32 N(0, 1/n) matrices, orders drawn
+    uniformly from {64, 128, 256, 512, 1024} (seed 5), tiles from the autotuner,
+    one batched call; against one call per matrix (a seeded sample, scaled)."""
+    import torch
+    import avs
+    from avs import workloads
+    sizes = workloads.batch_sizes(args.batch_count, 5)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    mats = [torch.randn((int(m), int(m)), generator=g, device="cuda") / np.sqrt(m) for m in sizes]
+    tiles = {int(m): avs.autotune_tile(int(m), handle=h) for m in sorted(set(int(x) for x in sizes))}
+    r = avs.Report()
+    avs.svdvals_batched(mats, tiles=[tiles[int(m)] for m in sizes], report=r, handle=h)  # graph capture
+    torch.cuda.synchronize()
+    times, dev = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        outs = avs.svdvals_batched(mats, tiles=[tiles[int(m)] for m in sizes], report=r, handle=h)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+        dev.append(r.t_total_ms / 1e3)
+    wall = float(np.median(times))
+    # one call per matrix, FP32 and plain FP64, on a seeded sample of the same list
+    rng = np.random.default_rng(6)
+    idx = rng.choice(len(mats), size=min(256, len(mats)), replace=False)
+    for i in idx[:4]:
+        avs.my_CU_svdval(mats[i], tiles[int(sizes[i])], handle=h)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in idx:
+        avs.my_CU_svdval(mats[i], tiles[int(sizes[i])], handle=h)
+    torch.cuda.synchronize()
+    one32 = (time.perf_counter() - t0) / len(idx) * len(mats)
+    idx64 = idx[:64]
+    m64 = {int(i): mats[i].double() for i in idx64}
+    t0 = time.perf_counter()
+    for i in idx64:
+        avs.my_CU_svdval(m64[int(i)], tiles[int(sizes[i])], handle=h)
+    torch.cuda.synchronize()
+    one64 = (time.perf_counter() - t0) / len(idx64) * len(mats)
+    err = 0.0
+    for i in idx[:16]:
+        ref = np.linalg.svd(mats[i].double().cpu().numpy(), compute_uv=False)
+        err = max(err, float(np.max(np.abs(outs[i].double().cpu().numpy() - ref)) / ref[0]))
+    return {"workload": "%d FP32 matrices, orders uniform over {64,128,256,512,1024} (seed 5), N(0,1/n)"
+                        % len(mats),
+            "tiles": tiles, "svds_per_s": len(mats) / wall, "wall_s": wall, "device_s": float(np.median(dev)),
+            "stage_s": {"stage1": r.t_stage1_ms / 1e3, "stage2": r.t_stage2_ms / 1e3, "stage3": r.t_stage3_ms / 1e3},
+            "kernel_launches": int(r.kernel_launches),
+            "one_at_a_time_fp32_svds_per_s": len(mats) / one32,
+            "one_at_a_time_plain_fp64_svds_per_s": len(mats) / one64,
+            "one_at_a_time_sample": "%d (FP32) and %d (FP64) matrices of the list, scaled" % (len(idx), len(idx64)),
+            "speedup_vs_one_at_a_time_plain_fp64": one64 / wall,
+            "max_rel_sigma_err_vs_lapack_fp64": err, "checked": 16}
+
+
+def run_serving(args):
+    from avs import serve_bench
+    res = serve_bench.run(requests=args.serve_requests, rate=args.serve_rate, seed=7, workers=4, check=8,
+                          one_at_a_time=True)
+    res["note"] = ("bounded sample of the serving stream (orders log-uniform in [128, 8192], 70% FP32 / 30% "
+                   "FP64, half Gaussian, half geometric spectrum); latency = completion - submission")
+    return res
 
 
 def main():
@@ -235,6 +364,7 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     stage = {"stage1": 0.0, "stage2": 0.0, "stage3": 0.0}
+    update_ms = 0.0
     launches = 0
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(local) as clk:
@@ -245,9 +375,12 @@ def main():
             stage["stage1"] += rep.t_stage1_ms
             stage["stage2"] += rep.t_stage2_ms
             stage["stage3"] += rep.t_stage3_ms
+            update_ms += rep.t_update_ms
             launches += rep.kernel_launches
         end.record()
         torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     ms = start.elapsed_time(end)
     if world > 1:
         t = torch.tensor([ms], device=dev)
@@ -255,6 +388,7 @@ def main():
         ms = float(t.item())
     sigma = s.double().cpu().numpy()
     stage = {k: v / args.steps for k, v in stage.items()}
+    update_ms /= args.steps
 
     # e2e: host matrix in, host sigma out, through avs_svdvals_s
     a_cm = np.asfortranarray(a_host.T)
@@ -263,40 +397,52 @@ def main():
         t0 = time.perf_counter()
         s_host = avs.my_CU_svdval(a_cm, b, precision=args.precision, handle=h)
         e2e_times.append(time.perf_counter() - t0)
-    e2e = {"value": float(np.mean(e2e_times)) if e2e_times else None, "unit": UNIT, "h2d_bytes_per_step": int(n * n * 4),
-           "d2h_bytes_per_step": int(n * 4), "steps": args.e2e_steps}
-
-    # accuracy of this mode against the plain FP64 GPU path (whose parity with
-    # LAPACK gesdd is covered by the tests)
-    accuracy = None
-    plain = None
-    if not args.no_plain and args.precision != "fp64":
-        A64 = A.double()
-        r64 = avs.Report()
-        t0 = time.perf_counter()
-        s64 = avs.my_CU_svdval(A64, b, precision="fp64", report=r64, handle=h).cpu().numpy()
-        plain = {"s_per_svd": r64.t_total_ms / 1e3, "wall_s": time.perf_counter() - t0,
-                 "stage_ms": {"stage1": r64.t_stage1_ms, "stage2": r64.t_stage2_ms, "stage3": r64.t_stage3_ms},
-                 "speedup_of_this_mode": (r64.t_total_ms / 1e3) / (ms / 1e3 / args.steps)}
-        accuracy = {"vs": "plain FP64 GPU path", "max_abs_err_over_sigma_max":
-                    float(np.max(np.abs(sigma - s64)) / s64[0]),
-                    "host_vs_device_max_diff": float(np.max(np.abs(s_host.astype(np.float64) - sigma)))}
-        del A64
+    e2e = {"value": float(np.mean(e2e_times)) if e2e_times else None, "unit": UNIT,
+           "h2d_bytes_per_step": int(n * n * 4), "d2h_bytes_per_step": int(n * 4), "steps": args.e2e_steps,
+           "entry_point": "avs_svdvals_s (host pointers; copies inside)"}
 
     line = {"metric": METRIC, "value": ms / 1e3 / (args.steps * world), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision != "fp64" else "f64",
             "data": "synthetic N(0,1/n), PCG64-seeded torch generator (seed 4 + 1000*rank)",
             "config": dict(workload_desc(args), parallelism="replicas" if world > 1 else "single"),
-            "stage_ms": stage, "roofline": roofline(args, stage), "e2e": e2e,
-            "gpu_launches": int(launches), "clocks": clk.summary(), "accuracy": accuracy, "plain_fp64": plain}
-    if rank == 0 and not args.no_cpu:
+            "stage_ms": stage, "roofline": roofline(args, stage, update_ms),
+            "roofline_tensor_updates": tensor_roofline(args, update_ms), "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clk.summary()}
+
+    extras = rank == 0 and world == 1
+    s64 = None
+    if extras and not args.no_plain and args.precision != "fp64":
+        # the plain FP64 GPU path on the same matrix: the accuracy reference of
+        # the FP32-class modes (its own parity with LAPACK gesdd is in the tests)
+        A64 = A.double()
+        r64 = avs.Report()
+        t0 = time.perf_counter()
+        s64 = avs.my_CU_svdval(A64, b, precision="fp64", report=r64, handle=h).cpu().numpy()
+        line["plain_fp64"] = {
+            "s_per_svd": r64.t_total_ms / 1e3, "wall_s": time.perf_counter() - t0,
+            "stage_ms": {"stage1": r64.t_stage1_ms, "stage2": r64.t_stage2_ms, "stage3": r64.t_stage3_ms},
+            "speedup_of_headline_mode": (r64.t_total_ms / 1e3) / (ms / 1e3 / args.steps)}
+        line["accuracy"] = {
+            "vs": "plain FP64 GPU path", "mode": args.precision,
+            "max_abs_err_over_sigma_max": float(np.max(np.abs(sigma - s64)) / s64[0]),
+            "tolerance": 1e-5,
+            "host_vs_device_max_diff": float(np.max(np.abs(s_host.astype(np.float64) - sigma)))}
+        del A64
+    if extras and not args.no_modes:
+        line["modes"] = run_modes(args, A, h, s64)
+    del A
+    if extras and not args.no_batched:
+        line["batched"] = run_batched(args, h)
+    h.close()
+    if extras and not args.no_serving:
+        line["serving"] = run_serving(args)
+    if extras and not args.no_cpu:
         line["cpu_baseline"] = cpu_sample(args, steps=1)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
-    h.close()
 
 
 if __name__ == "__main__":

@@ -95,6 +95,8 @@ typedef struct avs_report {
     int64_t workspace_bytes;
     int32_t precision;   /* precision mode that ran */
     int32_t status;
+    double t_update_ms;  /* tensor-core modes: the trailing updates inside stage 1 (copies of Y,
+                            the two tcgen05 GEMMs and the chain), summed over the half-steps */
 } avs_report;
 
 /* ---- handle ---------------------------------------------------------------- */
