@@ -229,32 +229,44 @@ __device__ __forceinline__ void tgk_count_f_k(const float2 *__restrict__ a, int6
 }
 
 // k-th largest singular value of the scaled problem (a = squared scaled
-// off-diagonals, bound = the scale), returned unscaled.  Multisection: three
-// interior shifts per pass split the bracket in four (two bits per pass).
-__device__ double bisect_df_one(const float2 *a, int64_t n, int64_t k, double rel_tol, double bound) {
+// off-diagonals, bound = the scale), returned unscaled.  Multisection by a
+// group of G consecutive lanes: each lane counts at K = 3 shifts (one pass
+// over a, three interleaved recurrences), so a pass splits the bracket into
+// G*K + 1 parts; the group agrees on the first shift whose count exceeds the
+// target with G-lane shuffles.  FP32 passes first (to ~1e-6 of the scale),
+// then a double-float verified bracket and double-float passes to rel_tol.
+template <int G>
+__device__ double bisect_df_grp(const float2 *a, int64_t n, int64_t k, double rel_tol, double bound, int gl,
+                                unsigned gmask) {
     if (bound == 0.0) return 0.0;
+    constexpr int K = 3, NSH = G * K, NI = NSH + 1;
     const int64_t m = 2 * n - 1;
     const float pivmin = 1e-36f;
     const int64_t target = 2 * n - 1 - k;
+    auto group_first = [&](const int (&c)[K]) {
+        int first = NSH;
+#pragma unroll
+        for (int j = K - 1; j >= 0; --j)
+            if (c[j] > target) first = gl * K + j;
+#pragma unroll
+        for (int o = G / 2; o >= 1; o >>= 1) first = min(first, __shfl_xor_sync(gmask, first, o));
+        return first;
+    };
     // FP32 phase on the scaled problem (all values in [0, 1]); count(x) > target <=> x > sigma_k
     float flo = 0.0f, fhi = 1.0f + 1e-6f;
-    for (int it = 0; it < 10; ++it) {
-        const float w = fhi - flo;
-        float x[3] = {flo + 0.25f * w, flo + 0.5f * w, flo + 0.75f * w};
-        if (!(x[0] > flo && x[2] < fhi && x[0] < x[1] && x[1] < x[2])) break;
-        int c[3];
-        tgk_count_f_k<3>(a, m, x, pivmin, c);
-        if (c[0] > target) {
-            fhi = x[0];
-        } else if (c[1] > target) {
-            flo = x[0];
-            fhi = x[1];
-        } else if (c[2] > target) {
-            flo = x[1];
-            fhi = x[2];
-        } else {
-            flo = x[2];
-        }
+    for (int it = 0; it < 24 && fhi - flo > 1e-6f; ++it) {
+        const float w = (fhi - flo) * (1.0f / NI);
+        if (!(flo + w > flo) || !(fhi - w < fhi)) break;
+        float x[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) x[j] = flo + w * (float)(gl * K + j + 1);
+        int c[K];
+        tgk_count_f_k<K>(a, m, x, pivmin, c);
+        const int first = group_first(c);
+        const float nlo = flo + w * (float)first;
+        const float nhi = first == NSH ? fhi : flo + w * (float)(first + 1);
+        flo = nlo;
+        fhi = nhi;
     }
     // verified bracket in double-float
     df64 lo = df64{0.0f, 0.0f}, hi = df64{1.0f + 1e-6f, 0.0f};
@@ -270,33 +282,41 @@ __device__ double bisect_df_one(const float2 *a, int64_t n, int64_t k, double re
     for (int it = 0; it < 60; ++it) {
         const df64 width = df_sub(hi, lo);
         if (width.hi <= tol) break;
-        const df64 q4 = df64{0.25f * width.hi, 0.25f * width.lo};
-        df64 x[3];
-        x[0] = df_add(lo, q4);
-        x[1] = df_add(x[0], q4);
-        x[2] = df_add(x[1], q4);
-        int c[3];
-        tgk_count_df_k<3>(a, m, x, pivmin, c);
-        if (c[0] > target) {
-            hi = x[0];
-        } else if (c[1] > target) {
-            lo = x[0];
-            hi = x[1];
-        } else if (c[2] > target) {
-            lo = x[1];
-            hi = x[2];
-        } else {
-            lo = x[2];
-        }
+        const df64 q = df64{width.hi * (1.0f / NI), width.lo * (1.0f / NI)};
+        df64 x[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) x[j] = df_add(lo, df_mul_f(q, (float)(gl * K + j + 1)));
+        int c[K];
+        tgk_count_df_k<K>(a, m, x, pivmin, c);
+        const int first = group_first(c);
+        const df64 nlo = first == 0 ? lo : df_add(lo, df_mul_f(q, (float)first));
+        const df64 nhi = first == NSH ? hi : df_add(lo, df_mul_f(q, (float)(first + 1)));
+        lo = nlo;
+        hi = nhi;
     }
     const df64 c = df_add(lo, hi);
     return bound * 0.5 * df_to_double(c);
 }
 
+// Lanes per value.  A group of G lanes does more counts per value (about 1,
+// 2.3 and 3.2 times those of one lane for G = 1, 4, 8) in fewer dependent
+// passes, which pays while the values alone leave the GPU short of threads
+// (measured on GB300: G = 1 is fastest from n = 8192 values, G = 4/8 below).
+inline int bisect_group(int64_t nvalues) {
+    if (nvalues >= 8192) return 1;
+    if (nvalues >= 1024) return 4;
+    return 8;
+}
+
+template <int G>
 __global__ void bisect_df_kernel(const float2 *a, int64_t n, double rel_tol, const double *scratch, double *sigma) {
-    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    sigma[k] = bisect_df_one(a, n, k, rel_tol, scratch[0]);
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t k = t / G;
+    const int gl = (int)(t % G);
+    if (k >= n) return;  // whole groups: G divides the block size
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+    const double v = bisect_df_grp<G>(a, n, k, rel_tol, scratch[0], gl, gmask);
+    if (gl == 0) sigma[k] = v;
 }
 
 template <typename T>
@@ -413,9 +433,15 @@ int stage3_bisect_df(const double *dd, const double *de, int64_t n, double rel_t
     const int pb = (int)std::min<int64_t>((2 * n + 255) / 256, 1024);
     tgk_prep_df_kernel<<<pb, 256, 0, s>>>(dd, de, n, dscratch, dpairs);
     AVS_CUDA_TRY(cudaGetLastError());
-    const int threads = bisect_threads(n);
-    bisect_df_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, s>>>(dpairs, n, rel_tol, dscratch,
-                                                                                  dsigma);
+    const int G = bisect_group(n);
+    const int64_t nt = n * G;
+    const unsigned blocks = (unsigned)((nt + 127) / 128);
+    if (G == 1)
+        bisect_df_kernel<1><<<blocks, 128, 0, s>>>(dpairs, n, rel_tol, dscratch, dsigma);
+    else if (G == 4)
+        bisect_df_kernel<4><<<blocks, 128, 0, s>>>(dpairs, n, rel_tol, dscratch, dsigma);
+    else
+        bisect_df_kernel<8><<<blocks, 128, 0, s>>>(dpairs, n, rel_tol, dscratch, dsigma);
     AVS_CUDA_TRY(cudaGetLastError());
     if (launches) *launches += 3;
     return AVS_SUCCESS;
@@ -468,12 +494,17 @@ __global__ void tgk_prep_df_batched(const double *d, const double *e, int64_t n,
         a[zb * (2 * n) + i] = make_float2(h, (float)(sq - (double)h));
     }
 }
+template <int G>
 __global__ void bisect_df_batched(const float2 *a, int64_t n, int batch, double rel_tol, const double *scratch,
                                   double *sigma) {
-    const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t g = t / G;
+    const int gl = (int)(t % G);
     if (g >= n * (int64_t)batch) return;
     const int64_t zb = g / n, k = g % n;
-    sigma[g] = bisect_df_one(a + zb * (2 * n), n, k, rel_tol, scratch[zb * 4]);
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+    const double v = bisect_df_grp<G>(a + zb * (2 * n), n, k, rel_tol, scratch[zb * 4], gl, gmask);
+    if (gl == 0) sigma[g] = v;
 }
 }  // namespace
 
@@ -488,9 +519,14 @@ int stage3_bisect_df_batched(const double *dd, const double *de, int64_t n, int 
                                                                                               dscratch, dpairs);
     AVS_CUDA_TRY(cudaGetLastError());
     const int64_t nv = n * (int64_t)batch;
-    const int threads = bisect_threads(nv);
-    bisect_df_batched<<<(unsigned)((nv + threads - 1) / threads), threads, 0, s>>>(dpairs, n, batch, rel_tol,
-                                                                                   dscratch, dsigma);
+    const int G = bisect_group(nv);
+    const unsigned blocks = (unsigned)((nv * G + 127) / 128);
+    if (G == 1)
+        bisect_df_batched<1><<<blocks, 128, 0, s>>>(dpairs, n, batch, rel_tol, dscratch, dsigma);
+    else if (G == 4)
+        bisect_df_batched<4><<<blocks, 128, 0, s>>>(dpairs, n, batch, rel_tol, dscratch, dsigma);
+    else
+        bisect_df_batched<8><<<blocks, 128, 0, s>>>(dpairs, n, batch, rel_tol, dscratch, dsigma);
     AVS_CUDA_TRY(cudaGetLastError());
     if (launches) *launches += 3;
     return AVS_SUCCESS;
