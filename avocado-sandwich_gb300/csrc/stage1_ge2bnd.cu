@@ -219,7 +219,7 @@ template <typename T>
 size_t panel3_smem_bytes(int b) {
     return sizeof(T) * (32 /* tau, scalars */ + (size_t)ldpad(b) * kIB /* X */ + (size_t)b * kIB /* Yr */ +
                         (size_t)kIB * b /* Rt */ + (size_t)kIB * b /* Ws */ + 2 * kIB * kIB /* Tm, G */ +
-                        8 * kIB /* part */ + 8 + 2 * kIB /* spart, dsum, rvs */ + 4 /* align */ +
+                        16 * kIB /* part */ + 8 + 2 * kIB /* spart, dsum, rvs */ + 4 /* align */ +
                         2 * chunk_elems<T>(b) /* C chunks */) +
            sizeof(double) * 16;
 }
@@ -251,8 +251,8 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
     T *Ws = Rt + (size_t)kIB * b;                            // kIB * b, Ws[l + j*kIB]
     T *Tm = Ws + (size_t)kIB * b;                            // kIB * kIB, Tm[l + i*kIB]
     T *G = Tm + kIB * kIB;                                   // kIB * kIB
-    T *part = G + kIB * kIB;                                 // 8 * kIB
-    T *dsum = part + 8 * kIB;                                // kIB
+    T *part = G + kIB * kIB;                                 // 2 x 8 * kIB (double-buffered)
+    T *dsum = part + 16 * kIB;                               // end of the small arrays
     // C chunks (16-byte aligned): LAYOUT 0 [column][row], LAYOUT 1 [row][column]
     T *cbuf0 = reinterpret_cast<T *>((reinterpret_cast<uintptr_t>(dsum + 2 * kIB + 8) + 15) & ~(uintptr_t)15);
     T *cbuf1 = cbuf0 + chunk_elems<T>(b);
@@ -300,12 +300,14 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
         }
         __syncthreads();
 
-        // ---- the 16 reflectors of the block, one per step, all threads
+        // ---- the 16 reflectors of the block, one per step, all threads.  One
+        // barrier per reflector: the warp partial sums are double-buffered, and
+        // every warp forms the (identical) scalars and column sums itself.
         for (int i = 0; i < kIB; ++i) {
             const int c = c0 + i;
+            const int pb = i & 1;
             if (geqrt && c == b - 1) {
                 if (tid == 0) stau[i] = T(0);
-                __syncthreads();
                 continue;
             }
             const bool live = (t < b) && (geqrt ? (t > c) : true);
@@ -326,51 +328,54 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                     pv[q] = keep + __shfl_xor_sync(0xffffffffu, send, h);
                 }
             }
-            // after the rounds lane L holds the sum of index (L & 15) in pv[0]; add the half-warp partner
             pv[0] += __shfl_xor_sync(0xffffffffu, pv[0], 16);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) sq = PScal<T>::shfl_add(sq, o);
-            if (lane < kIB) part[wid * kIB + lane] = pv[0];  // lane L holds index L & 15
-            if (lane == 0) spart[wid] = sq;
+            if (lane < kIB) part[pb * 8 * kIB + wid * kIB + lane] = pv[0];  // lane L holds index L & 15
+            if (lane == 0) spart[pb * 8 + wid] = sq;
             __syncthreads();
-            if (tid == 0) {
-                Acc s_all = PScal<T>::zero();
-                for (int w = 0; w < kNT / 32; ++w) s_all = PScal<T>::shfl_add_local(s_all, spart[w]);
-                const T alpha = geqrt ? X[c + i * ldx] : Rt[i + c * kIB];
-                T out[6];
+            Acc s_all = PScal<T>::zero();
+#pragma unroll
+            for (int w = 0; w < kNT / 32; ++w) s_all = PScal<T>::shfl_add_local(s_all, spart[pb * 8 + w]);
+            const T alpha = geqrt ? X[c + i * ldx] : Rt[i + c * kIB];
+            // lane 0 of each warp forms the scalars (FP64 scalars are costly on
+            // every lane), the warp reads them with shuffles
+            T out[6];
+            if (lane == 0) {
                 PScal<T>::compute(s_all, alpha, out);
                 if (!isfinite(out[5]) || !isfinite(out[0])) {
-                    atomicCAS(args.err, kDevOk, kDevNonfinite);
+                    if (tid == 0) atomicCAS(args.err, kDevOk, kDevNonfinite);
                     out[5] = out[1] = out[2] = out[3] = T(0);
                     out[4] = alpha;
                 }
-                stau[i] = out[5];
-                scal[0] = out[0]; scal[1] = out[1]; scal[2] = out[2]; scal[3] = out[3]; scal[4] = out[4];
             }
-            if (tid > i && tid < kIB) {
-                T acc = T(0);
 #pragma unroll
-                for (int w = 0; w < kNT / 32; ++w) acc += part[w * kIB + tid];
-                dsum[tid] = acc;
-            }
+            for (int q = 0; q < 6; ++q) out[q] = __shfl_sync(0xffffffffu, out[q], 0);
+            // column sums of the 16 dot products: lane L sums column L & 15
+            T dmine = T(0);
+#pragma unroll
+            for (int w = 0; w < kNT / 32; ++w) dmine += part[pb * 8 * kIB + w * kIB + (lane & 15)];
             T rvr[kIB];
 #pragma unroll
             for (int jj = 0; jj < kIB; ++jj) rvr[jj] = geqrt ? X[c + jj * ldx] : Rt[i + (c0 + jj) * kIB];
-            __syncthreads();
-            const T tv = stau[i];
+            const T tv = out[5];
+            if (tid == 0) stau[i] = tv;
             if (tv == T(0)) {
                 if (live) X[t + i * ldx] = T(0);
-                continue;  // no barrier needed: the next step reads only own rows until its first barrier
+                continue;  // the next step reads only own rows until its barrier
             }
-            const T nu = scal[0], tc = scal[1], f = scal[2], inv = scal[3];
+            const T nu = out[0], tc = out[1], f = out[2], inv = out[3];
+            T dsv[kIB];
+#pragma unroll
+            for (int jj = 0; jj < kIB; ++jj) dsv[jj] = __shfl_sync(0xffffffffu, dmine, jj);
             if (live) {
 #pragma unroll
                 for (int jj = 0; jj < kIB; ++jj)
-                    if (jj > i) X[t + jj * ldx] -= x * (f * (nu * rvr[jj] + dsum[jj]));
+                    if (jj > i) X[t + jj * ldx] -= x * (f * (nu * rvr[jj] + dsv[jj]));
                 X[t + i * ldx] = x * inv;
             }
             if (tid < kIB && tid >= i) {
-                const T nv = (tid == i) ? scal[4] : rvr[tid] - tc * (nu * rvr[tid] + dsum[tid]);
+                const T nv = (tid == i) ? out[4] : rvr[tid] - tc * (nu * rvr[tid] + dmine);
                 if (geqrt) X[c + tid * ldx] = nv;
                 else Rt[i + (c0 + tid) * kIB] = nv;
             }

@@ -125,24 +125,39 @@ __global__ void __launch_bounds__(kWNT) tbuild_kernel(TBuildArgs args) {
         else if (bl > bi) Tf[l + (size_t)i * b] = T(0);
     }
     __syncthreads();
-    // ---- 3. column blocks J = 1..nb-1: T[0:c0, J] = -T[0:c0,0:c0] G[0:c0, J] T_JJ
-    T *Y1 = chunk;  // (b) x kWIB
+    // ---- 3. column blocks J = 1..nb-1: T[0:c0, J] = -T[0:c0,0:c0] G[0:c0, J] T_JJ.
+    // G's block (in Tf's column block J) and T_JJ are staged in shared memory;
+    // thread r owns row r: 16 accumulators over m (T upper triangular, zeros
+    // below the diagonal), one coalesced load of T(r, m) per m, then the 16 x 16
+    // product with T_JJ in registers.
+    T *Gs = chunk;              // c0 x kWIB, Gs[m * kWIB + q]
+    T *TJ = Gs + b * kWIB;      // kWIB x kWIB, TJ[qq + q * kWIB]
     for (int J = 1; J < nb; ++J) {
         const int c0 = J * kWIB;
         for (int idx = tid; idx < c0 * kWIB; idx += kWNT) {
-            const int r = idx % c0, q = idx / c0;
-            T s = T(0);
-            for (int m = r; m < c0; ++m) s += Tf[r + (size_t)m * b] * Tf[m + (size_t)(c0 + q) * b];
-            Y1[r + q * b] = s;
+            const int m = idx % c0, q = idx / c0;
+            Gs[m * kWIB + q] = Tf[m + (size_t)(c0 + q) * b];
         }
+        for (int idx = tid; idx < kWIB * kWIB; idx += kWNT) TJ[idx] = tb[(size_t)J * kWIB * kWIB + idx];
         __syncthreads();
-        for (int idx = tid; idx < c0 * kWIB; idx += kWNT) {
-            const int r = idx % c0, q = idx / c0;
-            T s = T(0);
+        const int r = tid;
+        if (r < c0) {
+            T acc[kWIB];
 #pragma unroll
-            for (int qq = 0; qq < kWIB; ++qq)
-                s += Y1[r + qq * b] * tb[(size_t)J * kWIB * kWIB + qq + q * kWIB];
-            Tf[r + (size_t)(c0 + q) * b] = -s;
+            for (int q = 0; q < kWIB; ++q) acc[q] = T(0);
+#pragma unroll 8
+            for (int m = 0; m < c0; ++m) {
+                const T t = Tf[r + (size_t)m * b];
+#pragma unroll
+                for (int q = 0; q < kWIB; ++q) acc[q] += t * Gs[m * kWIB + q];
+            }
+#pragma unroll
+            for (int q = 0; q < kWIB; ++q) {
+                T v = T(0);
+#pragma unroll
+                for (int qq = 0; qq < kWIB; ++qq) v += acc[qq] * TJ[qq + q * kWIB];
+                Tf[r + (size_t)(c0 + q) * b] = -v;
+            }
         }
         __syncthreads();
     }
