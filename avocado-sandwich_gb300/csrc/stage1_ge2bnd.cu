@@ -334,14 +334,14 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
             if (lane < kIB) part[pb * 8 * kIB + wid * kIB + lane] = pv[0];  // lane L holds index L & 15
             if (lane == 0) spart[pb * 8 + wid] = sq;
             __syncthreads();
-            Acc s_all = PScal<T>::zero();
-#pragma unroll
-            for (int w = 0; w < kNT / 32; ++w) s_all = PScal<T>::shfl_add_local(s_all, spart[pb * 8 + w]);
             const T alpha = geqrt ? X[c + i * ldx] : Rt[i + c * kIB];
             // lane 0 of each warp forms the scalars (FP64 scalars are costly on
             // every lane), the warp reads them with shuffles
             T out[6];
             if (lane == 0) {
+                Acc s_all = PScal<T>::zero();
+#pragma unroll
+                for (int w = 0; w < kNT / 32; ++w) s_all = PScal<T>::shfl_add_local(s_all, spart[pb * 8 + w]);
                 PScal<T>::compute(s_all, alpha, out);
                 if (!isfinite(out[5]) || !isfinite(out[0])) {
                     if (tid == 0) atomicCAS(args.err, kDevOk, kDevNonfinite);
