@@ -31,7 +31,7 @@ import numpy as np
 __all__ = [
     "AvsError", "Handle", "lib", "library_path", "my_CU_svdval", "svdvals", "Blockbidiag", "extract_band",
     "bidiagonalize", "diag_lapack", "geqrt_tile", "tsqrt_tile", "to_device", "from_device", "PREC",
-    "NOT_IMPLEMENTED", "EXPORTED_SYMBOLS", "Report", "svdvals_batched", "autotune_tile", "Server",
+    "NOT_IMPLEMENTED", "EXPORTED_SYMBOLS", "Report", "svdvals_batched", "autotune_tile", "Server", "tiled_QR",
     "estimate_bytes",
 ]
 
@@ -49,6 +49,7 @@ EXPORTED_SYMBOLS = [
     "avs_band_to_bidiag_dev", "avs_bidiag_svals_dev", "avs_bidiag_svals_noalloc",
     "avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d", "avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d",
     "avs_svdvals_batched_dev_s", "avs_autotune_tile", "avs_trim", "avs_workspace_bytes", "avs_estimate_bytes",
+    "avs_geqrf_dev_s", "avs_geqrf_dev_d",
     "avs_serve_create", "avs_serve_submit", "avs_serve_wait", "avs_serve_stats_get", "avs_serve_destroy",
 ]
 
@@ -122,6 +123,8 @@ def lib():
         L.avs_bidiag_svals_noalloc.argtypes = [I64, P, P, P, ctypes.c_double, P]
         L.avs_svdvals_batched_dev_s.argtypes = [P, I32, P, P, P, P, P, OP, RP]
         L.avs_autotune_tile.argtypes = [P, I64, I32, ctypes.POINTER(ctypes.c_int32)]
+        for nm in ("avs_geqrf_dev_s", "avs_geqrf_dev_d"):
+            getattr(L, nm).argtypes = [P, I64, I64, I32, P, P, OP, RP]
         L.avs_trim.argtypes = [P]
         L.avs_workspace_bytes.argtypes = [P, ctypes.POINTER(I64), ctypes.POINTER(I64)]
         L.avs_estimate_bytes.argtypes = [I64, I32, I32, I32, ctypes.POINTER(I64)]
@@ -309,6 +312,28 @@ def autotune_tile(n, sample=16, handle=None):
     best = ctypes.c_int32(0)
     _check(lib().avs_autotune_tile(h.ptr, int(n), int(sample), ctypes.byref(best)), "avs_autotune_tile")
     return best.value
+
+
+def tiled_QR(A, tile, precision=None, handle=None, report=None):
+    """tiled_QR! (KAbasedSVD/src/tiledalgos.jl:6-15) in place on a CUDA tensor
+    holding a column-major n x n matrix: R in the upper triangle, the
+    Householder vectors below.  Returns the tau values as a CUDA tensor of
+    nt * nt * tile elements (panel k, tile row r, reflector l at
+    (k * nt + r) * tile + l)."""
+    import torch
+    h = handle or default_handle()
+    if A.dim() != 2 or A.shape[0] != A.shape[1]:
+        raise NotImplementedError("Not implemented")
+    n = A.shape[0]
+    nt = n // tile if tile > 0 else 0
+    tau = torch.zeros(max(nt * nt * max(tile, 1), 1), dtype=A.dtype, device=A.device)
+    o = Opts(_prec(precision), 0, 0.0, ctypes.c_void_p(torch.cuda.current_stream(A.device).cuda_stream))
+    r = report if report is not None else Report()
+    fn = lib().avs_geqrf_dev_d if A.dtype == torch.float64 else lib().avs_geqrf_dev_s
+    rc = fn(h.ptr, n, max(A.stride(0), 1), int(tile), ctypes.c_void_p(A.data_ptr()),
+            ctypes.c_void_p(tau.data_ptr()), ctypes.byref(o), ctypes.byref(r))
+    _check(rc, "avs_geqrf_dev")
+    return tau
 
 
 def Blockbidiag(A, tile, handle=None):

@@ -501,6 +501,58 @@ int blockbidiag_dev(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *dA, 
     return rc;
 }
 
+// tiled_QR! (KAbasedSVD/src/tiledalgos.jl:6-15) in place on a device matrix.
+template <typename T>
+int geqrf_dev(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *dA, T *dtau, const avs_opts *opts,
+              avs_report *rep) {
+    int rc = check_common(h, n, n, lda, tile, dA, dA);
+    if (rep) {
+        std::memset(rep, 0, sizeof(*rep));
+        rep->status = rc;
+    }
+    if (rc != AVS_SUCCESS || n == 0) return rc;
+    const int prec = resolve_precision(opts ? opts->precision : 0, sizeof(T) == 8);
+    if (storage_elem(prec) != sizeof(T)) return AVS_ERR_UNSUPPORTED;  // tiles are the input type
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    const int split = sizeof(T) == 4 ? tc_split_of(prec, tile) : 0;
+    const Layout L = make_layout(n, tile, sizeof(T), 0, split);
+    if ((rc = ensure_ws(h, L.total)) != AVS_SUCCESS) return rc;
+    cudaStream_t s = (opts && opts->stream) ? reinterpret_cast<cudaStream_t>(opts->stream) : h->stream;
+    int *err = reinterpret_cast<int *>(ws_at(h, L.off_err));
+    AVS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+    Stage1Work w1;
+    w1.tau = ws_at(h, L.off_tau);
+    w1.tblk = ws_at(h, L.off_tblk);
+    w1.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags1));
+    w1.err = err;
+    w1.tfull = ws_at(h, L.off_tfull);
+    w1.tc_split = split;
+    w1.tc_ws = split ? ws_at(h, L.off_tc) : nullptr;
+    int64_t launches = 0;
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
+    const bool aligned = (reinterpret_cast<uintptr_t>(dA) % 16 == 0) && lda == n;
+    if (aligned) {
+        if ((rc = stage1_geqrf<T>(dA, n, n, tile, w1, dtau, s, &launches)) != AVS_SUCCESS) return rc;
+    } else {  // the kernels want a 16-byte aligned matrix with ld n: run on a copy
+        T *W = reinterpret_cast<T *>(ws_at(h, L.off_w));
+        AVS_CUDA_TRY(cudaMemcpy2DAsync(W, sizeof(T) * n, dA, sizeof(T) * lda, sizeof(T) * n, n,
+                                       cudaMemcpyDeviceToDevice, s));
+        if ((rc = stage1_geqrf<T>(W, n, n, tile, w1, dtau, s, &launches)) != AVS_SUCCESS) return rc;
+        AVS_CUDA_TRY(cudaMemcpy2DAsync(dA, sizeof(T) * lda, W, sizeof(T) * n, sizeof(T) * n, n,
+                                       cudaMemcpyDeviceToDevice, s));
+    }
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
+    AVS_CUDA_TRY(cudaMemcpyAsync(h->h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    rc = finish_status(h, s);
+    if (rep) {
+        rep->t_stage1_ms = rep->t_total_ms = ev_ms(h->ev[0], h->ev[1]);
+        rep->kernel_launches = launches;
+        rep->precision = prec;
+        rep->status = rc;
+    }
+    return rc;
+}
+
 template <typename T>
 int extract_band_dev(avs_handle *h, int64_t n, int64_t lda, int32_t bw, const T *dA, double *dB, int64_t ldb) {
     if (!h) return -1;
@@ -578,6 +630,14 @@ int avs_blockbidiag_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, f
 int avs_blockbidiag_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *dA, const avs_opts *opts,
                           avs_report *report) {
     return blockbidiag_dev<double>(h, n, lda, tile, dA, opts, report);
+}
+int avs_geqrf_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *dA, float *dtau,
+                    const avs_opts *opts, avs_report *report) {
+    return geqrf_dev<float>(h, n, lda, tile, dA, dtau, opts, report);
+}
+int avs_geqrf_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *dA, double *dtau,
+                    const avs_opts *opts, avs_report *report) {
+    return geqrf_dev<double>(h, n, lda, tile, dA, dtau, opts, report);
 }
 int avs_extract_band_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t bw, const float *dA, double *dB,
                            int64_t ldb) {

@@ -121,6 +121,8 @@ struct TcBufs {
 TcBufs stage1_tc_carve(void *ws, int64_t n, int b, int fmt);
 size_t stage1_tc_bytes(int64_t n, int b, int fmt);
 int stage1_tc_planes(const float *x, int64_t n, int fmt, const TcBufs &tb, cudaStream_t s);
+int stage1_tc_planes_block(const float *x, int64_t n, int64_t r0, int64_t j0, int fmt, const TcBufs &tb,
+                           cudaStream_t s);
 int stage1_tc_transpose(const float *src, float *dst, int64_t n, int64_t i0, int64_t j0, int fmt, const TcBufs &tb,
                         cudaStream_t s);
 int stage1_tc_update(float *x, int64_t n, int b, int pr, int pc, int P, const Stage1Work &w, const TcBufs &tb,
@@ -135,6 +137,9 @@ int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr,
 
 template <typename T>
 int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cudaStream_t s, int64_t *launches);
+template <typename T>
+int stage1_geqrf(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, T *dtau, cudaStream_t s,
+                 int64_t *launches);
 
 template <typename T>
 int stage1_geqrt_tile(T *dA, int b, T *dtau, const Stage1Work &w, cudaStream_t s);

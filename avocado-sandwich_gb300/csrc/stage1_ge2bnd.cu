@@ -854,6 +854,53 @@ int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cud
     return AVS_SUCCESS;
 }
 
+// Tiled QR (tiled_QR!, KAbasedSVD/src/tiledalgos.jl:6-15): the QR half-steps
+// of GE2BND alone.  On return R is in the upper triangle and the reflectors
+// below it (unit lower V in the diagonal tiles, full V in the tiles below);
+// dtau (optional) receives the tau of panel k, tile row r, reflector l at
+// dtau[(k * nt + r) * b + l] (rows r >= k).
+template <typename T>
+int stage1_geqrf(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, T *dtau, cudaStream_t s,
+                 int64_t *launches) {
+    const int nt = (int)(n / b);
+    int rc;
+    const bool tc = sizeof(T) == 4 && w.tc_split && w.tc_ws && b >= 128 && lda == n && w.batch <= 1;
+    TcBufs tb{};
+    if (tc) tb = stage1_tc_carve(w.tc_ws, n, b, w.tc_split);
+    for (int k = 0; k < nt; ++k) {
+        const int P = nt - k;
+        if ((rc = launch_panel<T, 0>(dA, lda, b, k, k, P, 0, w, s)) != AVS_SUCCESS) return rc;
+        if (launches) ++*launches;
+        if (dtau)
+            AVS_CUDA_TRY(cudaMemcpyAsync(dtau + ((size_t)k * nt + k) * b, w.tau, sizeof(T) * (size_t)P * b,
+                                         cudaMemcpyDeviceToDevice, s));
+        if (k == nt - 1) break;
+        if constexpr (sizeof(T) == 4) {
+            if (tc) {
+                // operand planes of the trailing block as the update reads it now
+                const int64_t r0 = (int64_t)k * b, j0 = (int64_t)(k + 1) * b;
+                if ((rc = stage1_tc_planes_block(reinterpret_cast<float *>(dA), n, r0, j0, w.tc_split, tb, s)) !=
+                    AVS_SUCCESS)
+                    return rc;
+                if ((rc = stage1_tbuild<float>(reinterpret_cast<float *>(dA), n, b, 0, k, k, P, w, s)) != AVS_SUCCESS)
+                    return rc;
+                if ((rc = timed_update(reinterpret_cast<float *>(dA), n, b, k, k, P, w, tb, s, launches)) !=
+                    AVS_SUCCESS)
+                    return rc;
+                if (launches) *launches += 2;
+                continue;
+            }
+        }
+        if (b >= 128 && w.tfull)
+            rc = stage1_update_full<T>(dA, lda, n, b, 0, k, k, P, w, s);
+        else
+            rc = launch_update<T, 0>(dA, lda, n, b, k, k, P, w, s);
+        if (rc != AVS_SUCCESS) return rc;
+        if (launches) *launches += (b >= 128 && w.tfull) ? 2 : 1;
+    }
+    return AVS_SUCCESS;
+}
+
 template <typename T>
 int stage1_geqrt_tile(T *dA, int b, T *dtau, const Stage1Work &w, cudaStream_t s) {
     int rc = launch_panel<T, 0>(dA, b, b, 0, 0, 1, 0, w, s);
@@ -875,6 +922,10 @@ int stage1_tsqrt_pair(T *dRB, int b, T *dtau, const Stage1Work &w, cudaStream_t 
 template int stage1_ge2bnd<float>(float *, int64_t, int64_t, int, const Stage1Work &, cudaStream_t, int64_t *);
 template int stage1_ge2bnd<double>(double *, int64_t, int64_t, int, const Stage1Work &, cudaStream_t, int64_t *);
 template int stage1_geqrt_tile<float>(float *, int, float *, const Stage1Work &, cudaStream_t);
+template int stage1_geqrf<float>(float *, int64_t, int64_t, int, const Stage1Work &, float *, cudaStream_t,
+                                 int64_t *);
+template int stage1_geqrf<double>(double *, int64_t, int64_t, int, const Stage1Work &, double *, cudaStream_t,
+                                  int64_t *);
 template int stage1_geqrt_tile<double>(double *, int, double *, const Stage1Work &, cudaStream_t);
 template int stage1_tsqrt_pair<float>(float *, int, float *, const Stage1Work &, cudaStream_t);
 template int stage1_tsqrt_pair<double>(double *, int, double *, const Stage1Work &, cudaStream_t);

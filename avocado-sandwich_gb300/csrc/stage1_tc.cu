@@ -14,6 +14,8 @@
 // Operand planes (rounded TF32, TF32 hi/lo, BF16, BF16 hi/lo) of the trailing
 // block come out of the transposes; those of Y out of a copy kernel; those of
 // W out of the chain.
+#include <algorithm>
+
 #include "avs_common.cuh"
 #include "tc_gemm.cuh"
 
@@ -67,7 +69,25 @@ __global__ void planes_kernel(const float *x, int64_t count, int fmt, void *ph, 
         tc::put_operand(fmt, ph, pl, i, x[i]);
 }
 
+// planes of the block rows r0.., columns j0.. of x (same indexing)
+__global__ void planes_block_kernel(const float *x, int64_t n, int64_t r0, int64_t j0, int fmt, void *ph, void *pl) {
+    const int64_t rows = n - r0;
+    for (int64_t c = j0 + blockIdx.y; c < n; c += gridDim.y)
+        for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x)
+            tc::put_operand(fmt, ph, pl, (r0 + r) + c * n, x[(r0 + r) + c * n]);
+}
+
 }  // namespace
+
+int stage1_tc_planes_block(const float *x, int64_t n, int64_t r0, int64_t j0, int fmt, const TcBufs &tb,
+                           cudaStream_t s) {
+    if (r0 >= n || j0 >= n) return AVS_SUCCESS;
+    const unsigned gy = (unsigned)std::min<int64_t>(n - j0, 4096);
+    planes_block_kernel<<<dim3((unsigned)std::min<int64_t>((n - r0 + 255) / 256, 64), gy), 256, 0, s>>>(
+        x, n, r0, j0, fmt, tb.ph, tb.pl);
+    AVS_CUDA_TRY(cudaGetLastError());
+    return AVS_SUCCESS;
+}
 
 TcBufs stage1_tc_carve(void *ws, int64_t n, int b, int fmt) {
     TcBufs t{};

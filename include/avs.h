@@ -135,6 +135,18 @@ int avs_blockbidiag_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, f
                           avs_report *report);
 int avs_blockbidiag_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *dA, const avs_opts *opts,
                           avs_report *report);
+/* tiled_QR! (KAbasedSVD/src/tiledalgos.jl:6-15) on a TiledMatrix in place: the QR
+ * half-steps of Blockbidiag! alone (GEQRT of the diagonal tile, TSQRT down the
+ * panel, compact-WY updates of the trailing tiles).  On return R is in the upper
+ * triangle, the Householder vectors below it (unit lower V in the diagonal
+ * tiles, V in the tiles below, as the reference leaves them).  dtau (may be
+ * NULL; nt * nt * tile elements, nt = n / tile) receives the tau of panel k,
+ * tile row r >= k, reflector l at dtau[(k * nt + r) * tile + l].  opts->precision
+ * selects the update arithmetic as for avs_svdvals (FP32: SIMT or tensor cores). */
+int avs_geqrf_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *dA, float *dtau,
+                    const avs_opts *opts, avs_report *report);
+int avs_geqrf_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *dA, double *dtau,
+                    const avs_opts *opts, avs_report *report);
 /* Copy the upper band 0 <= j - i <= bw of a dense n x n matrix into a dense
  * FP64 n x n matrix with zeros elsewhere (the reference's banded array). */
 int avs_extract_band_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t bw, const float *dA, double *dB,
