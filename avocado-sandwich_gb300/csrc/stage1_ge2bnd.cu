@@ -208,6 +208,10 @@ template <typename T>
 __host__ __device__ constexpr int chunk_rows() { return sizeof(T) == 8 ? 16 : 32; }
 template <typename T, int LAYOUT>
 __host__ __device__ inline int chunk_ld(int b) { return LAYOUT == 0 ? chunk_rows<T>() + 4 : b + 4; }
+// chunks in flight: the first ones are issued when a block starts, so their
+// loads overlap the block's reflectors
+template <typename T>
+__host__ __device__ constexpr int chunk_bufs() { return sizeof(T) == 8 ? 2 : 4; }
 template <typename T>
 __host__ __device__ inline size_t chunk_elems(int b) {
     // the larger of the two layouts: [b][CR + 4] or [CR][b + 4]
@@ -220,7 +224,7 @@ size_t panel3_smem_bytes(int b) {
     return sizeof(T) * (32 /* tau, scalars */ + (size_t)ldpad(b) * kIB /* X */ + (size_t)b * kIB /* Yr */ +
                         (size_t)kIB * b /* Rt */ + (size_t)kIB * b /* Ws */ + 2 * kIB * kIB /* Tm, G */ +
                         16 * kIB /* part */ + 8 + 2 * kIB /* spart, dsum, rvs */ + 4 /* align */ +
-                        2 * chunk_elems<T>(b) /* C chunks */) +
+                        chunk_bufs<T>() * chunk_elems<T>(b) /* C chunks */) +
            sizeof(double) * 16;
 }
 
@@ -255,7 +259,6 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
     T *dsum = part + 16 * kIB;                               // end of the small arrays
     // C chunks (16-byte aligned): LAYOUT 0 [column][row], LAYOUT 1 [row][column]
     T *cbuf0 = reinterpret_cast<T *>((reinterpret_cast<uintptr_t>(dsum + 2 * kIB + 8) + 15) & ~(uintptr_t)15);
-    T *cbuf1 = cbuf0 + chunk_elems<T>(b);
 
     __shared__ int s_role, s_ok;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -299,6 +302,41 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
             }
         }
         __syncthreads();
+
+        // ---- first chunks of the trailing columns (their loads overlap the reflectors)
+        const int jbase = c0 + kIB;
+        const int nrest = b - jbase;
+        const int tstart = geqrt ? c0 : 0;  // rows above c0 have Y = 0 for GEQRT
+        constexpr int CR = chunk_rows<T>();
+        constexpr int NBUF = chunk_bufs<T>();
+        const int cld = chunk_ld<T, LAYOUT>(b);
+        const int nch = nrest > 0 ? (b - tstart + CR - 1) / CR : 0;
+        auto issue = [&](int ch) {  // one cp.async group per chunk (empty past the last)
+            if (ch < nch) {
+                constexpr int VEC = 16 / (int)sizeof(T);  // elements per 16-byte copy
+                T *buf = cbuf0 + (size_t)(ch % NBUF) * chunk_elems<T>(b);
+                const int t0 = tstart + ch * CR;
+                const int rows = min(CR, b - t0);
+                if (LAYOUT == 0) {  // column j: rows t0.. contiguous
+                    const int per = rows / VEC;
+                    for (int idx = tid; idx < nrest * per; idx += kNT) {
+                        const int j = idx / per, r = (idx % per) * VEC;
+                        cp_async16(buf + j * cld + r, &V(row0 + t0 + r, col0 + jbase + j));
+                    }
+                } else {  // row t: columns contiguous
+                    const int per = nrest / VEC;
+                    for (int idx = tid; idx < rows * per; idx += kNT) {
+                        const int r = idx / per, j = (idx % per) * VEC;
+                        cp_async16(buf + r * cld + j, &V(row0 + t0 + r, col0 + jbase + j));
+                    }
+                }
+            }
+            cp_async_commit();
+        };
+        if (nrest > 0) {
+#pragma unroll
+            for (int q = 0; q < NBUF; ++q) issue(q);
+        }
 
         // ---- the 16 reflectors of the block, one per step, all threads.  One
         // barrier per reflector: the warp partial sums are double-buffered, and
@@ -433,49 +471,19 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
         if (tid < kIB * kIB) tblk_out[(size_t)cb * kIB * kIB + tid] = Tm[tid];
 
         // ---- apply to the rest of the tile
-        const int jbase = c0 + kIB;
-        const int nrest = b - jbase;
-        const int tstart = geqrt ? c0 : 0;  // rows above c0 have Y = 0 for GEQRT
         if (nrest > 0) {
             // (a) Z = Y^T C: the rows tstart..b-1 of C stream through shared
-            // memory in chunks of CR rows (cp.async, two chunks in flight);
-            // thread j owns column j and all 16 reflectors (Y rows broadcast).
+            // memory in chunks of CR rows (cp.async ring of NBUF chunks, issued
+            // since the block started); thread j owns column j and all 16
+            // reflectors (Y rows broadcast).
             {
-                constexpr int CR = chunk_rows<T>();
-                constexpr int VEC = 16 / (int)sizeof(T);  // elements per 16-byte copy
-                const int cld = chunk_ld<T, LAYOUT>(b);
-                const int nch = (b - tstart + CR - 1) / CR;
-                auto issue = [&](int ch, T *buf) {
-                    const int t0 = tstart + ch * CR;
-                    const int rows = min(CR, b - t0);
-                    if (LAYOUT == 0) {  // column j: rows t0.. contiguous
-                        const int per = rows / VEC;
-                        for (int idx = tid; idx < nrest * per; idx += kNT) {
-                            const int j = idx / per, r = (idx % per) * VEC;
-                            cp_async16(buf + j * cld + r, &V(row0 + t0 + r, col0 + jbase + j));
-                        }
-                    } else {  // row t: columns contiguous
-                        const int per = nrest / VEC;
-                        for (int idx = tid; idx < rows * per; idx += kNT) {
-                            const int r = idx / per, j = (idx % per) * VEC;
-                            cp_async16(buf + r * cld + j, &V(row0 + t0 + r, col0 + jbase + j));
-                        }
-                    }
-                    cp_async_commit();
-                };
                 T z[kIB];
 #pragma unroll
                 for (int l = 0; l < kIB; ++l) z[l] = T(0);
-                issue(0, cbuf0);
                 for (int ch = 0; ch < nch; ++ch) {
-                    if (ch + 1 < nch) {
-                        issue(ch + 1, (ch & 1) ? cbuf0 : cbuf1);
-                        cp_async_wait<1>();
-                    } else {
-                        cp_async_wait<0>();
-                    }
+                    cp_async_wait<NBUF - 1>();
                     __syncthreads();
-                    const T *buf = (ch & 1) ? cbuf1 : cbuf0;
+                    const T *buf = cbuf0 + (size_t)(ch % NBUF) * chunk_elems<T>(b);
                     const int t0 = tstart + ch * CR;
                     const int rows = min(CR, b - t0);
                     const int j = tid;
@@ -488,7 +496,9 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                         }
                     }
                     __syncthreads();
+                    issue(ch + NBUF);
                 }
+                cp_async_wait<0>();
                 if (tid < nrest) {
 #pragma unroll
                     for (int l = 0; l < kIB; ++l) Ws[l + tid * kIB] = z[l];
