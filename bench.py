@@ -59,8 +59,8 @@ def parse():
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--no-serving", action="store_true")
     p.add_argument("--batch-count", type=int, default=4096)
-    p.add_argument("--serve-requests", type=int, default=40)
-    p.add_argument("--serve-rate", type=float, default=6.0)
+    p.add_argument("--serve-requests", type=int, default=120)
+    p.add_argument("--serve-rate", type=float, default=12.0)
     p.add_argument("--cpu-sample-n", type=int, default=2048)
     p.add_argument("--no-cpu", action="store_true")
     return p.parse_args()
@@ -328,7 +328,7 @@ def run_batched(args, h):
 def run_serving(args):
     from avs import serve_bench
     res = serve_bench.run(requests=args.serve_requests, rate=args.serve_rate, seed=7, workers=4, check=8,
-                          one_at_a_time=True)
+                          one_at_a_time=True, baseline_every=3)
     res["note"] = ("bounded sample of the serving stream (orders log-uniform in [128, 8192], 70% FP32 / 30% "
                    "FP64, half Gaussian, half geometric spectrum); latency = completion - submission")
     return res
