@@ -2,7 +2,7 @@
 
 Headline workload (the precision configuration of the tiled SVD): n = 16384,
 tile 256, i.i.d. N(0, 1/n) entries from a seeded generator, FP32 tiles with
-the trailing compact-WY updates on the tensor cores in split TF32 (three TF32
+the trailing compact-WY updates on the tensor cores in split BF16 (three BF16
 products per product, FP32 accumulation: FP32-class accuracy, stated against
 the plain FP64 GPU path).  Every timed step runs the whole path -- copy of the
 input into the workspace, GE2BND, bulge chase, bisection -- on an input
@@ -10,8 +10,8 @@ already resident in HBM (1 GiB per matrix, larger than L2).  ``e2e`` times the
 same call through the host C-ABI entry point (avs_svdvals_s: host matrix in,
 host singular values out, copies inside the timed region).
 
-Also reported (single GPU): ``modes`` -- the other precision modes (TF32,
-split BF16, BF16, FP32 SIMT) with their singular-value errors; ``plain_fp64``
+Also reported (single GPU): ``modes`` -- the other precision modes (split
+TF32, TF32, BF16, FP32 SIMT) with their singular-value errors; ``plain_fp64``
 -- the plain FP64 GPU path on the same matrix; ``batched`` -- 4096 FP32
 matrices of orders drawn from {64..1024} in one batched call against one call
 per matrix; ``serving`` -- a bounded Poisson request stream through the
@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=16384)
     p.add_argument("--tile", type=int, default=256)
-    p.add_argument("--precision", default="tf32x3")
+    p.add_argument("--precision", default="bf16x3")
     p.add_argument("--e2e-steps", type=int, default=1)
     p.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     p.add_argument("--no-modes", action="store_true", help="skip the other precision modes")
@@ -255,7 +255,7 @@ def run_modes(args, A, h, s64):
     """The other precision modes on the same matrix: one warm-up, one timed call."""
     import avs
     out = {}
-    for p in ("tf32", "bf16x3", "bf16", "fp32"):
+    for p in ("tf32x3", "tf32", "bf16x3", "bf16", "fp32"):
         if p == args.precision:
             continue
         r = avs.Report()
