@@ -168,10 +168,11 @@ __global__ void __launch_bounds__(kChaseThreads) chase_kernel(double *ab, int64_
 template <int BW, int CC = (BW >= 128 ? 8 : (BW == 64 ? 4 : (BW == 32 ? 2 : 1)))>
 struct ChaseCfg {
     static constexpr int C = CC;  // CTAs per cluster (one sweep per cluster)
-    // threads per CTA: 16-CTA clusters run 256-thread CTAs, two per SM, so
-    // that the stalls of one sweep's CTA overlap the work of another's
-    static constexpr int NT = CC >= 16 ? 256 : 512;
-    static constexpr int MINB = NT == 256 ? 2 : 1;
+    // 512 threads per CTA: an op's latency (the sweep wavefront's step) falls
+    // with the threads that share it (measured: 128-thread CTAs, several per
+    // SM, were slower at every band width)
+    static constexpr int NT = 512;
+    static constexpr int MINB = 1;
     static constexpr int RPC = 2 * BW / C;          // R op: rows per CTA (64 or 32)
     static constexpr int G = NT / RPC;              // R op: column groups
     static constexpr int CPG = BW / G;              // R op: columns per group
@@ -499,14 +500,6 @@ int launch_chase_cluster(typename ChaseAr<S>::St *dAB, int64_t n, int64_t ldab, 
     cfg.stream = s;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    if (Cfg::C > 8) {
-        static std::atomic<bool> attr_set{false};
-        if (!attr_set) {
-            AVS_CUDA_TRY(cudaFuncSetAttribute(chase_cluster_kernel<BW, S, CC>,
-                                              cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
-            attr_set = true;
-        }
-    }
     int max_clusters = 0;
     cfg.gridDim = dim3(Cfg::C * 64);
     if (cudaOccupancyMaxActiveClusters(&max_clusters, chase_cluster_kernel<BW, S, CC>, &cfg) != cudaSuccess ||
