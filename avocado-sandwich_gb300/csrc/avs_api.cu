@@ -132,7 +132,7 @@ int resolve_precision(int32_t requested, bool input_double) {
     return requested;
 }
 
-// Storage element size of the stage-1 tiles for a precision mode (0 = not provided by this build).
+// Storage element size of the stage-1 tiles for a precision mode (0 = mode not provided).
 size_t storage_elem(int prec) {
     switch (prec) {
         case AVS_PREC_FP64: return 8;
@@ -375,7 +375,7 @@ const char *avs_strerror(int status) {
         case AVS_ERR_TIMEOUT: return "a bounded device-side wait timed out";
         case AVS_ERR_NONFINITE: return "non-finite value met in the factorisation";
         case AVS_ERR_NO_DEVICE: return "no usable CUDA device";
-        case AVS_ERR_UNSUPPORTED: return "valid request not provided by this build";
+        case AVS_ERR_UNSUPPORTED: return "valid request not supported by the library";
         case AVS_ERR_INTERNAL: return "internal error";
         case AVS_ERR_TOO_LARGE: return "size exceeds the static scratch of the allocation-free entry point";
         default: return status < 0 ? "invalid argument" : "unknown error";

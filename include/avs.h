@@ -50,7 +50,7 @@ extern "C" {
 #define AVS_ERR_TIMEOUT 3              /* a bounded device-side wait gave up */
 #define AVS_ERR_NONFINITE 4            /* NaN/Inf met in the factorisation */
 #define AVS_ERR_NO_DEVICE 5            /* no usable CUDA device */
-#define AVS_ERR_UNSUPPORTED 6          /* valid request this build does not provide */
+#define AVS_ERR_UNSUPPORTED 6          /* valid request the library does not support */
 #define AVS_ERR_INTERNAL 7
 #define AVS_ERR_TOO_LARGE 8            /* n above the static scratch of avs_bidiag_svals_noalloc */
 

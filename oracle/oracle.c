@@ -2,7 +2,7 @@
  * Oracle library (TEST INFRASTRUCTURE ONLY): a CPU restatement of the
  * reference's tiled singular-value path, evelyne-ringoot/Avocado-sandwich
  * my_CU_svdval (CUDAbasedSVD/SVD_GPU.jl:257-283) on the KernelAbstractions
- * building blocks (the .jl files of KAbasedSVD/src).  It is the checker for the CUDA
+ * building blocks (the .jl files of KAbasedSVD/src).  It is the parity reference for the CUDA
  * library and the timed CPU baseline; the product never links or calls it.
  *
  * Stage 3 of the reference is LAPACK bdsdc('U','N') (KAbasedSVD/src/

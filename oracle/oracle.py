@@ -1,6 +1,6 @@
 """ctypes wrapper around ``liboracle.so`` (built from ``oracle.c`` by ``make``).
 
-TEST INFRASTRUCTURE ONLY -- the checker for the CUDA library.
+TEST INFRASTRUCTURE ONLY -- the parity reference for the CUDA library.
 
 Functions mirror the reference building blocks (paths inside
 evelyne-ringoot/Avocado-sandwich):

@@ -4,7 +4,7 @@
  * This file is the oracle: it is included twice by oracle.c, once with
  * OT = float (suffix _s) and once with OT = double (suffix _d).  Nothing in the
  * product library links it; only tests/, __graft_entry__.smoke() and bench.py's
- * CPU-baseline leg load it, as the checker.
+ * CPU-baseline leg load it, as the parity reference.
  *
  * What it restates (paths are inside evelyne-ringoot/Avocado-sandwich):
  *   - GEQRT tile kernel            KAbasedSVD/src/QRkernels.jl:3-66
