@@ -341,6 +341,12 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
         // ---- the 16 reflectors of the block, one per step, all threads.  One
         // barrier per reflector: the warp partial sums are double-buffered, and
         // every warp forms the (identical) scalars and column sums itself.
+        // Every warp reads the pivot row (alpha and the row the reflector
+        // updates) after the step's barrier, so warp 0 keeps the updated pivot
+        // row in registers and stores it after the next barrier: no later step
+        // reads that row before the Gram matrix below.
+        T *pend_at = nullptr;
+        T pend_v = T(0);
         for (int i = 0; i < kIB; ++i) {
             const int c = c0 + i;
             const int pb = i & 1;
@@ -372,6 +378,10 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
             if (lane < kIB) part[pb * 8 * kIB + wid * kIB + lane] = pv[0];  // lane L holds index L & 15
             if (lane == 0) spart[pb * 8 + wid] = sq;
             __syncthreads();
+            if (pend_at) {  // the previous step's pivot row, read by every warp before this barrier
+                *pend_at = pend_v;
+                pend_at = nullptr;
+            }
             const T alpha = geqrt ? X[c + i * ldx] : Rt[i + c * kIB];
             // lane 0 of each warp forms the scalars (FP64 scalars are costly on
             // every lane), the warp reads them with shuffles
@@ -413,11 +423,12 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                 X[t + i * ldx] = x * inv;
             }
             if (tid < kIB && tid >= i) {
-                const T nv = (tid == i) ? out[4] : rvr[tid] - tc * (nu * rvr[tid] + dmine);
-                if (geqrt) X[c + tid * ldx] = nv;
-                else Rt[i + (c0 + tid) * kIB] = nv;
+                pend_v = (tid == i) ? out[4] : rvr[tid] - tc * (nu * rvr[tid] + dmine);
+                pend_at = geqrt ? &X[c + tid * ldx] : &Rt[i + (c0 + tid) * kIB];
             }
         }
+        __syncthreads();
+        if (pend_at) *pend_at = pend_v;
         __syncthreads();
 
         // ---- Gram matrix of the block's reflectors, T (warp 0), masked Y

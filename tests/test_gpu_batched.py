@@ -59,6 +59,29 @@ def test_batched_tile128(avs_mod, torch_cuda):
         assert rel_err(got, sl.svdvals(a.astype(np.float64))) < TOL32
 
 
+@pytest.mark.parametrize("n,tile,count", [(512, 32, 64), (512, 64, 64), (1024, 128, 40)])
+def test_batched_large_batch_copies(avs_mod, torch_cuda, n, tile, count):
+    """Many copies of one matrix in one call: every copy gives the single
+    call's values bit for bit.  With this many CTAs the panel kernels of
+    different matrices share SMs, so warps of one CTA drift apart in time."""
+    hosts, devs = _mats(avs_mod, [n], 300 + tile)
+    copies = [devs[0].clone() for _ in range(count)]
+    outs = avs_mod.svdvals_batched(copies, tiles=tile)
+    single = avs_mod.my_CU_svdval(devs[0], tile).cpu().numpy()
+    for o in outs:
+        assert np.array_equal(o.cpu().numpy(), single), rel_err(o.cpu().numpy(), single)
+    assert rel_err(single, sl.svdvals(hosts[0].astype(np.float64))) < TOL32
+
+
+def test_batched_large_batch_distinct(avs_mod, torch_cuda):
+    """48 distinct matrices of order 512, tile 64: each within the FP32
+    tolerance of LAPACK."""
+    hosts, devs = _mats(avs_mod, [512] * 48, 404)
+    outs = avs_mod.svdvals_batched(devs, tiles=64)
+    for a, o in zip(hosts, outs):
+        assert rel_err(o.cpu().numpy(), sl.svdvals(a.astype(np.float64))) < TOL32
+
+
 def test_batched_solo_vs_mix(avs_mod, torch_cuda):
     """A matrix gives bit-identical values alone and inside a mixed batch."""
     hosts, devs = _mats(avs_mod, [128, 64, 128, 256, 128, 64], 5)
