@@ -50,6 +50,8 @@ EXPORTED_SYMBOLS = [
     "avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d", "avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d",
     "avs_svdvals_batched_dev_s", "avs_autotune_tile", "avs_trim", "avs_workspace_bytes", "avs_estimate_bytes",
     "avs_geqrf_dev_s", "avs_geqrf_dev_d",
+    "avs_blockbidiag_ooc_s", "avs_blockbidiag_ooc_d", "avs_svdvals_ooc_s", "avs_svdvals_ooc_d",
+    "avs_geqrf_ooc_s", "avs_geqrf_ooc_d", "avs_ooc_plan",
     "avs_serve_create", "avs_serve_submit", "avs_serve_wait", "avs_serve_stats_get", "avs_serve_destroy",
 ]
 
@@ -125,6 +127,14 @@ def lib():
         L.avs_autotune_tile.argtypes = [P, I64, I32, ctypes.POINTER(ctypes.c_int32)]
         for nm in ("avs_geqrf_dev_s", "avs_geqrf_dev_d"):
             getattr(L, nm).argtypes = [P, I64, I64, I32, P, P, OP, RP]
+        for nm in ("avs_blockbidiag_ooc_s", "avs_blockbidiag_ooc_d"):
+            getattr(L, nm).argtypes = [P, I64, I64, I32, P, I64, RP]
+        for nm in ("avs_svdvals_ooc_s", "avs_svdvals_ooc_d"):
+            getattr(L, nm).argtypes = [P, I64, I64, I32, P, P, I64, OP, RP]
+        for nm in ("avs_geqrf_ooc_s", "avs_geqrf_ooc_d"):
+            getattr(L, nm).argtypes = [P, I64, I64, I32, P, P, I64, RP]
+        L.avs_ooc_plan.argtypes = [I64, I32, I32, I64, ctypes.POINTER(I32), ctypes.POINTER(I64),
+                                   ctypes.POINTER(I32)]
         L.avs_trim.argtypes = [P]
         L.avs_workspace_bytes.argtypes = [P, ctypes.POINTER(I64), ctypes.POINTER(I64)]
         L.avs_estimate_bytes.argtypes = [I64, I32, I32, I32, ctypes.POINTER(I64)]
@@ -348,6 +358,69 @@ def Blockbidiag(A, tile, handle=None):
     rc = fn(h.ptr, n, n, int(tile), ctypes.c_void_p(A.data_ptr()), None, ctypes.byref(r))
     _check(rc, "avs_blockbidiag_dev")
     return r
+
+
+def _ooc_matrix(A):
+    a = A
+    if not isinstance(a, np.ndarray) or a.ndim != 2 or a.shape[0] != a.shape[1]:
+        raise NotImplementedError("Not implemented")
+    if a.dtype not in (np.float32, np.float64) or not a.flags.f_contiguous or not a.flags.writeable:
+        raise TypeError("out-of-core calls work in place on a writeable Fortran-ordered float32/float64 array")
+    return a
+
+
+def ooc_plan(n, tile, dtype=np.float32, device_bytes=0):
+    """(slab, device bytes, in-core step) of the out-of-core calls for this device budget."""
+    slab, nb, frm = ctypes.c_int32(0), ctypes.c_int64(0), ctypes.c_int32(0)
+    rc = lib().avs_ooc_plan(int(n), int(tile), np.dtype(dtype).itemsize, int(device_bytes), ctypes.byref(slab),
+                            ctypes.byref(nb), ctypes.byref(frm))
+    _check(rc, "avs_ooc_plan")
+    return slab.value, nb.value, frm.value
+
+
+def OOC_Bidiag(A, tile, device_bytes=0, handle=None, report=None):
+    """OOC_Bidiag! (KAbasedSVD/src/tiledalgos.jl:248) in place on a host matrix
+    (numpy, Fortran order): the band reduction streams the matrix through at
+    most ``device_bytes`` of device memory (0: 90% of the free memory)."""
+    h = handle or default_handle()
+    a = _ooc_matrix(A)
+    fn = lib().avs_blockbidiag_ooc_d if a.dtype == np.float64 else lib().avs_blockbidiag_ooc_s
+    r = report if report is not None else Report()
+    rc = fn(h.ptr, a.shape[0], max(a.shape[0], 1), int(tile), ctypes.c_void_p(a.ctypes.data), int(device_bytes),
+            ctypes.byref(r))
+    _check(rc, "avs_blockbidiag_ooc")
+    return r
+
+
+def OOC_SVD(A, tile, device_bytes=0, handle=None, report=None, rel_tol=0.0):
+    """OOC_SVD! (KAbasedSVD/src/tiledalgos.jl:253-260) in place on a host matrix
+    (numpy, Fortran order); returns the singular values (descending)."""
+    h = handle or default_handle()
+    a = _ooc_matrix(A)
+    out = np.empty(a.shape[0], dtype=a.dtype)
+    fn = lib().avs_svdvals_ooc_d if a.dtype == np.float64 else lib().avs_svdvals_ooc_s
+    o = Opts(0, 0, float(rel_tol), None)
+    r = report if report is not None else Report()
+    rc = fn(h.ptr, a.shape[0], max(a.shape[0], 1), int(tile), ctypes.c_void_p(a.ctypes.data),
+            ctypes.c_void_p(out.ctypes.data), int(device_bytes), ctypes.byref(o), ctypes.byref(r))
+    _check(rc, "avs_svdvals_ooc")
+    return out
+
+
+def OOC_QR(A, tile, device_bytes=0, handle=None, report=None):
+    """OOC_QR! (KAbasedSVD/src/tiledalgos.jl:247) in place on a host matrix
+    (numpy, Fortran order); returns tau (nt * nt * tile, layout of tiled_QR)."""
+    h = handle or default_handle()
+    a = _ooc_matrix(A)
+    n = a.shape[0]
+    nt = n // int(tile) if tile else 0
+    tau = np.zeros(max(nt * nt * int(tile), 1), dtype=a.dtype)
+    fn = lib().avs_geqrf_ooc_d if a.dtype == np.float64 else lib().avs_geqrf_ooc_s
+    r = report if report is not None else Report()
+    rc = fn(h.ptr, n, max(n, 1), int(tile), ctypes.c_void_p(a.ctypes.data), ctypes.c_void_p(tau.ctypes.data),
+            int(device_bytes), ctypes.byref(r))
+    _check(rc, "avs_geqrf_ooc")
+    return tau
 
 
 def extract_band(A, bw, handle=None):

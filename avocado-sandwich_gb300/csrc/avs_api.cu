@@ -1,5 +1,6 @@
 // C ABI of the GB300 tiled SVD: handle, workspace, argument checks and the
 // three-stage pipeline behind my_CU_svdval (CUDAbasedSVD/SVD_GPU.jl:257-283).
+#include <algorithm>
 #include <cfloat>
 #include <cstdio>
 #include <cstdlib>
@@ -207,6 +208,44 @@ float ev_ms(cudaEvent_t a, cudaEvent_t b) {
     return ms;
 }
 
+// Stages 2 and 3 from the band of W (entries W[r + c*ldw], 0 <= c - r <= b):
+// bulge chase, bisection, sigma_out (type TO, device).  Records ev[2] between
+// the stages and ev[3] at the end; the status word is the layout's.
+template <typename S, typename TO>
+int run_stages23(avs_handle *h, const Layout &L, int64_t n, int b, const S *W, int64_t ldw, TO *sigma_out,
+                 double rel_tol, bool fp64_stages, cudaStream_t s, int64_t *launches) {
+    int rc;
+    int *err = reinterpret_cast<int *>(ws_at(h, L.off_err));
+    double *AB = reinterpret_cast<double *>(ws_at(h, L.off_ab));
+    double *dd = reinterpret_cast<double *>(ws_at(h, L.off_d));
+    double *de = reinterpret_cast<double *>(ws_at(h, L.off_e));
+    Stage2Work w2;
+    w2.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags2));
+    w2.err = err;
+    if (fp64_stages) {
+        if ((rc = extract_band_compact<S>(W, n, ldw, b, AB, L.ldab, s)) != AVS_SUCCESS) return rc;
+        ++*launches;
+        if ((rc = stage2_chase(AB, n, b, L.ldab, dd, de, w2, s, h->num_sms, launches)) != AVS_SUCCESS) return rc;
+    } else {
+        // the FP64 band buffer holds the float2 band (same size)
+        if ((rc = stage2_chase_df<S>(W, n, ldw, b, reinterpret_cast<float2 *>(AB), L.ldab, dd, de, w2, s,
+                                     h->num_sms, launches)) != AVS_SUCCESS)
+            return rc;
+    }
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[2], s));
+    double *sig = reinterpret_cast<double *>(ws_at(h, L.off_sig));
+    if (fp64_stages)
+        rc = stage3_bisect(dd, de, n, rel_tol, sig, reinterpret_cast<double *>(ws_at(h, L.off_scr)), s, launches);
+    else
+        rc = stage3_bisect_df(dd, de, n, rel_tol, sig, reinterpret_cast<double *>(ws_at(h, L.off_scr)),
+                              reinterpret_cast<float2 *>(ws_at(h, L.off_pairs)), s, launches);
+    if (rc != AVS_SUCCESS) return rc;
+    if ((rc = cast_from_double<TO>(sig, sigma_out, n, s)) != AVS_SUCCESS) return rc;
+    ++*launches;
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[3], s));
+    return AVS_SUCCESS;
+}
+
 // The pipeline on device data.  S = tile storage type.  src holds the input
 // (type TI, leading dimension lds) on the device; sigma_out (type TO) on the device.
 template <typename S, typename TI, typename TO>
@@ -242,33 +281,8 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
     }
     if ((rc = stage1_ge2bnd<S>(W, n, n, b, w1, s, &launches)) != AVS_SUCCESS) return rc;
     AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
-    double *AB = reinterpret_cast<double *>(ws_at(h, L.off_ab));
-    double *dd = reinterpret_cast<double *>(ws_at(h, L.off_d));
-    double *de = reinterpret_cast<double *>(ws_at(h, L.off_e));
-    Stage2Work w2;
-    w2.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags2));
-    w2.err = err;
-    if (fp64_stages) {
-        if ((rc = extract_band_compact<S>(W, n, n, b, AB, L.ldab, s)) != AVS_SUCCESS) return rc;
-        ++launches;
-        if ((rc = stage2_chase(AB, n, b, L.ldab, dd, de, w2, s, h->num_sms, &launches)) != AVS_SUCCESS) return rc;
-    } else {
-        // the FP64 band buffer holds the float2 band (same size)
-        if ((rc = stage2_chase_df<S>(W, n, n, b, reinterpret_cast<float2 *>(AB), L.ldab, dd, de, w2, s, h->num_sms,
-                                     &launches)) != AVS_SUCCESS)
-            return rc;
-    }
-    AVS_CUDA_TRY(cudaEventRecord(h->ev[2], s));
-    double *sig = reinterpret_cast<double *>(ws_at(h, L.off_sig));
-    if (fp64_stages)
-        rc = stage3_bisect(dd, de, n, rel_tol, sig, reinterpret_cast<double *>(ws_at(h, L.off_scr)), s, &launches);
-    else
-        rc = stage3_bisect_df(dd, de, n, rel_tol, sig, reinterpret_cast<double *>(ws_at(h, L.off_scr)),
-                              reinterpret_cast<float2 *>(ws_at(h, L.off_pairs)), s, &launches);
-    if (rc != AVS_SUCCESS) return rc;
-    if ((rc = cast_from_double<TO>(sig, sigma_out, n, s)) != AVS_SUCCESS) return rc;
-    ++launches;
-    AVS_CUDA_TRY(cudaEventRecord(h->ev[3], s));
+    if ((rc = run_stages23<S, TO>(h, L, n, b, W, n, sigma_out, rel_tol, fp64_stages, s, &launches)) != AVS_SUCCESS)
+        return rc;
     AVS_CUDA_TRY(cudaMemcpyAsync(h->h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     rc = finish_status(h, s);
     if (rep) {
@@ -619,9 +633,154 @@ int tile_kernel(avs_handle *h, int32_t b, T *dA, T *dB, T *dtau, bool ts) {
     AVS_CUDA_TRY(cudaMemcpyAsync(h->h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     return finish_status(h, s);
 }
+
+// Out-of-core entry points (OOC_Bidiag! / OOC_SVD! / OOC_QR!, tiledalgos.jl:232-260).
+enum OocMode { kOocBand = 0, kOocSvd = 1, kOocQr = 2 };
+
+// Upper band (0 <= c - r <= b) of the host matrix A into band storage on the
+// device: element (r, c) at band[b + r + c*b], i.e. the band of the matrix
+// (band + b) with leading dimension b.  Columns c >= b are one strided copy.
+template <typename T>
+int band_to_device(const T *A, int64_t n, int64_t lda, int b, T *band, cudaStream_t s) {
+    for (int64_t c = 0; c < std::min<int64_t>(b, n); ++c)
+        AVS_CUDA_TRY(cudaMemcpyAsync(band + b + c * b, A + c * lda, sizeof(T) * (size_t)(c + 1),
+                                     cudaMemcpyHostToDevice, s));
+    if (n > b)
+        AVS_CUDA_TRY(cudaMemcpy2DAsync(band + (int64_t)b * (b + 1), sizeof(T) * (size_t)(b + 1), A + (int64_t)b * lda,
+                                       sizeof(T) * (size_t)(lda + 1), sizeof(T) * (size_t)(b + 1), (size_t)(n - b),
+                                       cudaMemcpyHostToDevice, s));
+    return AVS_SUCCESS;
+}
+
+template <typename T>
+int ooc_call(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *A, T *sigma, T *tau, int mode,
+             int64_t device_bytes, const avs_opts *opts, avs_report *rep) {
+    int rc = check_common(h, n, n, lda, tile, A, mode == kOocSvd ? static_cast<const void *>(sigma) : A);
+    if (rep) {
+        std::memset(rep, 0, sizeof(*rep));
+        rep->status = rc;
+    }
+    if (rc != AVS_SUCCESS || n == 0) return rc;
+    if (device_bytes < 0) return -8;
+    const int prec = resolve_precision(opts ? opts->precision : 0, sizeof(T) == 8);
+    // the slabs run the SIMT 16-reflector-block update in the input's type
+    if (prec != (sizeof(T) == 8 ? AVS_PREC_FP64 : AVS_PREC_FP32)) return AVS_ERR_UNSUPPORTED;
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    size_t budget = (size_t)device_bytes;
+    if (budget == 0) {
+        size_t fr = 0, tot = 0;
+        AVS_CUDA_TRY(cudaMemGetInfo(&fr, &tot));
+        budget = fr / 10 * 9 + h->ws_bytes;
+    }
+    if (budget <= 256) return AVS_ERR_OOM;
+    const OocPlan plan = ooc_plan(n, tile, sizeof(T), budget - 256);
+    if (plan.slab < 1) return AVS_ERR_OOM;
+    const Layout L = make_layout(n, tile, 0, 0, 0);  // stages 2-3 only (no n x n buffers)
+    const size_t band_off = L.total;
+    const size_t need23 = mode == kOocSvd ? band_off + align_up(sizeof(T) * (size_t)n * (tile + 1)) : 0;
+    if ((rc = ensure_ws(h, std::max(256 + plan.bytes, need23))) != AVS_SUCCESS) return rc;
+    cudaStream_t s = h->stream;
+    // pin the caller's matrix for the duration of the call (pageable copies
+    // still work when it cannot be registered)
+    const size_t a_bytes = sizeof(T) * ((size_t)lda * (size_t)(n - 1) + (size_t)n);
+    bool registered = cudaHostRegister(A, a_bytes, cudaHostRegisterDefault) == cudaSuccess;
+    if (!registered) cudaGetLastError();
+    int *err = reinterpret_cast<int *>(ws_at(h, L.off_err));  // offset 0, outside the slab region
+    OocStats st;
+    int64_t launches = 0;
+    rc = AVS_SUCCESS;
+    auto step = [&]() -> int {
+        AVS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+        AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
+        int r = ooc_ge2bnd<T>(A, n, lda, tile, mode == kOocQr, mode == kOocQr ? tau : nullptr, plan, ws_at(h, 256),
+                              err, s, &st);
+        if (r != AVS_SUCCESS) return r;
+        AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
+        if (mode == kOocSvd) {
+            T *band = reinterpret_cast<T *>(ws_at(h, band_off));
+            if ((r = band_to_device<T>(A, n, lda, tile, band, s)) != AVS_SUCCESS) return r;
+            const bool f64 = fp64_stages(prec, opts);
+            T *dout = reinterpret_cast<T *>(ws_at(h, L.off_out));
+            if ((r = run_stages23<T, T>(h, L, n, tile, band + tile, tile, dout, bisect_tol(f64, opts), f64, s,
+                                        &launches)) != AVS_SUCCESS)
+                return r;
+            AVS_CUDA_TRY(cudaMemcpyAsync(sigma, dout, sizeof(T) * (size_t)n, cudaMemcpyDeviceToHost, s));
+        } else {
+            AVS_CUDA_TRY(cudaEventRecord(h->ev[2], s));
+            AVS_CUDA_TRY(cudaEventRecord(h->ev[3], s));
+        }
+        AVS_CUDA_TRY(cudaMemcpyAsync(h->h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        return finish_status(h, s);
+    };
+    rc = step();
+    if (rc != AVS_SUCCESS) cudaStreamSynchronize(s);  // no copy into A may be left in flight
+    if (registered) cudaHostUnregister(A);
+    if (rep) {
+        if (rc == AVS_SUCCESS) {
+            rep->t_stage1_ms = ev_ms(h->ev[0], h->ev[1]);
+            rep->t_stage2_ms = ev_ms(h->ev[1], h->ev[2]);
+            rep->t_stage3_ms = ev_ms(h->ev[2], h->ev[3]);
+            rep->t_total_ms = ev_ms(h->ev[0], h->ev[3]);
+        }
+        rep->kernel_launches = launches + st.launches;
+        rep->workspace_bytes = (int64_t)h->ws_bytes;
+        rep->precision = prec;
+        rep->status = rc;
+    }
+    return rc;
+}
 }  // namespace
 
 extern "C" {
+
+int avs_ooc_plan(int64_t n, int32_t tile, int32_t elem_bytes, int64_t device_bytes, int32_t *slab, int64_t *bytes,
+                 int32_t *incore_from) {
+    if (n < 0) return -1;
+    if (!is_pow2(tile) || tile < 16 || (n > 0 && n % tile != 0)) return AVS_ERR_NOT_IMPLEMENTED;
+    if (tile > kMaxTile) return AVS_ERR_UNSUPPORTED;
+    if (elem_bytes != 4 && elem_bytes != 8) return -3;
+    if (device_bytes <= 0) return -4;
+    const OocPlan p = device_bytes > 256 ? ooc_plan(n, tile, (size_t)elem_bytes, (size_t)device_bytes - 256)
+                                         : OocPlan{};
+    const int64_t nt = n / tile;
+    int64_t from = nt;
+    for (int64_t k = 0; p.slab > 0 && k < nt; ++k) {
+        const int64_t m = n - k * tile;
+        if ((size_t)elem_bytes * (size_t)m * (size_t)m <= 2 * p.slab_bytes) {
+            from = k;
+            break;
+        }
+    }
+    if (slab) *slab = p.slab;
+    if (bytes) *bytes = p.slab > 0 ? (int64_t)(p.bytes + 256) : 0;
+    if (incore_from) *incore_from = (int32_t)from;
+    return AVS_SUCCESS;
+}
+
+int avs_blockbidiag_ooc_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *A, int64_t device_bytes,
+                          avs_report *report) {
+    return ooc_call<float>(h, n, lda, tile, A, nullptr, nullptr, kOocBand, device_bytes, nullptr, report);
+}
+int avs_blockbidiag_ooc_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *A, int64_t device_bytes,
+                          avs_report *report) {
+    return ooc_call<double>(h, n, lda, tile, A, nullptr, nullptr, kOocBand, device_bytes, nullptr, report);
+}
+int avs_svdvals_ooc_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *A, float *sigma,
+                      int64_t device_bytes, const avs_opts *opts, avs_report *report) {
+    return ooc_call<float>(h, n, lda, tile, A, sigma, nullptr, kOocSvd, device_bytes, opts, report);
+}
+int avs_svdvals_ooc_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *A, double *sigma,
+                      int64_t device_bytes, const avs_opts *opts, avs_report *report) {
+    return ooc_call<double>(h, n, lda, tile, A, sigma, nullptr, kOocSvd, device_bytes, opts, report);
+}
+int avs_geqrf_ooc_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *A, float *tau, int64_t device_bytes,
+                    avs_report *report) {
+    return ooc_call<float>(h, n, lda, tile, A, nullptr, tau, kOocQr, device_bytes, nullptr, report);
+}
+int avs_geqrf_ooc_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *A, double *tau,
+                    int64_t device_bytes, avs_report *report) {
+    return ooc_call<double>(h, n, lda, tile, A, nullptr, tau, kOocQr, device_bytes, nullptr, report);
+}
 
 int avs_blockbidiag_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *dA, const avs_opts *opts,
                           avs_report *report) {

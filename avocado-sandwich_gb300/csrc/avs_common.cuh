@@ -138,6 +138,29 @@ int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr,
 template <typename T>
 int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cudaStream_t s, int64_t *launches);
 template <typename T>
+int stage1_panel(T *dA, int64_t lda, int b, int layout, int pr, int pc, int P, int first_role, const Stage1Work &w,
+                 cudaStream_t s);
+template <typename T>
+int stage1_update(T *dA, int64_t lda, int64_t ncols, int b, int layout, int pr, int pc, int P, int first_role,
+                  const Stage1Work &w, cudaStream_t s);
+
+// Out-of-core GE2BND / tiled QR on a host matrix (column-major, lda), through
+// device memory dws of ws_bytes (ooc_plan gives the slab size and the bytes).
+struct OocPlan {
+    int slab;            // tile rows (columns) per slab below the top tile
+    size_t bytes;        // device bytes the driver uses
+    size_t slab_bytes;   // one slab buffer
+};
+OocPlan ooc_plan(int64_t n, int b, size_t elem, size_t budget);
+struct OocStats {
+    double h2d_bytes = 0, d2h_bytes = 0;
+    int64_t launches = 0, slabs = 0;
+    int64_t incore_from = -1;  // step at which the trailing block went in core (-1: never)
+};
+template <typename T>
+int ooc_ge2bnd(T *A, int64_t n, int64_t lda, int b, bool qr_only, T *tau_host, const OocPlan &plan, void *dws,
+               int *err, cudaStream_t s, OocStats *st);
+template <typename T>
 int stage1_geqrf(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, T *dtau, cudaStream_t s,
                  int64_t *launches);
 

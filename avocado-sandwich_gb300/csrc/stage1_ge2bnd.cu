@@ -68,7 +68,8 @@ struct UpdateArgs {
     int64_t n;
     int b;
     int pr, pc, P;
-    int width;  // strip width
+    int first_role;  // 1: the top tile's own (GEQRT) blocks were applied earlier
+    int width;       // strip width
     const void *tblk;
     int64_t sA, sTblk;  // per-matrix strides (blockIdx.y = matrix)
 };
@@ -659,7 +660,7 @@ __global__ void __launch_bounds__(kNT) update_kernel(UpdateArgs args) {
     };
 
     load_strip(Top, top0);
-    for (int p = 0; p < args.P; ++p) {
+    for (int p = args.first_role; p < args.P; ++p) {
         const bool geqrt = (p == 0);
         const int64_t r0 = (int64_t)(args.pr + p) * b;
         T *Tp = geqrt ? Top : Ap;
@@ -766,7 +767,7 @@ int launch_panel(T *dA, int64_t lda, int b, int pr, int pc, int P, int first_rol
 
 template <typename T, int LAYOUT>
 int launch_update(T *dA, int64_t lda, int64_t n, int b, int pr, int pc, int P, const Stage1Work &w,
-                  cudaStream_t s) {
+                  cudaStream_t s, int first_role = 0) {
     const int width = sizeof(T) == 8 ? 32 : 64;
     static std::atomic<bool> attr_set{false};
     if (!attr_set) {
@@ -784,6 +785,7 @@ int launch_update(T *dA, int64_t lda, int64_t n, int b, int pr, int pc, int P, c
     a.pr = pr;
     a.pc = pc;
     a.P = P;
+    a.first_role = first_role;
     a.width = width;
     a.tblk = w.tblk;
     a.sA = w.sA;
@@ -939,6 +941,30 @@ int stage1_tsqrt_pair(T *dRB, int b, T *dtau, const Stage1Work &w, cudaStream_t 
                                  cudaMemcpyDeviceToDevice, s));
     return AVS_SUCCESS;
 }
+
+// One panel (P tiles down tile column pc from tile row pr, roles first_role..P-1)
+// and its 16-reflector-block trailing update over the columns right of the
+// panel up to ncols, on the view `layout` (0: columns, 1: transposed) of dA.
+// The building blocks of the out-of-core driver, which runs a half-step as a
+// sequence of such slabs with the top tile row carried from slab to slab.
+template <typename T>
+int stage1_panel(T *dA, int64_t lda, int b, int layout, int pr, int pc, int P, int first_role, const Stage1Work &w,
+                 cudaStream_t s) {
+    return layout == 0 ? launch_panel<T, 0>(dA, lda, b, pr, pc, P, first_role, w, s)
+                       : launch_panel<T, 1>(dA, lda, b, pr, pc, P, first_role, w, s);
+}
+template <typename T>
+int stage1_update(T *dA, int64_t lda, int64_t ncols, int b, int layout, int pr, int pc, int P, int first_role,
+                  const Stage1Work &w, cudaStream_t s) {
+    return layout == 0 ? launch_update<T, 0>(dA, lda, ncols, b, pr, pc, P, w, s, first_role)
+                       : launch_update<T, 1>(dA, lda, ncols, b, pr, pc, P, w, s, first_role);
+}
+template int stage1_panel<float>(float *, int64_t, int, int, int, int, int, int, const Stage1Work &, cudaStream_t);
+template int stage1_panel<double>(double *, int64_t, int, int, int, int, int, int, const Stage1Work &, cudaStream_t);
+template int stage1_update<float>(float *, int64_t, int64_t, int, int, int, int, int, int, const Stage1Work &,
+                                  cudaStream_t);
+template int stage1_update<double>(double *, int64_t, int64_t, int, int, int, int, int, int, const Stage1Work &,
+                                   cudaStream_t);
 
 template int stage1_ge2bnd<float>(float *, int64_t, int64_t, int, const Stage1Work &, cudaStream_t, int64_t *);
 template int stage1_ge2bnd<double>(double *, int64_t, int64_t, int, const Stage1Work &, cudaStream_t, int64_t *);

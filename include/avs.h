@@ -15,8 +15,10 @@
  * column-major (Julia's layout) with a leading dimension.  "Host" entry points
  * take host pointers and do the host<->device copies themselves (the
  * Matrix{Float32} method); "_dev" entry points take device pointers that the
- * caller owns (the CuMatrix{Float32} method).  The input matrix is never
- * modified (the reference copies it first, SVD_GPU.jl:259,273).  Singular
+ * caller owns (the CuMatrix{Float32} method).  The input matrix of the SVD
+ * entry points is never modified (the reference copies it first,
+ * SVD_GPU.jl:259,273); the building blocks and the out-of-core calls work in
+ * place, as their reference counterparts do.  Singular
  * values are returned in descending order, like LAPACK bdsdc.
  *
  * Status codes: 0 success; -i the i-th argument is invalid (LAPACK info
@@ -147,6 +149,43 @@ int avs_geqrf_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *
                     const avs_opts *opts, avs_report *report);
 int avs_geqrf_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *dA, double *dtau,
                     const avs_opts *opts, avs_report *report);
+
+/* ---- out of core (host matrices larger than the device budget) -----------------
+ * OOC_Bidiag! / OOC_SVD! / OOC_QR! (KAbasedSVD/src/tiledalgos.jl:232-260) over a
+ * LargeTiledMatrix (TiledMatrix.jl:121-186): A stays in host memory
+ * (column-major, lda) and is overwritten in place, as in the reference.  Each
+ * half-step streams the tile rows (QR) or tile columns (LQ) of its trailing
+ * block through the device in slabs sized by device_bytes (0 = 90% of the
+ * free device memory), the top tile carried from slab to slab; once the
+ * trailing block fits, it is finished in device memory (the reference's
+ * kswitch tail).  The band and the Householder vectors come out as those of
+ * avs_blockbidiag_dev / avs_geqrf_dev with the 16-reflector-block update (the
+ * same kernels in the same order), in the input's type (FP32 or FP64; other
+ * precision modes return AVS_ERR_UNSUPPORTED).  A is pinned with
+ * cudaHostRegister for the call when possible.  avs_svdvals_ooc_* then copies
+ * the band to the device and returns sigma (descending) in host memory, where
+ * the reference's OOC_SVD! returns the bidiagonal (tiledalgos.jl:256-259).
+ * tau of the QR form: host, nt * nt * tile elements, layout of avs_geqrf_dev
+ * (may be NULL).  device_bytes below what one slab needs returns AVS_ERR_OOM. */
+int avs_blockbidiag_ooc_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *A, int64_t device_bytes,
+                          avs_report *report);
+int avs_blockbidiag_ooc_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *A, int64_t device_bytes,
+                          avs_report *report);
+int avs_svdvals_ooc_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *A, float *sigma,
+                      int64_t device_bytes, const avs_opts *opts, avs_report *report);
+int avs_svdvals_ooc_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *A, double *sigma,
+                      int64_t device_bytes, const avs_opts *opts, avs_report *report);
+int avs_geqrf_ooc_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *A, float *tau, int64_t device_bytes,
+                    avs_report *report);
+/* The slab plan of the calls above (host only, no device needed): for order n,
+ * tile, element size (4 or 8) and device_bytes > 0, *slab = tile rows per slab
+ * (0: device_bytes too small), *bytes = device bytes the call holds,
+ * *incore_from = the step k from which the trailing block is finished in
+ * device memory in the band form (nt: never).  Pointers may be NULL. */
+int avs_ooc_plan(int64_t n, int32_t tile, int32_t elem_bytes, int64_t device_bytes, int32_t *slab, int64_t *bytes,
+                 int32_t *incore_from);
+int avs_geqrf_ooc_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *A, double *tau,
+                    int64_t device_bytes, avs_report *report);
 /* Copy the upper band 0 <= j - i <= bw of a dense n x n matrix into a dense
  * FP64 n x n matrix with zeros elsewhere (the reference's banded array). */
 int avs_extract_band_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t bw, const float *dA, double *dB,

@@ -97,3 +97,24 @@ def test_serve_and_batched_without_gpu(avs_mod):
     assert lib.avs_svdvals_batched_dev_s(None, 1, None, None, None, None, None, None, None) == -1
     with pytest.raises(avs_mod.AvsError):
         avs_mod.Server()
+
+
+def test_ooc_plan_host_logic(avs_mod):
+    """The out-of-core slab plan is host arithmetic: more device memory gives
+    larger slabs and an earlier in-core tail; too little gives slab 0, and the
+    reference's "Not implemented" rules apply."""
+    s1, b1, f1 = avs_mod.ooc_plan(4096, 64, "float32", 64 << 20)
+    s2, b2, f2 = avs_mod.ooc_plan(4096, 64, "float32", 256 << 20)
+    assert 1 <= s1 < s2 and b1 <= (64 << 20) and b2 <= (256 << 20)
+    assert f2 <= f1 <= 4096 // 64
+    assert avs_mod.ooc_plan(4096, 64, "float32", 1 << 20)[0] == 0
+    s8, _, _ = avs_mod.ooc_plan(4096, 64, "float64", 64 << 20)
+    assert s8 < s1
+    # the whole matrix in budget: in core from the first step
+    assert avs_mod.ooc_plan(1024, 64, "float32", 64 << 20)[2] == 0
+    with pytest.raises(NotImplementedError):
+        avs_mod.ooc_plan(96, 64, "float32", 1 << 20)
+    lib = avs_mod.lib()
+    assert lib.avs_ooc_plan(1024, 64, 4, 0, None, None, None) == -4
+    assert lib.avs_ooc_plan(1024, 64, 2, 1 << 20, None, None, None) == -3
+    assert lib.avs_blockbidiag_ooc_s(None, 64, 64, 16, None, 0, None) == -1
