@@ -133,7 +133,7 @@ int stage1_chain_tc2(float *x, int64_t n, int b, int pr, int pc, int P, const fl
 
 template <typename T>
 int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const Stage1Work &w,
-                       cudaStream_t s);
+                       cudaStream_t s, int first_role = 0);
 
 template <typename T>
 int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cudaStream_t s, int64_t *launches);

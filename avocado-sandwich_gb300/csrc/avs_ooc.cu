@@ -9,12 +9,13 @@
 // row k stays on the device for the whole half-step; the tile rows below it
 // come in slabs of `slab` tile rows.  Each slab buffer holds [top row; slab
 // rows] as one column-major matrix, so the in-core panel kernel (GEQRT on the
-// first slab, TSQRT roles 1..slab after it) and the 16-reflector-block trailing
-// update run on it unchanged; the top row is carried to the next slab buffer
-// by a device copy.  The flat-tree order of the TSQRTs is the in-core one, so
-// the result is the in-core result with the same kernels.  An LQ half-step is
-// the same on tile columns (the kernels' transposed view of the buffer).  Once
-// the trailing block fits in the slab memory it is copied in, finished by the
+// first slab, TSQRT roles 1..slab after it) and the in-core trailing update
+// (full-T for tiles >= 128, 16-reflector blocks below) run on it unchanged; the
+// top row is carried to the next slab buffer by a device copy.  The flat-tree
+// order of the TSQRTs and the update kernels are the in-core ones, so the
+// result is the in-core SIMT result bit for bit.  An LQ half-step is the same
+// on tile columns (the kernels' transposed view of the buffer).  Once the
+// trailing block fits in the slab memory it is copied in, finished by the
 // in-core driver and copied back.
 #include <algorithm>
 #include <utility>
@@ -27,7 +28,7 @@ namespace {
 inline size_t al256(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct OocBufs {
-    void *tau, *tblk;
+    void *tau, *tblk, *tfull;
     int *flags;
     char *X[2];      // slab buffers
     char *region;    // both slab buffers as one region (the in-core tail)
@@ -43,6 +44,8 @@ OocBufs carve(void *ws, int64_t n, int b, size_t elem, int slab) {
     off = al256(off + elem * (size_t)(nt + 1) * b);
     o.tblk = p + off;
     off = al256(off + elem * (size_t)(nt + 1) * (b / 16) * 256);
+    o.tfull = b >= 128 ? p + off : nullptr;
+    off = al256(off + (b >= 128 ? elem * (size_t)(nt + 1) * b * b : 0));
     o.flags = reinterpret_cast<int *>(p + off);
     off = al256(off + sizeof(int) * (size_t)(nt + 4));
     const size_t sb = al256(elem * (size_t)(1 + slab) * b * n);
@@ -56,7 +59,7 @@ OocBufs carve(void *ws, int64_t n, int b, size_t elem, int slab) {
 size_t fixed_bytes(int64_t n, int b, size_t elem) {
     const int64_t nt = n / b;
     return al256(elem * (size_t)(nt + 1) * b) + al256(elem * (size_t)(nt + 1) * (b / 16) * 256) +
-           al256(sizeof(int) * (size_t)(nt + 4)) + 256;
+           al256(b >= 128 ? elem * (size_t)(nt + 1) * b * b : 0) + al256(sizeof(int) * (size_t)(nt + 4)) + 256;
 }
 
 // cudaMemcpy2DAsync of `height` runs of `width` elements
@@ -156,7 +159,7 @@ int ooc_ge2bnd(T *A, int64_t n, int64_t lda, int b, bool qr_only, T *tau_host, c
     w.tblk = ob.tblk;
     w.flags = ob.flags;
     w.err = err;
-    w.tfull = nullptr;  // 16-reflector-block updates throughout
+    w.tfull = ob.tfull;  // full-T updates for tiles >= 128, as in core
     int rc;
     for (int k = 0; k < nt; ++k) {
         const int64_t kb = (int64_t)k * b, m = n - kb;

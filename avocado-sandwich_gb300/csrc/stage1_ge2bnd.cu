@@ -943,10 +943,12 @@ int stage1_tsqrt_pair(T *dRB, int b, T *dtau, const Stage1Work &w, cudaStream_t 
 }
 
 // One panel (P tiles down tile column pc from tile row pr, roles first_role..P-1)
-// and its 16-reflector-block trailing update over the columns right of the
-// panel up to ncols, on the view `layout` (0: columns, 1: transposed) of dA.
-// The building blocks of the out-of-core driver, which runs a half-step as a
-// sequence of such slabs with the top tile row carried from slab to slab.
+// and its trailing update over the columns right of the panel up to ncols, on
+// the view `layout` (0: columns, 1: transposed) of dA: the full-T update for
+// tiles >= 128 when w.tfull is given (as in stage1_ge2bnd), else the
+// 16-reflector-block one.  The building blocks of the out-of-core driver,
+// which runs a half-step as a sequence of such slabs with the top tile row
+// carried from slab to slab.
 template <typename T>
 int stage1_panel(T *dA, int64_t lda, int b, int layout, int pr, int pc, int P, int first_role, const Stage1Work &w,
                  cudaStream_t s) {
@@ -956,6 +958,7 @@ int stage1_panel(T *dA, int64_t lda, int b, int layout, int pr, int pc, int P, i
 template <typename T>
 int stage1_update(T *dA, int64_t lda, int64_t ncols, int b, int layout, int pr, int pc, int P, int first_role,
                   const Stage1Work &w, cudaStream_t s) {
+    if (b >= 128 && w.tfull) return stage1_update_full<T>(dA, lda, ncols, b, layout, pr, pc, P, w, s, first_role);
     return layout == 0 ? launch_update<T, 0>(dA, lda, ncols, b, pr, pc, P, w, s, first_role)
                        : launch_update<T, 1>(dA, lda, ncols, b, pr, pc, P, w, s, first_role);
 }

@@ -41,6 +41,7 @@ struct TBuildArgs {
     const void *tblk;  // [P][b/16][256]
     void *tfull;       // [P][b*b], T(l, i) at l + i*b
     int64_t sA, sTblk, sTfull;  // per-matrix strides (blockIdx.y = matrix)
+    int first_role;    // tiles first_role..P-1 (1: the top tile's T was built earlier)
 };
 
 // ---------------------------------------------------------------------------
@@ -50,7 +51,7 @@ __global__ void __launch_bounds__(kWNT) tbuild_kernel(TBuildArgs args) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int b = args.b;
     const int nb = b / kWIB;
-    const int p = blockIdx.x;
+    const int p = blockIdx.x + args.first_role;
     const int64_t zb = blockIdx.y;
     const bool geqrt = (p == 0);
     const int tid = threadIdx.x;
@@ -173,6 +174,7 @@ struct UpdFullArgs {
     int pr, pc, P;
     const void *tfull;
     int64_t sA, sTfull;  // per-matrix strides (blockIdx.y = matrix)
+    int first_role;      // 1: the top tile's own reflectors were applied earlier
 };
 
 // A-operand sources for the three products.
@@ -335,7 +337,7 @@ __global__ void __launch_bounds__(kWNT) update_full_kernel(UpdFullArgs args) {
     __syncthreads();
     T acc[8][C::CB];
     T apr[8][C::CB];
-    for (int p = 0; p < args.P; ++p) {
+    for (int p = args.first_role; p < args.P; ++p) {
         UpdCtx<T, LAYOUT, B> ctx;
         ctx.V = V;
         ctx.Tf = reinterpret_cast<const T *>(args.tfull) + zb * args.sTfull + (size_t)p * B * B;
@@ -394,7 +396,8 @@ size_t upd_full_smem() {
 }
 
 template <typename T, int LAYOUT, int B>
-int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const Stage1Work &w, cudaStream_t s) {
+int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const Stage1Work &w, cudaStream_t s,
+                    int first_role) {
     using C = UCfg<T, B>;
     static std::atomic<bool> attr{false};
     const size_t smem = upd_full_smem<T, B>();
@@ -405,7 +408,7 @@ int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const 
     }
     const int64_t ncols = n - (int64_t)(pc + 1) * B;
     if (ncols <= 0) return AVS_SUCCESS;
-    UpdFullArgs a{dA, lda, n, B, pr, pc, P, w.tfull, w.sA, w.sTfull};
+    UpdFullArgs a{dA, lda, n, B, pr, pc, P, w.tfull, w.sA, w.sTfull, first_role};
     const unsigned gx = (unsigned)((ncols + C::W - 1) / C::W);
     update_full_kernel<T, LAYOUT, B><<<dim3(gx, w.batch > 0 ? w.batch : 1), kWNT, smem, s>>>(a);
     AVS_CUDA_TRY(cudaGetLastError());
@@ -413,7 +416,8 @@ int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const 
 }
 
 template <typename T, int LAYOUT>
-int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const Stage1Work &w, cudaStream_t s) {
+int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const Stage1Work &w, cudaStream_t s,
+                  int first_role = 0) {
     static std::atomic<bool> attr{false};
     const size_t smem = sizeof(T) * (size_t)32 * (256 + 1) > sizeof(T) * (size_t)256 * 256 / 16
                             ? sizeof(T) * (size_t)32 * (256 + 1)
@@ -423,8 +427,8 @@ int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const 
             cudaFuncSetAttribute(tbuild_kernel<T, LAYOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
-    TBuildArgs a{dA, lda, b, pr, pc, P, w.tblk, w.tfull, w.sA, w.sTblk, w.sTfull};
-    tbuild_kernel<T, LAYOUT><<<dim3(P, w.batch > 0 ? w.batch : 1), kWNT, smem, s>>>(a);
+    TBuildArgs a{dA, lda, b, pr, pc, P, w.tblk, w.tfull, w.sA, w.sTblk, w.sTfull, first_role};
+    tbuild_kernel<T, LAYOUT><<<dim3(P - first_role, w.batch > 0 ? w.batch : 1), kWNT, smem, s>>>(a);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
 }
@@ -442,25 +446,26 @@ template int stage1_tbuild<float>(const float *, int64_t, int, int, int, int, in
 template int stage1_tbuild<double>(const double *, int64_t, int, int, int, int, int, const Stage1Work &,
                                    cudaStream_t);
 
-// Full-T trailing update of one half-step (tiles 128 and 256).
+// Full-T trailing update of one half-step (tiles 128 and 256), tiles
+// first_role..P-1 of the panel.
 template <typename T>
 int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const Stage1Work &w,
-                       cudaStream_t s) {
+                       cudaStream_t s, int first_role) {
     int rc;
     if (layout == 0) {
-        if ((rc = launch_tbuild<T, 0>(dA, lda, b, pr, pc, P, w, s)) != AVS_SUCCESS) return rc;
-        return b == 256 ? launch_upd_full<T, 0, 256>(dA, lda, n, pr, pc, P, w, s)
-                        : launch_upd_full<T, 0, 128>(dA, lda, n, pr, pc, P, w, s);
+        if ((rc = launch_tbuild<T, 0>(dA, lda, b, pr, pc, P, w, s, first_role)) != AVS_SUCCESS) return rc;
+        return b == 256 ? launch_upd_full<T, 0, 256>(dA, lda, n, pr, pc, P, w, s, first_role)
+                        : launch_upd_full<T, 0, 128>(dA, lda, n, pr, pc, P, w, s, first_role);
     }
-    if ((rc = launch_tbuild<T, 1>(dA, lda, b, pr, pc, P, w, s)) != AVS_SUCCESS) return rc;
-    return b == 256 ? launch_upd_full<T, 1, 256>(dA, lda, n, pr, pc, P, w, s)
-                    : launch_upd_full<T, 1, 128>(dA, lda, n, pr, pc, P, w, s);
+    if ((rc = launch_tbuild<T, 1>(dA, lda, b, pr, pc, P, w, s, first_role)) != AVS_SUCCESS) return rc;
+    return b == 256 ? launch_upd_full<T, 1, 256>(dA, lda, n, pr, pc, P, w, s, first_role)
+                    : launch_upd_full<T, 1, 128>(dA, lda, n, pr, pc, P, w, s, first_role);
 }
 
 template int stage1_update_full<float>(float *, int64_t, int64_t, int, int, int, int, int, const Stage1Work &,
-                                       cudaStream_t);
+                                       cudaStream_t, int);
 
 template int stage1_update_full<double>(double *, int64_t, int64_t, int, int, int, int, int, const Stage1Work &,
-                                        cudaStream_t);
+                                        cudaStream_t, int);
 
 }  // namespace avs

@@ -158,10 +158,10 @@ int avs_geqrf_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double 
  * block through the device in slabs sized by device_bytes (0 = 90% of the
  * free device memory), the top tile carried from slab to slab; once the
  * trailing block fits, it is finished in device memory (the reference's
- * kswitch tail).  The band and the Householder vectors come out as those of
- * avs_blockbidiag_dev / avs_geqrf_dev with the 16-reflector-block update (the
- * same kernels in the same order), in the input's type (FP32 or FP64; other
- * precision modes return AVS_ERR_UNSUPPORTED).  A is pinned with
+ * kswitch tail).  The band and the Householder vectors come out bit for bit
+ * as those of avs_blockbidiag_dev / avs_geqrf_dev in the input's type (the
+ * same kernels in the same order; FP32 or FP64, other precision modes return
+ * AVS_ERR_UNSUPPORTED).  A is pinned with
  * cudaHostRegister for the call when possible.  avs_svdvals_ooc_* then copies
  * the band to the device and returns sigma (descending) in host memory, where
  * the reference's OOC_SVD! returns the bidiagonal (tiledalgos.jl:256-259).

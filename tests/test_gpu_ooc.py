@@ -1,9 +1,8 @@
 """GPU tests of the out-of-core forms (OOC_Bidiag!, OOC_SVD!, OOC_QR!;
 KAbasedSVD/src/tiledalgos.jl:232-260): the matrix stays in host memory and
 passes through a small device budget in slabs.  The slabs run the in-core
-kernels in the in-core order, so with the 16-reflector-block update (tiles up
-to 64) the result equals the in-core device result bit for bit; every form is
-also checked against LAPACK.  Budgets are chosen with the planner so that the
+kernels in the in-core order, so the result equals the in-core device result
+bit for bit; every form is also checked against LAPACK.  Budgets are chosen with the planner so that the
 runs cover one-tile slabs, uneven last slabs and the in-core tail."""
 import numpy as np
 import pytest
@@ -43,9 +42,9 @@ def band_svals(a, tile):
     return np.linalg.svd(m, compute_uv=False)
 
 
-@pytest.mark.parametrize("tile,slab", [(16, 1), (32, 1), (32, 3), (64, 2)])
+@pytest.mark.parametrize("tile,slab", [(16, 1), (32, 1), (32, 3), (64, 2), (128, 2), (256, 2)])
 def test_ooc_bidiag_equals_incore(avs_mod, torch_cuda, tile, slab):
-    n = 16 * tile
+    n = {128: 8, 256: 12}.get(tile, 16) * tile
     a = gaussian(n, np.float32, tile + slab)
     ref = sl.svdvals(a.astype(np.float64))
     dev = avs_mod.to_device(a)
