@@ -48,7 +48,7 @@ EXPORTED_SYMBOLS = [
     "avs_blockbidiag_dev_s", "avs_blockbidiag_dev_d", "avs_extract_band_dev_s", "avs_extract_band_dev_d",
     "avs_band_to_bidiag_dev", "avs_bidiag_svals_dev", "avs_bidiag_svals_noalloc",
     "avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d", "avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d",
-    "avs_svdvals_batched_dev_s", "avs_autotune_tile", "avs_trim", "avs_workspace_bytes", "avs_estimate_bytes",
+    "avs_svdvals_batched_dev_s", "avs_bidiag_batched_dev_s", "avs_autotune_tile", "avs_trim", "avs_workspace_bytes", "avs_estimate_bytes",
     "avs_geqrf_dev_s", "avs_geqrf_dev_d",
     "avs_blockbidiag_ooc_s", "avs_blockbidiag_ooc_d", "avs_svdvals_ooc_s", "avs_svdvals_ooc_d",
     "avs_geqrf_ooc_s", "avs_geqrf_ooc_d", "avs_ooc_plan",
@@ -124,6 +124,7 @@ def lib():
         L.avs_bidiag_svals_dev.argtypes = [P, I64, P, P, P, ctypes.c_double, RP]
         L.avs_bidiag_svals_noalloc.argtypes = [I64, P, P, P, ctypes.c_double, P]
         L.avs_svdvals_batched_dev_s.argtypes = [P, I32, P, P, P, P, P, OP, RP]
+        L.avs_bidiag_batched_dev_s.argtypes = [P, I32, P, P, P, P, P, P, OP, RP]
         L.avs_autotune_tile.argtypes = [P, I64, I32, ctypes.POINTER(ctypes.c_int32)]
         for nm in ("avs_geqrf_dev_s", "avs_geqrf_dev_d"):
             getattr(L, nm).argtypes = [P, I64, I64, I32, P, P, OP, RP]
@@ -313,6 +314,52 @@ def svdvals_batched(mats, tiles=None, report=None, handle=None, rel_tol=0.0):
     rc = lib().avs_svdvals_batched_dev_s(h.ptr, cnt, n, ld, None if tiles is None else tt, pa, ps,
                                          ctypes.byref(opt), ctypes.byref(r))
     _check(rc, "avs_svdvals_batched_dev_s")
+    return outs
+
+
+def bidiag_batched(mats, tiles=None, report=None, handle=None):
+    """The batched pipeline up to the bidiagonal: for each square float32 CUDA
+    matrix (column-major, see ``to_device``) the diagonal d and superdiagonal e
+    (FP64 CUDA tensors of n values; e[n-1] = 0) of a bidiagonal B with
+    A = U B V^T, V e1 = e1 -- unique up to signs, so |d| and |e| are those of
+    LAPACK gebrd (the quantity RMT/rmt.jl:24-31 reads)."""
+    import torch
+    h = handle or default_handle()
+    cnt = len(mats)
+    if cnt == 0:
+        return []
+    if isinstance(tiles, int):
+        tiles = [tiles] * cnt
+    n = (ctypes.c_int64 * cnt)()
+    ld = (ctypes.c_int64 * cnt)()
+    tt = (ctypes.c_int32 * cnt)()
+    pa = (ctypes.c_void_p * cnt)()
+    pd = (ctypes.c_void_p * cnt)()
+    pe = (ctypes.c_void_p * cnt)()
+    outs = []
+    dev = None
+    for i, A in enumerate(mats):
+        if not _is_torch_cuda(A) or A.dim() != 2 or A.dtype != torch.float32:
+            raise TypeError("bidiag_batched takes 2-D float32 CUDA tensors")
+        if A.shape[0] != A.shape[1]:
+            raise NotImplementedError("Not implemented")
+        if A.stride(1) != 1:
+            A = A.contiguous()
+            mats[i] = A
+        dev = A.device
+        n[i] = A.shape[0]
+        ld[i] = max(A.stride(0), 1)
+        tt[i] = 0 if tiles is None else int(tiles[i])
+        pa[i] = A.data_ptr()
+        d = torch.empty(A.shape[0], dtype=torch.float64, device=A.device)
+        e = torch.empty(A.shape[0], dtype=torch.float64, device=A.device)
+        pd[i], pe[i] = d.data_ptr(), e.data_ptr()
+        outs.append((d, e))
+    opt = Opts(0, 0, 0.0, ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    r = report if report is not None else Report()
+    rc = lib().avs_bidiag_batched_dev_s(h.ptr, cnt, n, ld, None if tiles is None else tt, pa, pd, pe,
+                                        ctypes.byref(opt), ctypes.byref(r))
+    _check(rc, "avs_bidiag_batched_dev_s")
     return outs
 
 

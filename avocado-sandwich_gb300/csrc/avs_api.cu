@@ -40,7 +40,7 @@ struct avs_handle {
         int64_t kernels = 0;
         cudaEvent_t ev[4] = {};  // recorded inside the graph: start, after stage 1, 2, 3
     };
-    std::map<std::tuple<int64_t, int, int>, Graph> graphs;
+    std::map<std::tuple<int64_t, int, int, int>, Graph> graphs;  // (n, tile, count, output form)
     void drop_graphs() {
         for (auto &kv : graphs) {
             cudaGraphExecDestroy(kv.second.exec);
@@ -937,7 +937,7 @@ BatchLayout batch_layout(int64_t n, int b, int cnt) {
     L.sig = take(sizeof(double) * (size_t)cnt * n);
     L.scr = take(sizeof(double) * (size_t)cnt * 4);
     L.pairs = take(sizeof(float2) * (size_t)cnt * 2 * n);
-    L.ptrs = take(sizeof(void *) * 3 * (size_t)cnt + 64);
+    L.ptrs = take(sizeof(void *) * 4 * (size_t)cnt + 64);
     L.total = o + 256;
     return L;
 }
@@ -949,6 +949,15 @@ __global__ void gather_kernel(const float *const *src, const int64_t *lds, float
     float *w = dst + zb * n * n;
     for (int64_t c = blockIdx.x; c < n; c += gridDim.x)
         for (int64_t r = threadIdx.x; r < n; r += blockDim.x) w[r + c * n] = a[r + c * ld];
+}
+
+__global__ void scatter_de_kernel(const double *d, const double *e, double *const *dst_d, double *const *dst_e,
+                                  int64_t n, int cnt) {
+    const int64_t total = n * (int64_t)cnt;
+    for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
+        dst_d[g / n][g % n] = d[g];
+        dst_e[g / n][g % n] = (g % n) + 1 < n ? e[g] : 0.0;
+    }
 }
 
 __global__ void scatter_kernel(const double *sig, float *const *dst, int64_t n, int cnt) {
@@ -986,12 +995,13 @@ int ensure_pinned(avs_handle *h, size_t bytes) {
 
 // The launches of one group (gather .. scatter), captured once per shape.
 int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cnt, double tol, cudaStream_t s,
-                   const cudaEvent_t *ev, int64_t *launches) {
+                   const cudaEvent_t *ev, int64_t *launches, bool bidiag) {
     char *base = reinterpret_cast<char *>(h->bws);
     float *W = reinterpret_cast<float *>(base + L.W);
     const float *const *src = reinterpret_cast<const float *const *>(base + L.ptrs);
     float *const *dst = reinterpret_cast<float *const *>(base + L.ptrs + sizeof(void *) * cnt);
     const int64_t *lds = reinterpret_cast<const int64_t *>(base + L.ptrs + 2 * sizeof(void *) * cnt);
+    double *const *dst_e = reinterpret_cast<double *const *>(base + L.ptrs + 3 * sizeof(void *) * cnt);
     int *err = reinterpret_cast<int *>(base + L.err);
     const int64_t nt = n / b;
     AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[0], s, cudaEventRecordExternal));
@@ -1022,6 +1032,14 @@ int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cn
                                  h->num_sms, launches);
     if (rc != AVS_SUCCESS) return rc;
     AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal));
+    if (bidiag) {  // the bidiagonal itself: d and e of each matrix to the caller's vectors
+        scatter_de_kernel<<<(unsigned)std::min<int64_t>((n * cnt + 255) / 256, 8192), 256, 0, s>>>(
+            dd, de, reinterpret_cast<double *const *>(dst), dst_e, n, cnt);
+        AVS_CUDA_TRY(cudaGetLastError());
+        AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal));
+        if (launches) *launches += 2;
+        return AVS_SUCCESS;
+    }
     double *sig = reinterpret_cast<double *>(base + L.sig);
     rc = stage3_bisect_df_batched(dd, de, n, cnt, tol, sig, reinterpret_cast<double *>(base + L.scr),
                                   reinterpret_cast<float2 *>(base + L.pairs), s, launches);
@@ -1055,9 +1073,11 @@ bool valid_tile(int64_t n, int t) { return is_pow2(t) && t >= 16 && t <= kMaxTil
 
 }  // namespace
 
-extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
-                                         const int32_t *tile, const float *const *dA, float *const *dsigma,
-                                         const avs_opts *opts, avs_report *rep) {
+// Batched calls: out1 = sigma (FP32) or d (FP64), out2 = e (FP64, bidiagonal form only).
+static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda, const int32_t *tile,
+                        const float *const *dA, void *const *out1, void *const *out2, bool bidiag,
+                        const avs_opts *opts, avs_report *rep) {
+    void *const *dsigma = out1;
     if (rep) std::memset(rep, 0, sizeof(*rep));
     if (!h) return -1;
     if (count < 0) return -2;
@@ -1066,6 +1086,7 @@ extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int
     if (!lda) return -4;
     if (!dA) return -6;
     if (!dsigma) return -7;
+    if (bidiag && !out2) return -8;
     std::vector<int> tiles(count);
     for (int i = 0; i < count; ++i) {
         if (n[i] < 0) return -3;
@@ -1074,6 +1095,7 @@ extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int
         if (t != 0 && !valid_tile(n[i], t)) return (t > kMaxTile && is_pow2(t)) ? AVS_ERR_UNSUPPORTED
                                                                                 : AVS_ERR_NOT_IMPLEMENTED;
         if (n[i] > 0 && (!dA[i] || !dsigma[i])) return dA[i] ? -7 : -6;
+        if (bidiag && n[i] > 0 && !out2[i]) return -8;
         tiles[i] = t;
     }
     AVS_CUDA_TRY(cudaSetDevice(h->device));
@@ -1096,7 +1118,7 @@ extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int
     size_t pin_need = sizeof(int) * 16 * (groups.size() + 1);
     for (auto &g : groups) {
         need = std::max(need, batch_layout(g.first.first, g.first.second, (int)g.second.size()).total);
-        pin_need += sizeof(void *) * 3 * g.second.size();
+        pin_need += sizeof(void *) * 4 * g.second.size();
     }
     int rc;
     if ((rc = ensure_bws(h, need)) != AVS_SUCCESS) return rc;
@@ -1124,18 +1146,19 @@ extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int
         for (int q = 0; q < cnt; ++q) {
             tab[q] = const_cast<float *>(dA[g.second[q]]);
             tab[cnt + q] = dsigma[g.second[q]];
+            tab[3 * cnt + q] = bidiag ? out2[g.second[q]] : nullptr;
             reinterpret_cast<int64_t *>(tab + 2 * cnt)[q] = lda[g.second[q]];
         }
-        AVS_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(h->bws) + L.ptrs, tab, sizeof(void *) * 3 * cnt,
+        AVS_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(h->bws) + L.ptrs, tab, sizeof(void *) * 4 * cnt,
                                      cudaMemcpyHostToDevice, s));
-        const auto key = std::make_tuple(gn, gb, cnt);
+        const auto key = std::make_tuple(gn, gb, cnt, bidiag ? 1 : 0);
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
             avs_handle::Graph gr;
             for (cudaEvent_t &e : gr.ev) AVS_CUDA_TRY(cudaEventCreate(&e));
             cudaGraph_t graph;
             AVS_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            rc = group_launches(h, L, gn, gb, cnt, tol, s, gr.ev, &gr.kernels);
+            rc = group_launches(h, L, gn, gb, cnt, tol, s, gr.ev, &gr.kernels, bidiag);
             cudaError_t ce = cudaStreamEndCapture(s, &graph);
             if (rc == AVS_SUCCESS && ce == cudaSuccess) {
                 ce = cudaGraphInstantiate(&gr.exec, graph, 0);
@@ -1153,7 +1176,7 @@ extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int
         ran.push_back(&it->second);
         AVS_CUDA_TRY(cudaMemcpyAsync(h_status + 16 * gi, reinterpret_cast<char *>(h->bws) + L.err, sizeof(int),
                                      cudaMemcpyDeviceToHost, s));
-        tab += 3 * cnt;
+        tab += 4 * cnt;
         ++gi;
     }
     AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
@@ -1184,6 +1207,20 @@ extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int
         rep->status = rc;
     }
     return rc;
+}
+
+extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
+                                         const int32_t *tile, const float *const *dA, float *const *dsigma,
+                                         const avs_opts *opts, avs_report *rep) {
+    return batched_call(h, count, n, lda, tile, dA, reinterpret_cast<void *const *>(dsigma), nullptr, false, opts,
+                        rep);
+}
+
+extern "C" int avs_bidiag_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
+                                        const int32_t *tile, const float *const *dA, double *const *dd,
+                                        double *const *de, const avs_opts *opts, avs_report *rep) {
+    return batched_call(h, count, n, lda, tile, dA, reinterpret_cast<void *const *>(dd),
+                        reinterpret_cast<void *const *>(de), true, opts, rep);
 }
 
 // Autotuner: time each valid tile in {32, 64, 128} on `sample` seeded random

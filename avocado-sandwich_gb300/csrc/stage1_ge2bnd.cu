@@ -182,14 +182,15 @@ struct PScal<float> {
 // ---------------------------------------------------------------------------
 // Panel kernel (roles, schedule and outputs as described at the top):
 //   * every thread owns one row of the 16-column slice (b <= 256 rows, 256
-//     threads); the 16 dot products of a reflector step
-//     are reduced with a warp reduce-scatter (16 shuffles) and one shared-memory
-//     pass across warps: two barriers per reflector;
+//     threads); the 16 dot products of a reflector step are reduced with a
+//     warp reduce-scatter (16 shuffles) and one double-buffered shared-memory
+//     pass across warps: one barrier per reflector;
 //   * the masked reflector block Y is written once per block (row-major, so the
-//     apply reads it with 16-byte loads);
-//   * the apply to the rest of the tile is Z = Y^T C (threads own 4 x 4 output
-//     blocks, C streamed from L2 in 16-byte vectors), W = T^T Z (+ top rows),
-//     C -= Y W (threads own rows, W broadcast from shared memory).
+//     apply reads a row of it as 16 consecutive values);
+//   * the apply to the rest of the tile is Z = Y^T C (thread j owns column j; C
+//     streams through shared memory in row chunks, cp.async ring issued at the
+//     start of the block), W = T^T Z (+ top rows), C -= Y W (threads own rows,
+//     W broadcast from shared memory).
 
 template <typename T>
 __device__ __forceinline__ void ld4(const T *p, T (&v)[4]) {

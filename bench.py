@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--no-modes", action="store_true", help="skip the other precision modes")
     p.add_argument("--no-batched", action="store_true")
     p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--no-ooc", action="store_true", help="skip the out-of-core run")
+    p.add_argument("--ooc-budget-mb", type=int, default=512)
     p.add_argument("--batch-count", type=int, default=4096)
     p.add_argument("--serve-requests", type=int, default=120)
     p.add_argument("--serve-rate", type=float, default=12.0)
@@ -325,6 +327,28 @@ def run_batched(args, h):
             "max_rel_sigma_err_vs_lapack_fp64": err, "checked": 16}
 
 
+def run_ooc(args, a_host, s64, h):
+    """Out-of-core form (OOC_SVD!) on the same matrix, kept in host memory and
+    streamed through a device budget smaller than the matrix."""
+    import avs
+    budget = args.ooc_budget_mb << 20
+    slab, used, incore_from = avs.ooc_plan(args.n, args.tile, np.float32, budget)
+    a = np.asfortranarray(a_host.T)  # the headline's column-major matrix, host copy (overwritten)
+    r = avs.Report()
+    t0 = time.perf_counter()
+    sig = avs.OOC_SVD(a, args.tile, device_bytes=budget, report=r, handle=h)
+    wall = time.perf_counter() - t0
+    out = {"workload": "OOC_SVD! of the headline matrix (FP32, host resident, %d MiB of device memory for a "
+                       "%d MiB matrix)" % (args.ooc_budget_mb, args.n * args.n * 4 >> 20),
+           "s_per_svd": wall, "stage_ms": {"stage1": r.t_stage1_ms, "stage2": r.t_stage2_ms,
+                                           "stage3": r.t_stage3_ms},
+           "slab_tile_rows": slab, "device_bytes": used, "in_core_from_step": incore_from,
+           "n_steps": args.n // args.tile}
+    if s64 is not None:
+        out["max_abs_err_over_sigma_max_vs_fp64"] = float(np.max(np.abs(sig.astype(np.float64) - s64)) / s64[0])
+    return out
+
+
 def run_serving(args):
     from avs import serve_bench
     res = serve_bench.run(requests=args.serve_requests, rate=args.serve_rate, seed=7, workers=4, check=8,
@@ -432,6 +456,8 @@ def main():
     if extras and not args.no_modes:
         line["modes"] = run_modes(args, A, h, s64)
     del A
+    if extras and not args.no_ooc:
+        line["out_of_core"] = run_ooc(args, a_host, s64, h)
     if extras and not args.no_batched:
         line["batched"] = run_batched(args, h)
     h.close()

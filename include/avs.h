@@ -236,6 +236,15 @@ int avs_bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, doub
 int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
                               const int32_t *tile, const float *const *dA, float *const *dsigma,
                               const avs_opts *opts, avs_report *report);
+/* The same batched pipeline stopped after the bulge chase: the bidiagonal B of
+ * each matrix (A = U B V^T, V e1 = e1), d (n values) and e (n values, the last
+ * one 0) to the caller's FP64 device vectors dd[i], de[i].  B is unique up to
+ * the signs of its entries, so |d| and |e| equal those of LAPACK gebrd on the
+ * same matrix to the FP32 rounding of the band reduction: the quantity the
+ * random-matrix sampling client reads (RMT/rmt.jl:24-31, d of gebrd!). */
+int avs_bidiag_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
+                             const int32_t *tile, const float *const *dA, double *const *dd, double *const *de,
+                             const avs_opts *opts, avs_report *report);
 
 /* Autotuner of the batched path: times tiles 32, 64 and 128 (those that divide
  * n with at least two tiles) on `sample` seeded random matrices of order n,

@@ -143,3 +143,37 @@ def test_golden_fixtures(oracle_mod):
         np.testing.assert_allclose(s, g[name + "_sigma_oracle"], rtol=0, atol=1e-14 * s[0])
         rt = 1e-5 if a.dtype == np.float32 else 1e-12
         assert np.max(np.abs(s - g[name + "_sigma_lapack"])) <= rt * s[0]
+
+
+def test_gebd2_oracle_relations():
+    """The numpy restatement of LAPACK's bidiagonal reduction, pinned by the
+    relations that define it (no golden vectors exist for gebrd): the
+    bidiagonal carries the singular values; with V e1 = e1, B^T B = V^T A^T A V
+    has (1,1) entry ||a_1||^2 = d_1^2, and ||A^T a_1||^2 = d_1^2 (d_1^2 + e_1^2)."""
+    import numpy as np
+    from oracle import gebrd
+    rng = np.random.default_rng(12)
+    for n in (2, 7, 64):
+        a = rng.standard_normal((n, n))
+        d, e = gebrd.gebd2(a)
+        b = np.diag(d) + np.diag(e, 1)
+        np.testing.assert_allclose(np.linalg.svd(b, compute_uv=False), np.linalg.svd(a, compute_uv=False),
+                                   rtol=1e-12, atol=1e-12)
+        assert abs(abs(d[0]) - np.linalg.norm(a[:, 0])) < 1e-12 * np.linalg.norm(a)
+        if n > 1:
+            # (A^T A) e1 = V (B^T B) e1 and V e1 = e1: ||A^T a_1||^2 = d1^2 (d1^2 + e1^2)
+            lhs = np.linalg.norm(a.T @ a[:, 0]) ** 2
+            assert abs(lhs - d[0] ** 2 * (d[0] ** 2 + e[0] ** 2)) < 1e-10 * lhs
+    # a zero column gives an identity reflector
+    d, e = gebrd.gebd2(np.zeros((3, 3)))
+    assert not np.any(d) and not np.any(e)
+
+
+def test_rmt_oracle_statistics_shape():
+    import numpy as np
+    from oracle import gebrd
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((3, 4, 8, 8))
+    m, c, times = gebrd.mou_process_covar(x + np.swapaxes(x, 2, 3), 0.05, 2)
+    assert m.shape == (4,) and c.shape == (4,) and np.allclose(times, np.arange(4) * 0.0125)
+    assert np.all(m > 0)
