@@ -324,6 +324,30 @@ int svdvals_dev(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, 
     return run_pipeline<float, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, split, s, rep);
 }
 
+// Page-locks a caller's host range for the duration of a call (large ranges
+// only): the copy from page-locked memory is one DMA at the link's rate, where a
+// pageable copy goes through the driver's staging buffers.  A range that
+// cannot be registered (already page-locked, or refused) is copied as it is.
+// The stream is drained before the range is released.
+struct HostPin {
+    void *p = nullptr;
+    cudaStream_t s = nullptr;
+    HostPin(const void *ptr, size_t bytes, cudaStream_t stream) : s(stream) {
+        if (bytes < (size_t(32) << 20)) return;
+        void *q = const_cast<void *>(ptr);
+        if (cudaHostRegister(q, bytes, cudaHostRegisterDefault) == cudaSuccess ||
+            (cudaGetLastError(), cudaHostRegister(q, bytes, cudaHostRegisterReadOnly) == cudaSuccess))
+            p = q;
+        else
+            cudaGetLastError();
+    }
+    ~HostPin() {
+        if (!p) return;
+        cudaStreamSynchronize(s);
+        cudaHostUnregister(p);
+    }
+};
+
 template <typename T>
 int svdvals_host(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const T *A, T *sigma,
                  const avs_opts *opts, avs_report *rep) {
@@ -343,6 +367,7 @@ int svdvals_host(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile,
     if ((rc = ensure_ws(h, L.total)) != AVS_SUCCESS) return rc;
     cudaStream_t s = h->stream;
     T *stage = reinterpret_cast<T *>(ws_at(h, L.off_stage));
+    const HostPin pin(A, sizeof(T) * ((size_t)lda * (size_t)(n - 1) + (size_t)n), s);
     AVS_CUDA_TRY(cudaEventRecord(h->ev[4], s));
     AVS_CUDA_TRY(cudaMemcpy2DAsync(stage, sizeof(T) * (size_t)n, A, sizeof(T) * (size_t)lda, sizeof(T) * (size_t)n,
                                    (size_t)n, cudaMemcpyHostToDevice, s));
