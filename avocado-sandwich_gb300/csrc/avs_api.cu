@@ -84,7 +84,7 @@ Layout make_layout(int64_t n, int b, size_t elem, size_t stage_elem, int tc_fmt 
     L.off_tfull = o;
     o = align_up(o + (b >= 128 ? elem * (size_t)(nt + 1) * (size_t)b * (size_t)b : 0));
     L.off_flags1 = o;
-    o = align_up(o + sizeof(int) * (size_t)(nt + 4));
+    o = align_up(o + sizeof(int) * (size_t)(2 * nt + 4));
     L.off_flags2 = o;
     o = align_up(o + sizeof(int) * (size_t)(n + 4));
     L.ldab = 3 * (int64_t)b;
@@ -954,7 +954,7 @@ BatchLayout batch_layout(int64_t n, int b, int cnt) {
     L.tau = take(sizeof(float) * (size_t)cnt * (nt + 1) * b);
     L.tblk = take(sizeof(float) * (size_t)cnt * (nt + 1) * (b / 16) * 256);
     L.tfull = take(b >= 128 ? sizeof(float) * (size_t)cnt * (nt + 1) * b * b : 0);
-    L.f1 = take(sizeof(int) * (size_t)cnt * (nt + 4));
+    L.f1 = take(sizeof(int) * (size_t)cnt * (2 * nt + 4));
     L.ab = take(sizeof(float2) * (size_t)cnt * 3 * b * n);
     L.f2 = take(sizeof(int) * ((size_t)cnt * (n + 1) + 4));
     L.d = take(sizeof(double) * (size_t)cnt * n);
@@ -1044,7 +1044,7 @@ int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cn
     w1.sTau = (nt + 1) * b;
     w1.sTblk = (nt + 1) * (b / 16) * 256;
     w1.sTfull = (nt + 1) * (int64_t)b * b;
-    w1.sFlags = nt + 4;
+    w1.sFlags = 2 * nt + 4;
     int rc = stage1_ge2bnd<float>(W, n, n, b, w1, s, launches);
     if (rc != AVS_SUCCESS) return rc;
     AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[1], s, cudaEventRecordExternal));

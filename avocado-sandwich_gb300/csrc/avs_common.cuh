@@ -88,7 +88,7 @@ void set_last_cuda_error(cudaError_t e);
 struct Stage1Work {
     void *tau;        // [nt][b] of T
     void *tblk;       // [nt][b/ib][ib*ib] of T
-    int *flags;       // ticket (1) + progress (nt) + err (1), reset per launch
+    int *flags;       // ticket (1) + two progress counters per tile (2 nt), reset per launch
     int *err;         // device status word (shared with other stages)
     void *tfull;      // [nt][b*b] of T: full compact-WY factors (tiles 128, 256)
     void *tc_ws = nullptr;  // tensor-core update buffers (stage1_tc_bytes), FP32 tiles

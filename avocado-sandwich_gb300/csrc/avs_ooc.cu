@@ -47,7 +47,7 @@ OocBufs carve(void *ws, int64_t n, int b, size_t elem, int slab) {
     o.tfull = b >= 128 ? p + off : nullptr;
     off = al256(off + (b >= 128 ? elem * (size_t)(nt + 1) * b * b : 0));
     o.flags = reinterpret_cast<int *>(p + off);
-    off = al256(off + sizeof(int) * (size_t)(nt + 4));
+    off = al256(off + sizeof(int) * (size_t)(2 * nt + 4));
     const size_t sb = al256(elem * (size_t)(1 + slab) * b * n);
     o.region = p + off;
     o.X[0] = p + off;
@@ -59,7 +59,7 @@ OocBufs carve(void *ws, int64_t n, int b, size_t elem, int slab) {
 size_t fixed_bytes(int64_t n, int b, size_t elem) {
     const int64_t nt = n / b;
     return al256(elem * (size_t)(nt + 1) * b) + al256(elem * (size_t)(nt + 1) * (b / 16) * 256) +
-           al256(b >= 128 ? elem * (size_t)(nt + 1) * b * b : 0) + al256(sizeof(int) * (size_t)(nt + 4)) + 256;
+           al256(b >= 128 ? elem * (size_t)(nt + 1) * b * b : 0) + al256(sizeof(int) * (size_t)(2 * nt + 4)) + 256;
 }
 
 // cudaMemcpy2DAsync of `height` runs of `width` elements

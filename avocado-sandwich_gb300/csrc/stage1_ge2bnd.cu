@@ -20,8 +20,12 @@
 // (#tiles + b/16) block steps instead of #tiles * b reflector steps.  Within a
 // block the 16 reflectors are generated one column at a time, their
 // compact-WY factor T (16 x 16) is formed, and the block is applied to the rest
-// of the tile with it.  Roles are handed out by an atomic ticket in launch
-// order, so a role only ever waits on a role already running: no co-residency
+// of the tile with it.  A role hands block cb on in two parts: the 16 x 16
+// diagonal block of the top rows right after its reflectors (all the next
+// role's reflectors read), and the trailing top rows after its apply (which the
+// next role reads only in its own apply), so the step between roles is one
+// reflector loop.  Roles are handed out by an atomic ticket in launch order,
+// so a role only ever waits on a role already running: no co-residency
 // assumption, and every wait is bounded.
 //
 // Trailing update kernel.  One CTA owns a column strip of the trailing matrix,
@@ -57,7 +61,7 @@ struct PanelArgs {
     void *tau;       // [P][b]
     void *tblk;      // [P][b/kIB][kIB*kIB]
     int *ticket;
-    int *progress;   // [P]
+    int *progress;   // [2P]: diagonal block handed on, trailing top rows handed on
     int *err;
     int64_t sA, sTau, sTblk, sFlags;  // per-matrix strides (blockIdx.y = matrix)
 };
@@ -281,31 +285,17 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
     T *tblk_out = reinterpret_cast<T *>(args.tblk) + zb * args.sTblk + (size_t)p * nb * kIB * kIB;
     const int t = tid;  // my row (b <= 256)
 
+    int *full = progress + args.P;  // per role: block cb's trailing top rows are final
     for (int cb = 0; cb < nb; ++cb) {
         const int c0 = cb * kIB;
-        if (tid == 0) {
-            bool ok = true;
-            if (p > args.first_role) ok = wait_geq(progress + p - 1, cb + 1, args.err);
-            s_ok = ok;
-        }
-        __syncthreads();
-        if (!s_ok) return;
+        // ---- the role's own tile (no other role writes it): the block's 16
+        // columns and the first chunks of its trailing columns load while the
+        // role waits for the previous one
         for (int idx = tid; idx < b * kIB; idx += kNT) {
             int tt, l;
             if (LAYOUT == 0) { tt = idx % b; l = idx / b; } else { l = idx % kIB; tt = idx / kIB; }
             X[tt + l * ldx] = __ldcg(&V(row0 + tt, col0 + c0 + l));
         }
-        if (!geqrt) {
-            const int ncols = b - c0;
-            for (int idx = tid; idx < kIB * ncols; idx += kNT) {
-                int l, j;
-                if (LAYOUT == 0) { l = idx % kIB; j = idx / kIB; } else { j = idx % ncols; l = idx / ncols; }
-                Rt[l + (c0 + j) * kIB] = __ldcg(&V(top0 + c0 + l, col0 + c0 + j));
-            }
-        }
-        __syncthreads();
-
-        // ---- first chunks of the trailing columns (their loads overlap the reflectors)
         const int jbase = c0 + kIB;
         const int nrest = b - jbase;
         const int tstart = geqrt ? c0 : 0;  // rows above c0 have Y = 0 for GEQRT
@@ -339,6 +329,26 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
 #pragma unroll
             for (int q = 0; q < NBUF; ++q) issue(q);
         }
+        // ---- the diagonal 16 x 16 block of the top rows, once the previous
+        // role's reflectors of this block are in it (TSQRT)
+        if (tid == 0) {
+            bool ok = true;
+            if (p > args.first_role) ok = wait_geq(progress + p - 1, cb + 1, args.err);
+            s_ok = ok;
+        }
+        __syncthreads();
+        if (!s_ok) {
+            cp_async_wait<0>();
+            return;
+        }
+        if (!geqrt) {
+            for (int idx = tid; idx < kIB * kIB; idx += kNT) {
+                int l, j;
+                if (LAYOUT == 0) { l = idx % kIB; j = idx / kIB; } else { j = idx % kIB; l = idx / kIB; }
+                Rt[l + (c0 + j) * kIB] = __ldcg(&V(top0 + c0 + l, col0 + c0 + j));
+            }
+        }
+        __syncthreads();
 
         // ---- the 16 reflectors of the block, one per step, all threads.  One
         // barrier per reflector: the warp partial sums are double-buffered, and
@@ -432,6 +442,16 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
         __syncthreads();
         if (pend_at) *pend_at = pend_v;
         __syncthreads();
+        // the diagonal block of the top rows is final for this role: back to
+        // global memory (handed on after the barrier below) -- a TSQRT role's
+        // successor needs only this block for its own reflectors
+        if (!geqrt) {
+            for (int idx = tid; idx < kIB * kIB; idx += kNT) {
+                int l, jx;
+                if (LAYOUT == 0) { l = idx % kIB; jx = idx / kIB; } else { jx = idx % kIB; l = idx / kIB; }
+                V(top0 + c0 + l, col0 + c0 + jx) = Rt[l + (c0 + jx) * kIB];
+            }
+        }
 
         // ---- Gram matrix of the block's reflectors, T (warp 0), masked Y
         {
@@ -462,6 +482,10 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
             Yr[tt * kIB + l] = y;
         }
         __syncthreads();
+        if (!geqrt && tid == 0) {
+            __threadfence();
+            st_release(progress + p, cb + 1);
+        }
         if (wid == 0) {
             if (lane < kIB) Tm[lane + lane * kIB] = stau[lane];
             __syncwarp();
@@ -481,6 +505,10 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
         }
         if (tid < kIB) tau_out[c0 + tid] = stau[tid];
         __syncthreads();
+        if (geqrt && tid == 0) {  // the block's rows of the top tile are written back above
+            __threadfence();
+            st_release(progress, cb + 1);
+        }
         if (tid < kIB * kIB) tblk_out[(size_t)cb * kIB * kIB + tid] = Tm[tid];
 
         // ---- apply to the rest of the tile
@@ -518,6 +546,18 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                 }
             }
             __syncthreads();
+            // the trailing top rows, once the previous role's (b) is in them
+            if (!geqrt) {
+                if (tid == 0) s_ok = (p > args.first_role) ? wait_geq(full + p - 1, cb + 1, args.err) : true;
+                __syncthreads();
+                if (!s_ok) return;
+                for (int idx = tid; idx < kIB * nrest; idx += kNT) {
+                    int l, j;
+                    if (LAYOUT == 0) { l = idx % kIB; j = idx / kIB; } else { j = idx % nrest; l = idx / nrest; }
+                    Rt[l + (jbase + j) * kIB] = __ldcg(&V(top0 + c0 + l, col0 + jbase + j));
+                }
+                __syncthreads();
+            }
             // (b) W = T^T (Z + top rows); top rows -= W
             for (int jr = tid; jr < nrest; jr += kNT) {
                 T zc[kIB];
@@ -536,19 +576,18 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                 }
             }
             __syncthreads();
-            // The top rows are final for this block: a TSQRT role hands the
-            // block to the next role now, before updating its own tile (c).
+            // The trailing top rows are final for this block: a TSQRT role
+            // hands them to the next role now, before updating its own tile (c).
             if (!geqrt) {
-                const int ncols = b - c0;
-                for (int idx = tid; idx < kIB * ncols; idx += kNT) {
+                for (int idx = tid; idx < kIB * nrest; idx += kNT) {
                     int l, jx;
-                    if (LAYOUT == 0) { l = idx % kIB; jx = idx / kIB; } else { jx = idx % ncols; l = idx / ncols; }
-                    V(top0 + c0 + l, col0 + c0 + jx) = Rt[l + (c0 + jx) * kIB];
+                    if (LAYOUT == 0) { l = idx % kIB; jx = idx / kIB; } else { jx = idx % nrest; l = idx / nrest; }
+                    V(top0 + c0 + l, col0 + jbase + jx) = Rt[l + (jbase + jx) * kIB];
                 }
                 __syncthreads();
                 if (tid == 0) {
                     __threadfence();
-                    st_release(progress + p, cb + 1);
+                    st_release(full + p, cb + 1);
                 }
             }
             // (c) C -= Y W: thread owns row t; 16 columns per group, the next
@@ -594,23 +633,13 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                 }
             }
         } else if (!geqrt) {
-            // no columns right of the block: the top rows of the block are final
-            const int ncols = b - c0;
-            for (int idx = tid; idx < kIB * ncols; idx += kNT) {
-                int l, jx;
-                if (LAYOUT == 0) { l = idx % kIB; jx = idx / kIB; } else { jx = idx % ncols; l = idx / ncols; }
-                V(top0 + c0 + l, col0 + c0 + jx) = Rt[l + (c0 + jx) * kIB];
-            }
-            __syncthreads();
-            if (tid == 0) {
-                __threadfence();
-                st_release(progress + p, cb + 1);
-            }
+            // no columns right of the block (the diagonal block went back above)
+            if (tid == 0) st_release(full + p, cb + 1);
         }
         __syncthreads();
         if (geqrt && tid == 0) {
             __threadfence();
-            st_release(progress + p, cb + 1);
+            st_release(full, cb + 1);
         }
     }
 }
@@ -743,7 +772,7 @@ int launch_panel(T *dA, int64_t lda, int b, int pr, int pc, int P, int first_rol
         attr_set = true;
     }
     const int batch = w.batch > 0 ? w.batch : 1;
-    AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(batch > 1 ? w.sFlags * batch : P + 1), s));
+    AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(batch > 1 ? w.sFlags * batch : 2 * P + 1), s));
     PanelArgs a;
     a.a = dA;
     a.lda = lda;
