@@ -395,22 +395,39 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                 pend_at = nullptr;
             }
             const T alpha = geqrt ? X[c + i * ldx] : Rt[i + c * kIB];
-            // lane 0 of each warp forms the scalars (FP64 scalars are costly on
-            // every lane), the warp reads them with shuffles
             T out[6];
-            if (lane == 0) {
-                Acc s_all = PScal<T>::zero();
-#pragma unroll
-                for (int w = 0; w < kNT / 32; ++w) s_all = PScal<T>::shfl_add_local(s_all, spart[pb * 8 + w]);
+            if constexpr (sizeof(T) == 4) {
+                // FP32 tiles: every lane forms the (double-float) scalars -- no
+                // divergence, and the loads below overlap them.  The 8 warp
+                // partials are summed by a 3-level shuffle tree; df_add is
+                // commutative, so every lane of every warp gets the same sum.
+                Acc s_all = spart[pb * 8 + (lane & 7)];
+                s_all = PScal<T>::shfl_add(s_all, 1);
+                s_all = PScal<T>::shfl_add(s_all, 2);
+                s_all = PScal<T>::shfl_add(s_all, 4);
                 PScal<T>::compute(s_all, alpha, out);
                 if (!isfinite(out[5]) || !isfinite(out[0])) {
                     if (tid == 0) atomicCAS(args.err, kDevOk, kDevNonfinite);
                     out[5] = out[1] = out[2] = out[3] = T(0);
                     out[4] = alpha;
                 }
-            }
+            } else {
+                // FP64 tiles: lane 0 of each warp forms the scalars (FP64 is
+                // costly on every lane), the warp reads them with shuffles
+                if (lane == 0) {
+                    Acc s_all = PScal<T>::zero();
 #pragma unroll
-            for (int q = 0; q < 6; ++q) out[q] = __shfl_sync(0xffffffffu, out[q], 0);
+                    for (int w = 0; w < kNT / 32; ++w) s_all = PScal<T>::shfl_add_local(s_all, spart[pb * 8 + w]);
+                    PScal<T>::compute(s_all, alpha, out);
+                    if (!isfinite(out[5]) || !isfinite(out[0])) {
+                        if (tid == 0) atomicCAS(args.err, kDevOk, kDevNonfinite);
+                        out[5] = out[1] = out[2] = out[3] = T(0);
+                        out[4] = alpha;
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 6; ++q) out[q] = __shfl_sync(0xffffffffu, out[q], 0);
+            }
             // column sums of the 16 dot products: lane L sums column L & 15
             T dmine = T(0);
 #pragma unroll
