@@ -299,11 +299,13 @@ __device__ double bisect_df_grp(const float2 *a, int64_t n, int64_t k, double re
 }
 
 // Lanes per value.  A group of G lanes does more counts per value (about 1,
-// 2.3 and 3.2 times those of one lane for G = 1, 4, 8) in fewer dependent
-// passes, which pays while the values alone leave the GPU short of threads
-// (measured on GB300: G = 1 is fastest from n = 8192 values, G = 4/8 below).
+// 1.4, 2.3 and 3.2 times those of one lane for G = 1, 2, 4, 8) in fewer
+// dependent passes, which pays while the values alone leave the GPU short of
+// threads (measured on GB300 at n = 16384 values: 121 ms with G = 1, 98 ms
+// with G = 2, 146 ms with G = 4; G = 4/8 below 8192 values).
 inline int bisect_group(int64_t nvalues) {
-    if (nvalues >= 8192) return 1;
+    if (nvalues >= 65536) return 1;
+    if (nvalues >= 8192) return 2;
     if (nvalues >= 1024) return 4;
     return 8;
 }
@@ -438,6 +440,8 @@ int stage3_bisect_df(const double *dd, const double *de, int64_t n, double rel_t
     const unsigned blocks = (unsigned)((nt + 127) / 128);
     if (G == 1)
         bisect_df_kernel<1><<<blocks, 128, 0, s>>>(dpairs, n, rel_tol, dscratch, dsigma);
+    else if (G == 2)
+        bisect_df_kernel<2><<<blocks, 128, 0, s>>>(dpairs, n, rel_tol, dscratch, dsigma);
     else if (G == 4)
         bisect_df_kernel<4><<<blocks, 128, 0, s>>>(dpairs, n, rel_tol, dscratch, dsigma);
     else
@@ -523,6 +527,8 @@ int stage3_bisect_df_batched(const double *dd, const double *de, int64_t n, int 
     const unsigned blocks = (unsigned)((nv * G + 127) / 128);
     if (G == 1)
         bisect_df_batched<1><<<blocks, 128, 0, s>>>(dpairs, n, batch, rel_tol, dscratch, dsigma);
+    else if (G == 2)
+        bisect_df_batched<2><<<blocks, 128, 0, s>>>(dpairs, n, batch, rel_tol, dscratch, dsigma);
     else if (G == 4)
         bisect_df_batched<4><<<blocks, 128, 0, s>>>(dpairs, n, batch, rel_tol, dscratch, dsigma);
     else
