@@ -298,9 +298,8 @@ __device__ double bisect_df_grp(const float2 *a, int64_t n, int64_t k, double re
     return bound * 0.5 * df_to_double(c);
 }
 
-// Lanes per value.  A group of G lanes does more counts per value (about 1,
-// 1.4, 2.3 and 3.2 times those of one lane for G = 1, 2, 4, 8) in fewer
-// dependent passes, which pays while the values alone leave the GPU short of
+// Lanes per value.  A group of G lanes does more counts per value (about 2.3
+// and 3.2 times those of one lane for G = 4, 8) in fewer dependent passes, which pays while the values alone leave the GPU short of
 // threads (measured on GB300 at n = 16384 values: 121 ms with G = 1, 98 ms
 // with G = 2, 146 ms with G = 4; G = 4/8 below 8192 values).
 inline int bisect_group(int64_t nvalues) {
