@@ -95,10 +95,23 @@ def cpu_sample(args, steps=1):
         times.append(time.perf_counter() - t0)
     scale = (args.n / ns) ** 3
     t = float(np.median(times))
-    return {"value": t * scale, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
-            "sample": "oracle (C restatement of Blockbidiag! + bidiagonalize + bidiagonal singular values), "
-                      "n=%d tile %d float32, %d run(s), median %.2f s, scaled by (%d/%d)^3 (extrapolated)"
-                      % (ns, b, steps, t, args.n, ns)}
+    out = {"value": t * scale, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+           "sample": "oracle (C restatement of Blockbidiag! + bidiagonalize + bidiagonal singular values), "
+                     "n=%d tile %d float32, %d run(s), median %.2f s, scaled by (%d/%d)^3 (extrapolated)"
+                     % (ns, b, steps, t, args.n, ns)}
+    # stage-2 comparator: LAPACK dgbbrd (the reference BRD code's, bulgechasing2.jl:142-170)
+    from oracle import lapack
+    if lapack.available():
+        rng = np.random.default_rng(4)
+        full = rng.standard_normal((ns, ns))
+        band = np.triu(full) - np.triu(full, b + 1)
+        t0 = time.perf_counter()
+        lapack.gbbrd(band, b)
+        tg = time.perf_counter() - t0
+        out["stage2_lapack_dgbbrd"] = {"n": ns, "bw": b, "s": tg, "s_scaled_to_n": tg * (args.n / ns) ** 2,
+                                       "note": "OpenBLAS (scipy's) dgbbrd, one thread of the host; band reduction "
+                                               "is O(n^2 b), scaled by (n/%d)^2 (extrapolated)" % ns}
+    return out
 
 
 class Clocks:

@@ -177,3 +177,42 @@ def test_rmt_oracle_statistics_shape():
     m, c, times = gebrd.mou_process_covar(x + np.swapaxes(x, 2, 3), 0.05, 2)
     assert m.shape == (4,) and c.shape == (4,) and np.allclose(times, np.arange(4) * 0.0125)
     assert np.all(m > 0)
+
+
+def test_oracle_bisection_vs_lapack_bdsdc(oracle_mod):
+    """Stage 3 pinned to the routine the reference calls: LAPACK dbdsdc('U','N')
+    (bulgechasing.jl:50-53) from the OpenBLAS scipy bundles."""
+    from oracle import lapack
+    if not lapack.available():
+        pytest.skip("scipy's OpenBLAS LAPACKE symbols not found")
+    rng = np.random.default_rng(21)
+    for n in (1, 2, 7, 100, 500):
+        d = rng.standard_normal(n)
+        e = rng.standard_normal(max(n - 1, 0))
+        ref = lapack.bdsdc(d, e)
+        got = oracle_mod.bidiag_svals(d, e)
+        assert np.max(np.abs(got - ref)) <= 1e-13 * max(ref[0], 1)
+    # graded: both keep relative accuracy
+    d = 10.0 ** -np.arange(0, 12)
+    e = 1e-3 * d[:-1]
+    ref = lapack.bdsdc(d, e)
+    assert np.max(np.abs(oracle_mod.bidiag_svals(d, e, rel_tol=1e-30) - ref) / ref) < 1e-10
+
+
+def test_gbbrd_comparator_relations():
+    """LAPACK dgbbrd (the reference BRD code's comparator, bulgechasing2.jl:142-170)
+    gives the Golub-Kahan bidiagonal of the band: the gebd2 oracle's up to signs."""
+    from oracle import gebrd, lapack
+    if not lapack.available():
+        pytest.skip("scipy's OpenBLAS LAPACKE symbols not found")
+    rng = np.random.default_rng(22)
+    for n, bw in ((40, 4), (200, 16), (256, 64)):
+        a = rng.standard_normal((n, n))
+        band = np.triu(a) - np.triu(a, bw + 1)
+        d, e = lapack.gbbrd(band, bw)
+        dg, eg = gebrd.gebd2(band)
+        k = min(20, n - 1)
+        assert np.max(np.abs(np.abs(d[:k]) - np.abs(dg[:k]))) < 1e-12 * np.linalg.norm(band, 2)
+        assert np.max(np.abs(np.abs(e[:k]) - np.abs(eg[:k]))) < 1e-12 * np.linalg.norm(band, 2)
+        ref = np.linalg.svd(band, compute_uv=False)
+        np.testing.assert_allclose(lapack.bdsdc(d, e), ref, rtol=0, atol=1e-13 * ref[0])
