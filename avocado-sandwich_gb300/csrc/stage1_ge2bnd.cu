@@ -460,13 +460,18 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
         if (pend_at) *pend_at = pend_v;
         __syncthreads();
         // the diagonal block of the top rows is final for this role: back to
-        // global memory (handed on after the barrier below) -- a TSQRT role's
-        // successor needs only this block for its own reflectors
+        // global memory and handed on -- a TSQRT role's successor needs only
+        // this block for its own reflectors
         if (!geqrt) {
             for (int idx = tid; idx < kIB * kIB; idx += kNT) {
                 int l, jx;
                 if (LAYOUT == 0) { l = idx % kIB; jx = idx / kIB; } else { jx = idx % kIB; l = idx / kIB; }
                 V(top0 + c0 + l, col0 + c0 + jx) = Rt[l + (c0 + jx) * kIB];
+            }
+            __syncthreads();
+            if (tid == 0) {
+                __threadfence();
+                st_release(progress + p, cb + 1);
             }
         }
 
@@ -499,10 +504,6 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
             Yr[tt * kIB + l] = y;
         }
         __syncthreads();
-        if (!geqrt && tid == 0) {
-            __threadfence();
-            st_release(progress + p, cb + 1);
-        }
         if (wid == 0) {
             if (lane < kIB) Tm[lane + lane * kIB] = stau[lane];
             __syncwarp();
