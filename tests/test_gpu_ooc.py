@@ -59,6 +59,17 @@ def test_ooc_bidiag_equals_incore(avs_mod, torch_cuda, tile, slab):
     assert np.max(np.abs(band_svals(a, tile) - ref)) / ref[0] < 1e-5
 
 
+@pytest.mark.parametrize("tile,slab", [(32, 2), (128, 1)])
+def test_ooc_bidiag_equals_incore_fp64(avs_mod, torch_cuda, tile, slab):
+    n = 8 * tile
+    a = gaussian(n, np.float64, 3 * tile)
+    dev = avs_mod.to_device(a)
+    avs_mod.Blockbidiag(dev, tile)
+    incore = avs_mod.from_device(dev)
+    avs_mod.OOC_Bidiag(a, tile, device_bytes=budget_for(avs_mod, n, tile, np.float64, slab))
+    assert np.array_equal(a, incore)
+
+
 @pytest.mark.parametrize("dtype,tol", [(np.float32, 1e-5), (np.float64, 1e-12)])
 @pytest.mark.parametrize("tile", [32, 128, 256])
 def test_ooc_svd_matches_lapack(avs_mod, torch_cuda, dtype, tol, tile):
