@@ -165,14 +165,15 @@ __global__ void __launch_bounds__(kChaseThreads) chase_kernel(double *ab, int64_
     }
 }
 
-template <int BW, int CC = (BW >= 128 ? 8 : (BW == 64 ? 4 : (BW == 32 ? 2 : 1)))>
+template <int BW, int CC = (BW >= 128 ? 8 : (BW == 64 ? 4 : (BW == 32 ? 2 : 1))), int NTT = 512>
 struct ChaseCfg {
     static constexpr int C = CC;  // CTAs per cluster (one sweep per cluster)
-    // 512 threads per CTA: an op's latency (the sweep wavefront's step) falls
-    // with the threads that share it (measured: 128-thread CTAs, several per
-    // SM, were slower at every band width)
-    static constexpr int NT = 512;
-    static constexpr int MINB = 1;
+    // One matrix: 512 threads per CTA -- an op's latency (the sweep wavefront's
+    // step) falls with the threads that share it (128-thread CTAs, several per
+    // SM, were slower at every band width).  A batch of small bands is
+    // throughput-bound instead: smaller CTAs, several sweeps per SM.
+    static constexpr int NT = NTT;
+    static constexpr int MINB = 512 / NTT;  // same registers per SM as one 512-thread CTA
     static constexpr int RPC = 2 * BW / C;          // R op: rows per CTA (64 or 32)
     static constexpr int G = NT / RPC;              // R op: column groups
     static constexpr int CPG = BW / G;              // R op: columns per group
@@ -335,11 +336,11 @@ __device__ __forceinline__ void warp_reflector(const BandT<S> &A, bool row, int6
     }
 }
 
-template <int BW, typename S, int CC>
-__global__ void __launch_bounds__(ChaseCfg<BW, CC>::NT, ChaseCfg<BW, CC>::MINB) chase_cluster_kernel(typename ChaseAr<S>::St *ab_base, int64_t n, int64_t ldab,
+template <int BW, typename S, int CC, int NTT = 512>
+__global__ void __launch_bounds__(ChaseCfg<BW, CC, NTT>::NT, ChaseCfg<BW, CC, NTT>::MINB) chase_cluster_kernel(typename ChaseAr<S>::St *ab_base, int64_t n, int64_t ldab,
                                                             int *ticket, int *done_base, int *err, int batch,
                                                             int64_t sAB, int64_t sDone) {
-    using Cfg = ChaseCfg<BW, CC>;
+    using Cfg = ChaseCfg<BW, CC, NTT>;
     using Ar = ChaseAr<S>;
     using V = typename Ar::V;
     cg::cluster_group cluster = cg::this_cluster();
@@ -485,10 +486,10 @@ __global__ void __launch_bounds__(ChaseCfg<BW, CC>::NT, ChaseCfg<BW, CC>::MINB) 
     }
 }
 
-template <int BW, typename S, int CC = ChaseCfg<BW>::C>
+template <int BW, typename S, int CC = ChaseCfg<BW>::C, int NTT = 512>
 int launch_chase_cluster(typename ChaseAr<S>::St *dAB, int64_t n, int64_t ldab, const Stage2Work &w, cudaStream_t s,
                          int num_sms, int batch = 1, int64_t sAB = 0, int64_t sDone = 0) {
-    using Cfg = ChaseCfg<BW, CC>;
+    using Cfg = ChaseCfg<BW, CC, NTT>;
     cudaLaunchConfig_t cfg = {};
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -502,7 +503,7 @@ int launch_chase_cluster(typename ChaseAr<S>::St *dAB, int64_t n, int64_t ldab, 
     cfg.numAttrs = 1;
     int max_clusters = 0;
     cfg.gridDim = dim3(Cfg::C * 64);
-    if (cudaOccupancyMaxActiveClusters(&max_clusters, chase_cluster_kernel<BW, S, CC>, &cfg) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveClusters(&max_clusters, chase_cluster_kernel<BW, S, CC, NTT>, &cfg) != cudaSuccess ||
         max_clusters <= 0) {
         cudaGetLastError();
         max_clusters = std::max(1, num_sms / Cfg::C);
@@ -511,7 +512,7 @@ int launch_chase_cluster(typename ChaseAr<S>::St *dAB, int64_t n, int64_t ldab, 
     const int64_t want = std::max<int64_t>(1, ((n / BW) / 2 + 2) * (int64_t)batch);
     const int64_t clusters = std::min<int64_t>(std::min<int64_t>(want, max_clusters), (n - 1) * (int64_t)batch);
     cfg.gridDim = dim3((unsigned)(clusters * Cfg::C));
-    AVS_CUDA_TRY(cudaLaunchKernelEx(&cfg, chase_cluster_kernel<BW, S, CC>, dAB, n, ldab, w.flags, w.flags + 1, w.err,
+    AVS_CUDA_TRY(cudaLaunchKernelEx(&cfg, chase_cluster_kernel<BW, S, CC, NTT>, dAB, n, ldab, w.flags, w.flags + 1, w.err,
                                     batch, sAB, sDone));
     return AVS_SUCCESS;
 }
@@ -715,14 +716,17 @@ int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float
     if (n >= 2) {
         AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)((n + 1) * (int64_t)batch + 1), s));
         int rc;
-        // small bands: few CTAs per sweep (the batch supplies the parallelism).
-        // Measured on 4096 matrices of orders 64..1024 (stage 2): band 32 C = 2
-        // 984 ms vs C = 1 1035 ms; band 64 C = 1 877 ms vs C = 2/4 1251/1223 ms;
-        // band 128 C = 2 1280 ms vs C = 4/8 1879/3289 ms.
+        // small bands: few, small CTAs per sweep (the batch supplies the
+        // parallelism).  Measured on the matrices of 4096 of orders 64..1024
+        // that each band divides (stage 2; clusters x threads per CTA):
+        // band 32: 1 x 128 499 ms, 2 x 64 503, 2 x 128 554, 2 x 256 588,
+        // 2 x 512 979, 1 x 512 1035; band 64: 2 x 128 670, 1 x 256 687,
+        // 1 x 512 876, 2/4 x 512 1251/1223; band 128: 2 x 512 1278, 4 x 256
+        // 1281, 4/8 x 512 1879/3289.
         switch (bw) {
             case 16: rc = launch_chase_cluster<16, df64, 1>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
-            case 32: rc = launch_chase_cluster<32, df64, 2>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
-            case 64: rc = launch_chase_cluster<64, df64, 1>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
+            case 32: rc = launch_chase_cluster<32, df64, 1, 128>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
+            case 64: rc = launch_chase_cluster<64, df64, 2, 128>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
             case 128: rc = launch_chase_cluster<128, df64, 2>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
             case 256: rc = launch_chase_cluster<256, df64, 8>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
             default: rc = AVS_ERR_UNSUPPORTED;
