@@ -717,8 +717,8 @@ int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float
         AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)((n + 1) * (int64_t)batch + 1), s));
         int rc;
         // small bands: few, small CTAs per sweep (the batch supplies the
-        // parallelism).  Measured on the matrices of 4096 of orders 64..1024
-        // that each band divides (stage 2; clusters x threads per CTA):
+        // parallelism).  Measured on the 4096-matrix workload (orders 64..1024;
+        // the matrices each band divides), stage 2, CTAs per cluster x threads:
         // band 32: 1 x 128 499 ms, 2 x 64 503, 2 x 128 554, 2 x 256 588,
         // 2 x 512 979, 1 x 512 1035; band 64: 2 x 128 670, 1 x 256 687,
         // 1 x 512 876, 2/4 x 512 1251/1223; band 128: 2 x 512 1278, 4 x 256
