@@ -723,10 +723,20 @@ int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float
         // 2 x 512 979, 1 x 512 1035; band 64: 2 x 128 670, 1 x 256 687,
         // 1 x 512 876, 2/4 x 512 1251/1223; band 128: 2 x 512 1278, 4 x 256
         // 1281, 4/8 x 512 1879/3289.
+        // The small CTAs pay only while the batch keeps every SM busy with
+        // several sweeps (a sweep has about (n / bw) / 2 siblings in flight);
+        // a short batch is latency-bound and keeps 512-thread CTAs.
+        const bool wide = (int64_t)batch * std::max<int64_t>(1, (n / bw) / 2) >= 4 * (int64_t)num_sms;
         switch (bw) {
             case 16: rc = launch_chase_cluster<16, df64, 1>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
-            case 32: rc = launch_chase_cluster<32, df64, 1, 128>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
-            case 64: rc = launch_chase_cluster<64, df64, 2, 128>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
+            case 32:
+                rc = wide ? launch_chase_cluster<32, df64, 1, 128>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1)
+                          : launch_chase_cluster<32, df64, 2>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1);
+                break;
+            case 64:
+                rc = wide ? launch_chase_cluster<64, df64, 2, 128>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1)
+                          : launch_chase_cluster<64, df64, 1>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1);
+                break;
             case 128: rc = launch_chase_cluster<128, df64, 2>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
             case 256: rc = launch_chase_cluster<256, df64, 8>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
             default: rc = AVS_ERR_UNSUPPORTED;

@@ -73,6 +73,20 @@ def test_batched_large_batch_copies(avs_mod, torch_cuda, n, tile, count):
     assert rel_err(single, sl.svdvals(hosts[0].astype(np.float64))) < TOL32
 
 
+@pytest.mark.parametrize("tile,count", [(32, 160), (64, 320)])
+def test_batched_wide_batch_equals_single(avs_mod, torch_cuda, tile, count):
+    """A batch wide enough for the small-CTA chase (many sweeps per SM) gives
+    each matrix the single call's values bit for bit."""
+    hosts, devs = _mats(avs_mod, [256] * 4, 900 + tile)
+    mats = [devs[i % 4].clone() for i in range(count)]
+    outs = avs_mod.svdvals_batched(mats, tiles=tile)
+    for i in range(4):
+        single = avs_mod.my_CU_svdval(devs[i], tile).cpu().numpy()
+        for o in outs[i::4]:
+            assert np.array_equal(o.cpu().numpy(), single), rel_err(o.cpu().numpy(), single)
+        assert rel_err(single, sl.svdvals(hosts[i].astype(np.float64))) < TOL32
+
+
 def test_batched_large_batch_distinct(avs_mod, torch_cuda):
     """48 distinct matrices of order 512, tile 64: each within the FP32
     tolerance of LAPACK."""
