@@ -371,8 +371,6 @@ int svdvals_host(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile,
     AVS_CUDA_TRY(cudaEventRecord(h->ev[4], s));
     AVS_CUDA_TRY(cudaMemcpy2DAsync(stage, sizeof(T) * (size_t)n, A, sizeof(T) * (size_t)lda, sizeof(T) * (size_t)n,
                                    (size_t)n, cudaMemcpyHostToDevice, s));
-    avs_opts o2 = opts ? *opts : avs_opts{};
-    o2.stream = s;
     avs_report r2{};
     const bool f64 = fp64_stages(prec, opts);
     const double tol = bisect_tol(f64, opts);
@@ -409,7 +407,11 @@ const char *avs_strerror(int status) {
     switch (status) {
         case AVS_SUCCESS: return "success";
         case AVS_ERR_NOT_IMPLEMENTED: return "Not implemented";
-        case AVS_ERR_CUDA: return "CUDA runtime error";
+        case AVS_ERR_CUDA: {  // names the last CUDA error this thread met in the library
+            static thread_local char msg[192];
+            std::snprintf(msg, sizeof msg, "CUDA runtime error (%s)", cudaGetErrorString(g_last_cuda));
+            return msg;
+        }
         case AVS_ERR_OOM: return "out of device memory";
         case AVS_ERR_TIMEOUT: return "a bounded device-side wait timed out";
         case AVS_ERR_NONFINITE: return "non-finite value met in the factorisation";

@@ -90,8 +90,6 @@ int32_t pick_tile(avs_server *S, Slot &sl, const Request *r) {
     return rule_tile(r->n);
 }
 
-size_t elem_of(int32_t dtype) { return dtype == AVS_DTYPE_F64 ? 8 : 4; }
-
 // Bytes a slot holds after running a group of `cnt` requests of order n: the
 // workspace the group uses grows to what it needs, the other one stays.
 size_t held_after(const Slot &sl, int64_t ws_single, int64_t ws_batched, int64_t n, int32_t tile, int32_t dtype,

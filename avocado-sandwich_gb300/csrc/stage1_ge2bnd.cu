@@ -49,7 +49,6 @@ namespace {
 
 constexpr int kIB = 16;    // reflectors per compact-WY block
 constexpr int kNT = 256;   // threads per CTA (16 columns x 16 row groups)
-constexpr int kCW = 32;    // column chunk of the in-panel apply
 
 struct PanelArgs {
     void *a;

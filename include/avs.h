@@ -57,9 +57,10 @@ extern "C" {
 #define AVS_ERR_TOO_LARGE 8            /* n above the static scratch of avs_bidiag_svals_noalloc */
 
 /* ---- precision modes of the trailing WY updates (stage 1) ---------------- */
-/* Householder generation/scaling, bulge chase and bisection always run in FP64
- * scalars; these modes select the storage type of the tiles and the arithmetic
- * of the compact-WY trailing updates. */
+/* Householder generation/scaling, bulge chase and bisection run in FP64 (plain
+ * mode) or double-float (FP32-class modes, see the flags below) scalars; these
+ * modes select the storage type of the tiles and the arithmetic of the
+ * compact-WY trailing updates. */
 #define AVS_PREC_DEFAULT 0 /* FP64 for the _d entry points, FP32 for _s */
 #define AVS_PREC_FP64 1    /* plain path: FP64 tiles, FP64 updates */
 #define AVS_PREC_FP32 2    /* FP32 tiles, FP32 SIMT updates */
@@ -107,6 +108,8 @@ int avs_create(avs_handle **h, int device);
 int avs_destroy(avs_handle *h);
 /* Pre-grow the workspace for (n, tile, precision) so that later calls allocate nothing. */
 int avs_reserve(avs_handle *h, int64_t n, int32_t tile, int32_t precision);
+/* Message of a status code; for AVS_ERR_CUDA it names the last CUDA runtime error the calling
+ * thread met inside the library. */
 const char *avs_strerror(int status);
 int avs_version(void);
 
