@@ -216,3 +216,40 @@ def test_gbbrd_comparator_relations():
         assert np.max(np.abs(np.abs(e[:k]) - np.abs(eg[:k]))) < 1e-12 * np.linalg.norm(band, 2)
         ref = np.linalg.svd(band, compute_uv=False)
         np.testing.assert_allclose(lapack.bdsdc(d, e), ref, rtol=0, atol=1e-13 * ref[0])
+
+
+@pytest.mark.parametrize("n,bw", [(160, 4), (160, 16), (256, 64), (512, 16)])
+def test_brd_hierarchical_reduction(n, bw):
+    """The reference's hierarchical band reduction (BRD bidiag!, factor 4),
+    restated: the result is exactly bidiagonal, keeps the singular values
+    (its own test, bulgechasing2.jl:101-116), and its bidiagonal is the
+    Golub-Kahan one (right transforms never touch column 1): |d|, |e| equal
+    gebd2's."""
+    from oracle import brd, gebrd
+    rng = np.random.default_rng(n + bw)
+    a = np.triu(np.tril(rng.random((n, n)), bw))
+    s = brd.bidiag(a, bw)
+    off = s.copy()
+    off[np.arange(n), np.arange(n)] = 0
+    off[np.arange(n - 1), np.arange(1, n)] = 0
+    assert not np.any(off)
+    ref = np.linalg.svd(a, compute_uv=False)
+    assert np.max(np.abs(np.linalg.svd(s, compute_uv=False) - ref)) < 1e-12 * ref[0]
+    dg, eg = gebrd.gebd2(a)
+    k = 16
+    assert np.max(np.abs(np.abs(np.diag(s)[:k]) - np.abs(dg[:k]))) < 1e-12 * ref[0]
+    assert np.max(np.abs(np.abs(np.diag(s, 1)[:k]) - np.abs(eg[:k]))) < 1e-12 * ref[0]
+
+
+def test_brd_short_propagation_range():
+    """Documented divergence: at n = 64, bandwidth 4, the reference's
+    propagation range 0:n stops the last kernels early and the values are
+    wrong; running every kernel to the end (iters = 4n) gives them exactly."""
+    from oracle import brd
+    rng = np.random.default_rng(0)
+    a = np.triu(np.tril(rng.random((64, 64)), 4))
+    ref = np.linalg.svd(a, compute_uv=False)
+    short = np.linalg.svd(brd.bidiag(a, 4), compute_uv=False)
+    full = np.linalg.svd(brd.bidiag(a, 4, iters=4 * 64), compute_uv=False)
+    assert np.max(np.abs(short - ref)) > 1e-6 * ref[0]
+    assert np.max(np.abs(full - ref)) < 1e-12 * ref[0]
