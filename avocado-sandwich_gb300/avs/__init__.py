@@ -51,7 +51,7 @@ EXPORTED_SYMBOLS = [
     "avs_svdvals_batched_dev_s", "avs_bidiag_batched_dev_s", "avs_autotune_tile", "avs_trim", "avs_workspace_bytes", "avs_estimate_bytes",
     "avs_geqrf_dev_s", "avs_geqrf_dev_d",
     "avs_blockbidiag_ooc_s", "avs_blockbidiag_ooc_d", "avs_svdvals_ooc_s", "avs_svdvals_ooc_d",
-    "avs_geqrf_ooc_s", "avs_geqrf_ooc_d", "avs_ooc_plan",
+    "avs_geqrf_ooc_s", "avs_geqrf_ooc_d", "avs_ooc_plan", "avs_selftest_timeout",
     "avs_serve_create", "avs_serve_submit", "avs_serve_wait", "avs_serve_stats_get", "avs_serve_destroy",
 ]
 
@@ -137,6 +137,7 @@ def lib():
         L.avs_ooc_plan.argtypes = [I64, I32, I32, I64, ctypes.POINTER(I32), ctypes.POINTER(I64),
                                    ctypes.POINTER(I32)]
         L.avs_trim.argtypes = [P]
+        L.avs_selftest_timeout.argtypes = [P]
         L.avs_workspace_bytes.argtypes = [P, ctypes.POINTER(I64), ctypes.POINTER(I64)]
         L.avs_estimate_bytes.argtypes = [I64, I32, I32, I32, ctypes.POINTER(I64)]
         L.avs_serve_create.argtypes = [ctypes.POINTER(P), ctypes.POINTER(ServeConfig)]
@@ -361,6 +362,12 @@ def bidiag_batched(mats, tiles=None, report=None, handle=None):
                                         ctypes.byref(opt), ctypes.byref(r))
     _check(rc, "avs_bidiag_batched_dev_s")
     return outs
+
+
+def selftest_timeout(handle=None):
+    """Status of the bounded-wait check (AVS_ERR_TIMEOUT = 3 when the failure path works)."""
+    h = handle or default_handle()
+    return lib().avs_selftest_timeout(h.ptr)
 
 
 def autotune_tile(n, sample=16, handle=None):

@@ -66,7 +66,7 @@ def build(verbose=False, force=False, extra_flags=()):
             if verbose and msg:
                 print(msg)
     if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs + ["-lpthread"]
+        cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs + ["-lpthread", "-ldl"]
         run(cmd)
     return LIB
 

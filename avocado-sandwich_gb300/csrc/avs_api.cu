@@ -10,6 +10,8 @@
 #include <tuple>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "avs_common.cuh"
 #include "tc_gemm.cuh"
 
@@ -199,6 +201,15 @@ int finish_status(avs_handle *h, cudaStream_t s) {
     return AVS_SUCCESS;
 }
 
+// NVTX range around the host side of a stage (the launches it enqueues), for
+// profilers' timelines.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 float ev_ms(cudaEvent_t a, cudaEvent_t b) {
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
@@ -279,10 +290,17 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
         w1.ev_cap = pairs;
         w1.ev_used = &upd_used;
     }
-    if ((rc = stage1_ge2bnd<S>(W, n, n, b, w1, s, &launches)) != AVS_SUCCESS) return rc;
+    {
+        NvtxRange r("avs stage 1: GE2BND");
+        if ((rc = stage1_ge2bnd<S>(W, n, n, b, w1, s, &launches)) != AVS_SUCCESS) return rc;
+    }
     AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
-    if ((rc = run_stages23<S, TO>(h, L, n, b, W, n, sigma_out, rel_tol, fp64_stages, s, &launches)) != AVS_SUCCESS)
-        return rc;
+    {
+        NvtxRange r("avs stages 2-3: chase, bisection");
+        if ((rc = run_stages23<S, TO>(h, L, n, b, W, n, sigma_out, rel_tol, fp64_stages, s, &launches)) !=
+            AVS_SUCCESS)
+            return rc;
+    }
     AVS_CUDA_TRY(cudaMemcpyAsync(h->h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     rc = finish_status(h, s);
     if (rep) {
@@ -719,6 +737,7 @@ int ooc_call(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *A, T *sigma
     auto step = [&]() -> int {
         AVS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
         AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
+        NvtxRange range("avs out-of-core stage 1");
         int r = ooc_ge2bnd<T>(A, n, lda, tile, mode == kOocQr, mode == kOocQr ? tau : nullptr, plan, ws_at(h, 256),
                               err, s, &st);
         if (r != AVS_SUCCESS) return r;
@@ -1169,6 +1188,7 @@ static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const in
         const int gb = g.first.second;
         const int cnt = (int)g.second.size();
         const BatchLayout L = batch_layout(gn, gb, cnt);
+        NvtxRange range("avs batched group");
         // pointer tables: sources, destinations, leading dimensions
         for (int q = 0; q < cnt; ++q) {
             tab[q] = const_cast<float *>(dA[g.second[q]]);
@@ -1300,6 +1320,30 @@ extern "C" int avs_autotune_tile(avs_handle *h, int64_t n, int32_t sample, int32
     h->tuned[n] = bt;
     if (best) *best = bt;
     return AVS_SUCCESS;
+}
+
+// ===========================================================================
+// Failure path check: one thread waits, with a short bound, on a flag that
+// nothing sets -- the wait every cross-CTA dependency of the library uses.
+namespace {
+__global__ void timeout_probe_kernel(const int *flag, int *err, long long limit) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) wait_geq_n(flag, 1, err, limit);
+}
+}  // namespace
+
+extern "C" int avs_selftest_timeout(avs_handle *h) {
+    if (!h) return -1;
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    int rc = ensure_ws(h, 256);
+    if (rc != AVS_SUCCESS) return rc;
+    cudaStream_t s = h->stream;
+    int *err = reinterpret_cast<int *>(h->ws);
+    int *flag = err + 16;
+    AVS_CUDA_TRY(cudaMemsetAsync(h->ws, 0, 256, s));
+    timeout_probe_kernel<<<1, 32, 0, s>>>(flag, err, 1ll << 22);  // >= 2^22 sleeps of 64 ns
+    AVS_CUDA_TRY(cudaGetLastError());
+    AVS_CUDA_TRY(cudaMemcpyAsync(h->h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    return finish_status(h, s);
 }
 
 // ===========================================================================

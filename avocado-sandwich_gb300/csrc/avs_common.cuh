@@ -50,17 +50,20 @@ __device__ __forceinline__ void st_release(int *p, int v) {
 // Bounded wait until *flag >= target.  Called by one thread; returns false on
 // timeout (after recording kDevTimeout in *err) or when another CTA already
 // failed.  Never spins forever.
-__device__ __forceinline__ bool wait_geq(const int *flag, int target, int *err) {
+__device__ __forceinline__ bool wait_geq_n(const int *flag, int target, int *err, long long limit) {
     long long it = 0;
     while (ld_acquire(flag) < target) {
         if (ld_acquire(err) != kDevOk) return false;
-        if (++it > kSpinLimit) {
+        if (++it > limit) {
             atomicCAS(err, kDevOk, kDevTimeout);
             return false;
         }
         __nanosleep(64);
     }
     return true;
+}
+__device__ __forceinline__ bool wait_geq(const int *flag, int target, int *err) {
+    return wait_geq_n(flag, target, err, kSpinLimit);
 }
 
 template <typename T>

@@ -255,6 +255,12 @@ int avs_bidiag_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, con
  * returns it in *best (may be NULL).  sample <= 0 means 16. */
 int avs_autotune_tile(avs_handle *h, int64_t n, int32_t sample, int32_t *best);
 
+/* Failure-path check: a kernel waits, with a short bound (about 0.3 s), on a
+ * flag that nothing sets -- the bounded wait that every cross-CTA dependency
+ * of the library uses.  Returns AVS_ERR_TIMEOUT, and the handle and the CUDA
+ * context stay usable. */
+int avs_selftest_timeout(avs_handle *h);
+
 /* Release the handle's cached device workspace, pinned tables and captured
  * graphs (the handle stays usable; the next call allocates again). */
 int avs_trim(avs_handle *h);

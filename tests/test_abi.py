@@ -118,3 +118,8 @@ def test_ooc_plan_host_logic(avs_mod):
     assert lib.avs_ooc_plan(1024, 64, 4, 0, None, None, None) == -4
     assert lib.avs_ooc_plan(1024, 64, 2, 1 << 20, None, None, None) == -3
     assert lib.avs_blockbidiag_ooc_s(None, 64, 64, 16, None, 0, None) == -1
+
+
+def test_selftest_timeout_argument_check(avs_mod):
+    assert avs_mod.lib().avs_selftest_timeout(None) == -1
+    assert b"CUDA runtime error" in avs_mod.lib().avs_strerror(1)
