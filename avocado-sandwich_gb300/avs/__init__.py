@@ -45,13 +45,14 @@ PREC = {"default": 0, "fp64": 1, "fp32": 2, "tf32": 3, "tf32x3": 4, "bf16": 5, "
 EXPORTED_SYMBOLS = [
     "avs_create", "avs_destroy", "avs_reserve", "avs_strerror", "avs_version",
     "avs_svdvals_s", "avs_svdvals_d", "avs_svdvals_dev_s", "avs_svdvals_dev_d",
-    "avs_blockbidiag_dev_s", "avs_blockbidiag_dev_d", "avs_extract_band_dev_s", "avs_extract_band_dev_d",
+    "avs_blockbidiag_dev_s", "avs_blockbidiag_dev_d", "avs_blockbidiag_tau_dev_s", "avs_blockbidiag_tau_dev_d",
+    "avs_extract_band_dev_s", "avs_extract_band_dev_d",
     "avs_band_to_bidiag_dev", "avs_bidiag_svals_dev", "avs_bidiag_svals_noalloc",
     "avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d", "avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d",
     "avs_svdvals_batched_dev_s", "avs_bidiag_batched_dev_s", "avs_autotune_tile", "avs_trim", "avs_workspace_bytes", "avs_estimate_bytes",
     "avs_geqrf_dev_s", "avs_geqrf_dev_d",
     "avs_blockbidiag_ooc_s", "avs_blockbidiag_ooc_d", "avs_svdvals_ooc_s", "avs_svdvals_ooc_d",
-    "avs_geqrf_ooc_s", "avs_geqrf_ooc_d", "avs_ooc_plan", "avs_selftest_timeout",
+    "avs_geqrf_ooc_s", "avs_geqrf_ooc_d", "avs_ooc_plan", "avs_selftest_timeout", "avs_kernel_arch",
     "avs_serve_create", "avs_serve_submit", "avs_serve_wait", "avs_serve_stats_get", "avs_serve_destroy",
 ]
 
@@ -118,6 +119,8 @@ def lib():
             getattr(L, nm).argtypes = [P, I64, I64, I64, I32, P, P, OP, RP]
         for nm in ("avs_blockbidiag_dev_s", "avs_blockbidiag_dev_d"):
             getattr(L, nm).argtypes = [P, I64, I64, I32, P, OP, RP]
+        for nm in ("avs_blockbidiag_tau_dev_s", "avs_blockbidiag_tau_dev_d"):
+            getattr(L, nm).argtypes = [P, I64, I64, I32, P, P, P, OP, RP]
         for nm in ("avs_extract_band_dev_s", "avs_extract_band_dev_d"):
             getattr(L, nm).argtypes = [P, I64, I64, I32, P, P, I64]
         L.avs_band_to_bidiag_dev.argtypes = [P, I64, I32, P, I64, P, P, RP]
@@ -138,6 +141,7 @@ def lib():
                                    ctypes.POINTER(I32)]
         L.avs_trim.argtypes = [P]
         L.avs_selftest_timeout.argtypes = [P]
+        L.avs_kernel_arch.argtypes = [I, ctypes.POINTER(I32), ctypes.POINTER(I32)]
         L.avs_workspace_bytes.argtypes = [P, ctypes.POINTER(I64), ctypes.POINTER(I64)]
         L.avs_estimate_bytes.argtypes = [I64, I32, I32, I32, ctypes.POINTER(I64)]
         L.avs_serve_create.argtypes = [ctypes.POINTER(P), ctypes.POINTER(ServeConfig)]
@@ -229,10 +233,13 @@ def my_CU_svdval(A, block_size, precision=None, report=None, handle=None, rel_to
     ``A`` is a numpy array (the ``Matrix{Float32}`` method, host copies inside
     the call) or a CUDA torch tensor holding the matrix column-major (the
     ``CuMatrix{Float32}`` method, result returned as a CUDA tensor).  float32
-    and float64 are supported; the input is never modified.
+    and float64 are supported; the input is never modified.  ``stages``
+    selects the arithmetic of the bulge chase and the bisection: "auto" (FP64
+    for the plain FP64 mode, double-float for the FP32-class modes), "fp64" or
+    "df64" (AVS_FLAG_FP64_STAGES / AVS_FLAG_DF64_STAGES).
     """
     h = handle or default_handle()
-    o = Opts(_prec(precision), 0, float(rel_tol), None)
+    o = Opts(_prec(precision), STAGES[stages], float(rel_tol), None)
     r = report if report is not None else Report()
     if _is_torch_cuda(A):
         import torch
@@ -370,6 +377,14 @@ def selftest_timeout(handle=None):
     return lib().avs_selftest_timeout(h.ptr)
 
 
+def kernel_arch(device=0):
+    """(binaryVersion, ptxVersion) of the library's device code as loaded on
+    ``device`` (103 = sm_103a)."""
+    bv, pv = ctypes.c_int32(0), ctypes.c_int32(0)
+    _check(lib().avs_kernel_arch(int(device), ctypes.byref(bv), ctypes.byref(pv)), "avs_kernel_arch")
+    return bv.value, pv.value
+
+
 def autotune_tile(n, sample=16, handle=None):
     """Tile the batched path uses for order n (timed on the device, cached on the handle)."""
     h = handle or default_handle()
@@ -412,6 +427,30 @@ def Blockbidiag(A, tile, handle=None):
     rc = fn(h.ptr, n, n, int(tile), ctypes.c_void_p(A.data_ptr()), None, ctypes.byref(r))
     _check(rc, "avs_blockbidiag_dev")
     return r
+
+
+def Blockbidiag_tau(A, tile, precision=None, handle=None, report=None):
+    """Blockbidiag! in place on a CUDA tensor holding a column-major n x n
+    matrix, keeping the tau of every reflector: returns (tau_q, tau_p), CUDA
+    tensors of nt * nt * tile elements laid out as avs_blockbidiag_tau_dev
+    documents (QR half-step k, tile row r at (k * nt + r) * tile; LQ half-step
+    k, tile column c at (k * nt + c) * tile).  With the Householder vectors left
+    in A they give Q and P of A = Q B P^T."""
+    import torch
+    h = handle or default_handle()
+    if A.dim() != 2 or A.shape[0] != A.shape[1]:
+        raise NotImplementedError("Not implemented")
+    n = A.shape[0]
+    nt = n // tile if tile > 0 else 0
+    tq = torch.zeros(max(nt * nt * max(tile, 1), 1), dtype=A.dtype, device=A.device)
+    tp = torch.zeros_like(tq)
+    o = Opts(_prec(precision), 0, 0.0, ctypes.c_void_p(torch.cuda.current_stream(A.device).cuda_stream))
+    r = report if report is not None else Report()
+    fn = lib().avs_blockbidiag_tau_dev_d if A.dtype == torch.float64 else lib().avs_blockbidiag_tau_dev_s
+    rc = fn(h.ptr, n, max(A.stride(0), 1), int(tile), ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(tq.data_ptr()),
+            ctypes.c_void_p(tp.data_ptr()), ctypes.byref(o), ctypes.byref(r))
+    _check(rc, "avs_blockbidiag_tau_dev")
+    return tq, tp
 
 
 def _ooc_matrix(A):

@@ -512,17 +512,27 @@ int avs_svdvals_dev_d(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t 
 }  // extern "C"
 
 namespace {
+// Blockbidiag! in place.  with_prec: opts->precision selects the update
+// arithmetic of FP32 tiles (tensor-core modes included), as in avs_svdvals;
+// otherwise the input type's SIMT update runs.  dtq / dtp (may be NULL)
+// receive the tau of the QR / LQ half-steps.
 template <typename T>
 int blockbidiag_dev(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *dA, const avs_opts *opts,
-                    avs_report *rep) {
+                    avs_report *rep, T *dtq = nullptr, T *dtp = nullptr, bool with_prec = false) {
     int rc = check_common(h, n, n, lda, tile, dA, dA);
     if (rep) {
         std::memset(rep, 0, sizeof(*rep));
         rep->status = rc;
     }
     if (rc != AVS_SUCCESS || n == 0) return rc;
+    int prec = sizeof(T) == 8 ? AVS_PREC_FP64 : AVS_PREC_FP32;
+    if (with_prec) {
+        prec = resolve_precision(opts ? opts->precision : 0, sizeof(T) == 8);
+        if (storage_elem(prec) != sizeof(T)) return AVS_ERR_UNSUPPORTED;  // tiles are the input type
+    }
     AVS_CUDA_TRY(cudaSetDevice(h->device));
-    const Layout L = make_layout(n, tile, sizeof(T), 0);
+    const int split = sizeof(T) == 4 ? tc_split_of(prec, tile) : 0;
+    const Layout L = make_layout(n, tile, sizeof(T), 0, split);
     if ((rc = ensure_ws(h, L.total)) != AVS_SUCCESS) return rc;
     cudaStream_t s = (opts && opts->stream) ? reinterpret_cast<cudaStream_t>(opts->stream) : h->stream;
     int *err = reinterpret_cast<int *>(ws_at(h, L.off_err));
@@ -533,6 +543,10 @@ int blockbidiag_dev(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *dA, 
     w1.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags1));
     w1.err = err;
     w1.tfull = ws_at(h, L.off_tfull);
+    w1.tc_split = split;
+    w1.tc_ws = split ? ws_at(h, L.off_tc) : nullptr;
+    w1.tau_q_out = dtq;
+    w1.tau_p_out = dtp;
     int64_t launches = 0;
     AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
     // the stage-1 kernels move 16-byte vectors: a matrix that is not 16-byte
@@ -554,7 +568,7 @@ int blockbidiag_dev(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *dA, 
     if (rep) {
         rep->t_stage1_ms = rep->t_total_ms = ev_ms(h->ev[0], h->ev[1]);
         rep->kernel_launches = launches;
-        rep->precision = sizeof(T) == 8 ? AVS_PREC_FP64 : AVS_PREC_FP32;
+        rep->precision = prec;
         rep->status = rc;
     }
     return rc;
@@ -835,6 +849,15 @@ int avs_blockbidiag_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, f
 int avs_blockbidiag_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *dA, const avs_opts *opts,
                           avs_report *report) {
     return blockbidiag_dev<double>(h, n, lda, tile, dA, opts, report);
+}
+
+int avs_blockbidiag_tau_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *dA, float *dtau_q,
+                              float *dtau_p, const avs_opts *opts, avs_report *report) {
+    return blockbidiag_dev<float>(h, n, lda, tile, dA, opts, report, dtau_q, dtau_p, true);
+}
+int avs_blockbidiag_tau_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *dA, double *dtau_q,
+                              double *dtau_p, const avs_opts *opts, avs_report *report) {
+    return blockbidiag_dev<double>(h, n, lda, tile, dA, opts, report, dtau_q, dtau_p, true);
 }
 int avs_geqrf_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *dA, float *dtau,
                     const avs_opts *opts, avs_report *report) {
@@ -1344,6 +1367,23 @@ extern "C" int avs_selftest_timeout(avs_handle *h) {
     AVS_CUDA_TRY(cudaGetLastError());
     AVS_CUDA_TRY(cudaMemcpyAsync(h->h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     return finish_status(h, s);
+}
+
+// Architecture the library's kernels were built for, read back from the loaded
+// image by the runtime (binaryVersion 103 = sm_103).
+extern "C" int avs_kernel_arch(int device, int32_t *binary_version, int32_t *ptx_version) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        return AVS_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) return -1;
+    AVS_CUDA_TRY(cudaSetDevice(device));
+    cudaFuncAttributes fa{};
+    AVS_CUDA_TRY(cudaFuncGetAttributes(&fa, timeout_probe_kernel));
+    if (binary_version) *binary_version = fa.binaryVersion;
+    if (ptx_version) *ptx_version = fa.ptxVersion;
+    return AVS_SUCCESS;
 }
 
 // ===========================================================================

@@ -17,9 +17,10 @@ enum DeviceError : int {
 };
 
 // Upper bound on the spin iterations of any dependency wait.  Each iteration
-// sleeps ~100-200 ns (__nanosleep), so the bound is on the order of tens of
-// seconds -- far beyond any legitimate wait, short enough that a lost
-// dependency returns AVS_ERR_TIMEOUT instead of hanging the GPU.
+// makes two acquire loads and sleeps 64 ns (__nanosleep(64)), so the bound is at
+// least 2^27 x 64 ns = 8.6 s, more with the loads' latency -- far beyond any
+// legitimate wait, short enough that a lost dependency returns AVS_ERR_TIMEOUT
+// instead of hanging the GPU.
 constexpr long long kSpinLimit = 1ll << 27;
 
 // Column-major view of a matrix, optionally transposed: element (i, j) of the
@@ -101,6 +102,10 @@ struct Stage1Work {
     cudaEvent_t *ev_pairs = nullptr;
     int ev_cap = 0;
     int *ev_used = nullptr;
+    // optional (one matrix): the tau of every half-step, copied out after its
+    // panel -- QR half-step k, tile row r >= k at tau_q_out[(k * nt + r) * b + l];
+    // LQ half-step k, tile column c >= k + 1 at tau_p_out[(k * nt + c) * b + l]
+    void *tau_q_out = nullptr, *tau_p_out = nullptr;
     // batched mode: `batch` matrices at dA + z*sA, each with its own tau / T
     // blocks / full T / flag block at the given strides (elements, ints)
     int batch = 1;

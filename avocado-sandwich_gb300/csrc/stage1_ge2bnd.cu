@@ -843,6 +843,16 @@ int launch_update(T *dA, int64_t lda, int64_t n, int b, int pr, int pc, int P, c
     return AVS_SUCCESS;
 }
 
+// The tau of the panel just launched (roles 0..P-1 of half-step k, tile index
+// first + p) to the caller's array, when it asked for them.
+template <typename T>
+int copy_tau_out(void *out, const Stage1Work &w, int nt, int k, int first, int P, int b, cudaStream_t s) {
+    if (!out) return AVS_SUCCESS;
+    AVS_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<T *>(out) + ((size_t)k * nt + first) * b, w.tau,
+                                 sizeof(T) * (size_t)P * b, cudaMemcpyDeviceToDevice, s));
+    return AVS_SUCCESS;
+}
+
 }  // namespace
 
 // Tensor-core trailing update of one half-step, bracketed by a pair of the
@@ -874,6 +884,7 @@ int stage1_ge2bnd_tc(float *X, int64_t n, int b, const Stage1Work &w, cudaStream
         const int64_t kb = (int64_t)k * b, k1b = (int64_t)(k + 1) * b;
         const int P = nt - k;
         if ((rc = launch_panel<float, 0>(X, n, b, k, k, P, 0, w, s)) != AVS_SUCCESS) return rc;
+        if ((rc = copy_tau_out<float>(w.tau_q_out, w, nt, k, k, P, b, s)) != AVS_SUCCESS) return rc;
         if (launches) *launches += 1;
         if (k == nt - 1) break;  // no trailing columns left
         if ((rc = stage1_tbuild<float>(X, n, b, 0, k, k, P, w, s)) != AVS_SUCCESS) return rc;
@@ -883,6 +894,7 @@ int stage1_ge2bnd_tc(float *X, int64_t n, int b, const Stage1Work &w, cudaStream
         if ((rc = stage1_tc_transpose(X, XT, n, kb, k1b, fmt, tb, s)) != AVS_SUCCESS) return rc;
         const int PL = nt - k - 1;
         if ((rc = launch_panel<float, 0>(XT, n, b, k + 1, k, PL, 0, w, s)) != AVS_SUCCESS) return rc;
+        if ((rc = copy_tau_out<float>(w.tau_p_out, w, nt, k, k + 1, PL, b, s)) != AVS_SUCCESS) return rc;
         if ((rc = stage1_tbuild<float>(XT, n, b, 0, k + 1, k, PL, w, s)) != AVS_SUCCESS) return rc;
         if ((rc = timed_update(XT, n, b, k + 1, k, PL, w, tb, s, launches)) != AVS_SUCCESS) return rc;
         // and back: XT rows k1b.., columns kb.. -> X rows kb.., columns k1b..
@@ -904,6 +916,7 @@ int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cud
         // QR half-step: GEQRT(k,k) + TSQRT(row,k), Q^T applied to the row panels.
         const int P = nt - k;
         if ((rc = launch_panel<T, 0>(dA, lda, b, k, k, P, 0, w, s)) != AVS_SUCCESS) return rc;
+        if ((rc = copy_tau_out<T>(w.tau_q_out, w, nt, k, k, P, b, s)) != AVS_SUCCESS) return rc;
         if (b >= 128 && w.tfull)
             rc = stage1_update_full<T>(dA, lda, n, b, 0, k, k, P, w, s);
         else
@@ -914,6 +927,7 @@ int stage1_ge2bnd(T *dA, int64_t n, int64_t lda, int b, const Stage1Work &w, cud
         // LQ half-step: the same on the transposed view, top tile (k, k+1).
         const int PL = nt - k - 1;
         if ((rc = launch_panel<T, 1>(dA, lda, b, k + 1, k, PL, 0, w, s)) != AVS_SUCCESS) return rc;
+        if ((rc = copy_tau_out<T>(w.tau_p_out, w, nt, k, k + 1, PL, b, s)) != AVS_SUCCESS) return rc;
         if (b >= 128 && w.tfull)
             rc = stage1_update_full<T>(dA, lda, n, b, 1, k + 1, k, PL, w, s);
         else

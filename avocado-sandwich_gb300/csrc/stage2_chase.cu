@@ -421,14 +421,22 @@ __global__ void __launch_bounds__(ChaseCfg<BW, CC, NTT>::NT, ChaseCfg<BW, CC, NT
                         }
                     }
                 }
-                if (q == 0) {
-                    if (tid == 0) Ar::st(A.at(rho, c0), s_beta);
-                    for (int i = 1 + tid; i < L; i += blockDim.x) Ar::st(A.at(rho, c0 + i), Ar::zero());
-                }
             }
             __threadfence();
             cluster.sync();
-            if (q == 0 && tid == 0) st_release(done + j, 2 * m + 1);
+            // Every CTA of the cluster has read row rho for its reflector by
+            // now; only then does CTA 0 store beta and the annihilated zeros.
+            // Nothing later in this sweep reads row rho, and sweep j+1 sees the
+            // stores through the release below.
+            if (q == 0) {
+                if (L >= 2) {
+                    if (tid == 0) Ar::st(A.at(rho, c0), s_beta);
+                    for (int i = 1 + tid; i < L; i += blockDim.x) Ar::st(A.at(rho, c0 + i), Ar::zero());
+                    __threadfence();
+                }
+                __syncthreads();
+                if (tid == 0) st_release(done + j, 2 * m + 1);
+            }
             // ================= L op (op 2m+1) =================
             // Column c0 (rows c0..c1) is final after this sweep's R op and op
             // 2m+1 of sweep j-1 (covered by the R op's wait): reflector first.
@@ -472,14 +480,21 @@ __global__ void __launch_bounds__(ChaseCfg<BW, CC, NTT>::NT, ChaseCfg<BW, CC, NT
                         }
                     }
                 }
-                if (q == 0) {
-                    if (tid == 0) Ar::st(A.at(c0, c0), s_beta);
-                    for (int i = 1 + tid; i < L; i += blockDim.x) Ar::st(A.at(c0 + i, c0), Ar::zero());
-                }
             }
             __threadfence();
             cluster.sync();
-            if (q == 0 && tid == 0) st_release(done + j, 2 * m + 2);
+            // As in the R op: column c0 is overwritten only after every CTA has
+            // read it.  The next R op reads row c0 from column c0 + bw on and
+            // applies to columns >= c0 + bw, so it never meets these stores.
+            if (q == 0) {
+                if (L >= 2) {
+                    if (tid == 0) Ar::st(A.at(c0, c0), s_beta);
+                    for (int i = 1 + tid; i < L; i += blockDim.x) Ar::st(A.at(c0 + i, c0), Ar::zero());
+                    __threadfence();
+                }
+                __syncthreads();
+                if (tid == 0) st_release(done + j, 2 * m + 2);
+            }
             rho = c0;
             c0 += BW;
         }

@@ -140,6 +140,28 @@ int avs_blockbidiag_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, f
                           avs_report *report);
 int avs_blockbidiag_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *dA, const avs_opts *opts,
                           avs_report *report);
+/* Blockbidiag! with its reflectors kept: the band reduction above, plus the tau
+ * of every Householder reflector, so that Q and P of A = Q B P^T can be rebuilt
+ * from the vectors left in dA (the orthogonality / backward-error check of the
+ * band reduction).  The reference keeps tau in the TiledMatrix's nt x nt Tau
+ * grid (KAbasedSVD/src/TiledMatrix.jl:53-58; slots Tau[k,k] and Tau[row,k] of
+ * the QR half-step, Tau[k,k] and Tau[col,k] of the LQ half-step,
+ * TiledMatrix.jl:92-113), where the LQ half-step overwrites the QR one; here
+ * both are kept.  nt = n / tile; each array holds nt * nt * tile elements and
+ * may be NULL:
+ *   dtau_q[(k*nt + r)*tile + l]  QR half-step k, tile row r >= k, reflector l:
+ *       r == k: GEQRT of tile (k,k), v = unit lower column l of tile (k,k);
+ *       r >  k: TSQRT of [R_kk; A_rk], v = e_l on top, column l of tile (r,k) below;
+ *   dtau_p[(k*nt + c)*tile + l]  LQ half-step k, tile column c >= k+1, reflector l
+ *       (right reflectors, stored as rows): c == k+1: GELQT of tile (k,k+1), v =
+ *       unit upper row l of that tile; c > k+1: TSLQT, v = e_l on the left
+ *       (tile column k+1), row l of tile (k,c) on the right.
+ * opts->precision selects the update arithmetic of the _s form (FP32 SIMT or a
+ * tensor-core mode), as for avs_svdvals; the tiles keep the input's type. */
+int avs_blockbidiag_tau_dev_s(avs_handle *h, int64_t n, int64_t lda, int32_t tile, float *dA, float *dtau_q,
+                              float *dtau_p, const avs_opts *opts, avs_report *report);
+int avs_blockbidiag_tau_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t tile, double *dA, double *dtau_q,
+                              double *dtau_p, const avs_opts *opts, avs_report *report);
 /* tiled_QR! (KAbasedSVD/src/tiledalgos.jl:6-15) on a TiledMatrix in place: the QR
  * half-steps of Blockbidiag! alone (GEQRT of the diagonal tile, TSQRT down the
  * panel, compact-WY updates of the trailing tiles).  On return R is in the upper
@@ -212,11 +234,12 @@ int avs_bidiag_svals_dev(avs_handle *h, int64_t n, const double *dd, const doubl
  * (Julia's CUDA.jl, PyTorch's caching allocator), or a latency-critical loop
  * that must not pay cudaMalloc's implicit synchronisation.  Needs no handle;
  * runs on the current device and on `stream` (a cudaStream_t, NULL = legacy
- * default stream) and returns when the values are in dsigma.  Its scratch is a
- * static device array in the library (~512 KiB per GPU, held until exit), so
- * n <= 65536; larger n returns AVS_ERR_TOO_LARGE.  The first call on a device
- * looks the array's address up (call it once before any stream capture).
- * Calls share the array: calls that overlap on the GPU race on it. */
+ * default stream), and synchronises that stream before it returns, so the
+ * values are in dsigma on return.  Its scratch is a static device array in the
+ * library (~512 KiB per GPU, held until exit), so n <= 65536; larger n returns
+ * AVS_ERR_TOO_LARGE.  The first call on a device looks the array's address up:
+ * make that first call before any stream capture begins.  Calls share the
+ * array: calls that overlap on the GPU race on it. */
 int avs_bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *dsigma, double rel_tol,
                              void *stream);
 
@@ -260,6 +283,11 @@ int avs_autotune_tile(avs_handle *h, int64_t n, int32_t sample, int32_t *best);
  * of the library uses.  Returns AVS_ERR_TIMEOUT, and the handle and the CUDA
  * context stay usable. */
 int avs_selftest_timeout(avs_handle *h);
+
+/* Diagnostics (no counterpart in the reference): the architecture of the
+ * device code the runtime loaded from this library on `device`
+ * (cudaFuncAttributes binaryVersion, 103 for sm_103a, and ptxVersion). */
+int avs_kernel_arch(int device, int32_t *binary_version, int32_t *ptx_version);
 
 /* Release the handle's cached device workspace, pinned tables and captured
  * graphs (the handle stays usable; the next call allocates again). */

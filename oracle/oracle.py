@@ -24,7 +24,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
 
 __all__ = [
-    "build", "lib", "geqrt", "tsqrt", "apply1", "apply2", "blockbidiag", "bidiagonalize",
+    "build", "lib", "geqrt", "tsqrt", "apply1", "apply2", "blockbidiag", "blockbidiag_keep", "bidiagonalize",
     "bidiag_svals", "svdvals", "set_threads", "num_threads", "extract_bidiag", "extract_band",
 ]
 
@@ -50,6 +50,7 @@ def lib():
             getattr(L, "oracle_apply1" + suf).argtypes = [P, I64, I64, P, I64, P, I, I]
             getattr(L, "oracle_apply2" + suf).argtypes = [P, I64, P, I64, I64, P, I64, P, I, I]
             getattr(L, "oracle_blockbidiag" + suf).argtypes = [P, I64, I64, I]
+            getattr(L, "oracle_blockbidiag_keep" + suf).argtypes = [P, I64, I64, I, P, P]
             getattr(L, "oracle_bidiagonalize" + suf).argtypes = [P, I64, I64, I64]
             getattr(L, "oracle_svdvals" + suf).argtypes = [P, I64, I64, I, P, ctypes.c_double]
             getattr(L, "oracle_svdvals" + suf).restype = I
@@ -132,6 +133,20 @@ def blockbidiag(a, b):
     n = a.shape[0]
     getattr(lib(), "oracle_blockbidiag" + _suf(a))(_ptr(a), n, n, int(b))
     return a
+
+
+def blockbidiag_keep(a, b):
+    """Blockbidiag! on a copy of a, keeping the Householder vectors in the
+    tiles and every tau -> (matrix, tau_q, tau_p), tau layout of
+    avs_blockbidiag_tau_dev (QR half-step k, tile row r at (k*nt + r)*b; LQ
+    half-step k, tile column c at (k*nt + c)*b).  The band equals blockbidiag's."""
+    a = _fortran(a)
+    n = a.shape[0]
+    nt = n // int(b)
+    tq = np.zeros(max(nt * nt * int(b), 1), dtype=a.dtype)
+    tp = np.zeros_like(tq)
+    getattr(lib(), "oracle_blockbidiag_keep" + _suf(a))(_ptr(a), n, n, int(b), _ptr(tq), _ptr(tp))
+    return a, tq, tp
 
 
 def bidiagonalize(a, bw):

@@ -202,46 +202,75 @@ void OSUF(oracle_apply2)(OT *am, int64_t lda, OT *bm, int64_t ldb, int64_t ncols
 
 /*
  * GE2BND: Blockbidiag! (tiledalgos.jl:17-59) over the tile views of
- * TiledMatrix.jl:77-113.  On return a (n x n, column-major, lda) holds the
- * upper band 0 <= j - i <= b with exact zeros elsewhere (triu!/tril!/.= 0).
+ * TiledMatrix.jl:77-113.  keep == 0: on return a (n x n, column-major, lda)
+ * holds the upper band 0 <= j - i <= b with exact zeros elsewhere
+ * (triu!/tril!/.= 0), as in the reference.  keep != 0: the Householder vectors
+ * stay where the factorisations leave them (nothing later reads those
+ * entries, so the band is the same), and the tau of every tile factorisation
+ * go to tq / tp (nt * nt * b each; QR half-step k, tile row r at (k*nt + r)*b;
+ * LQ half-step k, tile column c at (k*nt + c)*b), where the reference's Tau
+ * grid keeps only the last one written to each slot.
  */
-void OSUF(oracle_blockbidiag)(OT *a, int64_t n, int64_t lda, int b) {
+static void OSUF(blockbidiag_impl)(OT *a, int64_t n, int64_t lda, int b, int keep, OT *tq, OT *tp) {
     int64_t nt = n / b;
     OSUF(oview) A = OSUF(ov_cm)(a, lda);
     OT *tau = (OT *)calloc((size_t)b, sizeof(OT));
 #define TILE(r, c) OSUF(ov_sub)(A, (int64_t)(r) * b, (int64_t)(c) * b)
+#define KEEP_TAU(dst, k, t)                                                            \
+    do {                                                                               \
+        if (keep) memcpy((dst) + ((size_t)(k) * nt + (t)) * b, tau, sizeof(OT) * b); \
+    } while (0)
     for (int64_t k = 0; k < nt; ++k) {
         /* QRandmulQt1!: QR1!, Qtapply1_par!, triu! */
+        memset(tau, 0, sizeof(OT) * b);
         OSUF(oracle_geqrt_v)(TILE(k, k), b, tau);
+        KEEP_TAU(tq, k, k);
         OSUF(oracle_apply1_v)(TILE(k, k + 1), (nt - k - 1) * b, TILE(k, k), tau, b, 1);
-        for (int i = 0; i < b; ++i)
-            for (int t = i + 1; t < b; ++t) *OSUF(oel)(TILE(k, k), t, i) = 0;
+        if (!keep)
+            for (int i = 0; i < b; ++i)
+                for (int t = i + 1; t < b; ++t) *OSUF(oel)(TILE(k, k), t, i) = 0;
         /* QRandmulQt2!: QR2!, Qtapply2_par!, tile .= 0 */
         for (int64_t row = k + 1; row < nt; ++row) {
             OSUF(oracle_tsqrt_v)(TILE(k, k), TILE(row, k), b, tau);
+            KEEP_TAU(tq, k, row);
             OSUF(oracle_apply2_v)(TILE(k, k + 1), TILE(row, k + 1), (nt - k - 1) * b, TILE(row, k), tau, b, 1);
-            for (int j = 0; j < b; ++j)
-                for (int t = 0; t < b; ++t) *OSUF(oel)(TILE(row, k), t, j) = 0;
+            if (!keep)
+                for (int j = 0; j < b; ++j)
+                    for (int t = 0; t < b; ++t) *OSUF(oel)(TILE(row, k), t, j) = 0;
         }
         if (k == nt - 1) break;
         /* LQandmulQt1!: LQ1! = QR1! on tile(k,k+1)', LQtapply1_par! on the
          * adjoint of the column panel below, tril! */
+        memset(tau, 0, sizeof(OT) * b);
         OSUF(oracle_geqrt_v)(OSUF(ov_adj)(TILE(k, k + 1)), b, tau);
+        KEEP_TAU(tp, k, k + 1);
         OSUF(oracle_apply1_v)(OSUF(ov_adj)(TILE(k + 1, k + 1)), (nt - k - 1) * b, OSUF(ov_adj)(TILE(k, k + 1)), tau,
                               b, 1);
-        for (int i = 0; i < b; ++i)
-            for (int t = i + 1; t < b; ++t) *OSUF(oel)(TILE(k, k + 1), i, t) = 0;
+        if (!keep)
+            for (int i = 0; i < b; ++i)
+                for (int t = i + 1; t < b; ++t) *OSUF(oel)(TILE(k, k + 1), i, t) = 0;
         /* LQandmulQt2!: LQ2! = QR2! on adjoints, LQtapply2_par!, tile .= 0 */
         for (int64_t col = k + 2; col < nt; ++col) {
             OSUF(oracle_tsqrt_v)(OSUF(ov_adj)(TILE(k, k + 1)), OSUF(ov_adj)(TILE(k, col)), b, tau);
+            KEEP_TAU(tp, k, col);
             OSUF(oracle_apply2_v)(OSUF(ov_adj)(TILE(k + 1, k + 1)), OSUF(ov_adj)(TILE(k + 1, col)),
                                   (nt - k - 1) * b, OSUF(ov_adj)(TILE(k, col)), tau, b, 1);
-            for (int j = 0; j < b; ++j)
-                for (int t = 0; t < b; ++t) *OSUF(oel)(TILE(k, col), t, j) = 0;
+            if (!keep)
+                for (int j = 0; j < b; ++j)
+                    for (int t = 0; t < b; ++t) *OSUF(oel)(TILE(k, col), t, j) = 0;
         }
     }
+#undef KEEP_TAU
 #undef TILE
     free(tau);
+}
+
+void OSUF(oracle_blockbidiag)(OT *a, int64_t n, int64_t lda, int b) {
+    OSUF(blockbidiag_impl)(a, n, lda, b, 0, NULL, NULL);
+}
+
+void OSUF(oracle_blockbidiag_keep)(OT *a, int64_t n, int64_t lda, int b, OT *tq, OT *tp) {
+    OSUF(blockbidiag_impl)(a, n, lda, b, 1, tq, tp);
 }
 
 /*

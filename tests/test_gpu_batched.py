@@ -144,3 +144,21 @@ def test_batched_edge_cases(avs_mod, torch_cuda):
     z = torch_cuda.zeros((64, 64), device="cuda", dtype=torch_cuda.float32)
     out = avs_mod.svdvals_batched([z], tiles=16)[0]
     assert torch_cuda.count_nonzero(out).item() == 0
+
+
+@pytest.mark.parametrize("tile,count", [(32, 8), (32, 140), (32, 160), (64, 8), (64, 290), (64, 320)])
+def test_batched_chase_branches_repeat(avs_mod, torch_cuda, tile, count):
+    """Order 256 at bands 32 and 64 with batch sizes on both sides of the
+    threshold at which the batched chase switches to small CTAs (batch x
+    (n / bw) / 2 >= 4 x SMs): both branches, called three times, give every
+    matrix the single call's values bit for bit."""
+    hosts, devs = _mats(avs_mod, [256] * 4, 1200 + tile + count)
+    singles = [avs_mod.my_CU_svdval(d, tile).cpu().numpy() for d in devs]
+    for rep in range(3):
+        mats = [devs[i % 4].clone() for i in range(count)]
+        outs = avs_mod.svdvals_batched(mats, tiles=tile)
+        for i, o in enumerate(outs):
+            got = o.cpu().numpy()
+            assert np.array_equal(got, singles[i % 4]), (rep, i, rel_err(got, singles[i % 4]))
+    for a, s in zip(hosts, singles):
+        assert rel_err(s, sl.svdvals(a.astype(np.float64))) < TOL32

@@ -29,3 +29,13 @@ def test_bounded_wait_times_out_and_context_survives(avs_mod, torch_cuda):
         assert avs_mod.selftest_timeout(handle=h) == 3
     finally:
         h.close()
+
+
+def test_loaded_device_code_is_sm103(avs_mod):
+    """The runtime reports the library's device code as built for sm_103
+    (cudaFuncAttributes.binaryVersion)."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    bv, pv = avs_mod.kernel_arch(0)
+    assert bv == 103, (bv, pv)

@@ -253,3 +253,20 @@ def test_brd_short_propagation_range():
     full = np.linalg.svd(brd.bidiag(a, 4, iters=4 * 64), compute_uv=False)
     assert np.max(np.abs(short - ref)) > 1e-6 * ref[0]
     assert np.max(np.abs(full - ref)) < 1e-12 * ref[0]
+
+
+@pytest.mark.parametrize("dt", [np.float64, np.float32])
+@pytest.mark.parametrize("n,b", [(64, 16), (128, 32), (256, 64)])
+def test_blockbidiag_reflectors_rebuild_q_p(oracle_mod, dt, n, b):
+    """The Householder vectors and tau that the tile factorisations leave
+    (QRkernels.jl:3-129 on the Blockbidiag! schedule, tiledalgos.jl:17-59)
+    rebuild Q and P with A = Q B P^T: backward error and loss of
+    orthogonality within n * eps of the element type.  Keeping the vectors
+    does not change the band."""
+    from oracle import reflectors
+    a = np.random.default_rng(n + b).standard_normal((n, n)).astype(dt)
+    out, tq, tp = oracle_mod.blockbidiag_keep(a, b)
+    assert np.array_equal(oracle_mod.extract_band(out, b), oracle_mod.extract_band(oracle_mod.blockbidiag(a, b), b))
+    back, oq, op = reflectors.checks(a, out, tq, tp, b)
+    eps = np.finfo(dt).eps
+    assert back < n * eps and oq < n * eps and op < n * eps, (back, oq, op)
