@@ -49,10 +49,11 @@ EXPORTED_SYMBOLS = [
     "avs_extract_band_dev_s", "avs_extract_band_dev_d",
     "avs_band_to_bidiag_dev", "avs_bidiag_svals_dev", "avs_bidiag_svals_noalloc",
     "avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d", "avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d",
-    "avs_svdvals_batched_dev_s", "avs_bidiag_batched_dev_s", "avs_autotune_tile", "avs_trim", "avs_workspace_bytes", "avs_estimate_bytes",
+    "avs_svdvals_batched_dev_s", "avs_bidiag_batched_dev_s", "avs_svdvals_batched_dev_d", "avs_bidiag_batched_dev_d", "avs_autotune_tile", "avs_trim", "avs_workspace_bytes", "avs_estimate_bytes",
     "avs_geqrf_dev_s", "avs_geqrf_dev_d",
     "avs_blockbidiag_ooc_s", "avs_blockbidiag_ooc_d", "avs_svdvals_ooc_s", "avs_svdvals_ooc_d",
     "avs_geqrf_ooc_s", "avs_geqrf_ooc_d", "avs_ooc_plan", "avs_selftest_timeout", "avs_kernel_arch",
+    "avs_measure_chase_rate",
     "avs_serve_create", "avs_serve_submit", "avs_serve_wait", "avs_serve_stats_get", "avs_serve_destroy",
 ]
 
@@ -126,8 +127,9 @@ def lib():
         L.avs_band_to_bidiag_dev.argtypes = [P, I64, I32, P, I64, P, P, RP]
         L.avs_bidiag_svals_dev.argtypes = [P, I64, P, P, P, ctypes.c_double, RP]
         L.avs_bidiag_svals_noalloc.argtypes = [I64, P, P, P, ctypes.c_double, P]
-        L.avs_svdvals_batched_dev_s.argtypes = [P, I32, P, P, P, P, P, OP, RP]
-        L.avs_bidiag_batched_dev_s.argtypes = [P, I32, P, P, P, P, P, P, OP, RP]
+        for sfx in ("s", "d"):
+            getattr(L, "avs_svdvals_batched_dev_" + sfx).argtypes = [P, I32, P, P, P, P, P, OP, RP]
+            getattr(L, "avs_bidiag_batched_dev_" + sfx).argtypes = [P, I32, P, P, P, P, P, P, OP, RP]
         L.avs_autotune_tile.argtypes = [P, I64, I32, ctypes.POINTER(ctypes.c_int32)]
         for nm in ("avs_geqrf_dev_s", "avs_geqrf_dev_d"):
             getattr(L, nm).argtypes = [P, I64, I64, I32, P, P, OP, RP]
@@ -142,6 +144,7 @@ def lib():
         L.avs_trim.argtypes = [P]
         L.avs_selftest_timeout.argtypes = [P]
         L.avs_kernel_arch.argtypes = [I, ctypes.POINTER(I32), ctypes.POINTER(I32)]
+        L.avs_measure_chase_rate.argtypes = [I, I32, ctypes.POINTER(ctypes.c_double)]
         L.avs_workspace_bytes.argtypes = [P, ctypes.POINTER(I64), ctypes.POINTER(I64)]
         L.avs_estimate_bytes.argtypes = [I64, I32, I32, I32, ctypes.POINTER(I64)]
         L.avs_serve_create.argtypes = [ctypes.POINTER(P), ctypes.POINTER(ServeConfig)]
@@ -278,14 +281,16 @@ svdvals = my_CU_svdval
 
 
 def svdvals_batched(mats, tiles=None, report=None, handle=None, rel_tol=0.0):
-    """Singular values of many independent square float32 matrices in one call.
+    """Singular values of many independent square matrices in one call.
 
-    ``mats`` is a list of CUDA torch tensors, each holding an n_i x n_i matrix
-    column-major (see ``to_device``); orders may differ.  ``tiles`` is None (the
-    autotuner picks a tile per order), an int for all, or a list.  Returns a
-    list of CUDA float32 tensors of n_i values each (descending).  This is the
-    batching client of the many-small-SVDs workload (RMT/rmt.jl:9-36), which the
-    reference serves one LAPACK call at a time.
+    ``mats`` is a list of CUDA torch tensors, all float32 or all float64, each
+    holding an n_i x n_i matrix column-major (see ``to_device``); orders may
+    differ.  ``tiles`` is None (the autotuner picks a tile per order), an int
+    for all, or a list.  Returns a list of CUDA tensors (the input dtype) of n_i
+    values each (descending).  This is the batching client of the
+    many-small-SVDs workload (RMT/rmt.jl:9-36), which the reference serves one
+    LAPACK call at a time.  float32: FP32 tiles, double-float stages 2-3;
+    float64: FP64 throughout.
     """
     import torch
     h = handle or default_handle()
@@ -301,9 +306,12 @@ def svdvals_batched(mats, tiles=None, report=None, handle=None, rel_tol=0.0):
     ps = (ctypes.c_void_p * cnt)()
     outs = []
     dev = None
+    dt = mats[0].dtype if _is_torch_cuda(mats[0]) else None
+    if dt not in (torch.float32, torch.float64):
+        raise TypeError("svdvals_batched takes 2-D float32 or float64 CUDA tensors")
     for i, A in enumerate(mats):
-        if not _is_torch_cuda(A) or A.dim() != 2 or A.dtype != torch.float32:
-            raise TypeError("svdvals_batched takes 2-D float32 CUDA tensors")
+        if not _is_torch_cuda(A) or A.dim() != 2 or A.dtype != dt:
+            raise TypeError("svdvals_batched takes 2-D CUDA tensors of one dtype (float32 or float64)")
         if A.shape[0] != A.shape[1]:
             raise NotImplementedError("Not implemented")
         if A.stride(1) != 1:
@@ -314,20 +322,21 @@ def svdvals_batched(mats, tiles=None, report=None, handle=None, rel_tol=0.0):
         ld[i] = max(A.stride(0), 1)
         tt[i] = 0 if tiles is None else int(tiles[i])
         pa[i] = A.data_ptr()
-        o = torch.empty(A.shape[0], dtype=torch.float32, device=A.device)
+        o = torch.empty(A.shape[0], dtype=dt, device=A.device)
         ps[i] = o.data_ptr()
         outs.append(o)
     opt = Opts(0, 0, float(rel_tol), ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
     r = report if report is not None else Report()
-    rc = lib().avs_svdvals_batched_dev_s(h.ptr, cnt, n, ld, None if tiles is None else tt, pa, ps,
-                                         ctypes.byref(opt), ctypes.byref(r))
-    _check(rc, "avs_svdvals_batched_dev_s")
+    fn = lib().avs_svdvals_batched_dev_d if dt == torch.float64 else lib().avs_svdvals_batched_dev_s
+    rc = fn(h.ptr, cnt, n, ld, None if tiles is None else tt, pa, ps, ctypes.byref(opt), ctypes.byref(r))
+    _check(rc, "avs_svdvals_batched_dev")
     return outs
 
 
 def bidiag_batched(mats, tiles=None, report=None, handle=None):
-    """The batched pipeline up to the bidiagonal: for each square float32 CUDA
-    matrix (column-major, see ``to_device``) the diagonal d and superdiagonal e
+    """The batched pipeline up to the bidiagonal: for each square CUDA matrix
+    (float32, or float64 computed in FP64 throughout; column-major, see
+    ``to_device``) the diagonal d and superdiagonal e
     (FP64 CUDA tensors of n values; e[n-1] = 0) of a bidiagonal B with
     A = U B V^T, V e1 = e1 -- unique up to signs, so |d| and |e| are those of
     LAPACK gebrd (the quantity RMT/rmt.jl:24-31 reads)."""
@@ -346,9 +355,12 @@ def bidiag_batched(mats, tiles=None, report=None, handle=None):
     pe = (ctypes.c_void_p * cnt)()
     outs = []
     dev = None
+    dt = mats[0].dtype if _is_torch_cuda(mats[0]) else None
+    if dt not in (torch.float32, torch.float64):
+        raise TypeError("bidiag_batched takes 2-D float32 or float64 CUDA tensors")
     for i, A in enumerate(mats):
-        if not _is_torch_cuda(A) or A.dim() != 2 or A.dtype != torch.float32:
-            raise TypeError("bidiag_batched takes 2-D float32 CUDA tensors")
+        if not _is_torch_cuda(A) or A.dim() != 2 or A.dtype != dt:
+            raise TypeError("bidiag_batched takes 2-D CUDA tensors of one dtype (float32 or float64)")
         if A.shape[0] != A.shape[1]:
             raise NotImplementedError("Not implemented")
         if A.stride(1) != 1:
@@ -365,9 +377,9 @@ def bidiag_batched(mats, tiles=None, report=None, handle=None):
         outs.append((d, e))
     opt = Opts(0, 0, 0.0, ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
     r = report if report is not None else Report()
-    rc = lib().avs_bidiag_batched_dev_s(h.ptr, cnt, n, ld, None if tiles is None else tt, pa, pd, pe,
-                                        ctypes.byref(opt), ctypes.byref(r))
-    _check(rc, "avs_bidiag_batched_dev_s")
+    fn = lib().avs_bidiag_batched_dev_d if dt == torch.float64 else lib().avs_bidiag_batched_dev_s
+    rc = fn(h.ptr, cnt, n, ld, None if tiles is None else tt, pa, pd, pe, ctypes.byref(opt), ctypes.byref(r))
+    _check(rc, "avs_bidiag_batched_dev")
     return outs
 
 
@@ -383,6 +395,13 @@ def kernel_arch(device=0):
     bv, pv = ctypes.c_int32(0), ctypes.c_int32(0)
     _check(lib().avs_kernel_arch(int(device), ctypes.byref(bv), ctypes.byref(pv)), "avs_kernel_arch")
     return bv.value, pv.value
+
+
+def chase_rate(device=0, fp64=False):
+    """Measured compute roof of the bulge chase (flops/s, 4 per element step)."""
+    r = ctypes.c_double(0.0)
+    _check(lib().avs_measure_chase_rate(int(device), 1 if fp64 else 0, ctypes.byref(r)), "avs_measure_chase_rate")
+    return r.value
 
 
 def autotune_tile(n, sample=16, handle=None):
@@ -596,8 +615,8 @@ class Server:
     ``submit(A)`` queues a host matrix (numpy float32 / float64, square) and
     returns a request id; ``wait(id)`` blocks until its values are ready and
     returns ``(sigma, latency_ms)``.  Several execution slots run groups
-    concurrently on the GPU; FP32 requests of the same order that are queued
-    together run as one batched call.  ``stats()`` gives p50/p99 latency,
+    concurrently on the GPU; requests of the same order and type that are
+    queued together run as one batched call.  ``stats()`` gives p50/p99 latency,
     throughput and the device memory held against the admission budget.
     """
 

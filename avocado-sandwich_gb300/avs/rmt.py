@@ -14,7 +14,9 @@ once, up to ``chunk`` matrices -- go through one batched call
 bidiagonal with V e1 = e1 is unique up to signs, so d_k^2 is gebrd's d_k^2.
 Orders that no tile of at least 16 divides are zero-padded to the next
 multiple of 16: the bidiagonal of [M 0; 0 0] is that of M followed by zeros.
-The matrices are FP32 (the batched path's type), the reference's FP64.
+``dtype`` selects the arithmetic: float64 (the reference's, LAPACK gebrd! in
+Float64, rmt.jl:23,28) runs the FP64 batched path throughout; float32 the FP32
+path (double-float stages).
 """
 import math
 
@@ -28,12 +30,12 @@ def padded_order(n, tile=16):
 
 
 def mou_process_covar(numtrials, matrixsize, numtimestep, timelength, kthsvdval, seed=0, tile=None,
-                      chunk=4096, noise=None, handle=None):
+                      chunk=4096, noise=None, handle=None, dtype="float64"):
     """generate_MOUprocess_covar (RMT/rmt.jl:9-36) on the GPU.
 
     Returns (mean of d_k^2 per time step, mean of the standardised products per
     time step, time grid), as the reference.  ``noise`` (optional) is a
-    (numtrials, numtimestep, n, n) float32 array of the symmetric G_i to use
+    (numtrials, numtimestep, n, n) array of the symmetric G_i to use
     instead of the seeded generator (for tests against the oracle)."""
     import torch
     n, nt, t, k = int(matrixsize), int(numtimestep), int(numtrials), int(kthsvdval)
@@ -46,14 +48,15 @@ def mou_process_covar(numtrials, matrixsize, numtimestep, timelength, kthsvdval,
         while tile > 16 and (npad % tile or npad // tile < 2):
             tile //= 2
     dev = torch.device("cuda", torch.cuda.current_device())
+    tdt = {"float64": torch.float64, "float32": torch.float32}[str(np.dtype(dtype))]
     gen = torch.Generator(device=dev).manual_seed(int(seed))
     h = handle or avs.default_handle()
 
     def draw(i):
         if noise is not None:
-            g = torch.as_tensor(np.asarray(noise[:, i], dtype=np.float32), device=dev)
+            g = torch.as_tensor(np.asarray(noise[:, i]), device=dev).to(tdt)
         else:
-            x = torch.randn((t, n, n), generator=gen, device=dev)
+            x = torch.randn((t, n, n), generator=gen, device=dev, dtype=tdt)
             g = x + x.transpose(1, 2)
         return g
 
@@ -74,7 +77,7 @@ def mou_process_covar(numtrials, matrixsize, numtimestep, timelength, kthsvdval,
     for i in range(nt):
         g = draw(i)
         m = g / math.sqrt(2.0) if i == 0 else m * (1.0 - dt) + g * math.sqrt(dt)
-        padded = torch.zeros((t, npad, npad), dtype=torch.float32, device=dev)
+        padded = torch.zeros((t, npad, npad), dtype=tdt, device=dev)
         padded[:, :n, :n] = m  # symmetric: row- and column-major views agree
         for j in range(t):
             pending.append(padded[j])

@@ -984,7 +984,9 @@ struct BatchLayout {
     size_t err, W, tau, tblk, tfull, f1, ab, f2, d, e, sig, scr, pairs, ptrs, total;
 };
 
-BatchLayout batch_layout(int64_t n, int b, int cnt) {
+// elem: bytes of the tile type (4: FP32 tiles and double-float stages 2-3;
+// 8: FP64 throughout).  The band takes 8 bytes per entry either way.
+BatchLayout batch_layout(int64_t n, int b, int cnt, size_t elem = 4) {
     BatchLayout L{};
     const int64_t nt = n / b;
     size_t o = 0;
@@ -994,10 +996,10 @@ BatchLayout batch_layout(int64_t n, int b, int cnt) {
         return at;
     };
     L.err = take(64);
-    L.W = take(sizeof(float) * (size_t)cnt * n * n);
-    L.tau = take(sizeof(float) * (size_t)cnt * (nt + 1) * b);
-    L.tblk = take(sizeof(float) * (size_t)cnt * (nt + 1) * (b / 16) * 256);
-    L.tfull = take(b >= 128 ? sizeof(float) * (size_t)cnt * (nt + 1) * b * b : 0);
+    L.W = take(elem * (size_t)cnt * n * n);
+    L.tau = take(elem * (size_t)cnt * (nt + 1) * b);
+    L.tblk = take(elem * (size_t)cnt * (nt + 1) * (b / 16) * 256);
+    L.tfull = take(b >= 128 ? elem * (size_t)cnt * (nt + 1) * b * b : 0);
     L.f1 = take(sizeof(int) * (size_t)cnt * (2 * nt + 4));
     L.ab = take(sizeof(float2) * (size_t)cnt * 3 * b * n);
     L.f2 = take(sizeof(int) * ((size_t)cnt * (n + 1) + 4));
@@ -1011,11 +1013,12 @@ BatchLayout batch_layout(int64_t n, int b, int cnt) {
     return L;
 }
 
-__global__ void gather_kernel(const float *const *src, const int64_t *lds, float *dst, int64_t n) {
+template <typename T>
+__global__ void gather_kernel(const T *const *src, const int64_t *lds, T *dst, int64_t n) {
     const int64_t zb = blockIdx.y;
-    const float *a = src[zb];
+    const T *a = src[zb];
     const int64_t ld = lds[zb];
-    float *w = dst + zb * n * n;
+    T *w = dst + zb * n * n;
     for (int64_t c = blockIdx.x; c < n; c += gridDim.x)
         for (int64_t r = threadIdx.x; r < n; r += blockDim.x) w[r + c * n] = a[r + c * ld];
 }
@@ -1029,10 +1032,11 @@ __global__ void scatter_de_kernel(const double *d, const double *e, double *cons
     }
 }
 
-__global__ void scatter_kernel(const double *sig, float *const *dst, int64_t n, int cnt) {
+template <typename T>
+__global__ void scatter_kernel(const double *sig, T *const *dst, int64_t n, int cnt) {
     const int64_t total = n * (int64_t)cnt;
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x)
-        dst[g / n][g % n] = (float)sig[g];
+        dst[g / n][g % n] = (T)sig[g];
 }
 
 int ensure_bws(avs_handle *h, size_t bytes) {
@@ -1063,19 +1067,21 @@ int ensure_pinned(avs_handle *h, size_t bytes) {
 }
 
 // The launches of one group (gather .. scatter), captured once per shape.
+// T = float: FP32 tiles, double-float stages 2-3; T = double: FP64 throughout.
+template <typename T>
 int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cnt, double tol, cudaStream_t s,
                    const cudaEvent_t *ev, int64_t *launches, bool bidiag) {
     char *base = reinterpret_cast<char *>(h->bws);
-    float *W = reinterpret_cast<float *>(base + L.W);
-    const float *const *src = reinterpret_cast<const float *const *>(base + L.ptrs);
-    float *const *dst = reinterpret_cast<float *const *>(base + L.ptrs + sizeof(void *) * cnt);
+    T *W = reinterpret_cast<T *>(base + L.W);
+    const T *const *src = reinterpret_cast<const T *const *>(base + L.ptrs);
+    T *const *dst = reinterpret_cast<T *const *>(base + L.ptrs + sizeof(void *) * cnt);
     const int64_t *lds = reinterpret_cast<const int64_t *>(base + L.ptrs + 2 * sizeof(void *) * cnt);
     double *const *dst_e = reinterpret_cast<double *const *>(base + L.ptrs + 3 * sizeof(void *) * cnt);
     int *err = reinterpret_cast<int *>(base + L.err);
     const int64_t nt = n / b;
     AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[0], s, cudaEventRecordExternal));
     AVS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
-    gather_kernel<<<dim3((unsigned)std::min<int64_t>(n, 1024), (unsigned)cnt), 256, 0, s>>>(src, lds, W, n);
+    gather_kernel<T><<<dim3((unsigned)std::min<int64_t>(n, 1024), (unsigned)cnt), 256, 0, s>>>(src, lds, W, n);
     AVS_CUDA_TRY(cudaGetLastError());
     Stage1Work w1;
     w1.tau = base + L.tau;
@@ -1089,7 +1095,7 @@ int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cn
     w1.sTblk = (nt + 1) * (b / 16) * 256;
     w1.sTfull = (nt + 1) * (int64_t)b * b;
     w1.sFlags = 2 * nt + 4;
-    int rc = stage1_ge2bnd<float>(W, n, n, b, w1, s, launches);
+    int rc = stage1_ge2bnd<T>(W, n, n, b, w1, s, launches);
     if (rc != AVS_SUCCESS) return rc;
     AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[1], s, cudaEventRecordExternal));
     Stage2Work w2;
@@ -1097,8 +1103,12 @@ int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cn
     w2.err = err;
     double *dd = reinterpret_cast<double *>(base + L.d);
     double *de = reinterpret_cast<double *>(base + L.e);
-    rc = stage2_chase_df_batched(W, n, b, cnt, reinterpret_cast<float2 *>(base + L.ab), 3 * (int64_t)b, dd, de, w2, s,
-                                 h->num_sms, launches);
+    if constexpr (sizeof(T) == 4)
+        rc = stage2_chase_df_batched(W, n, b, cnt, reinterpret_cast<float2 *>(base + L.ab), 3 * (int64_t)b, dd, de,
+                                     w2, s, h->num_sms, launches);
+    else
+        rc = stage2_chase_fp64_batched(W, n, b, cnt, reinterpret_cast<double *>(base + L.ab), 3 * (int64_t)b, dd, de,
+                                       w2, s, h->num_sms, launches);
     if (rc != AVS_SUCCESS) return rc;
     AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal));
     if (bidiag) {  // the bidiagonal itself: d and e of each matrix to the caller's vectors
@@ -1110,10 +1120,13 @@ int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cn
         return AVS_SUCCESS;
     }
     double *sig = reinterpret_cast<double *>(base + L.sig);
-    rc = stage3_bisect_df_batched(dd, de, n, cnt, tol, sig, reinterpret_cast<double *>(base + L.scr),
-                                  reinterpret_cast<float2 *>(base + L.pairs), s, launches);
+    if constexpr (sizeof(T) == 4)
+        rc = stage3_bisect_df_batched(dd, de, n, cnt, tol, sig, reinterpret_cast<double *>(base + L.scr),
+                                      reinterpret_cast<float2 *>(base + L.pairs), s, launches);
+    else
+        rc = stage3_bisect_batched(dd, de, n, cnt, tol, sig, reinterpret_cast<double *>(base + L.scr), s, launches);
     if (rc != AVS_SUCCESS) return rc;
-    scatter_kernel<<<(unsigned)std::min<int64_t>((n * cnt + 255) / 256, 8192), 256, 0, s>>>(sig, dst, n, cnt);
+    scatter_kernel<T><<<(unsigned)std::min<int64_t>((n * cnt + 255) / 256, 8192), 256, 0, s>>>(sig, dst, n, cnt);
     AVS_CUDA_TRY(cudaGetLastError());
     AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[3], s, cudaEventRecordExternal));
     if (launches) *launches += 2;
@@ -1142,9 +1155,10 @@ bool valid_tile(int64_t n, int t) { return is_pow2(t) && t >= 16 && t <= kMaxTil
 
 }  // namespace
 
-// Batched calls: out1 = sigma (FP32) or d (FP64), out2 = e (FP64, bidiagonal form only).
+// Batched calls: out1 = sigma (type T) or d (FP64), out2 = e (FP64, bidiagonal form only).
+template <typename T>
 static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda, const int32_t *tile,
-                        const float *const *dA, void *const *out1, void *const *out2, bool bidiag,
+                        const T *const *dA, void *const *out1, void *const *out2, bool bidiag,
                         const avs_opts *opts, avs_report *rep) {
     void *const *dsigma = out1;
     if (rep) std::memset(rep, 0, sizeof(*rep));
@@ -1186,7 +1200,7 @@ static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const in
     size_t need = 0;
     size_t pin_need = sizeof(int) * 16 * (groups.size() + 1);
     for (auto &g : groups) {
-        need = std::max(need, batch_layout(g.first.first, g.first.second, (int)g.second.size()).total);
+        need = std::max(need, batch_layout(g.first.first, g.first.second, (int)g.second.size(), sizeof(T)).total);
         pin_need += sizeof(void *) * 4 * g.second.size();
     }
     int rc;
@@ -1198,7 +1212,7 @@ static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const in
         AVS_CUDA_TRY(cudaEventRecord(h->ev[4], reinterpret_cast<cudaStream_t>(opts->stream)));
         AVS_CUDA_TRY(cudaStreamWaitEvent(s, h->ev[4], 0));
     }
-    const double tol = bisect_tol(false, opts);
+    const double tol = bisect_tol(sizeof(T) == 8, opts);
     // pinned layout: one status word per group (16 ints apart), then the pointer tables
     int *h_status = reinterpret_cast<int *>(h->pinned);
     void **tab = reinterpret_cast<void **>(h_status + 16 * (groups.size() + 1));
@@ -1210,25 +1224,25 @@ static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const in
         const int64_t gn = g.first.first;
         const int gb = g.first.second;
         const int cnt = (int)g.second.size();
-        const BatchLayout L = batch_layout(gn, gb, cnt);
+        const BatchLayout L = batch_layout(gn, gb, cnt, sizeof(T));
         NvtxRange range("avs batched group");
         // pointer tables: sources, destinations, leading dimensions
         for (int q = 0; q < cnt; ++q) {
-            tab[q] = const_cast<float *>(dA[g.second[q]]);
+            tab[q] = const_cast<T *>(dA[g.second[q]]);
             tab[cnt + q] = dsigma[g.second[q]];
             tab[3 * cnt + q] = bidiag ? out2[g.second[q]] : nullptr;
             reinterpret_cast<int64_t *>(tab + 2 * cnt)[q] = lda[g.second[q]];
         }
         AVS_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(h->bws) + L.ptrs, tab, sizeof(void *) * 4 * cnt,
                                      cudaMemcpyHostToDevice, s));
-        const auto key = std::make_tuple(gn, gb, cnt, bidiag ? 1 : 0);
+        const auto key = std::make_tuple(gn, gb, cnt, (bidiag ? 1 : 0) + (sizeof(T) == 8 ? 2 : 0));
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
             avs_handle::Graph gr;
             for (cudaEvent_t &e : gr.ev) AVS_CUDA_TRY(cudaEventCreate(&e));
             cudaGraph_t graph;
             AVS_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            rc = group_launches(h, L, gn, gb, cnt, tol, s, gr.ev, &gr.kernels, bidiag);
+            rc = group_launches<T>(h, L, gn, gb, cnt, tol, s, gr.ev, &gr.kernels, bidiag);
             cudaError_t ce = cudaStreamEndCapture(s, &graph);
             if (rc == AVS_SUCCESS && ce == cudaSuccess) {
                 ce = cudaGraphInstantiate(&gr.exec, graph, 0);
@@ -1273,7 +1287,7 @@ static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const in
         }
         rep->kernel_launches = launches;
         rep->workspace_bytes = (int64_t)h->bws_bytes;
-        rep->precision = AVS_PREC_FP32;
+        rep->precision = sizeof(T) == 8 ? AVS_PREC_FP64 : AVS_PREC_FP32;
         rep->status = rc;
     }
     return rc;
@@ -1288,6 +1302,20 @@ extern "C" int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int
 
 extern "C" int avs_bidiag_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
                                         const int32_t *tile, const float *const *dA, double *const *dd,
+                                        double *const *de, const avs_opts *opts, avs_report *rep) {
+    return batched_call(h, count, n, lda, tile, dA, reinterpret_cast<void *const *>(dd),
+                        reinterpret_cast<void *const *>(de), true, opts, rep);
+}
+
+extern "C" int avs_svdvals_batched_dev_d(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
+                                         const int32_t *tile, const double *const *dA, double *const *dsigma,
+                                         const avs_opts *opts, avs_report *rep) {
+    return batched_call(h, count, n, lda, tile, dA, reinterpret_cast<void *const *>(dsigma), nullptr, false, opts,
+                        rep);
+}
+
+extern "C" int avs_bidiag_batched_dev_d(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
+                                        const int32_t *tile, const double *const *dA, double *const *dd,
                                         double *const *de, const avs_opts *opts, avs_report *rep) {
     return batched_call(h, count, n, lda, tile, dA, reinterpret_cast<void *const *>(dd),
                         reinterpret_cast<void *const *>(de), true, opts, rep);
@@ -1386,6 +1414,22 @@ extern "C" int avs_kernel_arch(int device, int32_t *binary_version, int32_t *ptx
     return AVS_SUCCESS;
 }
 
+// Compute roof of the bulge chase on `device`: flops/s of its inner arithmetic
+// (double-float, or FP64 with fp64 != 0) with every SM busy and no memory traffic.
+extern "C" int avs_measure_chase_rate(int device, int32_t fp64, double *flops_per_s) {
+    if (!flops_per_s) return -3;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+        cudaGetLastError();
+        return AVS_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) return -1;
+    AVS_CUDA_TRY(cudaSetDevice(device));
+    int sms = 0;
+    AVS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    return stage2_rate(fp64, sms, flops_per_s);
+}
+
 // ===========================================================================
 // Memory accounting helpers (used by admission control of the serving loop).
 extern "C" int avs_trim(avs_handle *h) {
@@ -1414,8 +1458,8 @@ extern "C" int avs_estimate_bytes(int64_t n, int32_t tile, int32_t precision, in
     if (tile > kMaxTile) return AVS_ERR_UNSUPPORTED;
     if (count < 0) return -4;
     if (!bytes) return -5;
-    if (count >= 1) {  // batched FP32 group
-        *bytes = (int64_t)batch_layout(n, tile, count).total;
+    if (count >= 1) {  // batched group: FP64 tiles for AVS_PREC_FP64, FP32 otherwise
+        *bytes = (int64_t)batch_layout(n, tile, count, precision == AVS_PREC_FP64 ? 8 : 4).total;
         return AVS_SUCCESS;
     }
     const int prec = resolve_precision(precision, true);

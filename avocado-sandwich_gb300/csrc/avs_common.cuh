@@ -190,6 +190,7 @@ struct Stage2Work {
 };
 int stage2_chase(double *dAB, int64_t n, int bw, int64_t ldab, double *dd, double *de, const Stage2Work &w,
                  cudaStream_t s, int num_sms, int64_t *launches);
+int stage2_rate(int fp64, int num_sms, double *flops_per_s);
 
 template <typename T>
 int stage2_chase_df(const T *dW, int64_t n, int64_t ldw, int bw, float2 *dAB, int64_t ldab, double *dd, double *de,
@@ -198,6 +199,10 @@ int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float
                             double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
 int stage3_bisect_df_batched(const double *dd, const double *de, int64_t n, int batch, double rel_tol,
                              double *dsigma, double *dscratch, float2 *dpairs, cudaStream_t s, int64_t *launches);
+int stage2_chase_fp64_batched(const double *dW, int64_t n, int bw, int batch, double *dAB, int64_t ldab, double *dd,
+                              double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
+int stage3_bisect_batched(const double *dd, const double *de, int64_t n, int batch, double rel_tol, double *dsigma,
+                          double *dscratch, cudaStream_t s, int64_t *launches);
 int bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *dsigma, double rel_tol,
                          cudaStream_t s);
 int stage3_bisect_df(const double *dd, const double *de, int64_t n, double rel_tol, double *dsigma, double *dscratch,

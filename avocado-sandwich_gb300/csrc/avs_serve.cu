@@ -2,11 +2,12 @@
 // memory admission, on top of the C ABI of this library.
 //
 // Execution slots ("workers") each own an avs_handle (stream + workspace) and
-// a host thread.  A free slot takes the oldest queued request; an FP32 request
-// takes every other queued FP32 request of the same order along (up to
-// max_batch) into one batched call, so requests that arrive while others run
-// join the next group of their order.  Slots run concurrently, so groups of
-// different orders and FP64 requests overlap on the GPU.  Admission: a slot
+// a host thread.  A free slot takes the oldest queued request and every other
+// queued request of the same order and type along (up to max_batch) into one
+// batched call (FP32: FP32 tiles, double-float stages; FP64: FP64
+// throughout), so requests that arrive while others run join the next group
+// of their order.  Slots run concurrently, so groups of different orders and
+// types overlap on the GPU.  Admission: a slot
 // starts a group only while the device bytes held by all slots (workspaces +
 // input/output buffers) stay within the budget; otherwise it shrinks the
 // group, releases its own cached memory, or waits for others to finish (idle
@@ -90,18 +91,16 @@ int32_t pick_tile(avs_server *S, Slot &sl, const Request *r) {
     return rule_tile(r->n);
 }
 
-// Bytes a slot holds after running a group of `cnt` requests of order n: the
-// workspace the group uses grows to what it needs, the other one stays.
+// Bytes a slot holds after running a group of `cnt` requests of order n (a
+// batched group of either type): the batched workspace grows to what the
+// group needs, the single-call workspace stays.
 size_t held_after(const Slot &sl, int64_t ws_single, int64_t ws_batched, int64_t n, int32_t tile, int32_t dtype,
                   int cnt) {
     int64_t need = 0;
-    if (dtype == AVS_DTYPE_F32) {
-        avs_estimate_bytes(n, tile, AVS_PREC_FP32, cnt, &need);
-        const size_t io = (size_t)cnt * (size_t)(n * n + n) * 4 + 256;
-        return (size_t)ws_single + (size_t)std::max(ws_batched, need) + std::max(sl.io_bytes, io);
-    }
-    avs_estimate_bytes(n, tile, AVS_PREC_FP64, 0, &need);
-    return (size_t)std::max(ws_single, need) + (size_t)ws_batched + sl.io_bytes;
+    const size_t elem = dtype == AVS_DTYPE_F64 ? 8 : 4;
+    avs_estimate_bytes(n, tile, dtype == AVS_DTYPE_F64 ? AVS_PREC_FP64 : AVS_PREC_FP32, cnt, &need);
+    const size_t io = (size_t)cnt * (size_t)(n * n + n) * elem + 256;
+    return (size_t)ws_single + (size_t)std::max(ws_batched, need) + std::max(sl.io_bytes, io);
 }
 
 void release_slot(avs_server *S, Slot &sl, std::unique_lock<std::mutex> &lk) {
@@ -117,10 +116,13 @@ void release_slot(avs_server *S, Slot &sl, std::unique_lock<std::mutex> &lk) {
     S->cv_work.notify_all();
 }
 
-int run_f32_group(Slot &sl, std::vector<Request *> &g, int32_t tile) {
+// One batched call for a group of same-order requests of type T (FP32 tiles
+// with double-float stages, or FP64 throughout).
+template <typename T>
+int run_group(Slot &sl, std::vector<Request *> &g, int32_t tile) {
     const int cnt = (int)g.size();
     const int64_t n = g[0]->n;
-    const size_t need = (size_t)cnt * (size_t)(n * n + n) * 4 + 256;
+    const size_t need = (size_t)cnt * (size_t)(n * n + n) * sizeof(T) + 256;
     if (sl.io_bytes < need) {
         if (sl.io) cudaFree(sl.io);
         sl.io = nullptr;
@@ -131,26 +133,28 @@ int run_f32_group(Slot &sl, std::vector<Request *> &g, int32_t tile) {
         }
         sl.io_bytes = need;
     }
-    float *dA = reinterpret_cast<float *>(sl.io);
-    float *dS = dA + (size_t)cnt * n * n;
+    T *dA = reinterpret_cast<T *>(sl.io);
+    T *dS = dA + (size_t)cnt * n * n;
     std::vector<int64_t> nn(cnt, n), ld(cnt, n);
     std::vector<int32_t> tt(cnt, tile);
-    std::vector<const float *> pa(cnt);
-    std::vector<float *> ps(cnt);
+    std::vector<const T *> pa(cnt);
+    std::vector<T *> ps(cnt);
     for (int i = 0; i < cnt; ++i) {
         pa[i] = dA + (size_t)i * n * n;
         ps[i] = dS + (size_t)i * n;
-        AVS_CUDA_TRY(cudaMemcpy2DAsync(const_cast<float *>(pa[i]), sizeof(float) * n, g[i]->A,
-                                       sizeof(float) * g[i]->lda, sizeof(float) * n, n, cudaMemcpyHostToDevice,
-                                       sl.s));
+        AVS_CUDA_TRY(cudaMemcpy2DAsync(const_cast<T *>(pa[i]), sizeof(T) * n, g[i]->A, sizeof(T) * g[i]->lda,
+                                       sizeof(T) * n, n, cudaMemcpyHostToDevice, sl.s));
     }
     avs_opts o{};
     o.stream = sl.s;
-    int rc = avs_svdvals_batched_dev_s(sl.h, cnt, nn.data(), ld.data(), tt.data(), pa.data(), ps.data(), &o,
-                                       nullptr);
+    int rc;
+    if constexpr (sizeof(T) == 8)
+        rc = avs_svdvals_batched_dev_d(sl.h, cnt, nn.data(), ld.data(), tt.data(), pa.data(), ps.data(), &o, nullptr);
+    else
+        rc = avs_svdvals_batched_dev_s(sl.h, cnt, nn.data(), ld.data(), tt.data(), pa.data(), ps.data(), &o, nullptr);
     if (rc != AVS_SUCCESS) return rc;
     for (int i = 0; i < cnt; ++i)
-        AVS_CUDA_TRY(cudaMemcpyAsync(g[i]->sigma, ps[i], sizeof(float) * n, cudaMemcpyDeviceToHost, sl.s));
+        AVS_CUDA_TRY(cudaMemcpyAsync(g[i]->sigma, ps[i], sizeof(T) * n, cudaMemcpyDeviceToHost, sl.s));
     AVS_CUDA_TRY(cudaStreamSynchronize(sl.s));
     return AVS_SUCCESS;
 }
@@ -173,11 +177,9 @@ void slot_loop(avs_server *S, int k) {
         Request *head = S->queue.front();
         const int32_t tile = head->tile > 0 ? head->tile : rule_tile(head->n);
         std::vector<Request *> g{head};
-        if (head->dtype == AVS_DTYPE_F32) {
-            for (size_t q = 1; q < S->queue.size() && (int)g.size() < S->cfg.max_batch; ++q) {
-                Request *r = S->queue[q];
-                if (r->dtype == AVS_DTYPE_F32 && r->n == head->n && (r->tile == head->tile)) g.push_back(r);
-            }
+        for (size_t q = 1; q < S->queue.size() && (int)g.size() < S->cfg.max_batch; ++q) {
+            Request *r = S->queue[q];
+            if (r->dtype == head->dtype && r->n == head->n && (r->tile == head->tile)) g.push_back(r);
         }
         int64_t ws_single = 0, ws_batched = 0;
         avs_workspace_bytes(sl.h, &ws_single, &ws_batched);
@@ -221,14 +223,7 @@ void slot_loop(avs_server *S, int k) {
 
         int32_t t = tile;
         if (head->tile <= 0 && S->cfg.autotune) t = pick_tile(S, sl, head);
-        int rc;
-        if (head->dtype == AVS_DTYPE_F32) {
-            rc = run_f32_group(sl, g, t);
-        } else {
-            avs_opts o{};
-            rc = avs_svdvals_d(sl.h, head->n, head->n, head->lda, t, static_cast<const double *>(head->A),
-                               static_cast<double *>(head->sigma), &o, nullptr);
-        }
+        const int rc = head->dtype == AVS_DTYPE_F32 ? run_group<float>(sl, g, t) : run_group<double>(sl, g, t);
         int64_t ws_s = 0, ws_b = 0;
         avs_workspace_bytes(sl.h, &ws_s, &ws_b);
         const int64_t ws_after = ws_s + ws_b;

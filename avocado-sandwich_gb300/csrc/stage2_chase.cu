@@ -36,6 +36,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 
 #include "avs_common.cuh"
@@ -180,7 +181,16 @@ struct ChaseCfg {
     static constexpr int CPC = 2 * BW / C;          // L op: columns per CTA
     static constexpr int CPW = CPC / (NT / 32);     // L op: columns per warp
     static constexpr int RPL = BW >= 32 ? BW / 32 : 1;  // L op: rows per lane
+    // R op dot products: every row's sum runs over NCH fixed chunks of W0
+    // columns, each chunk accumulated in the same order and the chunks added
+    // in index order, whatever C and NT are -- so every configuration of a
+    // band width gives the same bits (a matrix's values do not depend on the
+    // batch it runs in).
+    static constexpr int NCH = 16;
+    static constexpr int W0 = BW / NCH;
+    static constexpr int CPT = CPG / W0;  // chunks per thread
     static_assert(CPG >= 1 && CPW >= 1, "chase configuration");
+    static_assert(W0 >= 1 && CPG % W0 == 0 && G * CPT == NCH, "chase chunking");
 };
 
 // Scalar arithmetic of the chase: FP64, or double-float pairs stored as float2.
@@ -210,6 +220,7 @@ struct ChaseAr<double> {
     static __device__ __forceinline__ V rcp(V a) { return 1.0 / a; }
     static __device__ __forceinline__ double to_double(V a) { return a; }
     static __device__ __forceinline__ St from_double(double a) { return a; }
+    static __device__ __forceinline__ V v_from_double(double a) { return a; }
     // dot-product accumulator: plain FMA chain
     using Acc = double;
     static __device__ __forceinline__ Acc acc_zero() { return 0.0; }
@@ -270,7 +281,11 @@ struct ChaseAr<df64> {
         const df64 v = df_from_double(a);
         return make_float2(v.hi, v.lo);
     }
+    static __device__ __forceinline__ V v_from_double(double a) { return df_from_double(a); }
 };
+
+__device__ __forceinline__ double st_to_double(double v) { return v; }
+__device__ __forceinline__ double st_to_double(float2 v) { return (double)v.x + (double)v.y; }
 
 template <typename S>
 struct BandT {
@@ -280,6 +295,12 @@ struct BandT {
     int ku;  // 2bw - 1
     __device__ __forceinline__ typename Ar::St *at(int64_t r, int64_t c) const { return ab + (ku + r - c) + c * ldab; }
 };
+
+// Split cluster barrier: every thread of every CTA arrives (release: its
+// earlier reads and writes are ordered before) and later waits (acquire).
+// Between the two a CTA keeps working; a thread waits before it arrives again.
+__device__ __forceinline__ void cluster_arrive() { asm volatile("barrier.cluster.arrive.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cluster_wait() { asm volatile("barrier.cluster.wait.aligned;" ::: "memory"); }
 
 template <typename S>
 __device__ __forceinline__ typename ChaseAr<S>::V warp_sum_s(typename ChaseAr<S>::V v) {
@@ -346,7 +367,7 @@ __global__ void __launch_bounds__(ChaseCfg<BW, CC, NTT>::NT, ChaseCfg<BW, CC, NT
     cg::cluster_group cluster = cg::this_cluster();
     const int q = (int)cluster.block_rank();
     __shared__ V sv[BW];
-    __shared__ V part[Cfg::G][Cfg::RPC];
+    __shared__ V part[Cfg::NCH][Cfg::RPC];
     __shared__ V wrow[Cfg::RPC];
     __shared__ V s_tau, s_beta;
     __shared__ int s_j;
@@ -380,6 +401,7 @@ __global__ void __launch_bounds__(ChaseCfg<BW, CC, NTT>::NT, ChaseCfg<BW, CC, NT
             if (L >= 2) {
                 if (wid == 0) warp_reflector<S, BW>(A, true, rho, c0, L, sv, &s_tau, &s_beta);
                 __syncthreads();
+                cluster_arrive();  // this CTA is done reading row rho
             }
             if (m > 0) {
                 if (tid == 0 && j > 0) wait_geq(done + j - 1, min(2 * m + 4, ops_prev), err);
@@ -392,23 +414,27 @@ __global__ void __launch_bounds__(ChaseCfg<BW, CC, NTT>::NT, ChaseCfg<BW, CC, NT
                     const int64_t r = rho + 1 + (int64_t)q * Cfg::RPC + rr;
                     const bool rv = (r <= c1);
                     V vals[Cfg::CPG];
-                    typename Ar::Acc a0 = Ar::acc_zero(), a1 = Ar::acc_zero();
 #pragma unroll
                     for (int k = 0; k < Cfg::CPG; ++k) {
                         const int ci = g * Cfg::CPG + k;
                         vals[k] = (rv && ci < L) ? Ar::ld(A.at(r, c0 + ci)) : Ar::zero();
                     }
 #pragma unroll
-                    for (int k = 0; k < Cfg::CPG; ++k) {
-                        const int ci = g * Cfg::CPG + k;
-                        if (ci < L) Ar::acc_add((k & 1) ? a1 : a0, vals[k], sv[ci]);
+                    for (int cc = 0; cc < Cfg::CPT; ++cc) {
+                        typename Ar::Acc a0 = Ar::acc_zero(), a1 = Ar::acc_zero();
+#pragma unroll
+                        for (int kk = 0; kk < Cfg::W0; ++kk) {
+                            const int k = cc * Cfg::W0 + kk;
+                            const int ci = g * Cfg::CPG + k;
+                            if (ci < L) Ar::acc_add((kk & 1) ? a1 : a0, vals[k], sv[ci]);
+                        }
+                        part[g * Cfg::CPT + cc][rr] = Ar::add(Ar::acc_value(a0), Ar::acc_value(a1));
                     }
-                    part[g][rr] = Ar::add(Ar::acc_value(a0), Ar::acc_value(a1));
                     __syncthreads();
                     if (g == 0) {
                         V w = Ar::zero();
 #pragma unroll
-                        for (int gg = 0; gg < Cfg::G; ++gg) w = Ar::add(w, part[gg][rr]);
+                        for (int c = 0; c < Cfg::NCH; ++c) w = Ar::add(w, part[c][rr]);
                         wrow[rr] = Ar::mul(w, tau);
                     }
                     __syncthreads();
@@ -421,28 +447,24 @@ __global__ void __launch_bounds__(ChaseCfg<BW, CC, NTT>::NT, ChaseCfg<BW, CC, NT
                         }
                     }
                 }
+                // Every CTA has read row rho (it arrived after its reflector);
+                // only then does CTA 0 overwrite it with beta and zeros.
+                cluster_wait();
+                if (q == 0) {
+                    if (tid == 0) Ar::st(A.at(rho, c0), s_beta);
+                    for (int i = 1 + tid; i < L; i += blockDim.x) Ar::st(A.at(rho, c0 + i), Ar::zero());
+                }
             }
             __threadfence();
             cluster.sync();
-            // Every CTA of the cluster has read row rho for its reflector by
-            // now; only then does CTA 0 store beta and the annihilated zeros.
-            // Nothing later in this sweep reads row rho, and sweep j+1 sees the
-            // stores through the release below.
-            if (q == 0) {
-                if (L >= 2) {
-                    if (tid == 0) Ar::st(A.at(rho, c0), s_beta);
-                    for (int i = 1 + tid; i < L; i += blockDim.x) Ar::st(A.at(rho, c0 + i), Ar::zero());
-                    __threadfence();
-                }
-                __syncthreads();
-                if (tid == 0) st_release(done + j, 2 * m + 1);
-            }
+            if (q == 0 && tid == 0) st_release(done + j, 2 * m + 1);
             // ================= L op (op 2m+1) =================
             // Column c0 (rows c0..c1) is final after this sweep's R op and op
             // 2m+1 of sweep j-1 (covered by the R op's wait): reflector first.
             if (L >= 2) {
                 if (wid == 0) warp_reflector<S, BW>(A, false, c0, c0, L, sv, &s_tau, &s_beta);
                 __syncthreads();
+                cluster_arrive();  // this CTA is done reading column c0
             }
             if (tid == 0 && j > 0) wait_geq(done + j - 1, min(2 * m + 5, ops_prev), err);
             __syncthreads();
@@ -480,21 +502,15 @@ __global__ void __launch_bounds__(ChaseCfg<BW, CC, NTT>::NT, ChaseCfg<BW, CC, NT
                         }
                     }
                 }
+                cluster_wait();  // as in the R op: column c0 is overwritten after every CTA has read it
+                if (q == 0) {
+                    if (tid == 0) Ar::st(A.at(c0, c0), s_beta);
+                    for (int i = 1 + tid; i < L; i += blockDim.x) Ar::st(A.at(c0 + i, c0), Ar::zero());
+                }
             }
             __threadfence();
             cluster.sync();
-            // As in the R op: column c0 is overwritten only after every CTA has
-            // read it.  The next R op reads row c0 from column c0 + bw on and
-            // applies to columns >= c0 + bw, so it never meets these stores.
-            if (q == 0) {
-                if (L >= 2) {
-                    if (tid == 0) Ar::st(A.at(c0, c0), s_beta);
-                    for (int i = 1 + tid; i < L; i += blockDim.x) Ar::st(A.at(c0 + i, c0), Ar::zero());
-                    __threadfence();
-                }
-                __syncthreads();
-                if (tid == 0) st_release(done + j, 2 * m + 2);
-            }
+            if (q == 0 && tid == 0) st_release(done + j, 2 * m + 2);
             rho = c0;
             c0 += BW;
         }
@@ -612,7 +628,75 @@ __global__ void bidiag_out_kernel(const double *ab, int64_t n, int bw, int64_t l
     }
 }
 
+// Compute roof of the chase: its inner arithmetic -- a compensated dot product
+// over 16 register values, the scaled reflector update of each value -- with
+// no memory traffic, on every SM.  One element step is 4 flops (multiply-add of
+// the dot, multiply-subtract of the update), the accounting of the chase's flop
+// count.
+template <typename S>
+__global__ void __launch_bounds__(512) chase_rate_kernel(typename ChaseAr<S>::St *out, int iters) {
+    using Ar = ChaseAr<S>;
+    using V = typename Ar::V;
+    constexpr int K = 16;
+    V vals[K], sv[K];
+    const float seed = 1.0f + 1e-3f * (float)(threadIdx.x & 63);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        vals[k] = Ar::v_from_double(seed + 0.01 * k);
+        sv[k] = Ar::v_from_double(0.5 / (k + 1));
+    }
+    const V tau = Ar::v_from_double(1e-3);
+    for (int it = 0; it < iters; ++it) {
+        typename Ar::Acc a0 = Ar::acc_zero(), a1 = Ar::acc_zero();
+#pragma unroll
+        for (int k = 0; k < K; ++k) Ar::acc_add((k & 1) ? a1 : a0, vals[k], sv[k]);
+        const V w = Ar::mul(Ar::add(Ar::acc_value(a0), Ar::acc_value(a1)), tau);
+#pragma unroll
+        for (int k = 0; k < K; ++k) vals[k] = Ar::sub(vals[k], Ar::mul(w, sv[k]));
+    }
+    V acc = Ar::zero();
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc = Ar::add(acc, vals[k]);
+    Ar::st(out + blockIdx.x * (int64_t)blockDim.x + threadIdx.x, acc);
+}
+
 }  // namespace
+
+// Measured rate (flops/s, 4 per element step) of the chase arithmetic in FP64
+// (fp64 != 0) or double-float, all SMs busy, timed with events; the output
+// buffer is allocated and freed here.
+int stage2_rate(int fp64, int num_sms, double *flops_per_s) {
+    const int threads = 512, blocks = num_sms * 4;
+    const int iters = fp64 ? 256 : 8192;
+    void *out = nullptr;
+    AVS_CUDA_TRY(cudaMalloc(&out, sizeof(double) * (size_t)blocks * threads));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {  // first launch warms up
+        cudaEventRecord(e0);
+        if (fp64)
+            chase_rate_kernel<double><<<blocks, threads>>>(reinterpret_cast<double *>(out), iters);
+        else
+            chase_rate_kernel<df64><<<blocks, threads>>>(reinterpret_cast<float2 *>(out), iters);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    const cudaError_t err = cudaGetLastError();
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    if (err != cudaSuccess) {
+        set_last_cuda_error(err);
+        return AVS_ERR_CUDA;
+    }
+    *flops_per_s = 4.0 * 16.0 * (double)iters * blocks * threads / (best * 1e-3);
+    return AVS_SUCCESS;
+}
 
 template <typename T>
 int extract_band_compact(const T *dA, int64_t n, int64_t lda, int bw, double *dAB, int64_t ldab, cudaStream_t s) {
@@ -690,43 +774,48 @@ template int stage2_chase_df<double>(const double *, int64_t, int64_t, int, floa
                                      const Stage2Work &, cudaStream_t, int, int64_t *);
 
 // ---------------------------------------------------------------------------
-// Batched chase (double-float): `batch` matrices of the same order n and band
-// width bw, stacked at stride n*n (tiles) / ldab*n (band) / n+1 (flags) / n (d, e).
+// Batched chase: `batch` matrices of the same order n and band width bw,
+// stacked at stride n*n (tiles) / ldab*n (band) / n+1 (flags) / n (d, e).
+// S = df64 (FP32 tiles, the FP32-class modes) or double (FP64 tiles).
 namespace {
-template <typename T>
-__global__ void extract_band_df_batched(const T *a, int64_t n, int bw, float2 *ab, int64_t ldab) {
+template <typename T, typename S>
+__global__ void extract_band_batched(const T *a, int64_t n, int bw, typename ChaseAr<S>::St *ab, int64_t ldab) {
     const int64_t c = blockIdx.x, zb = blockIdx.y;
     const int ku = 2 * bw - 1;
     const T *az = a + zb * n * n;
-    float2 *abz = ab + zb * ldab * n;
+    typename ChaseAr<S>::St *abz = ab + zb * ldab * n;
     for (int i = threadIdx.x; i <= bw; i += blockDim.x) {
         const int64_t r = c - bw + i;
-        if (r >= 0) abz[(ku + r - c) + c * ldab] = make_float2((float)az[r + c * n], 0.0f);
+        if (r >= 0) {
+            if constexpr (sizeof(typename ChaseAr<S>::St) == sizeof(float2) && sizeof(T) == 4 &&
+                          !std::is_same<S, double>::value)
+                abz[(ku + r - c) + c * ldab] = make_float2((float)az[r + c * n], 0.0f);  // exact
+            else
+                abz[(ku + r - c) + c * ldab] = ChaseAr<S>::from_double((double)az[r + c * n]);
+        }
     }
 }
-__global__ void bidiag_out_df_batched(const float2 *ab, int64_t n, int bw, int64_t ldab, double *d, double *e,
-                                      int batch) {
+template <typename S>
+__global__ void bidiag_out_batched(const typename ChaseAr<S>::St *ab, int64_t n, int bw, int64_t ldab, double *d,
+                                   double *e, int batch) {
     const int ku = 2 * bw - 1;
     const int64_t total = n * (int64_t)batch;
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
         const int64_t zb = g / n, i = g % n;
-        const float2 *abz = ab + zb * ldab * n;
-        const float2 x = abz[ku + i * ldab];
-        d[zb * n + i] = (double)x.x + (double)x.y;
-        if (i + 1 < n) {
-            const float2 y = abz[(ku - 1) + (i + 1) * ldab];
-            e[zb * n + i] = (double)y.x + (double)y.y;
-        } else {
-            e[zb * n + i] = 0.0;
-        }
+        const typename ChaseAr<S>::St *abz = ab + zb * ldab * n;
+        d[zb * n + i] = st_to_double(abz[ku + i * ldab]);
+        e[zb * n + i] = (i + 1 < n) ? st_to_double(abz[(ku - 1) + (i + 1) * ldab]) : 0.0;
     }
 }
 }  // namespace
 
-int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
-                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches) {
-    AVS_CUDA_TRY(cudaMemsetAsync(dAB, 0, sizeof(float2) * (size_t)ldab * (size_t)n * batch, s));
-    extract_band_df_batched<float><<<dim3((unsigned)n, (unsigned)batch), 128, 0, s>>>(dW, n, bw, dAB, ldab);
+template <typename T, typename S>
+int stage2_chase_batched(const T *dW, int64_t n, int bw, int batch, typename ChaseAr<S>::St *dAB, int64_t ldab,
+                         double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms,
+                         int64_t *launches) {
+    using St = typename ChaseAr<S>::St;
+    AVS_CUDA_TRY(cudaMemsetAsync(dAB, 0, sizeof(St) * (size_t)ldab * (size_t)n * batch, s));
+    extract_band_batched<T, S><<<dim3((unsigned)n, (unsigned)batch), 128, 0, s>>>(dW, n, bw, dAB, ldab);
     AVS_CUDA_TRY(cudaGetLastError());
     if (n >= 2) {
         AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)((n + 1) * (int64_t)batch + 1), s));
@@ -740,29 +829,52 @@ int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float
         // 1281, 4/8 x 512 1879/3289.
         // The small CTAs pay only while the batch keeps every SM busy with
         // several sweeps (a sweep has about (n / bw) / 2 siblings in flight);
-        // a short batch is latency-bound and keeps 512-thread CTAs.
-        const bool wide = (int64_t)batch * std::max<int64_t>(1, (n / bw) / 2) >= 4 * (int64_t)num_sms;
+        // a short batch is latency-bound and keeps 512-thread CTAs.  Every
+        // configuration of a band width computes the same bits (fixed
+        // reduction order), so a matrix's values do not depend on its batch.
+        // A batch whose sweeps in flight fit twice in the GPU with the single
+        // call's clusters (C = 8 at bands >= 128, 4 at 64, 2 at 32) is
+        // latency-bound and takes them: e.g. one n = 8192 matrix at band 128.
+        const int64_t inflight = (int64_t)batch * std::max<int64_t>(1, (n / bw) / 2);
+        const bool wide = inflight >= 4 * (int64_t)num_sms;
+        const int cdef = bw >= 128 ? 8 : (bw == 64 ? 4 : (bw == 32 ? 2 : 1));
+        const bool narrow = inflight <= 2 * (int64_t)(num_sms / cdef);
+        const int64_t sAB = ldab * n, sF = n + 1;
         switch (bw) {
-            case 16: rc = launch_chase_cluster<16, df64, 1>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
+            case 16: rc = launch_chase_cluster<16, S, 1>(dAB, n, ldab, w, s, num_sms, batch, sAB, sF); break;
             case 32:
-                rc = wide ? launch_chase_cluster<32, df64, 1, 128>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1)
-                          : launch_chase_cluster<32, df64, 2>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1);
+                rc = wide     ? launch_chase_cluster<32, S, 1, 128>(dAB, n, ldab, w, s, num_sms, batch, sAB, sF)
+                               : launch_chase_cluster<32, S, 2>(dAB, n, ldab, w, s, num_sms, batch, sAB, sF);
                 break;
             case 64:
-                rc = wide ? launch_chase_cluster<64, df64, 2, 128>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1)
-                          : launch_chase_cluster<64, df64, 1>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1);
+                rc = wide     ? launch_chase_cluster<64, S, 2, 128>(dAB, n, ldab, w, s, num_sms, batch, sAB, sF)
+                     : narrow ? launch_chase_cluster<64, S, 4>(dAB, n, ldab, w, s, num_sms, batch, sAB, sF)
+                              : launch_chase_cluster<64, S, 1>(dAB, n, ldab, w, s, num_sms, batch, sAB, sF);
                 break;
-            case 128: rc = launch_chase_cluster<128, df64, 2>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
-            case 256: rc = launch_chase_cluster<256, df64, 8>(dAB, n, ldab, w, s, num_sms, batch, ldab * n, n + 1); break;
+            case 128:
+                rc = narrow ? launch_chase_cluster<128, S, 8>(dAB, n, ldab, w, s, num_sms, batch, sAB, sF)
+                            : launch_chase_cluster<128, S, 2>(dAB, n, ldab, w, s, num_sms, batch, sAB, sF);
+                break;
+            case 256: rc = launch_chase_cluster<256, S, 8>(dAB, n, ldab, w, s, num_sms, batch, sAB, sF); break;
             default: rc = AVS_ERR_UNSUPPORTED;
         }
         if (rc != AVS_SUCCESS) return rc;
     }
     const int nb = (int)std::min<int64_t>((n * batch + 255) / 256, 8192);
-    bidiag_out_df_batched<<<nb > 0 ? nb : 1, 256, 0, s>>>(dAB, n, bw, ldab, dd, de, batch);
+    bidiag_out_batched<S><<<nb > 0 ? nb : 1, 256, 0, s>>>(dAB, n, bw, ldab, dd, de, batch);
     AVS_CUDA_TRY(cudaGetLastError());
     if (launches) *launches += 3;
     return AVS_SUCCESS;
+}
+
+int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
+                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches) {
+    return stage2_chase_batched<float, df64>(dW, n, bw, batch, dAB, ldab, dd, de, w, s, num_sms, launches);
+}
+
+int stage2_chase_fp64_batched(const double *dW, int64_t n, int bw, int batch, double *dAB, int64_t ldab, double *dd,
+                              double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches) {
+    return stage2_chase_batched<double, double>(dW, n, bw, batch, dAB, ldab, dd, de, w, s, num_sms, launches);
 }
 
 }  // namespace avs

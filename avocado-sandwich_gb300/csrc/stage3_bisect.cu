@@ -112,16 +112,13 @@ __device__ __forceinline__ int tgk_count_f32(const double *__restrict__ d, const
     return cnt;
 }
 
-__global__ void bisect_kernel(const double *d, const double *e, int64_t n, double rel_tol, const double *scratch,
-                              double *sigma) {
-    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k >= n) return;
+// The k-th largest singular value of the upper bidiagonal (d, e) of order n,
+// from the bound and pivot guard in scratch[0..1].
+__device__ double bisect_value(const double *d, const double *e, int64_t n, int64_t k, double rel_tol,
+                               const double *scratch) {
     const double bound = scratch[0];
     const double pivmin = scratch[1];
-    if (bound == 0.0) {
-        sigma[k] = 0.0;
-        return;
-    }
+    if (bound == 0.0) return 0.0;
     const double tol = rel_tol * bound;
     const int64_t target = 2 * n - 1 - k;  // TGK index (ascending) of the k-th largest sigma
     double lo = 0.0, hi = bound * (1.0 + 4.0 * DBL_EPSILON) + pivmin;
@@ -152,7 +149,14 @@ __global__ void bisect_kernel(const double *d, const double *e, int64_t n, doubl
         else
             lo = mid;
     }
-    sigma[k] = 0.5 * (lo + hi);
+    return 0.5 * (lo + hi);
+}
+
+__global__ void bisect_kernel(const double *d, const double *e, int64_t n, double rel_tol, const double *scratch,
+                              double *sigma) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    sigma[k] = bisect_value(d, e, n, k, rel_tol, scratch);
 }
 
 // ---- double-float bisection (the pipeline's stage 3 for FP32-class modes) ----
@@ -298,16 +302,15 @@ __device__ double bisect_df_grp(const float2 *a, int64_t n, int64_t k, double re
     return bound * 0.5 * df_to_double(c);
 }
 
-// Lanes per value.  A group of G lanes does more counts per value (about 2.3
-// and 3.2 times those of one lane for G = 4, 8) in fewer dependent passes, which pays while the values alone leave the GPU short of
-// threads (measured on GB300 at n = 16384 values: 121 ms with G = 1, 98 ms
-// with G = 2, 146 ms with G = 4; G = 4/8 below 8192 values).
-inline int bisect_group(int64_t nvalues) {
-    if (nvalues >= 65536) return 1;
-    if (nvalues >= 8192) return 2;
-    if (nvalues >= 1024) return 4;
-    return 8;
-}
+// Lanes per value, a function of the order alone: the single-matrix and the
+// batched calls of one order run the same multisection, so a matrix's values
+// are identical alone and in a batch (the final bracket depends on G).  A group
+// of G lanes does more counts per value (about 1.3, 2.3 and 3.2 times those of
+// one lane for G = 2, 4, 8) in fewer dependent passes; G = 2 measured fastest
+// at n = 16384 on GB300 (121 ms with G = 1, 98 ms with G = 2, 146 ms with
+// G = 4) and keeps the batched workloads, where values are plentiful, close
+// to the one-lane work.
+inline int bisect_group(int64_t n) { return n >= 65536 ? 1 : 2; }
 
 template <int G>
 __global__ void bisect_df_kernel(const float2 *a, int64_t n, double rel_tol, const double *scratch, double *sigma) {
@@ -511,6 +514,33 @@ __global__ void bisect_df_batched(const float2 *a, int64_t n, int batch, double 
 }
 }  // namespace
 
+// Batched FP64 bisection: the single-matrix kernel's per-value code, one
+// thread per value of every matrix (values identical to stage3_bisect's).
+namespace {
+__global__ void bisect_batched(const double *d, const double *e, int64_t n, int batch, double rel_tol,
+                               const double *scratch, double *sigma) {
+    const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (g >= n * (int64_t)batch) return;
+    const int64_t zb = g / n, k = g % n;
+    sigma[g] = bisect_value(d + zb * n, e + zb * n, n, k, rel_tol, scratch + zb * 4);
+}
+}  // namespace
+
+int stage3_bisect_batched(const double *dd, const double *de, int64_t n, int batch, double rel_tol, double *dsigma,
+                          double *dscratch, cudaStream_t s, int64_t *launches) {
+    if (n <= 0 || batch <= 0) return AVS_SUCCESS;
+    if (!(rel_tol > 0.0)) rel_tol = 2.0 * DBL_EPSILON;
+    tgk_bound_batched<<<batch, 256, 0, s>>>(dd, de, n, dscratch);
+    AVS_CUDA_TRY(cudaGetLastError());
+    const int64_t nv = n * (int64_t)batch;
+    const int threads = bisect_threads(nv);
+    bisect_batched<<<(unsigned)((nv + threads - 1) / threads), threads, 0, s>>>(dd, de, n, batch, rel_tol, dscratch,
+                                                                               dsigma);
+    AVS_CUDA_TRY(cudaGetLastError());
+    if (launches) *launches += 2;
+    return AVS_SUCCESS;
+}
+
 int stage3_bisect_df_batched(const double *dd, const double *de, int64_t n, int batch, double rel_tol,
                              double *dsigma, double *dscratch, float2 *dpairs, cudaStream_t s, int64_t *launches) {
     if (n <= 0 || batch <= 0) return AVS_SUCCESS;
@@ -522,7 +552,7 @@ int stage3_bisect_df_batched(const double *dd, const double *de, int64_t n, int 
                                                                                               dscratch, dpairs);
     AVS_CUDA_TRY(cudaGetLastError());
     const int64_t nv = n * (int64_t)batch;
-    const int G = bisect_group(nv);
+    const int G = bisect_group(n);
     const unsigned blocks = (unsigned)((nv * G + 127) / 128);
     if (G == 1)
         bisect_df_batched<1><<<blocks, 128, 0, s>>>(dpairs, n, batch, rel_tol, dscratch, dsigma);

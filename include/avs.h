@@ -271,6 +271,16 @@ int avs_svdvals_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, co
 int avs_bidiag_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
                              const int32_t *tile, const float *const *dA, double *const *dd, double *const *de,
                              const avs_opts *opts, avs_report *report);
+/* The same two batched calls for Float64 matrices, FP64 throughout (tiles,
+ * updates, bulge chase, bisection; the random-matrix client of RMT/rmt.jl runs
+ * gebrd! in Float64, rmt.jl:23,28).  Each matrix's values are bit-identical to
+ * those of avs_svdvals_dev_d / the FP64 pipeline on the same matrix. */
+int avs_svdvals_batched_dev_d(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
+                              const int32_t *tile, const double *const *dA, double *const *dsigma,
+                              const avs_opts *opts, avs_report *report);
+int avs_bidiag_batched_dev_d(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
+                             const int32_t *tile, const double *const *dA, double *const *dd, double *const *de,
+                             const avs_opts *opts, avs_report *report);
 
 /* Autotuner of the batched path: times tiles 32, 64 and 128 (those that divide
  * n with at least two tiles) on `sample` seeded random matrices of order n,
@@ -288,6 +298,12 @@ int avs_selftest_timeout(avs_handle *h);
  * device code the runtime loaded from this library on `device`
  * (cudaFuncAttributes binaryVersion, 103 for sm_103a, and ptxVersion). */
 int avs_kernel_arch(int device, int32_t *binary_version, int32_t *ptx_version);
+/* Diagnostics (no counterpart in the reference): the compute roof of the bulge
+ * chase on `device` -- flops per second of its inner arithmetic (compensated
+ * dot products and reflector updates, 4 flops per element step) in
+ * double-float (fp64 == 0) or FP64, from registers on every SM.  The call
+ * allocates and frees a small output buffer and synchronises the device. */
+int avs_measure_chase_rate(int device, int32_t fp64, double *flops_per_s);
 
 /* Release the handle's cached device workspace, pinned tables and captured
  * graphs (the handle stays usable; the next call allocates again). */
@@ -296,8 +312,9 @@ int avs_trim(avs_handle *h);
  * entry points and that of the batched entry point (either pointer may be NULL). */
 int avs_workspace_bytes(avs_handle *h, int64_t *single_bytes, int64_t *batched_bytes);
 /* Device workspace one call needs: count == 0 -> one avs_svdvals_{s,d} call of
- * order n with this tile and precision; count >= 1 -> one batched FP32 group of
- * `count` matrices of order n (the caller's inputs and outputs not included). */
+ * order n with this tile and precision; count >= 1 -> one batched group of
+ * `count` matrices of order n (FP64 group for AVS_PREC_FP64, FP32 otherwise;
+ * the caller's inputs and outputs not included). */
 int avs_estimate_bytes(int64_t n, int32_t tile, int32_t precision, int32_t count, int64_t *bytes);
 
 /* ---- serving loop ---------------------------------------------------------------
@@ -306,8 +323,8 @@ int avs_estimate_bytes(int64_t n, int32_t tile, int32_t precision, int32_t count
  * FP32 or FP64, any supported order) are queued by avs_serve_submit and run by
  * `workers` execution slots, each with its own handle and CUDA stream, so the
  * work of several requests overlaps on the GPU.  A free slot takes the oldest
- * queued request and, for FP32, every other queued FP32 request of the same
- * order (up to max_batch) into one batched call.  Admission is by device
+ * queued request and every other queued request of the same order and type
+ * (up to max_batch) into one batched call (avs_svdvals_batched_dev_s / _d).  Admission is by device
  * memory: a slot starts a group only while the bytes held by all slots stay
  * within hbm_budget_bytes; otherwise it shrinks the group, releases its own
  * cached workspace, or waits until others finish.  Each result equals the

@@ -162,3 +162,42 @@ def test_batched_chase_branches_repeat(avs_mod, torch_cuda, tile, count):
             assert np.array_equal(got, singles[i % 4]), (rep, i, rel_err(got, singles[i % 4]))
     for a, s in zip(hosts, singles):
         assert rel_err(s, sl.svdvals(a.astype(np.float64))) < TOL32
+
+
+@pytest.mark.parametrize("tile", [16, 32, 64, 128])
+def test_batched_fp64_equals_single(avs_mod, torch_cuda, tile):
+    """Float64 batches run FP64 throughout: every matrix's values equal the
+    single FP64 call's bit for bit and LAPACK's within 1e-12 (normwise)."""
+    sizes = [n for n in [64, 128, 256, 128, 512, 256, 64] if n % tile == 0 and n // tile >= 1]
+    rng = np.random.default_rng(2000 + tile)
+    hosts = [rng.standard_normal((n, n)) / np.sqrt(n) for n in sizes]
+    devs = [avs_mod.to_device(a) for a in hosts]
+    r = avs_mod.Report()
+    outs = avs_mod.svdvals_batched(devs, tiles=tile, report=r)
+    assert r.precision == 1  # AVS_PREC_FP64
+    for a, d, o in zip(hosts, devs, outs):
+        assert o.dtype == torch_cuda.float64
+        got = o.cpu().numpy()
+        single = avs_mod.my_CU_svdval(d, tile).cpu().numpy()
+        assert np.array_equal(got, single), rel_err(got, single)
+        assert rel_err(got, sl.svdvals(a)) < 1e-12
+
+
+@pytest.mark.parametrize("tile,count", [(32, 4), (32, 160), (64, 320)])
+def test_batched_fp64_chase_branches(avs_mod, torch_cuda, tile, count):
+    """FP64 batches on both sides of the small-CTA threshold equal the single
+    call bit for bit."""
+    rng = np.random.default_rng(3000 + tile + count)
+    hosts = [rng.standard_normal((256, 256)) / 16.0 for _ in range(4)]
+    devs = [avs_mod.to_device(a) for a in hosts]
+    singles = [avs_mod.my_CU_svdval(d, tile).cpu().numpy() for d in devs]
+    outs = avs_mod.svdvals_batched([devs[i % 4].clone() for i in range(count)], tiles=tile)
+    for i, o in enumerate(outs):
+        assert np.array_equal(o.cpu().numpy(), singles[i % 4])
+
+
+def test_batched_rejects_mixed_dtypes(avs_mod, torch_cuda):
+    a = avs_mod.to_device(np.eye(64, dtype=np.float32))
+    b = avs_mod.to_device(np.eye(64))
+    with pytest.raises(TypeError):
+        avs_mod.svdvals_batched([a, b], tiles=16)

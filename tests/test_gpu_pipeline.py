@@ -202,9 +202,9 @@ def test_double_float_stages_match_fp64_stages(avs_mod, torch_cuda, n, b):
 
 @pytest.mark.parametrize("n,b", [(512, 128), (1024, 128), (1024, 256), (2048, 256)])
 def test_tensor_core_modes(avs_mod, torch_cuda, n, b):
-    """Trailing updates on tcgen05: split TF32 (3 products) keeps FP32-class
-    accuracy (<= 1e-5 of sigma_max against LAPACK); single-pass TF32, split
-    BF16 and single-pass BF16 state their larger errors."""
+    """Trailing updates on tcgen05: split TF32 and split BF16 (3 products each)
+    keep FP32-class accuracy (<= 1e-5 of sigma_max against LAPACK);
+    single-pass TF32 and BF16 state their larger errors."""
     from avs import workloads
     a = workloads.gaussian(n, 31, 1.0 / np.sqrt(n), dtype=np.float32)
     lap = sl.svdvals(a.astype(np.float64))
@@ -217,6 +217,6 @@ def test_tensor_core_modes(avs_mod, torch_cuda, n, b):
     s1 = avs_mod.my_CU_svdval(a, b, precision="tf32")
     assert rel_err(s1, lap) < 5e-3
     sb3 = avs_mod.my_CU_svdval(a, b, precision="bf16x3")
-    assert rel_err(sb3, lap) < 5e-4
+    assert rel_err(sb3, lap) < 1e-5
     sb = avs_mod.my_CU_svdval(a, b, precision="bf16")
     assert rel_err(sb, lap) < 5e-2

@@ -58,7 +58,7 @@ def test_rmt_client_matches_oracle(avs_mod, torch_cuda, n, k):
     rng = np.random.default_rng(100 + n)
     x = rng.standard_normal((t, nt, n, n)).astype(np.float32)
     noise = x + np.swapaxes(x, 2, 3)
-    m_gpu, c_gpu, times = rmt.mou_process_covar(t, n, nt, tl, k, noise=noise, chunk=7)
+    m_gpu, c_gpu, times = rmt.mou_process_covar(t, n, nt, tl, k, noise=noise, chunk=7, dtype="float32")
     m_ref, c_ref, times_ref = gebrd.mou_process_covar(noise, tl, k)
     np.testing.assert_allclose(times, times_ref)
     np.testing.assert_allclose(m_gpu, m_ref, rtol=1e-4)
@@ -75,3 +75,39 @@ def test_rmt_client_seeded(avs_mod, torch_cuda):
     assert 0.5 * 101 < a[0][0] < 1.5 * 101
     with pytest.raises(ValueError):
         rmt.mou_process_covar(2, 16, 2, 0.05, 17)
+
+
+@pytest.mark.parametrize("n,tile", [(64, 16), (128, 32), (256, 64)])
+def test_bidiag_batched_fp64_matches_gebd2(avs_mod, torch_cuda, n, tile):
+    """The Float64 batched bidiagonal (FP64 throughout, the reference's type
+    for gebrd!, RMT/rmt.jl:23,28) matches gebd2 to FP64 rounding."""
+    from oracle import gebrd
+    rng = np.random.default_rng(7 * n + tile)
+    hosts = [rng.standard_normal((n, n)) for _ in range(4)]
+    outs = avs_mod.bidiag_batched([avs_mod.to_device(a) for a in hosts], tiles=tile)
+    for a, (d, e) in zip(hosts, outs):
+        d, e = d.cpu().numpy(), e.cpu().numpy()
+        dr, er = gebrd.gebd2(a)
+        scale = np.linalg.norm(a, 2)
+        lead = 16
+        assert np.max(np.abs(np.abs(d[:lead]) - np.abs(dr[:lead]))) / scale < 1e-12
+        assert np.max(np.abs(np.abs(e[:lead]) - np.abs(er[:lead]))) / scale < 1e-12
+        sv = np.linalg.svd(np.diag(d) + np.diag(e[:-1], 1), compute_uv=False)
+        ref = sl.svdvals(a)
+        assert np.max(np.abs(sv - ref)) / ref[0] < 1e-12
+
+
+@pytest.mark.parametrize("n,k", [(25, 1), (48, 3)])
+def test_rmt_client_fp64_matches_oracle(avs_mod, torch_cuda, n, k):
+    """The sampling client in Float64 (its default, as the reference) against
+    the oracle on the same noise."""
+    from avs import rmt
+    from oracle import gebrd
+    t, nt, tl = 5, 4, 0.05
+    rng = np.random.default_rng(300 + n)
+    x = rng.standard_normal((t, nt, n, n))
+    noise = x + np.swapaxes(x, 2, 3)
+    m_gpu, c_gpu, _ = rmt.mou_process_covar(t, n, nt, tl, k, noise=noise, chunk=7, dtype="float64")
+    m_ref, c_ref, _ = gebrd.mou_process_covar(noise, tl, k)
+    np.testing.assert_allclose(m_gpu, m_ref, rtol=1e-10)
+    np.testing.assert_allclose(c_gpu, c_ref, rtol=1e-8, atol=1e-10)

@@ -270,3 +270,27 @@ def test_blockbidiag_reflectors_rebuild_q_p(oracle_mod, dt, n, b):
     back, oq, op = reflectors.checks(a, out, tq, tp, b)
     eps = np.finfo(dt).eps
     assert back < n * eps and oq < n * eps and op < n * eps, (back, oq, op)
+
+
+@pytest.mark.parametrize("n,b", [(128, 32), (256, 64), (256, 128)])
+def test_cpu_band_bidiagonal_restatement(oracle_mod, n, b):
+    """The timed CPU baseline's stage 1 -- BandBidiagonal!(onGPU=false),
+    CUDAbasedSVD/SVD_GPU.jl:176-214, LAPACK dgeqrt/dgemqrt on stacked tile
+    pairs -- keeps the singular values and gives the band of Blockbidiag! up
+    to the signs of rows and columns (QR and LQ factors are unique up to
+    signs); the three timed stages return LAPACK's singular values."""
+    from oracle import cpu_baseline, lapack
+    if not lapack.available() or lapack._sym("dgeqrt") is None:
+        pytest.skip("LAPACKE dgeqrt/dgemqrt not in scipy's OpenBLAS")
+    a = np.random.default_rng(n + b).standard_normal((n, n))
+    band = cpu_baseline.band_bidiagonal(a, b)
+    i, j = np.indices(band.shape)
+    assert not np.any(band[(j - i < 0) | (j - i > b)])
+    ref = oracle_mod.extract_band(oracle_mod.blockbidiag(a, b), b)
+    assert np.max(np.abs(np.abs(band) - np.abs(ref))) / np.max(np.abs(ref)) < 1e-12
+    s = sl.svdvals(a)
+    assert np.max(np.abs(sl.svdvals(band) - s)) / s[0] < 1e-13
+    sig, ts = cpu_baseline.run(a.astype(np.float32), b)
+    s32 = sl.svdvals(a.astype(np.float32).astype(np.float64))
+    assert np.max(np.abs(sig - s32)) / s32[0] < 1e-12
+    assert set(ts) == {"stage1", "stage2", "stage3"} and min(ts.values()) >= 0
