@@ -40,7 +40,7 @@ _LIB = None
 _HANDLES = {}
 
 NOT_IMPLEMENTED = -100
-PREC = {"default": 0, "fp64": 1, "fp32": 2, "tf32": 3, "tf32x3": 4, "bf16": 5, "bf16x3": 6}
+PREC = {"default": 0, "fp64": 1, "fp32": 2, "tf32": 3, "tf32x3": 4, "bf16": 5, "bf16x3": 6, "fp64x2": 7}
 
 EXPORTED_SYMBOLS = [
     "avs_create", "avs_destroy", "avs_reserve", "avs_strerror", "avs_version",
@@ -55,6 +55,7 @@ EXPORTED_SYMBOLS = [
     "avs_geqrf_ooc_s", "avs_geqrf_ooc_d", "avs_ooc_plan", "avs_selftest_timeout", "avs_kernel_arch",
     "avs_measure_chase_rate",
     "avs_serve_create", "avs_serve_submit", "avs_serve_wait", "avs_serve_stats_get", "avs_serve_destroy",
+    "avs_serve_plan",
 ]
 
 
@@ -152,6 +153,7 @@ def lib():
         L.avs_serve_wait.argtypes = [P, I64, ctypes.c_double, ctypes.POINTER(I32), ctypes.POINTER(ctypes.c_double)]
         L.avs_serve_stats_get.argtypes = [P, ctypes.POINTER(ServeStats)]
         L.avs_serve_destroy.argtypes = [P]
+        L.avs_serve_plan.argtypes = [I64, I32, I32, ctypes.POINTER(I32), ctypes.POINTER(I32), ctypes.POINTER(I32)]
         for nm in ("avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d"):
             getattr(L, nm).argtypes = [P, I32, P, P]
         for nm in ("avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d"):
@@ -607,6 +609,18 @@ def estimate_bytes(n, tile, precision="fp32", count=0):
     _check(lib().avs_estimate_bytes(int(n), int(tile), _prec(precision), int(count), ctypes.byref(b)),
            "avs_estimate_bytes")
     return b.value
+
+
+def serve_plan(n, dtype, tile=0):
+    """(tile, precision mode name, batched) the serving loop uses for a request
+    of order n and numpy dtype (float32 / float64); a served result equals
+    my_CU_svdval(A, tile, precision=mode) bit for bit."""
+    t, p, bt = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
+    dt = 1 if np.dtype(dtype) == np.float64 else 0
+    _check(lib().avs_serve_plan(int(n), dt, int(tile), ctypes.byref(t), ctypes.byref(p), ctypes.byref(bt)),
+           "avs_serve_plan")
+    name = {v: k for k, v in PREC.items()}[p.value]
+    return t.value, name, bool(bt.value)
 
 
 class Server:

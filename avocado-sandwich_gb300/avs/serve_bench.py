@@ -12,13 +12,15 @@ itself costs no generation time.
 2. Load-latency curve: Poisson arrivals at fractions of that capacity (50% and
    80% by default, sustainable loads), p50/p99 latency per load.
 3. Parity of every request of every stream: bit-identical to the single-matrix
-   call on the same matrix (the tile rule of the server), and within tolerance
+   call on the same matrix (the server's tile and precision mode for it,
+   avs_serve_plan), and within tolerance
    (FP32 1e-5, FP64 1e-12, normwise) of an FP64 reference for that matrix --
    LAPACK dgesdd for n <= 2048, the prescribed spectrum for the geometric
    matrices, and the plain FP64 GPU path (itself held to 1e-12 of known spectra
    in the tests) for the larger Gaussian ones.
 4. One-at-a-time baselines: the same request list through blocking calls, in
-   each request's precision and through the plain FP64 path.
+   each request's precision (the server's mode for it) and through the plain
+   FP64 path.
 
     python -m avs.serve_bench --requests 200
 """
@@ -67,11 +69,11 @@ def make_pool(reqs, device="cuda"):
     return pool
 
 
-def rule_tile(n):
-    t = 32 if n <= 256 else (64 if n <= 1024 else 128)
-    while t > 16 and (n % t or t > n):
-        t //= 2
-    return t
+def single_call(a, handle):
+    """The single-matrix call a served request equals: the server's tile and
+    precision mode for its order and type (avs_serve_plan)."""
+    tile, mode, _ = avs.serve_plan(a.shape[0], a.dtype)
+    return avs.my_CU_svdval(a, tile, precision=mode, handle=handle)
 
 
 def errors(got, ref):
@@ -117,14 +119,14 @@ def references(pool):
     h = avs.Handle()
     for key, (a, exact) in pool.items():
         n = key[0]
-        single[key] = avs.my_CU_svdval(a, rule_tile(n), handle=h)
+        single[key] = single_call(a, h)
         if exact is not None:
             ref[key], src[key] = exact, "prescribed spectrum"
         elif n <= 2048:
             ref[key], src[key] = sl.svdvals(a.astype(np.float64), check_finite=False), "LAPACK dgesdd"
         else:
-            ref[key] = avs.my_CU_svdval(np.asfortranarray(a.astype(np.float64)), rule_tile(n), precision="fp64",
-                                        handle=h)
+            ref[key] = avs.my_CU_svdval(np.asfortranarray(a.astype(np.float64)), avs.serve_plan(n, np.float64)[0],
+                                        precision="fp64", handle=h)
             src[key] = "plain FP64 GPU path"
     h.close()
     return single, ref, src
@@ -191,16 +193,16 @@ def run(requests=120, rate=None, seed=7, workers=4, one_at_a_time=True, max_orde
         sub = reqs[::max(1, baseline_every)]
         h = avs.Handle()
         for key in sorted(set(sub)):
-            avs.my_CU_svdval(pool[key][0], rule_tile(key[0]), handle=h)
+            single_call(pool[key][0], h)
         t0 = time.perf_counter()
         for key in sub:
-            avs.my_CU_svdval(pool[key][0], rule_tile(key[0]), handle=h)
+            single_call(pool[key][0], h)
         res["one_at_a_time_svds_per_s"] = len(sub) / (time.perf_counter() - t0)
         wide = {k: np.asfortranarray(v[0].astype(np.float64)) for k, v in pool.items() if k in set(sub)}
         t_sum = 0.0
         for key in sub:
             t0 = time.perf_counter()
-            avs.my_CU_svdval(wide[key], rule_tile(key[0]), handle=h)
+            avs.my_CU_svdval(wide[key], avs.serve_plan(key[0], np.float64)[0], precision="fp64", handle=h)
             t_sum += time.perf_counter() - t0
         res["one_at_a_time_plain_fp64_svds_per_s"] = len(sub) / t_sum
         res["one_at_a_time_sample"] = "%d of the %d requests" % (len(sub), len(reqs))

@@ -138,7 +138,8 @@ int resolve_precision(int32_t requested, bool input_double) {
 // Storage element size of the stage-1 tiles for a precision mode (0 = mode not provided).
 size_t storage_elem(int prec) {
     switch (prec) {
-        case AVS_PREC_FP64: return 8;
+        case AVS_PREC_FP64:
+        case AVS_PREC_FP64X2: return 8;
         case AVS_PREC_FP32:
         case AVS_PREC_TF32:
         case AVS_PREC_TF32X3:
@@ -169,6 +170,9 @@ bool fp64_stages(int prec, const avs_opts *opts) {
     if (opts && (opts->flags & AVS_FLAG_DF64_STAGES)) return false;
     return prec == AVS_PREC_FP64;
 }
+
+// FP64 tiles with the full-T trailing updates in double-float (AVS_PREC_FP64X2).
+inline bool df_update_of(int prec) { return prec == AVS_PREC_FP64X2; }
 
 double bisect_tol(bool f64, const avs_opts *opts) {
     if (opts && opts->bisect_rel_tol > 0) return opts->bisect_rel_tol;
@@ -261,7 +265,8 @@ int run_stages23(avs_handle *h, const Layout &L, int64_t n, int b, const S *W, i
 // (type TI, leading dimension lds) on the device; sigma_out (type TO) on the device.
 template <typename S, typename TI, typename TO>
 int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src, int64_t lds, TO *sigma_out,
-                 double rel_tol, bool fp64_stages, int tc_split, cudaStream_t s, avs_report *rep) {
+                 double rel_tol, bool fp64_stages, int tc_split, cudaStream_t s, avs_report *rep,
+                 bool df_update = false) {
     int rc;
     int64_t launches = 0;
     S *W = reinterpret_cast<S *>(ws_at(h, L.off_w));
@@ -278,6 +283,7 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
     w1.tfull = ws_at(h, L.off_tfull);
     w1.tc_split = tc_split;
     w1.tc_ws = tc_split ? ws_at(h, L.off_tc) : nullptr;
+    w1.df_update = df_update ? 1 : 0;
     int upd_used = 0;
     if (tc_split && rep) {
         const int pairs = (int)(2 * (n / b));
@@ -338,7 +344,8 @@ int svdvals_dev(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, 
     if ((rc = ensure_ws(h, L.total)) != AVS_SUCCESS) return rc;
     const bool f64 = fp64_stages(prec, opts);
     const double tol = bisect_tol(f64, opts);
-    if (elem == 8) return run_pipeline<double, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, 0, s, rep);
+    if (elem == 8)
+        return run_pipeline<double, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, 0, s, rep, df_update_of(prec));
     return run_pipeline<float, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, split, s, rep);
 }
 
@@ -394,7 +401,7 @@ int svdvals_host(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile,
     const double tol = bisect_tol(f64, opts);
     T *dout = reinterpret_cast<T *>(ws_at(h, L.off_out));
     if (elem == 8)
-        rc = run_pipeline<double, T, T>(h, L, n, tile, stage, n, dout, tol, f64, 0, s, &r2);
+        rc = run_pipeline<double, T, T>(h, L, n, tile, stage, n, dout, tol, f64, 0, s, &r2, df_update_of(prec));
     else
         rc = run_pipeline<float, T, T>(h, L, n, tile, stage, n, dout, tol, f64, split, s, &r2);
     if (rc == AVS_SUCCESS) {
@@ -547,6 +554,7 @@ int blockbidiag_dev(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *dA, 
     w1.tc_ws = split ? ws_at(h, L.off_tc) : nullptr;
     w1.tau_q_out = dtq;
     w1.tau_p_out = dtp;
+    w1.df_update = (sizeof(T) == 8 && df_update_of(prec)) ? 1 : 0;
     int64_t launches = 0;
     AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
     // the stage-1 kernels move 16-byte vectors: a matrix that is not 16-byte
@@ -1070,7 +1078,7 @@ int ensure_pinned(avs_handle *h, size_t bytes) {
 // T = float: FP32 tiles, double-float stages 2-3; T = double: FP64 throughout.
 template <typename T>
 int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cnt, double tol, cudaStream_t s,
-                   const cudaEvent_t *ev, int64_t *launches, bool bidiag) {
+                   const cudaEvent_t *ev, int64_t *launches, bool bidiag, bool df_update) {
     char *base = reinterpret_cast<char *>(h->bws);
     T *W = reinterpret_cast<T *>(base + L.W);
     const T *const *src = reinterpret_cast<const T *const *>(base + L.ptrs);
@@ -1095,6 +1103,7 @@ int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cn
     w1.sTblk = (nt + 1) * (b / 16) * 256;
     w1.sTfull = (nt + 1) * (int64_t)b * b;
     w1.sFlags = 2 * nt + 4;
+    w1.df_update = (sizeof(T) == 8 && df_update) ? 1 : 0;
     int rc = stage1_ge2bnd<T>(W, n, n, b, w1, s, launches);
     if (rc != AVS_SUCCESS) return rc;
     AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[1], s, cudaEventRecordExternal));
@@ -1212,6 +1221,8 @@ static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const in
         AVS_CUDA_TRY(cudaEventRecord(h->ev[4], reinterpret_cast<cudaStream_t>(opts->stream)));
         AVS_CUDA_TRY(cudaStreamWaitEvent(s, h->ev[4], 0));
     }
+    // FP64 groups: AVS_PREC_FP64X2 takes the double-float trailing updates
+    const bool dfu = sizeof(T) == 8 && opts && df_update_of(opts->precision);
     const double tol = bisect_tol(sizeof(T) == 8, opts);
     // pinned layout: one status word per group (16 ints apart), then the pointer tables
     int *h_status = reinterpret_cast<int *>(h->pinned);
@@ -1235,14 +1246,14 @@ static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const in
         }
         AVS_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(h->bws) + L.ptrs, tab, sizeof(void *) * 4 * cnt,
                                      cudaMemcpyHostToDevice, s));
-        const auto key = std::make_tuple(gn, gb, cnt, (bidiag ? 1 : 0) + (sizeof(T) == 8 ? 2 : 0));
+        const auto key = std::make_tuple(gn, gb, cnt, (bidiag ? 1 : 0) + (sizeof(T) == 8 ? 2 : 0) + (dfu ? 4 : 0));
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
             avs_handle::Graph gr;
             for (cudaEvent_t &e : gr.ev) AVS_CUDA_TRY(cudaEventCreate(&e));
             cudaGraph_t graph;
             AVS_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            rc = group_launches<T>(h, L, gn, gb, cnt, tol, s, gr.ev, &gr.kernels, bidiag);
+            rc = group_launches<T>(h, L, gn, gb, cnt, tol, s, gr.ev, &gr.kernels, bidiag, dfu);
             cudaError_t ce = cudaStreamEndCapture(s, &graph);
             if (rc == AVS_SUCCESS && ce == cudaSuccess) {
                 ce = cudaGraphInstantiate(&gr.exec, graph, 0);
@@ -1287,7 +1298,7 @@ static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const in
         }
         rep->kernel_launches = launches;
         rep->workspace_bytes = (int64_t)h->bws_bytes;
-        rep->precision = sizeof(T) == 8 ? AVS_PREC_FP64 : AVS_PREC_FP32;
+        rep->precision = sizeof(T) == 8 ? (dfu ? AVS_PREC_FP64X2 : AVS_PREC_FP64) : AVS_PREC_FP32;
         rep->status = rc;
     }
     return rc;

@@ -97,6 +97,7 @@ struct Stage1Work {
     void *tfull;      // [nt][b*b] of T: full compact-WY factors (tiles 128, 256)
     void *tc_ws = nullptr;  // tensor-core update buffers (stage1_tc_bytes), FP32 tiles
     int tc_split = 0;       // operand format of the tensor-core update (tc::Fmt); 0: SIMT update
+    int df_update = 0;      // FP64 tiles: full-T trailing updates in double-float on the FP32 pipe
     // optional timing of the tensor-core updates: event pairs (start, end) per
     // half-step, at most ev_cap pairs; *ev_used counts the pairs recorded
     cudaEvent_t *ev_pairs = nullptr;

@@ -88,4 +88,23 @@ __device__ __forceinline__ df64 df_sqrt(df64 a) {
 __device__ __forceinline__ bool df_lt0(df64 a) { return a.hi < 0.0f || (a.hi == 0.0f && a.lo < 0.0f); }
 __device__ __forceinline__ float df_abs_hi(df64 a) { return fabsf(a.hi); }
 
+// A double-float value with arithmetic operators: the compute type of kernels
+// templated on their element type when the data is stored in FP64 (converted
+// on load, ~48 of the 53 significant bits kept, FP32's exponent range; rounded
+// back to FP64 on store).
+struct dfx {
+    df64 v;
+    __device__ __forceinline__ dfx() {}
+    __device__ __forceinline__ dfx(int x) : v(df64{(float)x, 0.0f}) {}
+    __device__ __forceinline__ explicit dfx(double x) : v(df_from_double(x)) {}
+    __device__ __forceinline__ explicit dfx(df64 x) : v(x) {}
+    __device__ __forceinline__ explicit operator double() const { return df_to_double(v); }
+};
+__device__ __forceinline__ dfx operator+(dfx a, dfx b) { return dfx(df_add(a.v, b.v)); }
+__device__ __forceinline__ dfx operator-(dfx a, dfx b) { return dfx(df_sub(a.v, b.v)); }
+__device__ __forceinline__ dfx operator*(dfx a, dfx b) { return dfx(df_mul(a.v, b.v)); }
+__device__ __forceinline__ dfx operator-(dfx a) { return dfx(df_neg(a.v)); }
+__device__ __forceinline__ dfx &operator+=(dfx &a, dfx b) { return a = a + b; }
+__device__ __forceinline__ dfx &operator-=(dfx &a, dfx b) { return a = a - b; }
+
 }  // namespace avs

@@ -20,6 +20,7 @@
 #include <algorithm>
 
 #include "avs_common.cuh"
+#include "df64.cuh"
 
 namespace avs {
 namespace {
@@ -194,7 +195,9 @@ struct UCfg {
     static_assert(CB >= 1 && PER >= 1, "update configuration");
 };
 
-template <typename T, int LAYOUT, int B, int WW = WCfg<T>::W>
+// T: element type in memory; CT: compute type (T itself, or dfx for FP64 data
+// updated in double-float arithmetic).
+template <typename T, int LAYOUT, int B, int WW = WCfg<T>::W, typename CT = T>
 struct UpdCtx {
     using C = UCfg<T, B, WW>;
     View<T, LAYOUT> V;
@@ -202,17 +205,15 @@ struct UpdCtx {
     int64_t row0, col0;
     bool geqrt;
     // element (k, m) of the A operand for source s (chunk-relative k0 added by caller)
-    __device__ __forceinline__ T a_elem(int s, int k, int m) const {
+    __device__ __forceinline__ CT a_elem(int s, int k, int m) const {
         if (s == kVrows) {  // V(k, m): Z = V^T ...
-            T v = V(row0 + k, col0 + m);
-            if (geqrt) v = (k == m) ? T(1) : (k > m ? v : T(0));
-            return v;
+            if (geqrt && k <= m) return (k == m) ? CT(1) : CT(0);
+            return CT(V(row0 + k, col0 + m));
         } else if (s == kTrows) {  // T(k, m)
-            return Tf[k + (size_t)m * B];
+            return CT(Tf[k + (size_t)m * B]);
         } else {  // V(m, k): ... -= V W
-            T v = V(row0 + m, col0 + k);
-            if (geqrt) v = (m == k) ? T(1) : (m > k ? v : T(0));
-            return v;
+            if (geqrt && m <= k) return (m == k) ? CT(1) : CT(0);
+            return CT(V(row0 + m, col0 + k));
         }
     }
     // chunk element index -> (k, m), coalesced for the source
@@ -223,14 +224,15 @@ struct UpdCtx {
 };
 
 // acc (+|-)= A(k, m)^T-view ... : acc[i][j] += sign * sum_k A(k, m0+i) * Bop(k, c0+j)
-template <typename T, int LAYOUT, int B, int WW = WCfg<T>::W>
-__device__ __forceinline__ void gemm(const UpdCtx<T, LAYOUT, B, WW> &ctx, int src, T (&acc)[8][UCfg<T, B, WW>::CB],
-                                     const T *Bop, T *chunk0, T *chunk1, bool neg) {
+template <typename T, int LAYOUT, int B, int WW = WCfg<T>::W, typename CT = T>
+__device__ __forceinline__ void gemm(const UpdCtx<T, LAYOUT, B, WW, CT> &ctx, int src,
+                                     CT (&acc)[8][UCfg<T, B, WW>::CB], const CT *Bop, CT *chunk0, CT *chunk1,
+                                     bool neg) {
     using C = UCfg<T, B, WW>;
     const int tid = threadIdx.x;
     const int m0 = tid % C::TM;  // rows m0 + TM*i: consecutive lanes, consecutive rows
     const int c0 = (tid / C::TM) * C::CB;
-    T pre[C::PER];
+    CT pre[C::PER];
     // prologue: chunk 0 into registers
 #pragma unroll
     for (int e = 0; e < C::PER; ++e) {
@@ -238,10 +240,10 @@ __device__ __forceinline__ void gemm(const UpdCtx<T, LAYOUT, B, WW> &ctx, int sr
         ctx.map(src, tid + e * kWNT, k, m);
         pre[e] = ctx.a_elem(src, k, m);
     }
-    T *bufs[2] = {chunk0, chunk1};
+    CT *bufs[2] = {chunk0, chunk1};
     const int nchunk = B / C::KC;
     for (int ch = 0; ch < nchunk; ++ch) {
-        T *cur = bufs[ch & 1];
+        CT *cur = bufs[ch & 1];
 #pragma unroll
         for (int e = 0; e < C::PER; ++e) {
             int k, m;
@@ -261,7 +263,7 @@ __device__ __forceinline__ void gemm(const UpdCtx<T, LAYOUT, B, WW> &ctx, int sr
         const int k0 = ch * C::KC;
 #pragma unroll 4
         for (int k = 0; k < C::KC; ++k) {
-            T av[8], bv[C::CB];
+            CT av[8], bv[C::CB];
 #pragma unroll
             for (int i = 0; i < 8; ++i) av[i] = cur[k * C::LDC + m0 + C::TM * i];
 #pragma unroll
@@ -282,14 +284,15 @@ __device__ __forceinline__ void gemm(const UpdCtx<T, LAYOUT, B, WW> &ctx, int sr
     __syncthreads();
 }
 
-template <typename T, int LAYOUT, int B>
+template <typename T, int LAYOUT, int B, typename CT = T>
 __global__ void __launch_bounds__(kWNT) update_full_kernel(UpdFullArgs args) {
     using C = UCfg<T, B>;
+    static_assert(sizeof(CT) == sizeof(T), "compute type of the element's size");
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *Top = reinterpret_cast<T *>(smem_raw);      // LDB x W, column-major
-    T *Buf = Top + (size_t)C::LDB * C::W;          // LDB x W
-    T *ch0 = Buf + (size_t)C::LDB * C::W;          // KC x LDC
-    T *ch1 = ch0 + (size_t)C::KC * C::LDC;
+    CT *Top = reinterpret_cast<CT *>(smem_raw);    // LDB x W, column-major
+    CT *Buf = Top + (size_t)C::LDB * C::W;         // LDB x W
+    CT *ch0 = Buf + (size_t)C::LDB * C::W;         // KC x LDC
+    CT *ch1 = ch0 + (size_t)C::KC * C::LDC;
     const int tid = threadIdx.x;
     const int64_t j0 = (int64_t)(args.pc + 1) * B + (int64_t)blockIdx.x * C::W;
     const int wc = (int)min((int64_t)C::W, args.n - j0);
@@ -300,45 +303,45 @@ __global__ void __launch_bounds__(kWNT) update_full_kernel(UpdFullArgs args) {
     const int m0 = tid % C::TM;
     const int c0 = (tid / C::TM) * C::CB;
 
-    auto load_strip = [&](T *S, int64_t r0) {
+    auto load_strip = [&](CT *S, int64_t r0) {
         for (int idx = tid; idx < B * C::W; idx += kWNT) {
             int t, c;
             if (LAYOUT == 0) { t = idx % B; c = idx / B; } else { c = idx % C::W; t = idx / C::W; }
-            S[t + c * C::LDB] = (c < wc) ? V(r0 + t, j0 + c) : T(0);
+            S[t + c * C::LDB] = (c < wc) ? CT(V(r0 + t, j0 + c)) : CT(0);
         }
     };
-    auto store_strip = [&](const T *S, int64_t r0) {
+    auto store_strip = [&](const CT *S, int64_t r0) {
         for (int idx = tid; idx < B * C::W; idx += kWNT) {
             int t, c;
             if (LAYOUT == 0) { t = idx % B; c = idx / B; } else { c = idx % C::W; t = idx / C::W; }
-            if (c < wc) V(r0 + t, j0 + c) = S[t + c * C::LDB];
+            if (c < wc) V(r0 + t, j0 + c) = (T)S[t + c * C::LDB];
         }
     };
-    auto get_blk = [&](const T *S, T (&r)[8][C::CB]) {
+    auto get_blk = [&](const CT *S, CT (&r)[8][C::CB]) {
 #pragma unroll
         for (int i = 0; i < 8; ++i)
 #pragma unroll
             for (int j = 0; j < C::CB; ++j) r[i][j] = S[(m0 + C::TM * i) + (c0 + j) * C::LDB];
     };
-    auto put_blk = [&](T *S, const T (&r)[8][C::CB]) {
+    auto put_blk = [&](CT *S, const CT (&r)[8][C::CB]) {
 #pragma unroll
         for (int i = 0; i < 8; ++i)
 #pragma unroll
             for (int j = 0; j < C::CB; ++j) S[(m0 + C::TM * i) + (c0 + j) * C::LDB] = r[i][j];
     };
-    auto zero = [&](T (&r)[8][C::CB]) {
+    auto zero = [&](CT (&r)[8][C::CB]) {
 #pragma unroll
         for (int i = 0; i < 8; ++i)
 #pragma unroll
-            for (int j = 0; j < C::CB; ++j) r[i][j] = T(0);
+            for (int j = 0; j < C::CB; ++j) r[i][j] = CT(0);
     };
 
     load_strip(Top, top0);
     __syncthreads();
-    T acc[8][C::CB];
-    T apr[8][C::CB];
+    CT acc[8][C::CB];
+    CT apr[8][C::CB];
     for (int p = args.first_role; p < args.P; ++p) {
-        UpdCtx<T, LAYOUT, B> ctx;
+        UpdCtx<T, LAYOUT, B, WCfg<T>::W, CT> ctx;
         ctx.V = V;
         ctx.Tf = reinterpret_cast<const T *>(args.tfull) + zb * args.sTfull + (size_t)p * B * B;
         ctx.row0 = (int64_t)(args.pr + p) * B;
@@ -346,30 +349,30 @@ __global__ void __launch_bounds__(kWNT) update_full_kernel(UpdFullArgs args) {
         ctx.geqrt = (p == 0);
         if (p == 0) {
             zero(acc);
-            gemm<T, LAYOUT, B>(ctx, kVrows, acc, Top, ch0, ch1, false);   // Z = Y0^T Top
+            gemm(ctx, kVrows, acc, Top, ch0, ch1, false);   // Z = Y0^T Top
             put_blk(Buf, acc);
             __syncthreads();
             zero(acc);
-            gemm<T, LAYOUT, B>(ctx, kTrows, acc, Buf, ch0, ch1, false);   // W = T0^T Z
+            gemm(ctx, kTrows, acc, Buf, ch0, ch1, false);   // W = T0^T Z
             put_blk(Buf, acc);
             __syncthreads();
             get_blk(Top, acc);
-            gemm<T, LAYOUT, B>(ctx, kVcols, acc, Buf, ch0, ch1, true);    // Top -= Y0 W
+            gemm(ctx, kVcols, acc, Buf, ch0, ch1, true);    // Top -= Y0 W
             put_blk(Top, acc);
             __syncthreads();
         } else {
             load_strip(Buf, ctx.row0);
             __syncthreads();
             get_blk(Top, acc);
-            gemm<T, LAYOUT, B>(ctx, kVrows, acc, Buf, ch0, ch1, false);   // Z = Top + V^T A_p
+            gemm(ctx, kVrows, acc, Buf, ch0, ch1, false);   // Z = Top + V^T A_p
             get_blk(Buf, apr);
             __syncthreads();
             put_blk(Buf, acc);
             __syncthreads();
             zero(acc);
-            gemm<T, LAYOUT, B>(ctx, kTrows, acc, Buf, ch0, ch1, false);   // W = T^T Z
+            gemm(ctx, kTrows, acc, Buf, ch0, ch1, false);   // W = T^T Z
             {
-                T tp[8][C::CB];
+                CT tp[8][C::CB];
                 get_blk(Top, tp);
 #pragma unroll
                 for (int i = 0; i < 8; ++i)
@@ -379,7 +382,7 @@ __global__ void __launch_bounds__(kWNT) update_full_kernel(UpdFullArgs args) {
             }
             put_blk(Buf, acc);
             __syncthreads();
-            gemm<T, LAYOUT, B>(ctx, kVcols, apr, Buf, ch0, ch1, true);    // A_p -= V W
+            gemm(ctx, kVcols, apr, Buf, ch0, ch1, true);    // A_p -= V W
             put_blk(Buf, apr);
             __syncthreads();
             store_strip(Buf, ctx.row0);
@@ -395,14 +398,14 @@ size_t upd_full_smem() {
     return sizeof(T) * (2 * (size_t)C::LDB * C::W + 2 * (size_t)C::KC * C::LDC);
 }
 
-template <typename T, int LAYOUT, int B>
+template <typename T, int LAYOUT, int B, typename CT = T>
 int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const Stage1Work &w, cudaStream_t s,
                     int first_role) {
     using C = UCfg<T, B>;
     static std::atomic<bool> attr{false};
     const size_t smem = upd_full_smem<T, B>();
     if (!attr) {
-        AVS_CUDA_TRY(cudaFuncSetAttribute(update_full_kernel<T, LAYOUT, B>,
+        AVS_CUDA_TRY(cudaFuncSetAttribute(update_full_kernel<T, LAYOUT, B, CT>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
@@ -410,9 +413,19 @@ int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const 
     if (ncols <= 0) return AVS_SUCCESS;
     UpdFullArgs a{dA, lda, n, B, pr, pc, P, w.tfull, w.sA, w.sTfull, first_role};
     const unsigned gx = (unsigned)((ncols + C::W - 1) / C::W);
-    update_full_kernel<T, LAYOUT, B><<<dim3(gx, w.batch > 0 ? w.batch : 1), kWNT, smem, s>>>(a);
+    update_full_kernel<T, LAYOUT, B, CT><<<dim3(gx, w.batch > 0 ? w.batch : 1), kWNT, smem, s>>>(a);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
+}
+
+// FP64 tiles: the update in FP64, or in double-float when the work asks for it.
+template <typename T, int LAYOUT, int B>
+int launch_upd_full_any(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const Stage1Work &w, cudaStream_t s,
+                        int first_role) {
+    if constexpr (sizeof(T) == 8) {
+        if (w.df_update) return launch_upd_full<T, LAYOUT, B, dfx>(dA, lda, n, pr, pc, P, w, s, first_role);
+    }
+    return launch_upd_full<T, LAYOUT, B>(dA, lda, n, pr, pc, P, w, s, first_role);
 }
 
 template <typename T, int LAYOUT>
@@ -454,12 +467,12 @@ int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr,
     int rc;
     if (layout == 0) {
         if ((rc = launch_tbuild<T, 0>(dA, lda, b, pr, pc, P, w, s, first_role)) != AVS_SUCCESS) return rc;
-        return b == 256 ? launch_upd_full<T, 0, 256>(dA, lda, n, pr, pc, P, w, s, first_role)
-                        : launch_upd_full<T, 0, 128>(dA, lda, n, pr, pc, P, w, s, first_role);
+        return b == 256 ? launch_upd_full_any<T, 0, 256>(dA, lda, n, pr, pc, P, w, s, first_role)
+                        : launch_upd_full_any<T, 0, 128>(dA, lda, n, pr, pc, P, w, s, first_role);
     }
     if ((rc = launch_tbuild<T, 1>(dA, lda, b, pr, pc, P, w, s, first_role)) != AVS_SUCCESS) return rc;
-    return b == 256 ? launch_upd_full<T, 1, 256>(dA, lda, n, pr, pc, P, w, s, first_role)
-                    : launch_upd_full<T, 1, 128>(dA, lda, n, pr, pc, P, w, s, first_role);
+    return b == 256 ? launch_upd_full_any<T, 1, 256>(dA, lda, n, pr, pc, P, w, s, first_role)
+                    : launch_upd_full_any<T, 1, 128>(dA, lda, n, pr, pc, P, w, s, first_role);
 }
 
 template int stage1_update_full<float>(float *, int64_t, int64_t, int, int, int, int, int, const Stage1Work &,

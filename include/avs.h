@@ -68,6 +68,9 @@ extern "C" {
 #define AVS_PREC_TF32X3 4  /* FP32 tiles, split TF32 (3 products) tensor-core updates */
 #define AVS_PREC_BF16 5    /* FP32 tiles, BF16 tensor-core updates, FP32 accumulate */
 #define AVS_PREC_BF16X3 6  /* FP32 tiles, split BF16 (3 products) tensor-core updates */
+#define AVS_PREC_FP64X2 7  /* FP64 tiles and panels; the full compact-WY trailing updates of tiles >= 128
+                              in double-float (two-term split FP32 products) on the FP32 pipe, stages 2
+                              and 3 in double-float: FP64-level accuracy (1e-12) at the FP32 pipe's rate */
 
 /* ---- avs_opts.flags ---------------------------------------------------------
  * Stages 2 and 3 (bulge chase, bisection) run in FP64 for AVS_PREC_FP64 and in
@@ -255,7 +258,8 @@ int avs_bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, doub
  * launch sequence is captured once in a CUDA graph (kept per (n, tile, group
  * size) on the handle) and replayed.  Results of a matrix do not depend on the
  * other matrices of the call.  Precision: FP32 tiles with double-float stages
- * 2 and 3 (the `precision` field of opts is ignored; bisect_rel_tol is used).
+ * 2 and 3 (the `precision` field of opts is ignored; bisect_rel_tol is used;
+ * the Float64 form below takes AVS_PREC_FP64X2).
  * The pointer arrays are host arrays.  The work runs on the handle's stream,
  * after the work queued so far on opts->stream (when given); the call blocks
  * until all values are written.  report->t_total_ms covers all groups. */
@@ -274,7 +278,9 @@ int avs_bidiag_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, con
 /* The same two batched calls for Float64 matrices, FP64 throughout (tiles,
  * updates, bulge chase, bisection; the random-matrix client of RMT/rmt.jl runs
  * gebrd! in Float64, rmt.jl:23,28).  Each matrix's values are bit-identical to
- * those of avs_svdvals_dev_d / the FP64 pipeline on the same matrix. */
+ * those of avs_svdvals_dev_d / the FP64 pipeline on the same matrix.
+ * opts->precision == AVS_PREC_FP64X2 runs the groups' trailing updates in
+ * double-float (values then equal avs_svdvals_dev_d's in that mode). */
 int avs_svdvals_batched_dev_d(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
                               const int32_t *tile, const double *const *dA, double *const *dsigma,
                               const avs_opts *opts, avs_report *report);
@@ -324,7 +330,9 @@ int avs_estimate_bytes(int64_t n, int32_t tile, int32_t precision, int32_t count
  * `workers` execution slots, each with its own handle and CUDA stream, so the
  * work of several requests overlaps on the GPU.  A free slot takes the oldest
  * queued request and every other queued request of the same order and type
- * (up to max_batch) into one batched call (avs_svdvals_batched_dev_s / _d).  Admission is by device
+ * (up to max_batch) into one batched call (avs_svdvals_batched_dev_s / _d);
+ * avs_serve_plan says which precision mode and tile a request gets and
+ * whether it is batched.  Admission is by device
  * memory: a slot starts a group only while the bytes held by all slots stay
  * within hbm_budget_bytes; otherwise it shrinks the group, releases its own
  * cached workspace, or waits until others finish.  Each result equals the
@@ -353,6 +361,14 @@ typedef struct avs_serve_stats {
 } avs_serve_stats;
 
 int avs_serve_create(avs_server **srv, const avs_serve_config *cfg);
+/* How the server runs a request of order n and type dtype (host only, no
+ * device needed): *tile_out (tile 0 = the server's rule), *precision (an
+ * AVS_PREC_* mode: FP32 SIMT updates for FP32 requests below order 2048,
+ * split-BF16 tensor-core updates above, AVS_PREC_FP64X2 for FP64 requests) and
+ * *batched (1: requests of the same order and type share batched calls; 0: the
+ * request runs alone).  A served result equals the single-matrix entry point's
+ * with this tile and precision, bit for bit.  Pointers may be NULL. */
+int avs_serve_plan(int64_t n, int32_t dtype, int32_t tile, int32_t *tile_out, int32_t *precision, int32_t *batched);
 /* Queue one request: n x n column-major A (ld lda) of type dtype in host memory,
  * n values to sigma (same type).  Both buffers must stay valid until the request
  * completes.  tile = 0 picks the tile.  Returns its id in *id. */

@@ -47,6 +47,10 @@ def test_plain_path_n8192_tile128_geometric(avs_mod, torch_cuda):
     a64, sig = workloads.geometric_spectrum(8192, 2, 3, 1e-6, dtype=np.float64, device="cuda")
     s64 = avs_mod.my_CU_svdval(a64, 128).cpu().numpy()
     n64, p64 = errs(s64, sig)
+    sx2 = avs_mod.my_CU_svdval(a64, 128, precision="fp64x2").cpu().numpy()
+    nx2, px2 = errs(sx2, sig)
+    print("n=8192 tile 128: FP64 with double-float updates (fp64x2) %.2e (per-value %.2e)" % (nx2, px2))
+    assert nx2 < 1e-12
     a32 = a64.float()
     del a64
     s32 = avs_mod.my_CU_svdval(a32, 128).cpu().numpy()

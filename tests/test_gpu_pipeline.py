@@ -220,3 +220,48 @@ def test_tensor_core_modes(avs_mod, torch_cuda, n, b):
     assert rel_err(sb3, lap) < 1e-5
     sb = avs_mod.my_CU_svdval(a, b, precision="bf16")
     assert rel_err(sb, lap) < 5e-2
+
+
+@pytest.mark.parametrize("n,b", [(512, 128), (1024, 128), (1024, 256), (2048, 128), (2048, 256)])
+def test_fp64x2_mode(avs_mod, torch_cuda, n, b):
+    """AVS_PREC_FP64X2: FP64 tiles and panels, the full compact-WY trailing
+    updates in double-float (two-term split FP32 products) and double-float
+    stages 2-3 -- FP64-level accuracy: within 1e-12 (normwise) of LAPACK on
+    Gaussian inputs and of the known spectrum on a graded one; the float32
+    entry point with this mode computes in FP64 tiles too."""
+    from avs import workloads
+    a = workloads.gaussian(n, 77, 1.0 / np.sqrt(n))
+    r = avs_mod.Report()
+    s = avs_mod.my_CU_svdval(a, b, precision="fp64x2", report=r)
+    assert r.precision == 7
+    assert rel_err(s, sl.svdvals(a)) < 1e-12
+    g, sig = workloads.geometric_spectrum(n, 5, 6, 1e-6)
+    assert rel_err(avs_mod.my_CU_svdval(g, b, precision="fp64x2"), sig) < 1e-12
+    a32 = a.astype(np.float32)
+    s32 = avs_mod.my_CU_svdval(a32, b, precision="fp64x2")
+    assert s32.dtype == np.float32
+    assert rel_err(s32, sl.svdvals(a32.astype(np.float64))) < 1e-6
+
+
+def test_fp64x2_batched_equals_single(avs_mod, torch_cuda):
+    """Batched FP64 groups in AVS_PREC_FP64X2 equal the single call in that
+    mode bit for bit."""
+    rng = np.random.default_rng(55)
+    hosts = [rng.standard_normal((n, n)) / np.sqrt(n) for n in (256, 512, 256, 512)]
+    devs = [avs_mod.to_device(a) for a in hosts]
+    import ctypes
+    h = avs_mod.default_handle()
+    cnt = len(devs)
+    outs = [torch_cuda.empty(d.shape[0], dtype=torch_cuda.float64, device=d.device) for d in devs]
+    nn = (ctypes.c_int64 * cnt)(*[d.shape[0] for d in devs])
+    tt = (ctypes.c_int32 * cnt)(*([128] * cnt))
+    pa = (ctypes.c_void_p * cnt)(*[d.data_ptr() for d in devs])
+    ps = (ctypes.c_void_p * cnt)(*[o.data_ptr() for o in outs])
+    o = avs_mod.Opts(7, 0, 0.0, None)
+    r = avs_mod.Report()
+    rc = avs_mod.lib().avs_svdvals_batched_dev_d(h.ptr, cnt, nn, nn, tt, pa, ps, ctypes.byref(o), ctypes.byref(r))
+    assert rc == 0 and r.precision == 7
+    for a, d, out in zip(hosts, devs, outs):
+        single = avs_mod.my_CU_svdval(d, 128, precision="fp64x2").cpu().numpy()
+        assert np.array_equal(out.cpu().numpy(), single)
+        assert rel_err(single, sl.svdvals(a)) < 1e-12

@@ -18,11 +18,11 @@ def torch_cuda():
     return torch
 
 
-def rule_tile(n):
-    t = 32 if n <= 256 else (64 if n <= 1024 else 128)
-    while t > 16 and (n % t or t > n):
-        t //= 2
-    return t
+def single_call(avs_mod, a):
+    """The single-matrix call that a served request must equal bit for bit:
+    the server's tile and precision mode for its order and type."""
+    tile, mode, _ = avs_mod.serve_plan(a.shape[0], a.dtype)
+    return avs_mod.my_CU_svdval(a, tile, precision=mode)
 
 
 def _requests(seed):
@@ -42,7 +42,7 @@ def test_serving_mix_equals_solo(avs_mod, torch_cuda):
     assert st["batches"] <= len(mats) and 0 < st["p50_ms"] <= st["p99_ms"] <= st["max_ms"]
     for a, (sig, lat) in zip(mats, outs):
         assert lat > 0
-        single = avs_mod.my_CU_svdval(a, rule_tile(a.shape[0]))
+        single = single_call(avs_mod, a)
         assert np.array_equal(sig, single)
         tol = 1e-12 if a.dtype == np.float64 else 1e-5
         ref = sl.svdvals(a.astype(np.float64))
@@ -64,7 +64,7 @@ def test_serving_groups_same_order(avs_mod, torch_cuda):
         st = srv.stats()
     assert st["completed"] == 64 and st["mean_batch"] > 2
     for a, s in zip(mats, outs):
-        assert np.array_equal(s, avs_mod.my_CU_svdval(a, 32))
+        assert np.array_equal(s, single_call(avs_mod, a))
 
 
 def test_serving_admission_budget(avs_mod, torch_cuda):
@@ -77,7 +77,7 @@ def test_serving_admission_budget(avs_mod, torch_cuda):
         ids = [srv.submit(a) for a in mats]
         for i, a in zip(ids, mats):
             s, _ = srv.wait(i)
-            assert np.array_equal(s, avs_mod.my_CU_svdval(a, 32))
+            assert np.array_equal(s, single_call(avs_mod, a))
         bid = srv.submit(big)
         with pytest.raises(avs_mod.AvsError) as ei:
             srv.wait(bid)
@@ -122,7 +122,7 @@ def test_serving_stream_four_slots_bitwise(avs_mod, torch_cuda):
     SMs with those of others -- the situation in which a cross-CTA ordering
     mistake shows up."""
     mats = _stream(21)
-    singles = [avs_mod.my_CU_svdval(a, rule_tile(a.shape[0])) for a in mats]
+    singles = [single_call(avs_mod, a) for a in mats]
     for a, s in zip(mats, singles):
         tol = 1e-12 if a.dtype == np.float64 else 1e-5
         ref = sl.svdvals(a.astype(np.float64))
@@ -169,3 +169,23 @@ def test_concurrent_single_calls_bitwise(avs_mod, torch_cuda):
         for h in handles:
             h.close()
     assert not errors, errors
+
+
+def test_serving_plan_and_large_requests(avs_mod, torch_cuda):
+    """The server's plan (avs_serve_plan): FP32 requests of order >= 2048 run
+    alone with split-BF16 tensor-core updates, smaller FP32 ones in batched
+    FP32 groups, FP64 requests in batched groups with double-float updates;
+    results equal the single call in the planned mode and stay within the
+    FP32 (1e-5) / FP64 (1e-12) tolerance of LAPACK."""
+    assert avs_mod.serve_plan(2048, np.float32) == (128, "bf16x3", False)
+    assert avs_mod.serve_plan(512, np.float32) == (64, "fp32", True)
+    assert avs_mod.serve_plan(2048, np.float64) == (128, "fp64x2", True)
+    rng = np.random.default_rng(41)
+    mats = [(rng.standard_normal((2048, 2048)) / 45.0).astype(dt) for dt in (np.float32, np.float64, np.float64)]
+    with avs_mod.Server(workers=2) as srv:
+        outs = [srv.wait(srv.submit(a))[0] for a in mats]
+    for a, o in zip(mats, outs):
+        assert np.array_equal(o, single_call(avs_mod, a))
+        ref = sl.svdvals(a.astype(np.float64))
+        tol = 1e-12 if a.dtype == np.float64 else 1e-5
+        assert np.max(np.abs(o - ref)) / ref[0] < tol
