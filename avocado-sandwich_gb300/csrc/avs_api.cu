@@ -1075,10 +1075,12 @@ int ensure_pinned(avs_handle *h, size_t bytes) {
 }
 
 // The launches of one group (gather .. scatter), captured once per shape.
-// T = float: FP32 tiles, double-float stages 2-3; T = double: FP64 throughout.
+// T = float: FP32 tiles, double-float stages 2-3.  T = double: FP64 tiles;
+// stages 2-3 in FP64 (f64_stages) or in double-float (AVS_PREC_FP64X2, as its
+// single call).
 template <typename T>
 int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cnt, double tol, cudaStream_t s,
-                   const cudaEvent_t *ev, int64_t *launches, bool bidiag, bool df_update) {
+                   const cudaEvent_t *ev, int64_t *launches, bool bidiag, bool df_update, bool f64_stages) {
     char *base = reinterpret_cast<char *>(h->bws);
     T *W = reinterpret_cast<T *>(base + L.W);
     const T *const *src = reinterpret_cast<const T *const *>(base + L.ptrs);
@@ -1112,12 +1114,13 @@ int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cn
     w2.err = err;
     double *dd = reinterpret_cast<double *>(base + L.d);
     double *de = reinterpret_cast<double *>(base + L.e);
-    if constexpr (sizeof(T) == 4)
+    if constexpr (sizeof(T) == 8)
+        if (f64_stages)
+            rc = stage2_chase_fp64_batched(W, n, b, cnt, reinterpret_cast<double *>(base + L.ab), 3 * (int64_t)b, dd,
+                                           de, w2, s, h->num_sms, launches);
+    if (sizeof(T) == 4 || !f64_stages)
         rc = stage2_chase_df_batched(W, n, b, cnt, reinterpret_cast<float2 *>(base + L.ab), 3 * (int64_t)b, dd, de,
                                      w2, s, h->num_sms, launches);
-    else
-        rc = stage2_chase_fp64_batched(W, n, b, cnt, reinterpret_cast<double *>(base + L.ab), 3 * (int64_t)b, dd, de,
-                                       w2, s, h->num_sms, launches);
     if (rc != AVS_SUCCESS) return rc;
     AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal));
     if (bidiag) {  // the bidiagonal itself: d and e of each matrix to the caller's vectors
@@ -1129,11 +1132,11 @@ int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cn
         return AVS_SUCCESS;
     }
     double *sig = reinterpret_cast<double *>(base + L.sig);
-    if constexpr (sizeof(T) == 4)
+    if (sizeof(T) == 8 && f64_stages)
+        rc = stage3_bisect_batched(dd, de, n, cnt, tol, sig, reinterpret_cast<double *>(base + L.scr), s, launches);
+    else
         rc = stage3_bisect_df_batched(dd, de, n, cnt, tol, sig, reinterpret_cast<double *>(base + L.scr),
                                       reinterpret_cast<float2 *>(base + L.pairs), s, launches);
-    else
-        rc = stage3_bisect_batched(dd, de, n, cnt, tol, sig, reinterpret_cast<double *>(base + L.scr), s, launches);
     if (rc != AVS_SUCCESS) return rc;
     scatter_kernel<T><<<(unsigned)std::min<int64_t>((n * cnt + 255) / 256, 8192), 256, 0, s>>>(sig, dst, n, cnt);
     AVS_CUDA_TRY(cudaGetLastError());
@@ -1221,9 +1224,11 @@ static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const in
         AVS_CUDA_TRY(cudaEventRecord(h->ev[4], reinterpret_cast<cudaStream_t>(opts->stream)));
         AVS_CUDA_TRY(cudaStreamWaitEvent(s, h->ev[4], 0));
     }
-    // FP64 groups: AVS_PREC_FP64X2 takes the double-float trailing updates
+    // FP64 groups: AVS_PREC_FP64X2 takes the double-float trailing updates and
+    // double-float stages 2-3 (FP64 stages on AVS_FLAG_FP64_STAGES), as its single call
     const bool dfu = sizeof(T) == 8 && opts && df_update_of(opts->precision);
-    const double tol = bisect_tol(sizeof(T) == 8, opts);
+    const bool f64s = sizeof(T) == 8 && (!dfu || (opts->flags & AVS_FLAG_FP64_STAGES));
+    const double tol = bisect_tol(f64s, opts);
     // pinned layout: one status word per group (16 ints apart), then the pointer tables
     int *h_status = reinterpret_cast<int *>(h->pinned);
     void **tab = reinterpret_cast<void **>(h_status + 16 * (groups.size() + 1));
@@ -1246,14 +1251,15 @@ static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const in
         }
         AVS_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(h->bws) + L.ptrs, tab, sizeof(void *) * 4 * cnt,
                                      cudaMemcpyHostToDevice, s));
-        const auto key = std::make_tuple(gn, gb, cnt, (bidiag ? 1 : 0) + (sizeof(T) == 8 ? 2 : 0) + (dfu ? 4 : 0));
+        const auto key = std::make_tuple(gn, gb, cnt,
+                                         (bidiag ? 1 : 0) + (sizeof(T) == 8 ? 2 : 0) + (dfu ? 4 : 0) + (f64s ? 8 : 0));
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
             avs_handle::Graph gr;
             for (cudaEvent_t &e : gr.ev) AVS_CUDA_TRY(cudaEventCreate(&e));
             cudaGraph_t graph;
             AVS_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            rc = group_launches<T>(h, L, gn, gb, cnt, tol, s, gr.ev, &gr.kernels, bidiag, dfu);
+            rc = group_launches<T>(h, L, gn, gb, cnt, tol, s, gr.ev, &gr.kernels, bidiag, dfu, f64s);
             cudaError_t ce = cudaStreamEndCapture(s, &graph);
             if (rc == AVS_SUCCESS && ce == cudaSuccess) {
                 ce = cudaGraphInstantiate(&gr.exec, graph, 0);

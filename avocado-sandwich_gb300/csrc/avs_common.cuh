@@ -198,6 +198,9 @@ int stage2_chase_df(const T *dW, int64_t n, int64_t ldw, int bw, float2 *dAB, in
                     const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
 int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
                             double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
+// FP64 tiles, double-float chase (the batched groups of AVS_PREC_FP64X2)
+int stage2_chase_df_batched(const double *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
+                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
 int stage3_bisect_df_batched(const double *dd, const double *de, int64_t n, int batch, double rel_tol,
                              double *dsigma, double *dscratch, float2 *dpairs, cudaStream_t s, int64_t *launches);
 int stage2_chase_fp64_batched(const double *dW, int64_t n, int bw, int batch, double *dAB, int64_t ldab, double *dd,

@@ -872,6 +872,11 @@ int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float
     return stage2_chase_batched<float, df64>(dW, n, bw, batch, dAB, ldab, dd, de, w, s, num_sms, launches);
 }
 
+int stage2_chase_df_batched(const double *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
+                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches) {
+    return stage2_chase_batched<double, df64>(dW, n, bw, batch, dAB, ldab, dd, de, w, s, num_sms, launches);
+}
+
 int stage2_chase_fp64_batched(const double *dW, int64_t n, int bw, int batch, double *dAB, int64_t ldab, double *dd,
                               double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches) {
     return stage2_chase_batched<double, double>(dW, n, bw, batch, dAB, ldab, dd, de, w, s, num_sms, launches);

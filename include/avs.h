@@ -279,8 +279,10 @@ int avs_bidiag_batched_dev_s(avs_handle *h, int32_t count, const int64_t *n, con
  * updates, bulge chase, bisection; the random-matrix client of RMT/rmt.jl runs
  * gebrd! in Float64, rmt.jl:23,28).  Each matrix's values are bit-identical to
  * those of avs_svdvals_dev_d / the FP64 pipeline on the same matrix.
- * opts->precision == AVS_PREC_FP64X2 runs the groups' trailing updates in
- * double-float (values then equal avs_svdvals_dev_d's in that mode). */
+ * opts->precision == AVS_PREC_FP64X2 runs the groups' trailing updates, bulge
+ * chase and bisection in double-float, as avs_svdvals_dev_d does in that mode
+ * (values then equal its values bit for bit; AVS_FLAG_FP64_STAGES keeps FP64
+ * stages 2-3). */
 int avs_svdvals_batched_dev_d(avs_handle *h, int32_t count, const int64_t *n, const int64_t *lda,
                               const int32_t *tile, const double *const *dA, double *const *dsigma,
                               const avs_opts *opts, avs_report *report);
