@@ -30,7 +30,7 @@ import numpy as np
 
 __all__ = [
     "AvsError", "Handle", "lib", "library_path", "my_CU_svdval", "svdvals", "Blockbidiag", "extract_band",
-    "bidiagonalize", "diag_lapack", "geqrt_tile", "tsqrt_tile", "to_device", "from_device", "PREC",
+    "bidiagonalize", "band_reduce", "diag_lapack", "geqrt_tile", "tsqrt_tile", "to_device", "from_device", "PREC",
     "NOT_IMPLEMENTED", "EXPORTED_SYMBOLS", "Report", "svdvals_batched", "autotune_tile", "Server", "tiled_QR",
     "estimate_bytes",
 ]
@@ -48,6 +48,7 @@ EXPORTED_SYMBOLS = [
     "avs_blockbidiag_dev_s", "avs_blockbidiag_dev_d", "avs_blockbidiag_tau_dev_s", "avs_blockbidiag_tau_dev_d",
     "avs_extract_band_dev_s", "avs_extract_band_dev_d",
     "avs_band_to_bidiag_dev", "avs_bidiag_svals_dev", "avs_bidiag_svals_noalloc",
+    "avs_band_reduce_dev_s", "avs_band_reduce_dev_d",
     "avs_geqrt_tile_dev_s", "avs_geqrt_tile_dev_d", "avs_tsqrt_tile_dev_s", "avs_tsqrt_tile_dev_d",
     "avs_svdvals_batched_dev_s", "avs_bidiag_batched_dev_s", "avs_svdvals_batched_dev_d", "avs_bidiag_batched_dev_d", "avs_autotune_tile", "avs_trim", "avs_workspace_bytes", "avs_estimate_bytes",
     "avs_geqrf_dev_s", "avs_geqrf_dev_d",
@@ -126,6 +127,8 @@ def lib():
         for nm in ("avs_extract_band_dev_s", "avs_extract_band_dev_d"):
             getattr(L, nm).argtypes = [P, I64, I64, I32, P, P, I64]
         L.avs_band_to_bidiag_dev.argtypes = [P, I64, I32, P, I64, P, P, RP]
+        for nm in ("avs_band_reduce_dev_s", "avs_band_reduce_dev_d"):
+            getattr(L, nm).argtypes = [P, I64, I32, I32, P, I64, RP]
         L.avs_bidiag_svals_dev.argtypes = [P, I64, P, P, P, ctypes.c_double, RP]
         L.avs_bidiag_svals_noalloc.argtypes = [I64, P, P, P, ctypes.c_double, P]
         for sfx in ("s", "d"):
@@ -561,6 +564,24 @@ def bidiagonalize(B, bw, handle=None):
                                       ctypes.c_void_p(d.data_ptr()), ctypes.c_void_p(e.data_ptr()), ctypes.byref(r))
     _check(rc, "avs_band_to_bidiag_dev")
     return d, e[: max(n - 1, 0)]
+
+
+def band_reduce(B, bw, tbw, handle=None):
+    """One stage of the hierarchical band reduction (the reference's bidiag!
+    with factor bw / tbw, BRD/src/bulgechasing2.jl:22-45) in place on a CUDA
+    tensor holding a dense column-major n x n upper band matrix of width bw
+    (FP32 or FP64; the arithmetic follows the type): on return it holds a band
+    of width tbw with the same singular values.  Returns the report."""
+    import torch
+    h = handle or default_handle()
+    n = B.shape[0]
+    if B.dim() != 2 or B.shape[0] != B.shape[1] or not B.is_contiguous():
+        raise ValueError("a contiguous square matrix is needed")
+    fn = lib().avs_band_reduce_dev_d if B.dtype == torch.float64 else lib().avs_band_reduce_dev_s
+    r = Report()
+    rc = fn(h.ptr, n, int(bw), int(tbw), ctypes.c_void_p(B.data_ptr()), n, ctypes.byref(r))
+    _check(rc, "avs_band_reduce_dev")
+    return r
 
 
 def diag_lapack(d, e, rel_tol=0.0, handle=None):

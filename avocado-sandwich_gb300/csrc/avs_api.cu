@@ -57,6 +57,7 @@ struct avs_handle {
 namespace {
 
 constexpr int kMaxTile = 256;
+constexpr int kMaxNarrowBand = 32;  // widest intermediate band of the hierarchical chase
 
 inline size_t align_up(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -64,8 +65,8 @@ inline bool is_pow2(int64_t x) { return x > 0 && (x & (x - 1)) == 0; }
 
 // Workspace carve-up for one call.
 struct Layout {
-    size_t off_w, off_stage, off_tau, off_tblk, off_flags1, off_flags2, off_err, off_ab, off_d, off_e, off_sig,
-        off_scr, off_out, off_tfull, off_pairs, off_tc, total;
+    size_t off_w, off_stage, off_tau, off_tblk, off_flags1, off_flags2, off_err, off_ab, off_ab2, off_d, off_e,
+        off_sig, off_scr, off_out, off_tfull, off_pairs, off_tc, total;
     int64_t ldab;
 };
 
@@ -92,6 +93,8 @@ Layout make_layout(int64_t n, int b, size_t elem, size_t stage_elem, int tc_fmt 
     L.ldab = 3 * (int64_t)b;
     L.off_ab = o;
     o = align_up(o + sizeof(double) * (size_t)L.ldab * (size_t)n);
+    L.off_ab2 = o;  // the narrow band of the hierarchical chase (width <= kMaxNarrowBand)
+    o = align_up(o + sizeof(double) * (size_t)(3 * kMaxNarrowBand) * (size_t)n);
     L.off_d = o;
     o = align_up(o + sizeof(double) * (size_t)n);
     L.off_e = o;
@@ -174,6 +177,17 @@ bool fp64_stages(int prec, const avs_opts *opts) {
 // FP64 tiles with the full-T trailing updates in double-float (AVS_PREC_FP64X2).
 inline bool df_update_of(int prec) { return prec == AVS_PREC_FP64X2; }
 
+inline int flags_of(const avs_opts *opts) { return opts ? opts->flags : 0; }
+
+// Stage 2 of a single call: the band of width b goes to width
+// narrow_band_of(b, flags) by the blocked band reduction, then to the
+// bidiagonal by the element chase (0: the element chase from width b).
+int narrow_band_of(int b, int flags) {
+    if (flags & AVS_FLAG_ONE_STAGE_CHASE) return 0;
+    const int t = (flags & AVS_FLAG_BAND32) ? 32 : 16;
+    return band_stage_supported(b, t) ? t : 0;
+}
+
 double bisect_tol(bool f64, const avs_opts *opts) {
     if (opts && opts->bisect_rel_tol > 0) return opts->bisect_rel_tol;
     return f64 ? 2.0 * DBL_EPSILON : 4e-14;
@@ -228,7 +242,7 @@ float ev_ms(cudaEvent_t a, cudaEvent_t b) {
 // the stages and ev[3] at the end; the status word is the layout's.
 template <typename S, typename TO>
 int run_stages23(avs_handle *h, const Layout &L, int64_t n, int b, const S *W, int64_t ldw, TO *sigma_out,
-                 double rel_tol, bool fp64_stages, cudaStream_t s, int64_t *launches) {
+                 double rel_tol, bool fp64_stages, cudaStream_t s, int64_t *launches, int flags) {
     int rc;
     int *err = reinterpret_cast<int *>(ws_at(h, L.off_err));
     double *AB = reinterpret_cast<double *>(ws_at(h, L.off_ab));
@@ -237,7 +251,19 @@ int run_stages23(avs_handle *h, const Layout &L, int64_t n, int b, const S *W, i
     Stage2Work w2;
     w2.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags2));
     w2.err = err;
-    if (fp64_stages) {
+    const int tbw = narrow_band_of(b, flags);
+    if (tbw > 0 && sizeof(S) == 8 && fp64_stages) {
+        if ((rc = stage2_chase_hier_fp64(reinterpret_cast<const double *>(W), n, ldw, b, tbw, AB,
+                                         reinterpret_cast<double *>(ws_at(h, L.off_ab2)), dd, de, w2, s, h->num_sms,
+                                         launches)) != AVS_SUCCESS)
+            return rc;
+    } else if (tbw > 0 && sizeof(S) == 4 && !fp64_stages) {
+        // the FP32 band of width b in the first half of AB (3b x n floats)
+        if ((rc = stage2_chase_hier_df(reinterpret_cast<const float *>(W), n, ldw, b, tbw,
+                                       reinterpret_cast<float *>(AB), reinterpret_cast<float2 *>(ws_at(h, L.off_ab2)),
+                                       dd, de, w2, s, h->num_sms, launches)) != AVS_SUCCESS)
+            return rc;
+    } else if (fp64_stages) {
         if ((rc = extract_band_compact<S>(W, n, ldw, b, AB, L.ldab, s)) != AVS_SUCCESS) return rc;
         ++*launches;
         if ((rc = stage2_chase(AB, n, b, L.ldab, dd, de, w2, s, h->num_sms, launches)) != AVS_SUCCESS) return rc;
@@ -266,7 +292,7 @@ int run_stages23(avs_handle *h, const Layout &L, int64_t n, int b, const S *W, i
 template <typename S, typename TI, typename TO>
 int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src, int64_t lds, TO *sigma_out,
                  double rel_tol, bool fp64_stages, int tc_split, cudaStream_t s, avs_report *rep,
-                 bool df_update = false) {
+                 bool df_update = false, int chase_flags = 0) {
     int rc;
     int64_t launches = 0;
     S *W = reinterpret_cast<S *>(ws_at(h, L.off_w));
@@ -303,7 +329,8 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
     AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
     {
         NvtxRange r("avs stages 2-3: chase, bisection");
-        if ((rc = run_stages23<S, TO>(h, L, n, b, W, n, sigma_out, rel_tol, fp64_stages, s, &launches)) !=
+        if ((rc = run_stages23<S, TO>(h, L, n, b, W, n, sigma_out, rel_tol, fp64_stages, s, &launches,
+                                      chase_flags)) !=
             AVS_SUCCESS)
             return rc;
     }
@@ -345,8 +372,10 @@ int svdvals_dev(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, 
     const bool f64 = fp64_stages(prec, opts);
     const double tol = bisect_tol(f64, opts);
     if (elem == 8)
-        return run_pipeline<double, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, 0, s, rep, df_update_of(prec));
-    return run_pipeline<float, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, split, s, rep);
+        return run_pipeline<double, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, 0, s, rep, df_update_of(prec),
+                                            flags_of(opts));
+    return run_pipeline<float, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, split, s, rep, false,
+                                       flags_of(opts));
 }
 
 // Page-locks a caller's host range for the duration of a call (large ranges
@@ -401,9 +430,11 @@ int svdvals_host(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile,
     const double tol = bisect_tol(f64, opts);
     T *dout = reinterpret_cast<T *>(ws_at(h, L.off_out));
     if (elem == 8)
-        rc = run_pipeline<double, T, T>(h, L, n, tile, stage, n, dout, tol, f64, 0, s, &r2, df_update_of(prec));
+        rc = run_pipeline<double, T, T>(h, L, n, tile, stage, n, dout, tol, f64, 0, s, &r2, df_update_of(prec),
+                                        flags_of(opts));
     else
-        rc = run_pipeline<float, T, T>(h, L, n, tile, stage, n, dout, tol, f64, split, s, &r2);
+        rc = run_pipeline<float, T, T>(h, L, n, tile, stage, n, dout, tol, f64, split, s, &r2, false,
+                                       flags_of(opts));
     if (rc == AVS_SUCCESS) {
         AVS_CUDA_TRY(cudaMemcpyAsync(sigma, dout, sizeof(T) * (size_t)n, cudaMemcpyDeviceToHost, s));
         AVS_CUDA_TRY(cudaEventRecord(h->ev[5], s));
@@ -770,7 +801,7 @@ int ooc_call(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *A, T *sigma
             const bool f64 = fp64_stages(prec, opts);
             T *dout = reinterpret_cast<T *>(ws_at(h, L.off_out));
             if ((r = run_stages23<T, T>(h, L, n, tile, band + tile, tile, dout, bisect_tol(f64, opts), f64, s,
-                                        &launches)) != AVS_SUCCESS)
+                                        &launches, opts ? opts->flags : 0)) != AVS_SUCCESS)
                 return r;
             AVS_CUDA_TRY(cudaMemcpyAsync(sigma, dout, sizeof(T) * (size_t)n, cudaMemcpyDeviceToHost, s));
         } else {
@@ -798,6 +829,46 @@ int ooc_call(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *A, T *sigma
     return rc;
 }
 }  // namespace
+
+template <typename R>
+int band_reduce_dev(avs_handle *h, int64_t n, int32_t bw, int32_t tbw, R *dB, int64_t ldb, avs_report *rep) {
+    if (!h) return -1;
+    if (n < 0) return -2;
+    if (bw < 1) return -3;
+    if (tbw < 1 || tbw >= bw) return -4;
+    if (n > 0 && !dB) return -5;
+    if (ldb < (n > 1 ? n : 1)) return -6;
+    if (rep) std::memset(rep, 0, sizeof(*rep));
+    if (!band_stage_supported(bw, tbw)) return AVS_ERR_UNSUPPORTED;
+    if (n == 0) return AVS_SUCCESS;
+    AVS_CUDA_TRY(cudaSetDevice(h->device));
+    const Layout L = make_layout(n, 1, 8, 0);
+    const int64_t ldab = 3 * (int64_t)bw;
+    const size_t ab_off = align_up(L.total);
+    const size_t fl_off = align_up(ab_off + sizeof(R) * (size_t)ldab * (size_t)n);
+    int rc = ensure_ws(h, align_up(fl_off + sizeof(int) * (size_t)(n + 4)));
+    if (rc != AVS_SUCCESS) return rc;
+    cudaStream_t s = h->stream;
+    int *err = reinterpret_cast<int *>(ws_at(h, L.off_err));
+    AVS_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+    R *AB = reinterpret_cast<R *>(ws_at(h, ab_off));
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[0], s));
+    if ((rc = dense_to_band<R, R>(dB, n, ldb, 0, bw, AB, ldab, 0, 1, s)) != AVS_SUCCESS) return rc;
+    Stage2Work w2;
+    w2.flags = reinterpret_cast<int *>(ws_at(h, fl_off));
+    w2.err = err;
+    if ((rc = band_stage<R>(AB, n, bw, tbw, ldab, w2, s, h->num_sms, 1, 0, 0)) != AVS_SUCCESS) return rc;
+    AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
+    if ((rc = band_to_dense<R>(AB, n, bw, ldab, dB, ldb, s)) != AVS_SUCCESS) return rc;
+    AVS_CUDA_TRY(cudaMemcpyAsync(h->h_err, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    rc = finish_status(h, s);
+    if (rep) {
+        rep->t_stage2_ms = rep->t_total_ms = ev_ms(h->ev[0], h->ev[1]);
+        rep->kernel_launches = 3;
+        rep->status = rc;
+    }
+    return rc;
+}
 
 extern "C" {
 
@@ -930,6 +1001,15 @@ int avs_band_to_bidiag_dev(avs_handle *h, int64_t n, int32_t bw, const double *d
         rep->status = rc;
     }
     return rc;
+}
+
+int avs_band_reduce_dev_s(avs_handle *h, int64_t n, int32_t bw, int32_t tbw, float *dB, int64_t ldb,
+                          avs_report *rep) {
+    return band_reduce_dev<float>(h, n, bw, tbw, dB, ldb, rep);
+}
+int avs_band_reduce_dev_d(avs_handle *h, int64_t n, int32_t bw, int32_t tbw, double *dB, int64_t ldb,
+                          avs_report *rep) {
+    return band_reduce_dev<double>(h, n, bw, tbw, dB, ldb, rep);
 }
 
 int avs_bidiag_svals_dev(avs_handle *h, int64_t n, const double *dd, const double *de, double *dsigma,

@@ -201,6 +201,29 @@ int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float
 // FP64 tiles, double-float chase (the batched groups of AVS_PREC_FP64X2)
 int stage2_chase_df_batched(const double *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
                             double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
+// Blocked band reduction bw -> tbw (stage2_band.cu), on a compact band
+// (A(r, c) at dAB[(r - c + 2bw - 1) + c * ldab], ldab >= 3 bw)
+template <typename R>
+int band_stage(R *dAB, int64_t n, int bw, int tbw, int64_t ldab, const Stage2Work &w, cudaStream_t s, int num_sms,
+               int batch, int64_t sAB, int64_t sDone);
+bool band_stage_supported(int bw, int tbw);
+template <typename TI, typename R>
+int dense_to_band(const TI *dA, int64_t n, int64_t lda, int64_t sA, int bw, R *dAB, int64_t ldab, int64_t sAB,
+                  int batch, cudaStream_t s);
+template <typename R, typename St>
+int band_to_band(const R *dAB1, int64_t n, int bw1, int64_t ldab1, int64_t sAB1, int bw2, St *dAB2, int64_t ldab2,
+                 int64_t sAB2, int batch, cudaStream_t s);
+template <typename R>
+int band_to_dense(const R *dAB, int64_t n, int bw, int64_t ldab, R *dA, int64_t lda, cudaStream_t s);
+// Hierarchical stage 2 (stage2_chase.cu): the band of width bw of dW
+// (W[r + c*ldw]) -> width tbw by the blocked band reduction, then the element
+// chase tbw -> 1; d and e out.  _df: FP32 band reduction, double-float chase;
+// _fp64: FP64 throughout.  dAB1 holds 3 bw x n elements, dAB2 3 tbw x n.
+int stage2_chase_hier_df(const float *dW, int64_t n, int64_t ldw, int bw, int tbw, float *dAB1, float2 *dAB2,
+                         double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
+int stage2_chase_hier_fp64(const double *dW, int64_t n, int64_t ldw, int bw, int tbw, double *dAB1, double *dAB2,
+                           double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms,
+                           int64_t *launches);
 int stage3_bisect_df_batched(const double *dd, const double *de, int64_t n, int batch, double rel_tol,
                              double *dsigma, double *dscratch, float2 *dpairs, cudaStream_t s, int64_t *launches);
 int stage2_chase_fp64_batched(const double *dW, int64_t n, int bw, int batch, double *dAB, int64_t ldab, double *dd,

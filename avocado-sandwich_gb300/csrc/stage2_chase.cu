@@ -773,6 +773,48 @@ template int stage2_chase_df<float>(const float *, int64_t, int64_t, int, float2
 template int stage2_chase_df<double>(const double *, int64_t, int64_t, int, float2 *, int64_t, double *, double *,
                                      const Stage2Work &, cudaStream_t, int, int64_t *);
 
+// Hierarchical stage 2: the blocked band reduction bw -> tbw (stage2_band.cu;
+// the reference's bidiag! stage, BRD/src/bulgechasing2.jl:22-45), then the
+// element chase tbw -> 1 above.
+int stage2_chase_hier_df(const float *dW, int64_t n, int64_t ldw, int bw, int tbw, float *dAB1, float2 *dAB2,
+                         double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches) {
+    const int64_t ldab1 = 3 * (int64_t)bw, ldab2 = 3 * (int64_t)tbw;
+    int rc;
+    if ((rc = dense_to_band<float, float>(dW, n, ldw, 0, bw, dAB1, ldab1, 0, 1, s)) != AVS_SUCCESS) return rc;
+    if ((rc = band_stage<float>(dAB1, n, bw, tbw, ldab1, w, s, num_sms, 1, 0, 0)) != AVS_SUCCESS) return rc;
+    if ((rc = band_to_band<float, float2>(dAB1, n, bw, ldab1, 0, tbw, dAB2, ldab2, 0, 1, s)) != AVS_SUCCESS)
+        return rc;
+    if (n >= 2) {
+        AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(n + 1), s));
+        if ((rc = launch_chase_any<df64>(dAB2, n, tbw, ldab2, w, s, num_sms)) != AVS_SUCCESS) return rc;
+    }
+    const int nb = (int)std::min<int64_t>((n + 255) / 256, 4096);
+    bidiag_out_df_kernel<<<nb > 0 ? nb : 1, 256, 0, s>>>(dAB2, n, tbw, ldab2, dd, de);
+    AVS_CUDA_TRY(cudaGetLastError());
+    if (launches) *launches += 5;
+    return AVS_SUCCESS;
+}
+
+int stage2_chase_hier_fp64(const double *dW, int64_t n, int64_t ldw, int bw, int tbw, double *dAB1, double *dAB2,
+                           double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms,
+                           int64_t *launches) {
+    const int64_t ldab1 = 3 * (int64_t)bw, ldab2 = 3 * (int64_t)tbw;
+    int rc;
+    if ((rc = dense_to_band<double, double>(dW, n, ldw, 0, bw, dAB1, ldab1, 0, 1, s)) != AVS_SUCCESS) return rc;
+    if ((rc = band_stage<double>(dAB1, n, bw, tbw, ldab1, w, s, num_sms, 1, 0, 0)) != AVS_SUCCESS) return rc;
+    if ((rc = band_to_band<double, double>(dAB1, n, bw, ldab1, 0, tbw, dAB2, ldab2, 0, 1, s)) != AVS_SUCCESS)
+        return rc;
+    if (n >= 2) {
+        AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(n + 1), s));
+        if ((rc = launch_chase_any<double>(dAB2, n, tbw, ldab2, w, s, num_sms)) != AVS_SUCCESS) return rc;
+    }
+    const int nb = (int)std::min<int64_t>((n + 255) / 256, 4096);
+    bidiag_out_kernel<<<nb > 0 ? nb : 1, 256, 0, s>>>(dAB2, n, tbw, ldab2, dd, de);
+    AVS_CUDA_TRY(cudaGetLastError());
+    if (launches) *launches += 5;
+    return AVS_SUCCESS;
+}
+
 // ---------------------------------------------------------------------------
 // Batched chase: `batch` matrices of the same order n and band width bw,
 // stacked at stride n*n (tiles) / ldab*n (band) / n+1 (flags) / n (d, e).

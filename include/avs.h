@@ -79,6 +79,15 @@ extern "C" {
  * override that choice. */
 #define AVS_FLAG_FP64_STAGES 1
 #define AVS_FLAG_DF64_STAGES 2
+/* Stage 2 of the single-matrix calls is hierarchical by default, as the
+ * reference's bidiag! (BRD/src/bulgechasing2.jl:22-45) and the halving of
+ * bidiagonalize (KAbasedSVD/src/bulgechasing.jl:33-42): a blocked band
+ * reduction (T rows per sweep, compact-WY applies; FP32 arithmetic in the
+ * FP32-class modes, FP64 with FP64 stages) takes the band of width tile (64,
+ * 128 or 256) to width 16, then the element chase takes it to the
+ * bidiagonal.  These flags change that: */
+#define AVS_FLAG_ONE_STAGE_CHASE 4 /* element chase straight from the band of width tile */
+#define AVS_FLAG_BAND32 8          /* intermediate band of width 32 instead of 16 */
 
 typedef struct avs_handle avs_handle;
 
@@ -225,6 +234,20 @@ int avs_extract_band_dev_d(avs_handle *h, int64_t n, int64_t lda, int32_t bw, co
  * (n-1) of an upper bidiagonal with the same singular values (FP64 bulge chase). */
 int avs_band_to_bidiag_dev(avs_handle *h, int64_t n, int32_t bw, const double *dB, int64_t ldb, double *dd,
                            double *de, avs_report *report);
+/* One stage of the hierarchical band reduction: bidiag! with factor bw / tbw
+ * (BRD/src/bulgechasing2.jl:22-45; LQ_QMUL / QR_QMUL, :4-20).  The upper band
+ * 0 <= j - i <= bw of the dense n x n matrix dB (leading dimension ldb;
+ * entries outside it are ignored) is reduced to an upper band of width tbw
+ * with the same singular values; dB receives every entry of the working band
+ * storage (rows j-2bw+1 .. j+bw-1 of column j; zero outside width tbw on
+ * return) and zeros elsewhere.  (bw, tbw) in {(256, 32), (256, 16), (128, 32),
+ * (128, 16), (64, 16)}, other pairs AVS_ERR_UNSUPPORTED.  _s: FP32 arithmetic,
+ * _d: FP64. */
+int avs_band_reduce_dev_s(avs_handle *h, int64_t n, int32_t bw, int32_t tbw, float *dB, int64_t ldb,
+                          avs_report *report);
+int avs_band_reduce_dev_d(avs_handle *h, int64_t n, int32_t bw, int32_t tbw, double *dB, int64_t ldb,
+                          avs_report *report);
+
 /* diag_lapack / LAPACK.bdsdc!('U','N',d,e) (bulgechasing.jl:50-53): singular
  * values of the upper bidiagonal, descending, by FP64 bisection on the
  * Golub-Kahan tridiagonal.  rel_tol as avs_opts.bisect_rel_tol. */

@@ -64,6 +64,31 @@ def _lq_qmul(a, r0, r1, c0, c1, n, ts):
     a[r0 - 1:re, c0 - 1:c1] = ll
 
 
+def stage(a, cbw, tbw, kernelsizeinit=32, iters=None):
+    """One stage of bidiag! (the body of its ``while cbw > 1`` loop) on a copy
+    of the dense upper band matrix a (FP64): band cbw -> band tbw with ts =
+    tbw; returns the copy.  ``iters`` as in ``bidiag``; None runs every kernel
+    to the end (4 n)."""
+    a = np.array(a, dtype=np.float64)
+    n = a.shape[1]
+    last = 4 * n if iters is None else int(iters)
+    ts = tbw
+    kernelsize = max(4, math.ceil(kernelsizeinit / tbw))
+    for sweeprow in range(1, n - 1 - ts + 1, kernelsize * ts):
+        for it in range(0, last + 1):
+            active = False
+            for kernelidx in range(1, kernelsize + 1):
+                row = sweeprow + kernelidx * ts + cbw * (it + 1 - 2 * kernelidx)
+                if it >= 2 * kernelidx - 2 and row < n:
+                    active = True
+                    rowstart = row + cbw - tbw if it == 2 * kernelidx - 2 else row
+                    _lq_qmul(a, rowstart, row + 2 * cbw - 1, row + cbw, row + 2 * cbw - 1, n, ts)
+                    _qr_qmul(a, row + cbw, row + 2 * cbw - 1, row + cbw, row + 3 * cbw - 1, n, ts)
+            if not active and it > 2 * kernelsize:
+                break
+    return a
+
+
 def bidiag(a, bandwidth, factor=4, kernelsizeinit=32, iters=None):
     """bidiag! on a copy of the dense upper band matrix a (FP64); returns it.
 
