@@ -255,22 +255,25 @@ int run_stages23(avs_handle *h, const Layout &L, int64_t n, int b, const S *W, i
     if (tbw > 0 && sizeof(S) == 8 && fp64_stages) {
         if ((rc = stage2_chase_hier_fp64(reinterpret_cast<const double *>(W), n, ldw, b, tbw, AB,
                                          reinterpret_cast<double *>(ws_at(h, L.off_ab2)), dd, de, w2, s, h->num_sms,
-                                         launches)) != AVS_SUCCESS)
+                                         launches, !(flags & AVS_FLAG_CLUSTER_CHASE))) != AVS_SUCCESS)
             return rc;
     } else if (tbw > 0 && sizeof(S) == 4 && !fp64_stages) {
         // the FP32 band of width b in the first half of AB (3b x n floats)
         if ((rc = stage2_chase_hier_df(reinterpret_cast<const float *>(W), n, ldw, b, tbw,
                                        reinterpret_cast<float *>(AB), reinterpret_cast<float2 *>(ws_at(h, L.off_ab2)),
-                                       dd, de, w2, s, h->num_sms, launches)) != AVS_SUCCESS)
+                                       dd, de, w2, s, h->num_sms, launches, !(flags & AVS_FLAG_CLUSTER_CHASE))) !=
+            AVS_SUCCESS)
             return rc;
     } else if (fp64_stages) {
         if ((rc = extract_band_compact<S>(W, n, ldw, b, AB, L.ldab, s)) != AVS_SUCCESS) return rc;
         ++*launches;
-        if ((rc = stage2_chase(AB, n, b, L.ldab, dd, de, w2, s, h->num_sms, launches)) != AVS_SUCCESS) return rc;
+        if ((rc = stage2_chase(AB, n, b, L.ldab, dd, de, w2, s, h->num_sms, launches,
+                               !(flags & AVS_FLAG_CLUSTER_CHASE))) != AVS_SUCCESS)
+            return rc;
     } else {
         // the FP64 band buffer holds the float2 band (same size)
         if ((rc = stage2_chase_df<S>(W, n, ldw, b, reinterpret_cast<float2 *>(AB), L.ldab, dd, de, w2, s,
-                                     h->num_sms, launches)) != AVS_SUCCESS)
+                                     h->num_sms, launches, !(flags & AVS_FLAG_CLUSTER_CHASE))) != AVS_SUCCESS)
             return rc;
     }
     AVS_CUDA_TRY(cudaEventRecord(h->ev[2], s));

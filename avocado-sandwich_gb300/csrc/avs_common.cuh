@@ -14,6 +14,7 @@ enum DeviceError : int {
     kDevOk = 0,
     kDevTimeout = 1,   // a bounded spin on a progress flag ran out
     kDevNonfinite = 2, // NaN/Inf met while generating a reflector
+    kDevInternal = 3,  // a kernel found its own bookkeeping inconsistent
 };
 
 // Upper bound on the spin iterations of any dependency wait.  Each iteration
@@ -189,13 +190,14 @@ struct Stage2Work {
     int *flags;  // ticket (1) + done (n) ; reset per launch
     int *err;
 };
+// window: bands 8/16/32 by the shared-memory window kernel (ldab == 3 bw)
 int stage2_chase(double *dAB, int64_t n, int bw, int64_t ldab, double *dd, double *de, const Stage2Work &w,
-                 cudaStream_t s, int num_sms, int64_t *launches);
+                 cudaStream_t s, int num_sms, int64_t *launches, bool window = false);
 int stage2_rate(int fp64, int num_sms, double *flops_per_s);
 
 template <typename T>
 int stage2_chase_df(const T *dW, int64_t n, int64_t ldw, int bw, float2 *dAB, int64_t ldab, double *dd, double *de,
-                    const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
+                    const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches, bool window = false);
 int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
                             double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
 // FP64 tiles, double-float chase (the batched groups of AVS_PREC_FP64X2)
@@ -219,11 +221,19 @@ int band_to_dense(const R *dAB, int64_t n, int bw, int64_t ldab, R *dA, int64_t 
 // (W[r + c*ldw]) -> width tbw by the blocked band reduction, then the element
 // chase tbw -> 1; d and e out.  _df: FP32 band reduction, double-float chase;
 // _fp64: FP64 throughout.  dAB1 holds 3 bw x n elements, dAB2 3 tbw x n.
+// window: the narrow band's element chase by the windowed multi-sweep kernel
+// (stage2_window.cu) instead of the cluster kernel.
 int stage2_chase_hier_df(const float *dW, int64_t n, int64_t ldw, int bw, int tbw, float *dAB1, float2 *dAB2,
-                         double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
+                         double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches,
+                         bool window);
 int stage2_chase_hier_fp64(const double *dW, int64_t n, int64_t ldw, int bw, int tbw, double *dAB1, double *dAB2,
                            double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms,
-                           int64_t *launches);
+                           int64_t *launches, bool window);
+// Element chase of a narrow band (width 8, 16 or 32; compact storage, ldab =
+// 3 bw) with G sweeps per CTA in a shared-memory window (stage2_window.cu).
+bool chase_window_supported(int bw);
+int stage2_chase_window_df(float2 *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s, int num_sms);
+int stage2_chase_window_fp64(double *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s, int num_sms);
 int stage3_bisect_df_batched(const double *dd, const double *de, int64_t n, int batch, double rel_tol,
                              double *dsigma, double *dscratch, float2 *dpairs, cudaStream_t s, int64_t *launches);
 int stage2_chase_fp64_batched(const double *dW, int64_t n, int bw, int batch, double *dAB, int64_t ldab, double *dd,

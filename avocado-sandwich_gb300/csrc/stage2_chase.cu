@@ -40,6 +40,7 @@
 #include <cmath>
 
 #include "avs_common.cuh"
+#include "chase_ar.cuh"
 #include "df64.cuh"
 
 namespace cg = cooperative_groups;
@@ -193,99 +194,6 @@ struct ChaseCfg {
     static_assert(W0 >= 1 && CPG % W0 == 0 && G * CPT == NCH, "chase chunking");
 };
 
-// Scalar arithmetic of the chase: FP64, or double-float pairs stored as float2.
-template <typename S>
-struct ChaseAr;
-
-template <>
-struct ChaseAr<double> {
-    using V = double;   // register value
-    using St = double;  // storage element
-    static __device__ __forceinline__ V zero() { return 0.0; }
-    static __device__ __forceinline__ V one() { return 1.0; }
-    static __device__ __forceinline__ V ld(const St *p) { return __ldcg(p); }
-    static __device__ __forceinline__ void st(St *p, V v) { *p = v; }
-    static __device__ __forceinline__ V add(V a, V b) { return a + b; }
-    static __device__ __forceinline__ V sub(V a, V b) { return a - b; }
-    static __device__ __forceinline__ V mul(V a, V b) { return a * b; }
-    static __device__ __forceinline__ V fma(V a, V b, V c) { return ::fma(a, b, c); }
-    static __device__ __forceinline__ V neg(V a) { return -a; }
-    static __device__ __forceinline__ V div(V a, V b) { return a / b; }
-    static __device__ __forceinline__ V sqrt(V a) { return ::sqrt(a); }
-    static __device__ __forceinline__ bool ge0(V a) { return a >= 0.0; }
-    static __device__ __forceinline__ bool gt0(V a) { return a > 0.0; }
-    static __device__ __forceinline__ bool iszero(V a) { return a == 0.0; }
-    static __device__ __forceinline__ V shfl_xor(V a, int o) { return __shfl_xor_sync(0xffffffffu, a, o); }
-    static __device__ __forceinline__ V shfl(V a, int src) { return __shfl_sync(0xffffffffu, a, src); }
-    static __device__ __forceinline__ V rcp(V a) { return 1.0 / a; }
-    static __device__ __forceinline__ double to_double(V a) { return a; }
-    static __device__ __forceinline__ St from_double(double a) { return a; }
-    static __device__ __forceinline__ V v_from_double(double a) { return a; }
-    // dot-product accumulator: plain FMA chain
-    using Acc = double;
-    static __device__ __forceinline__ Acc acc_zero() { return 0.0; }
-    static __device__ __forceinline__ void acc_add(Acc &a, V x, V y) { a = ::fma(x, y, a); }
-    static __device__ __forceinline__ V acc_value(Acc a) { return a; }
-};
-
-template <>
-struct ChaseAr<df64> {
-    using V = df64;
-    using St = float2;
-    static __device__ __forceinline__ V zero() { return df64{0.0f, 0.0f}; }
-    static __device__ __forceinline__ V one() { return df64{1.0f, 0.0f}; }
-    static __device__ __forceinline__ V ld(const St *p) {
-        const float2 v = __ldcg(p);
-        return df64{v.x, v.y};
-    }
-    static __device__ __forceinline__ void st(St *p, V v) { *p = make_float2(v.hi, v.lo); }
-    static __device__ __forceinline__ V add(V a, V b) { return df_add(a, b); }
-    static __device__ __forceinline__ V sub(V a, V b) { return df_sub(a, b); }
-    static __device__ __forceinline__ V mul(V a, V b) { return df_mul(a, b); }
-    static __device__ __forceinline__ V fma(V a, V b, V c) { return df_add(df_mul(a, b), c); }
-    static __device__ __forceinline__ V neg(V a) { return df_neg(a); }
-    static __device__ __forceinline__ V div(V a, V b) { return df_div(a, b); }
-    static __device__ __forceinline__ V sqrt(V a) { return df_sqrt(a); }
-    static __device__ __forceinline__ bool ge0(V a) { return !df_lt0(a); }
-    static __device__ __forceinline__ bool gt0(V a) { return a.hi > 0.0f || (a.hi == 0.0f && a.lo > 0.0f); }
-    static __device__ __forceinline__ bool iszero(V a) { return a.hi == 0.0f && a.lo == 0.0f; }
-    static __device__ __forceinline__ V shfl_xor(V a, int o) {
-        return df64{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)};
-    }
-    static __device__ __forceinline__ V shfl(V a, int src) {
-        return df64{__shfl_sync(0xffffffffu, a.hi, src), __shfl_sync(0xffffffffu, a.lo, src)};
-    }
-    static __device__ __forceinline__ V rcp(V a) { return df_rcp(a); }
-    static __device__ __forceinline__ double to_double(V a) { return df_to_double(a); }
-    // Dot-product accumulator in compensated FP32 (Ogita, Rump & Oishi,
-    // "Accurate sum and dot product", SIAM J. Sci. Comput. 26 (2005), Dot2):
-    // s carries the running FP32 sum, c the exact rounding errors of the sums
-    // and of the double-float products; the loop-carried chain is one add.
-    struct Acc {
-        float s, c;
-    };
-    static __device__ __forceinline__ Acc acc_zero() { return Acc{0.0f, 0.0f}; }
-    static __device__ __forceinline__ void acc_add(Acc &a, V x, V y) {
-        const float p = __fmul_rn(x.hi, y.hi);
-        float ep = __fmaf_rn(x.hi, y.hi, -p);
-        ep = __fmaf_rn(x.hi, y.lo, ep);
-        ep = __fmaf_rn(x.lo, y.hi, ep);
-        const float t = __fadd_rn(a.s, p);
-        const float z = __fsub_rn(t, a.s);
-        const float es = __fadd_rn(__fsub_rn(a.s, __fsub_rn(t, z)), __fsub_rn(p, z));
-        a.s = t;
-        a.c = __fadd_rn(a.c, __fadd_rn(es, ep));
-    }
-    static __device__ __forceinline__ V acc_value(Acc a) { return two_sum(a.s, a.c); }
-    static __device__ __forceinline__ St from_double(double a) {
-        const df64 v = df_from_double(a);
-        return make_float2(v.hi, v.lo);
-    }
-    static __device__ __forceinline__ V v_from_double(double a) { return df_from_double(a); }
-};
-
-__device__ __forceinline__ double st_to_double(double v) { return v; }
-__device__ __forceinline__ double st_to_double(float2 v) { return (double)v.x + (double)v.y; }
 
 template <typename S>
 struct BandT {
@@ -726,8 +634,12 @@ int dense_band_to_compact(const double *dB, int64_t n, int64_t ldb, int bw, doub
 }
 
 int stage2_chase(double *dAB, int64_t n, int bw, int64_t ldab, double *dd, double *de, const Stage2Work &w,
-                 cudaStream_t s, int num_sms, int64_t *launches) {
-    if (n >= 2 && bw >= 2) {
+                 cudaStream_t s, int num_sms, int64_t *launches, bool window) {
+    if (window && chase_window_supported(bw) && ldab == 3 * (int64_t)bw) {
+        const int rc = stage2_chase_window_fp64(dAB, n, bw, w, s, num_sms);
+        if (rc != AVS_SUCCESS) return rc;
+        if (launches) *launches += 1;
+    } else if (n >= 2 && bw >= 2) {
         AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(n + 1), s));
         int rc = launch_chase_any<double>(dAB, n, bw, ldab, w, s, num_sms);
         if (rc == AVS_ERR_UNSUPPORTED) {
@@ -753,11 +665,14 @@ int stage2_chase(double *dAB, int64_t n, int bw, int64_t ldab, double *dd, doubl
 // Double-float chase for the pipeline's FP32-class modes (tiles 16..256).
 template <typename T>
 int stage2_chase_df(const T *dW, int64_t n, int64_t ldw, int bw, float2 *dAB, int64_t ldab, double *dd, double *de,
-                    const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches) {
+                    const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches, bool window) {
     AVS_CUDA_TRY(cudaMemsetAsync(dAB, 0, sizeof(float2) * (size_t)ldab * (size_t)n, s));
     extract_band_df_kernel<T><<<(unsigned)n, 128, 0, s>>>(dW, n, ldw, bw, dAB, ldab);
     AVS_CUDA_TRY(cudaGetLastError());
-    if (n >= 2) {
+    if (window && chase_window_supported(bw) && ldab == 3 * (int64_t)bw) {
+        const int rc = stage2_chase_window_df(dAB, n, bw, w, s, num_sms);
+        if (rc != AVS_SUCCESS) return rc;
+    } else if (n >= 2) {
         AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(n + 1), s));
         const int rc = launch_chase_any<df64>(dAB, n, bw, ldab, w, s, num_sms);
         if (rc != AVS_SUCCESS) return rc;
@@ -769,22 +684,25 @@ int stage2_chase_df(const T *dW, int64_t n, int64_t ldw, int bw, float2 *dAB, in
     return AVS_SUCCESS;
 }
 template int stage2_chase_df<float>(const float *, int64_t, int64_t, int, float2 *, int64_t, double *, double *,
-                                    const Stage2Work &, cudaStream_t, int, int64_t *);
+                                    const Stage2Work &, cudaStream_t, int, int64_t *, bool);
 template int stage2_chase_df<double>(const double *, int64_t, int64_t, int, float2 *, int64_t, double *, double *,
-                                     const Stage2Work &, cudaStream_t, int, int64_t *);
+                                     const Stage2Work &, cudaStream_t, int, int64_t *, bool);
 
 // Hierarchical stage 2: the blocked band reduction bw -> tbw (stage2_band.cu;
 // the reference's bidiag! stage, BRD/src/bulgechasing2.jl:22-45), then the
 // element chase tbw -> 1 above.
 int stage2_chase_hier_df(const float *dW, int64_t n, int64_t ldw, int bw, int tbw, float *dAB1, float2 *dAB2,
-                         double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches) {
+                         double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches,
+                         bool window) {
     const int64_t ldab1 = 3 * (int64_t)bw, ldab2 = 3 * (int64_t)tbw;
     int rc;
     if ((rc = dense_to_band<float, float>(dW, n, ldw, 0, bw, dAB1, ldab1, 0, 1, s)) != AVS_SUCCESS) return rc;
     if ((rc = band_stage<float>(dAB1, n, bw, tbw, ldab1, w, s, num_sms, 1, 0, 0)) != AVS_SUCCESS) return rc;
     if ((rc = band_to_band<float, float2>(dAB1, n, bw, ldab1, 0, tbw, dAB2, ldab2, 0, 1, s)) != AVS_SUCCESS)
         return rc;
-    if (n >= 2) {
+    if (window && chase_window_supported(tbw)) {
+        if ((rc = stage2_chase_window_df(dAB2, n, tbw, w, s, num_sms)) != AVS_SUCCESS) return rc;
+    } else if (n >= 2) {
         AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(n + 1), s));
         if ((rc = launch_chase_any<df64>(dAB2, n, tbw, ldab2, w, s, num_sms)) != AVS_SUCCESS) return rc;
     }
@@ -797,14 +715,16 @@ int stage2_chase_hier_df(const float *dW, int64_t n, int64_t ldw, int bw, int tb
 
 int stage2_chase_hier_fp64(const double *dW, int64_t n, int64_t ldw, int bw, int tbw, double *dAB1, double *dAB2,
                            double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms,
-                           int64_t *launches) {
+                           int64_t *launches, bool window) {
     const int64_t ldab1 = 3 * (int64_t)bw, ldab2 = 3 * (int64_t)tbw;
     int rc;
     if ((rc = dense_to_band<double, double>(dW, n, ldw, 0, bw, dAB1, ldab1, 0, 1, s)) != AVS_SUCCESS) return rc;
     if ((rc = band_stage<double>(dAB1, n, bw, tbw, ldab1, w, s, num_sms, 1, 0, 0)) != AVS_SUCCESS) return rc;
     if ((rc = band_to_band<double, double>(dAB1, n, bw, ldab1, 0, tbw, dAB2, ldab2, 0, 1, s)) != AVS_SUCCESS)
         return rc;
-    if (n >= 2) {
+    if (window && chase_window_supported(tbw)) {
+        if ((rc = stage2_chase_window_fp64(dAB2, n, tbw, w, s, num_sms)) != AVS_SUCCESS) return rc;
+    } else if (n >= 2) {
         AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(n + 1), s));
         if ((rc = launch_chase_any<double>(dAB2, n, tbw, ldab2, w, s, num_sms)) != AVS_SUCCESS) return rc;
     }

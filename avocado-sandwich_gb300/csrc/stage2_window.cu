@@ -1,0 +1,306 @@
+// Stage 2b: element bulge chase of a narrow band (width BW = 8, 16, 32) ->
+// upper bidiagonal, with G consecutive sweeps per CTA in a shared-memory
+// window.
+//
+// The ops are those of the element chase in stage2_chase.cu (the reference's
+// bidiagonalize / block_bidiagonalize! with target width 1, KAbasedSVD/src/
+// bulgechasing.jl:18-40): sweep j, step m, pivot column c0 = j + 1 + m BW,
+// c1 = min(c0 + BW - 1, n - 1):
+//   R op: a right reflector from row rho (= j for m = 0, c0 - BW after)
+//     over columns c0..c1, applied to rows rho+1..c1;
+//   L op: a left reflector from column c0 over rows c0..c1, applied to
+//     columns c0+1..min(c0 + 2BW - 1, n - 1).
+// Op k of sweep j touches nothing that ops >= k+4 of sweep j-1 touch.
+//
+// Layout of the work.  A CTA owns the sweeps j0 .. j0+G-1 (groups handed out
+// in order by a ticket); compute warp i runs sweep j0+i, op t - 4i at tick t,
+// so the G sweeps advance in lockstep with the minimal lag, and all their
+// data stays in a window of W columns of the band in shared memory (column c
+// in slot c mod W).  A producer warp moves the band between the window and
+// global memory: before tick t it has loaded (cp.async, 16-byte chunks, L2
+// only) every column the tick touches, and it prefetches the columns of tick
+// t+2; after tick t it writes back the columns that no sweep of the group
+// touches again (those left of the trailing sweep's next pivot), and every
+// few ticks it publishes that boundary in retired[g] (release).  The next
+// group's producer loads a column only once retired[g] has passed it, so it
+// sees every update of this group, and this group never touches a column
+// again once it is retired: the result is the sequential chase's, bit for
+// bit, whatever the timing.  Compute warps touch only shared memory;
+// named barriers hand each tick between the producer and the compute warps.
+// Every wait on another CTA is bounded (kDevTimeout).
+//
+// Band storage in global memory: the element chase's compact form, A(r, c) at
+// AB[(r - c + 2BW - 1) + c * ldab], ldab = 3 BW.
+#include <algorithm>
+
+#include "avs_common.cuh"
+#include "chase_ar.cuh"
+
+namespace avs {
+namespace {
+
+template <int BW, int G>
+struct WinCfg {
+    static constexpr int KU = 2 * BW - 1;
+    static constexpr int LDAB = 3 * BW;         // storage rows per column (global)
+    static constexpr int LDW = 3 * BW + 2;      // window column stride (16-byte multiple; odd stride - 1)
+    static constexpr int W = 2 * G * BW + 2 * BW;  // window columns (span of a group's ops + prefetch)
+    static constexpr int NC = 32 * G;           // compute threads
+    static constexpr int NT = NC + 32;          // + the producer warp
+    static constexpr int CHUNKS = LDAB * 8 / 16;  // 16-byte chunks per column
+    static constexpr int PUB = 4;               // ticks between publications of the retired boundary
+    static_assert(BW % 2 == 0 && BW <= 32, "window chase band");
+    static constexpr size_t smem_bytes() { return 8 * ((size_t)W * LDW + (size_t)G * 32); }
+};
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void cp_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void bar_sync(int id, int cnt) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(cnt) : "memory"); }
+__device__ __forceinline__ void bar_arrive(int id, int cnt) {
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(cnt) : "memory");
+}
+
+template <typename S>
+__device__ __forceinline__ typename ChaseAr<S>::V wsum(typename ChaseAr<S>::V v) {
+    using Ar = ChaseAr<S>;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = Ar::add(v, Ar::shfl_xor(v, o));
+    return v;
+}
+
+// Per-sweep op geometry.
+struct WOp {
+    int c0, c1, hi;  // pivot column, last column of the reflector, last column touched
+};
+template <int BW>
+__device__ __forceinline__ int wops(int64_t n, int j) { return 2 * ((int)((n - j - 2) / BW) + 1); }
+template <int BW>
+__device__ __forceinline__ WOp wop(int64_t n, int j, int k) {
+    WOp o;
+    o.c0 = j + 1 + (k >> 1) * BW;
+    const int last = (int)(n - 1);
+    o.c1 = min(o.c0 + BW - 1, last);
+    o.hi = min(o.c0 + ((k & 1) ? 2 * BW - 1 : BW - 1), last);
+    return o;
+}
+
+template <int BW, typename S, int G>
+__global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
+    chase_win_kernel(typename ChaseAr<S>::St *ab, int64_t n, int *ticket, int *retired, int *err) {
+    using Cfg = WinCfg<BW, G>;
+    using Ar = ChaseAr<S>;
+    using V = typename Ar::V;
+    using St = typename Ar::St;
+    static_assert(sizeof(St) == 8 && sizeof(V) == 8, "8-byte band elements");
+    constexpr int KU = Cfg::KU, LDW = Cfg::LDW, W = Cfg::W, NC = Cfg::NC, NT = Cfg::NT, LDAB = Cfg::LDAB;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    St *win = reinterpret_cast<St *>(smem_raw);  // [W][LDW]
+    V *vbuf = reinterpret_cast<V *>(win + (size_t)W * LDW);  // [G][32]
+    __shared__ int s_g;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int nsweeps = (int)(n - 1);
+    const int ngroups = (nsweeps + G - 1) / G;
+    auto A = [&](int r, int c) -> St * { return win + (size_t)(c % W) * LDW + (r - c + KU); };
+
+    for (;;) {
+        if (tid == 0) s_g = atomicAdd(ticket, 1);
+        __syncthreads();
+        const int g = s_g;
+        __syncthreads();
+        if (g >= ngroups) return;
+        const int j0 = g * G;
+        const int gs = min(G, nsweeps - j0);
+        int nticks = 0;
+        for (int i = 0; i < gs; ++i) nticks = max(nticks, 4 * i + wops<BW>(n, j0 + i));
+        // columns [lo, .. ) not yet retired; the tick's highest column + 1
+        auto tick_need = [&](int t) -> int {
+            int need = 0;
+            for (int i = 0; i < gs; ++i) {
+                const int k = t - 4 * i;
+                if (k >= 0 && k < wops<BW>(n, j0 + i)) need = max(need, wop<BW>(n, j0 + i, k).hi + 1);
+            }
+            return need;
+        };
+        // after tick t: the lowest column any op of a later tick touches (n: none)
+        auto retire_after = [&](int t) -> int {
+            int lo = (int)n;
+            for (int i = 0; i < gs; ++i) {
+                const int k = t + 1 - 4 * i;
+                if (k < wops<BW>(n, j0 + i)) lo = min(lo, wop<BW>(n, j0 + i, max(k, 0)).c0);
+            }
+            return lo;
+        };
+
+        if (wid == G) {
+            // ---------------- producer warp ----------------
+            int lo_wb = j0 + 1;   // columns below are written back
+            int issued = j0 + 1;  // columns below are requested (cp.async)
+            int rp = (g == 0) ? (int)n : 0;  // last seen retired[g-1]
+            int pub = j0 + 1;     // last published boundary
+            for (int t = 0; t <= nticks; ++t) {
+                if (t > 0) {
+                    bar_sync(2, NT);  // compute warps finished tick t-1
+                    const int lo = min(retire_after(t - 1), issued);
+                    // write back the retired columns (16-byte chunks)
+                    for (int q = lane; q < (lo - lo_wb) * Cfg::CHUNKS; q += 32) {
+                        const int c = lo_wb + q / Cfg::CHUNKS, h = q % Cfg::CHUNKS;
+                        const uint4 v = *reinterpret_cast<const uint4 *>(win + (size_t)(c % W) * LDW + 2 * h);
+                        *reinterpret_cast<uint4 *>(ab + (size_t)c * LDAB + 2 * h) = v;
+                    }
+                    lo_wb = lo;
+                    __syncwarp();  // the slots just written back may be refilled below
+                }
+                if (t < nticks) {
+                    const int need = tick_need(t);
+                    const int pre = max(need, tick_need(t + 2));
+                    bool urgent = issued < need;
+                    if (urgent && rp < need) {
+                        if (lane == 0) wait_geq(retired + g - 1, need, err);
+                        __syncwarp();
+                        rp = max(need, __shfl_sync(0xffffffffu, lane == 0 ? ld_acquire(retired + g - 1) : 0, 0));
+                    }
+                    if (need > lo_wb + W && lane == 0) atomicCAS(err, kDevOk, kDevInternal);  // cannot happen
+                    const int tgt = max(issued, min(min(pre, rp), min(lo_wb + W, (int)n)));
+                    for (int q = lane; q < (tgt - issued) * Cfg::CHUNKS; q += 32) {
+                        const int c = issued + q / Cfg::CHUNKS, h = q % Cfg::CHUNKS;
+                        cp_async16(win + (size_t)(c % W) * LDW + 2 * h, ab + (size_t)c * LDAB + 2 * h);
+                    }
+                    cp_commit();
+                    issued = tgt;
+                    if (urgent) cp_wait_all();
+                    else cp_wait_prev();
+                    __syncwarp();
+                    __threadfence_block();
+                    bar_arrive(1, NT);  // the columns of tick t are in the window
+                    // refresh the view of the previous group without waiting on it
+                    if (g > 0 && rp < (int)n && lane == 0) rp = max(rp, ld_acquire(retired + g - 1));
+                    rp = __shfl_sync(0xffffffffu, rp, 0);
+                }
+                if ((t % Cfg::PUB == Cfg::PUB - 1 || t == nticks) && lo_wb > pub) {
+                    __syncwarp();
+                    if (lane == 0) {
+                        __threadfence();
+                        st_release(retired + g, t == nticks ? (int)n : lo_wb);
+                    }
+                    pub = lo_wb;
+                }
+                __syncwarp();
+            }
+            if (lane == 0 && pub < (int)n) {
+                __threadfence();
+                st_release(retired + g, (int)n);
+            }
+        } else {
+            // ---------------- compute warps: warp wid runs sweep j0 + wid ----------------
+            const int j = j0 + wid;
+            const int ops = (wid < gs) ? wops<BW>(n, j) : 0;
+            V *sv = vbuf + wid * 32;
+            for (int t = 0; t < nticks; ++t) {
+                bar_sync(1, NT);  // the tick's columns are loaded; the previous tick is done
+                const int k = t - 4 * wid;
+                if (k >= 0 && k < ops) {
+                    const WOp o = wop<BW>(n, j, k);
+                    const int L = o.c1 - o.c0 + 1;
+                    if (L >= 2) {
+                        const bool rop = (k & 1) == 0;
+                        const int rho = rop ? ((k == 0) ? j : o.c0 - BW) : o.c0;
+                        // reflector input: row rho (R op) or column c0 (L op), columns/rows c0..c1
+                        V x = Ar::zero();
+                        if (lane < L) x = Ar::lds(rop ? A(rho, o.c0 + lane) : A(o.c0 + lane, o.c0));
+                        typename Ar::Acc acc = Ar::acc_zero();
+                        if (lane >= 1 && lane < L) Ar::acc_add(acc, x, x);
+                        const V s = wsum<S>(Ar::acc_value(acc));
+                        const V alpha = Ar::shfl(x, 0);
+                        V tau = Ar::zero(), beta = alpha, scal = Ar::zero();
+                        if (Ar::gt0(s)) {
+                            const V nrm = Ar::sqrt(Ar::fma(alpha, alpha, s));
+                            beta = Ar::ge0(alpha) ? Ar::neg(nrm) : nrm;
+                            tau = Ar::mul(Ar::sub(beta, alpha), Ar::rcp(beta));
+                            scal = Ar::rcp(Ar::sub(alpha, beta));
+                        }
+                        if (lane < L) sv[lane] = (lane == 0) ? Ar::one() : Ar::mul(x, scal);
+                        __syncwarp();
+                        if (!Ar::iszero(tau)) {
+                            if (rop) {
+                                for (int r = rho + 1 + lane; r <= o.c1; r += 32) {
+                                    typename Ar::Acc a = Ar::acc_zero();
+                                    for (int i = 0; i < L; ++i) Ar::acc_add(a, Ar::lds(A(r, o.c0 + i)), sv[i]);
+                                    const V w = Ar::mul(Ar::acc_value(a), tau);
+                                    for (int i = 0; i < L; ++i) {
+                                        St *p = A(r, o.c0 + i);
+                                        Ar::st(p, Ar::sub(Ar::lds(p), Ar::mul(w, sv[i])));
+                                    }
+                                }
+                            } else {
+                                for (int c = o.c0 + 1 + lane; c <= o.hi; c += 32) {
+                                    typename Ar::Acc a = Ar::acc_zero();
+                                    for (int i = 0; i < L; ++i) Ar::acc_add(a, sv[i], Ar::lds(A(o.c0 + i, c)));
+                                    const V w = Ar::mul(Ar::acc_value(a), tau);
+                                    for (int i = 0; i < L; ++i) {
+                                        St *p = A(o.c0 + i, c);
+                                        Ar::st(p, Ar::sub(Ar::lds(p), Ar::mul(w, sv[i])));
+                                    }
+                                }
+                            }
+                        }
+                        // the pivot row / column: beta and zeros (no lane reads it any more)
+                        if (lane < L) {
+                            St *p = rop ? A(rho, o.c0 + lane) : A(o.c0 + lane, o.c0);
+                            Ar::st(p, lane == 0 ? beta : Ar::zero());
+                        }
+                    }
+                }
+                __syncwarp();
+                __threadfence_block();
+                bar_arrive(2, NT);  // tick t done
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <int BW, typename S, int G>
+int launch_win(typename ChaseAr<S>::St *dAB, int64_t n, const Stage2Work &w, cudaStream_t s, int num_sms) {
+    using Cfg = WinCfg<BW, G>;
+    const size_t smem = Cfg::smem_bytes();
+    auto kern = chase_win_kernel<BW, S, G>;
+    AVS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t ngroups = ((n - 1) + G - 1) / G;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ngroups, num_sms));
+    kern<<<grid, Cfg::NT, smem, s>>>(dAB, n, w.flags, w.flags + 1, w.err);
+    AVS_CUDA_TRY(cudaGetLastError());
+    return AVS_SUCCESS;
+}
+
+}  // namespace
+
+bool chase_window_supported(int bw) { return bw == 8 || bw == 16 || bw == 32; }
+
+// The band (width bw, compact storage with ldab = 3 bw) -> bidiagonal, in
+// place.  w.flags: n + 2 ints (zeroed here).
+template <typename S>
+static int chase_window(typename ChaseAr<S>::St *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s,
+                        int num_sms) {
+    if (n < 2) return AVS_SUCCESS;
+    if (n > ((int64_t)1 << 30)) return AVS_ERR_UNSUPPORTED;
+    AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(n + 2), s));
+    switch (bw) {
+        case 8: return launch_win<8, S, 8>(dAB, n, w, s, num_sms);
+        case 16: return launch_win<16, S, 8>(dAB, n, w, s, num_sms);
+        case 32: return launch_win<32, S, 3>(dAB, n, w, s, num_sms);
+        default: return AVS_ERR_UNSUPPORTED;
+    }
+}
+int stage2_chase_window_df(float2 *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s, int num_sms) {
+    return chase_window<df64>(dAB, n, bw, w, s, num_sms);
+}
+int stage2_chase_window_fp64(double *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s, int num_sms) {
+    return chase_window<double>(dAB, n, bw, w, s, num_sms);
+}
+
+}  // namespace avs

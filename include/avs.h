@@ -88,6 +88,10 @@ extern "C" {
  * bidiagonal.  These flags change that: */
 #define AVS_FLAG_ONE_STAGE_CHASE 4 /* element chase straight from the band of width tile */
 #define AVS_FLAG_BAND32 8          /* intermediate band of width 32 instead of 16 */
+/* The element chase of the narrow band runs G sweeps per CTA inside a
+ * shared-memory window by default; this flag runs it with one thread-block
+ * cluster per sweep on the band in global memory instead. */
+#define AVS_FLAG_CLUSTER_CHASE 16
 
 typedef struct avs_handle avs_handle;
 

@@ -96,3 +96,36 @@ def test_pipeline_hierarchical_vs_one_stage(avs_mod, torch_cuda, dtype, tile, pr
         assert np.max(np.abs(s - lap)) < tol * lap[0]
         outs.append(s)
     assert np.max(np.abs(outs[0] - outs[1])) < tol * lap[0]
+
+
+@pytest.mark.parametrize("dtype,n,tile,prec,tol", [(np.float32, 1024, 16, "fp32", 1e-5), (np.float32, 1024, 32, "fp32", 1e-5),
+                                                   (np.float32, 2048, 256, "bf16x3", 1e-5),
+                                                   (np.float64, 1024, 128, "fp64", 1e-12),
+                                                   (np.float64, 1024, 16, "fp64", 1e-12),
+                                                   (np.float64, 1024, 32, "fp64", 1e-12)])
+def test_window_chase_vs_cluster_chase(avs_mod, torch_cuda, dtype, n, tile, prec, tol):
+    """The narrow band's element chase in the shared-memory window (default)
+    and with one cluster per sweep (AVS_FLAG_CLUSTER_CHASE) agree within the
+    mode's tolerance, and both match LAPACK."""
+    import ctypes
+    if n % tile:
+        pytest.skip("tile does not divide n")
+    rng = np.random.default_rng(n + tile)
+    a = (rng.standard_normal((n, n)) / np.sqrt(n)).astype(dtype)
+    lap = sl.svdvals(a.astype(np.float64))
+    dA = avs_mod.to_device(a)
+    outs = []
+    for flags in (0, 16, 0):
+        torch = torch_cuda
+        sig = torch.empty(n, dtype=dA.dtype, device=dA.device)
+        o = avs_mod.Opts(avs_mod.PREC[prec], flags, 0.0, None)
+        r = avs_mod.Report()
+        fn = avs_mod.lib().avs_svdvals_dev_d if dtype == np.float64 else avs_mod.lib().avs_svdvals_dev_s
+        rc = fn(avs_mod.default_handle().ptr, n, n, n, tile, ctypes.c_void_p(dA.data_ptr()),
+                ctypes.c_void_p(sig.data_ptr()), ctypes.byref(o), ctypes.byref(r))
+        assert rc == 0
+        s = sig.cpu().numpy().astype(np.float64)
+        assert np.max(np.abs(s - lap)) < tol * lap[0]
+        outs.append(s)
+    assert np.max(np.abs(outs[0] - outs[1])) < tol * lap[0]
+    assert np.array_equal(outs[0], outs[2])  # the window chase is deterministic
