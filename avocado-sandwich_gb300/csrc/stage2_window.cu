@@ -191,6 +191,7 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                 }
                 __syncwarp();
             }
+            cp_wait_all();  // no copy into the window may outlive the group
             if (lane == 0 && pub < (int)n) {
                 __threadfence();
                 st_release(retired + g, (int)n);
