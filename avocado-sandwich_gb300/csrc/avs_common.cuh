@@ -17,12 +17,13 @@ enum DeviceError : int {
     kDevInternal = 3,  // a kernel found its own bookkeeping inconsistent
 };
 
-// Upper bound on the spin iterations of any dependency wait.  Each iteration
-// makes two acquire loads and sleeps 64 ns (__nanosleep(64)), so the bound is at
-// least 2^27 x 64 ns = 8.6 s, more with the loads' latency -- far beyond any
-// legitimate wait, short enough that a lost dependency returns AVS_ERR_TIMEOUT
-// instead of hanging the GPU.
+// Bounds of any dependency wait: at most kSpinLimit polls (two acquire loads
+// and a 64 ns sleep each, about 1 us with the loads' latency) and at most
+// kWaitNs of %globaltimer, whichever comes first -- far beyond any legitimate
+// wait, short enough that a lost dependency returns AVS_ERR_TIMEOUT instead of
+// hanging the GPU.
 constexpr long long kSpinLimit = 1ll << 27;
+constexpr long long kWaitNs = 4000000000ll;  // 4 s
 
 // Column-major view of a matrix, optionally transposed: element (i, j) of the
 // view is a[i + j*lda] (LAYOUT 0) or a[j + i*lda] (LAYOUT 1).  The LQ half of
@@ -49,23 +50,31 @@ __device__ __forceinline__ void st_release(int *p, int v) {
     asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Bounded wait until *flag >= target.  Called by one thread; returns false on
 // timeout (after recording kDevTimeout in *err) or when another CTA already
-// failed.  Never spins forever.
-__device__ __forceinline__ bool wait_geq_n(const int *flag, int target, int *err, long long limit) {
-    long long it = 0;
-    while (ld_acquire(flag) < target) {
+// failed.  Never spins forever: at most kSpinLimit polls and limit_ns of
+// %globaltimer.
+__device__ __forceinline__ bool wait_geq_n(const int *flag, int target, int *err, long long limit_ns) {
+    if (ld_acquire(flag) >= target) return true;
+    const unsigned long long t0 = global_ns();
+    for (long long it = 0;; ++it) {
+        if (ld_acquire(flag) >= target) return true;
         if (ld_acquire(err) != kDevOk) return false;
-        if (++it > limit) {
+        if (it > kSpinLimit || ((it & 63) == 63 && (long long)(global_ns() - t0) > limit_ns)) {
             atomicCAS(err, kDevOk, kDevTimeout);
             return false;
         }
         __nanosleep(64);
     }
-    return true;
 }
 __device__ __forceinline__ bool wait_geq(const int *flag, int target, int *err) {
-    return wait_geq_n(flag, target, err, kSpinLimit);
+    return wait_geq_n(flag, target, err, kWaitNs);
 }
 
 template <typename T>
