@@ -1072,7 +1072,7 @@ int avs_tsqrt_tile_dev_d(avs_handle *h, int32_t b, double *dR, double *dB, doubl
 namespace {
 
 struct BatchLayout {
-    size_t err, W, tau, tblk, tfull, f1, ab, f2, d, e, sig, scr, pairs, ptrs, total;
+    size_t err, W, tau, tblk, tfull, f1, ab, ab2, f2, d, e, sig, scr, pairs, ptrs, total;
 };
 
 // elem: bytes of the tile type (4: FP32 tiles and double-float stages 2-3;
@@ -1093,6 +1093,7 @@ BatchLayout batch_layout(int64_t n, int b, int cnt, size_t elem = 4) {
     L.tfull = take(b >= 128 ? elem * (size_t)cnt * (nt + 1) * b * b : 0);
     L.f1 = take(sizeof(int) * (size_t)cnt * (2 * nt + 4));
     L.ab = take(sizeof(float2) * (size_t)cnt * 3 * b * n);
+    L.ab2 = take(sizeof(double) * (size_t)cnt * 3 * kMaxNarrowBand * n);  // narrow band of the hierarchical chase
     L.f2 = take(sizeof(int) * ((size_t)cnt * (n + 1) + 4));
     L.d = take(sizeof(double) * (size_t)cnt * n);
     L.e = take(sizeof(double) * (size_t)cnt * n);
@@ -1163,7 +1164,8 @@ int ensure_pinned(avs_handle *h, size_t bytes) {
 // single call).
 template <typename T>
 int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cnt, double tol, cudaStream_t s,
-                   const cudaEvent_t *ev, int64_t *launches, bool bidiag, bool df_update, bool f64_stages) {
+                   const cudaEvent_t *ev, int64_t *launches, bool bidiag, bool df_update, bool f64_stages,
+                   int flags) {
     char *base = reinterpret_cast<char *>(h->bws);
     T *W = reinterpret_cast<T *>(base + L.W);
     const T *const *src = reinterpret_cast<const T *const *>(base + L.ptrs);
@@ -1197,13 +1199,21 @@ int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cn
     w2.err = err;
     double *dd = reinterpret_cast<double *>(base + L.d);
     double *de = reinterpret_cast<double *>(base + L.e);
-    if constexpr (sizeof(T) == 8)
+    // stage 2 as a single call of the same mode runs it (run_stages23)
+    const int tbw = narrow_band_of(b, flags);
+    const bool window = !(flags & AVS_FLAG_CLUSTER_CHASE);
+    if constexpr (sizeof(T) == 8) {
         if (f64_stages)
             rc = stage2_chase_fp64_batched(W, n, b, cnt, reinterpret_cast<double *>(base + L.ab), 3 * (int64_t)b, dd,
-                                           de, w2, s, h->num_sms, launches);
-    if (sizeof(T) == 4 || !f64_stages)
+                                           de, w2, s, h->num_sms, launches, tbw, window,
+                                           reinterpret_cast<double *>(base + L.ab2));
+        else
+            rc = stage2_chase_df_batched(W, n, b, cnt, reinterpret_cast<float2 *>(base + L.ab), 3 * (int64_t)b, dd,
+                                         de, w2, s, h->num_sms, launches, window);
+    } else {
         rc = stage2_chase_df_batched(W, n, b, cnt, reinterpret_cast<float2 *>(base + L.ab), 3 * (int64_t)b, dd, de,
-                                     w2, s, h->num_sms, launches);
+                                     w2, s, h->num_sms, launches, tbw, window, reinterpret_cast<float2 *>(base + L.ab2));
+    }
     if (rc != AVS_SUCCESS) return rc;
     AVS_CUDA_TRY(cudaEventRecordWithFlags(ev[2], s, cudaEventRecordExternal));
     if (bidiag) {  // the bidiagonal itself: d and e of each matrix to the caller's vectors
@@ -1334,15 +1344,17 @@ static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const in
         }
         AVS_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(h->bws) + L.ptrs, tab, sizeof(void *) * 4 * cnt,
                                      cudaMemcpyHostToDevice, s));
+        const int cflags = flags_of(opts) & (AVS_FLAG_ONE_STAGE_CHASE | AVS_FLAG_BAND32 | AVS_FLAG_CLUSTER_CHASE);
         const auto key = std::make_tuple(gn, gb, cnt,
-                                         (bidiag ? 1 : 0) + (sizeof(T) == 8 ? 2 : 0) + (dfu ? 4 : 0) + (f64s ? 8 : 0));
+                                         (bidiag ? 1 : 0) + (sizeof(T) == 8 ? 2 : 0) + (dfu ? 4 : 0) + (f64s ? 8 : 0) +
+                                             (cflags << 4));
         auto it = h->graphs.find(key);
         if (it == h->graphs.end()) {
             avs_handle::Graph gr;
             for (cudaEvent_t &e : gr.ev) AVS_CUDA_TRY(cudaEventCreate(&e));
             cudaGraph_t graph;
             AVS_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-            rc = group_launches<T>(h, L, gn, gb, cnt, tol, s, gr.ev, &gr.kernels, bidiag, dfu, f64s);
+            rc = group_launches<T>(h, L, gn, gb, cnt, tol, s, gr.ev, &gr.kernels, bidiag, dfu, f64s, cflags);
             cudaError_t ce = cudaStreamEndCapture(s, &graph);
             if (rc == AVS_SUCCESS && ce == cudaSuccess) {
                 ce = cudaGraphInstantiate(&gr.exec, graph, 0);

@@ -207,11 +207,17 @@ int stage2_rate(int fp64, int num_sms, double *flops_per_s);
 template <typename T>
 int stage2_chase_df(const T *dW, int64_t n, int64_t ldw, int bw, float2 *dAB, int64_t ldab, double *dd, double *de,
                     const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches, bool window = false);
+// Batched stage 2 (stage2_chase.cu): tbw > 0 runs the blocked band reduction
+// to width tbw first (dAB then holds the FP32 / FP64 band, 3 bw x n per
+// matrix; dAB2 the narrow band, 3 tbw x n per matrix); window: the element
+// chase in the shared-memory window where the band width allows it.
 int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
-                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
+                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches, int tbw,
+                            bool window, float2 *dAB2);
 // FP64 tiles, double-float chase (the batched groups of AVS_PREC_FP64X2)
 int stage2_chase_df_batched(const double *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
-                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
+                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches,
+                            bool window);
 // Blocked band reduction bw -> tbw (stage2_band.cu), on a compact band
 // (A(r, c) at dAB[(r - c + 2bw - 1) + c * ldab], ldab >= 3 bw)
 template <typename R>
@@ -241,12 +247,16 @@ int stage2_chase_hier_fp64(const double *dW, int64_t n, int64_t ldw, int bw, int
 // Element chase of a narrow band (width 8, 16 or 32; compact storage, ldab =
 // 3 bw) with G sweeps per CTA in a shared-memory window (stage2_window.cu).
 bool chase_window_supported(int bw);
-int stage2_chase_window_df(float2 *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s, int num_sms);
-int stage2_chase_window_fp64(double *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s, int num_sms);
+// batch matrices at stride sAB elements; w.flags: 1 + batch (n + 1) ints.
+int stage2_chase_window_df(float2 *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s, int num_sms,
+                           int batch = 1, int64_t sAB = 0);
+int stage2_chase_window_fp64(double *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s, int num_sms,
+                             int batch = 1, int64_t sAB = 0);
 int stage3_bisect_df_batched(const double *dd, const double *de, int64_t n, int batch, double rel_tol,
                              double *dsigma, double *dscratch, float2 *dpairs, cudaStream_t s, int64_t *launches);
 int stage2_chase_fp64_batched(const double *dW, int64_t n, int bw, int batch, double *dAB, int64_t ldab, double *dd,
-                              double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches);
+                              double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches,
+                              int tbw, bool window, double *dAB2);
 int stage3_bisect_batched(const double *dd, const double *de, int64_t n, int batch, double rel_tol, double *dsigma,
                           double *dscratch, cudaStream_t s, int64_t *launches);
 int bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *dsigma, double rel_tol,

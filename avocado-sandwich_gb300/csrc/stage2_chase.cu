@@ -759,27 +759,66 @@ __global__ void extract_band_batched(const T *a, int64_t n, int bw, typename Cha
 }
 template <typename S>
 __global__ void bidiag_out_batched(const typename ChaseAr<S>::St *ab, int64_t n, int bw, int64_t ldab, double *d,
-                                   double *e, int batch) {
+                                   double *e, int batch, int64_t sAB) {
     const int ku = 2 * bw - 1;
     const int64_t total = n * (int64_t)batch;
     for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < total; g += (int64_t)gridDim.x * blockDim.x) {
         const int64_t zb = g / n, i = g % n;
-        const typename ChaseAr<S>::St *abz = ab + zb * ldab * n;
+        const typename ChaseAr<S>::St *abz = ab + zb * sAB;
         d[zb * n + i] = st_to_double(abz[ku + i * ldab]);
         e[zb * n + i] = (i + 1 < n) ? st_to_double(abz[(ku - 1) + (i + 1) * ldab]) : 0.0;
     }
 }
 }  // namespace
 
+// Batched stage 2, the same choices as a single call's run_stages23 (so a
+// matrix's values do not depend on its batch): tbw > 0: the blocked band
+// reduction bw -> tbw (arithmetic T, band dAB as T elements, 3 bw x n per
+// matrix), then the element chase of the narrow band (dAB2, 3 tbw x n per
+// matrix); tbw == 0: the element chase from width bw.  window: the element
+// chase in the shared-memory window (bands 8/16/32) instead of clusters.
 template <typename T, typename S>
 int stage2_chase_batched(const T *dW, int64_t n, int bw, int batch, typename ChaseAr<S>::St *dAB, int64_t ldab,
                          double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms,
-                         int64_t *launches) {
+                         int64_t *launches, int tbw, bool window, typename ChaseAr<S>::St *dAB2) {
     using St = typename ChaseAr<S>::St;
+    if (tbw > 0) {
+        T *ab1 = reinterpret_cast<T *>(dAB);
+        const int64_t ldab1 = 3 * (int64_t)bw, sAB1 = ldab1 * n, ldab2 = 3 * (int64_t)tbw, sAB2 = ldab2 * n;
+        int rc;
+        if ((rc = dense_to_band<T, T>(dW, n, n, n * n, bw, ab1, ldab1, sAB1, batch, s)) != AVS_SUCCESS) return rc;
+        if ((rc = band_stage<T>(ab1, n, bw, tbw, ldab1, w, s, num_sms, batch, sAB1, n + 1)) != AVS_SUCCESS)
+            return rc;
+        if ((rc = band_to_band<T, St>(ab1, n, bw, ldab1, sAB1, tbw, dAB2, ldab2, sAB2, batch, s)) != AVS_SUCCESS)
+            return rc;
+        if (window && chase_window_supported(tbw)) {
+            rc = std::is_same<S, df64>::value
+                     ? stage2_chase_window_df(reinterpret_cast<float2 *>(dAB2), n, tbw, w, s, num_sms, batch, sAB2)
+                     : stage2_chase_window_fp64(reinterpret_cast<double *>(dAB2), n, tbw, w, s, num_sms, batch,
+                                                sAB2);
+        } else {
+            AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)((n + 1) * (int64_t)batch + 1), s));
+            rc = tbw == 16 ? launch_chase_cluster<16, S, 1>(dAB2, n, ldab2, w, s, num_sms, batch, sAB2, n + 1)
+                           : launch_chase_cluster<32, S, 2>(dAB2, n, ldab2, w, s, num_sms, batch, sAB2, n + 1);
+        }
+        if (rc != AVS_SUCCESS) return rc;
+        const int nb = (int)std::min<int64_t>((n * batch + 255) / 256, 8192);
+        bidiag_out_batched<S><<<nb > 0 ? nb : 1, 256, 0, s>>>(dAB2, n, tbw, ldab2, dd, de, batch, sAB2);
+        AVS_CUDA_TRY(cudaGetLastError());
+        if (launches) *launches += 5;
+        return AVS_SUCCESS;
+    }
     AVS_CUDA_TRY(cudaMemsetAsync(dAB, 0, sizeof(St) * (size_t)ldab * (size_t)n * batch, s));
     extract_band_batched<T, S><<<dim3((unsigned)n, (unsigned)batch), 128, 0, s>>>(dW, n, bw, dAB, ldab);
     AVS_CUDA_TRY(cudaGetLastError());
-    if (n >= 2) {
+    if (window && chase_window_supported(bw) && ldab == 3 * (int64_t)bw) {
+        const int rc = std::is_same<S, df64>::value
+                           ? stage2_chase_window_df(reinterpret_cast<float2 *>(dAB), n, bw, w, s, num_sms, batch,
+                                                    ldab * n)
+                           : stage2_chase_window_fp64(reinterpret_cast<double *>(dAB), n, bw, w, s, num_sms, batch,
+                                                      ldab * n);
+        if (rc != AVS_SUCCESS) return rc;
+    } else if (n >= 2) {
         AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)((n + 1) * (int64_t)batch + 1), s));
         int rc;
         // small bands: few, small CTAs per sweep (the batch supplies the
@@ -823,25 +862,31 @@ int stage2_chase_batched(const T *dW, int64_t n, int bw, int batch, typename Cha
         if (rc != AVS_SUCCESS) return rc;
     }
     const int nb = (int)std::min<int64_t>((n * batch + 255) / 256, 8192);
-    bidiag_out_batched<S><<<nb > 0 ? nb : 1, 256, 0, s>>>(dAB, n, bw, ldab, dd, de, batch);
+    bidiag_out_batched<S><<<nb > 0 ? nb : 1, 256, 0, s>>>(dAB, n, bw, ldab, dd, de, batch, ldab * n);
     AVS_CUDA_TRY(cudaGetLastError());
     if (launches) *launches += 3;
     return AVS_SUCCESS;
 }
 
 int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
-                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches) {
-    return stage2_chase_batched<float, df64>(dW, n, bw, batch, dAB, ldab, dd, de, w, s, num_sms, launches);
+                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches, int tbw,
+                            bool window, float2 *dAB2) {
+    return stage2_chase_batched<float, df64>(dW, n, bw, batch, dAB, ldab, dd, de, w, s, num_sms, launches, tbw,
+                                             window, dAB2);
 }
 
 int stage2_chase_df_batched(const double *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
-                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches) {
-    return stage2_chase_batched<double, df64>(dW, n, bw, batch, dAB, ldab, dd, de, w, s, num_sms, launches);
+                            double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches,
+                            bool window) {
+    return stage2_chase_batched<double, df64>(dW, n, bw, batch, dAB, ldab, dd, de, w, s, num_sms, launches, 0, window,
+                                              nullptr);
 }
 
 int stage2_chase_fp64_batched(const double *dW, int64_t n, int bw, int batch, double *dAB, int64_t ldab, double *dd,
-                              double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches) {
-    return stage2_chase_batched<double, double>(dW, n, bw, batch, dAB, ldab, dd, de, w, s, num_sms, launches);
+                              double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches,
+                              int tbw, bool window, double *dAB2) {
+    return stage2_chase_batched<double, double>(dW, n, bw, batch, dAB, ldab, dd, de, w, s, num_sms, launches, tbw,
+                                                window, dAB2);
 }
 
 }  // namespace avs

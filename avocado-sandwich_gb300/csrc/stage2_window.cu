@@ -91,7 +91,8 @@ __device__ __forceinline__ WOp wop(int64_t n, int j, int k) {
 
 template <int BW, typename S, int G>
 __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
-    chase_win_kernel(typename ChaseAr<S>::St *ab, int64_t n, int *ticket, int *retired, int *err) {
+    chase_win_kernel(typename ChaseAr<S>::St *ab_base, int64_t n, int batch, int64_t sAB, int *ticket,
+                     int *retired_base, int64_t sRet, int *err) {
     using Cfg = WinCfg<BW, G>;
     using Ar = ChaseAr<S>;
     using V = typename Ar::V;
@@ -110,9 +111,13 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
     for (;;) {
         if (tid == 0) s_g = atomicAdd(ticket, 1);
         __syncthreads();
-        const int g = s_g;
+        const int tk = s_g;
         __syncthreads();
+        // tickets are group-major over the batch: every matrix advances its own wavefront
+        const int g = tk / batch, zb = tk % batch;
         if (g >= ngroups) return;
+        St *ab = ab_base + (size_t)zb * sAB;
+        int *retired = retired_base + (size_t)zb * sRet;
         const int j0 = g * G;
         const int gs = min(G, nsweeps - j0);
         int nticks = 0;
@@ -266,14 +271,20 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
 }
 
 template <int BW, typename S, int G>
-int launch_win(typename ChaseAr<S>::St *dAB, int64_t n, const Stage2Work &w, cudaStream_t s, int num_sms) {
+int launch_win(typename ChaseAr<S>::St *dAB, int64_t n, const Stage2Work &w, cudaStream_t s, int num_sms, int batch,
+               int64_t sAB) {
     using Cfg = WinCfg<BW, G>;
     const size_t smem = Cfg::smem_bytes();
     auto kern = chase_win_kernel<BW, S, G>;
     AVS_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, Cfg::NT, smem) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
+    }
     const int64_t ngroups = ((n - 1) + G - 1) / G;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ngroups, num_sms));
-    kern<<<grid, Cfg::NT, smem, s>>>(dAB, n, w.flags, w.flags + 1, w.err);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ngroups * batch, (int64_t)num_sms * per_sm));
+    kern<<<grid, Cfg::NT, smem, s>>>(dAB, n, batch, sAB, w.flags, w.flags + 1, n + 1, w.err);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
 }
@@ -286,22 +297,24 @@ bool chase_window_supported(int bw) { return bw == 8 || bw == 16 || bw == 32; }
 // place.  w.flags: n + 2 ints (zeroed here).
 template <typename S>
 static int chase_window(typename ChaseAr<S>::St *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s,
-                        int num_sms) {
-    if (n < 2) return AVS_SUCCESS;
-    if (n > ((int64_t)1 << 30)) return AVS_ERR_UNSUPPORTED;
-    AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)(n + 2), s));
+                        int num_sms, int batch, int64_t sAB) {
+    if (n < 2 || batch < 1) return AVS_SUCCESS;
+    if (n > ((int64_t)1 << 30) || (int64_t)batch * n > ((int64_t)1 << 31) - 64) return AVS_ERR_UNSUPPORTED;
+    AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)((n + 1) * (int64_t)batch + 1), s));
     switch (bw) {
-        case 8: return launch_win<8, S, 8>(dAB, n, w, s, num_sms);
-        case 16: return launch_win<16, S, 8>(dAB, n, w, s, num_sms);
-        case 32: return launch_win<32, S, 3>(dAB, n, w, s, num_sms);
+        case 8: return launch_win<8, S, 8>(dAB, n, w, s, num_sms, batch, sAB);
+        case 16: return launch_win<16, S, 8>(dAB, n, w, s, num_sms, batch, sAB);
+        case 32: return launch_win<32, S, 3>(dAB, n, w, s, num_sms, batch, sAB);
         default: return AVS_ERR_UNSUPPORTED;
     }
 }
-int stage2_chase_window_df(float2 *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s, int num_sms) {
-    return chase_window<df64>(dAB, n, bw, w, s, num_sms);
+int stage2_chase_window_df(float2 *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s, int num_sms,
+                           int batch, int64_t sAB) {
+    return chase_window<df64>(dAB, n, bw, w, s, num_sms, batch, sAB);
 }
-int stage2_chase_window_fp64(double *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s, int num_sms) {
-    return chase_window<double>(dAB, n, bw, w, s, num_sms);
+int stage2_chase_window_fp64(double *dAB, int64_t n, int bw, const Stage2Work &w, cudaStream_t s, int num_sms,
+                             int batch, int64_t sAB) {
+    return chase_window<double>(dAB, n, bw, w, s, num_sms, batch, sAB);
 }
 
 }  // namespace avs
