@@ -180,10 +180,14 @@ inline bool df_update_of(int prec) { return prec == AVS_PREC_FP64X2; }
 inline int flags_of(const avs_opts *opts) { return opts ? opts->flags : 0; }
 
 // Stage 2 of a single call: the band of width b goes to width
-// narrow_band_of(b, flags) by the blocked band reduction, then to the
-// bidiagonal by the element chase (0: the element chase from width b).
-int narrow_band_of(int b, int flags) {
+// narrow_band_of(b, flags, fp64) by the blocked band reduction, then to the
+// bidiagonal by the element chase (0: the element chase from width b).  FP64
+// stages keep the one-stage chase unless asked (the FP64 block stage runs on
+// the FP64 pipe, 1/64 of the FP32 rate: slower than the one-stage FP64 chase,
+// measured 537 vs 315 ms at n = 8192, tile 128).
+int narrow_band_of(int b, int flags, bool fp64) {
     if (flags & AVS_FLAG_ONE_STAGE_CHASE) return 0;
+    if (fp64 && !(flags & AVS_FLAG_HIER_CHASE)) return 0;
     const int t = (flags & AVS_FLAG_BAND32) ? 32 : 16;
     return band_stage_supported(b, t) ? t : 0;
 }
@@ -251,7 +255,7 @@ int run_stages23(avs_handle *h, const Layout &L, int64_t n, int b, const S *W, i
     Stage2Work w2;
     w2.flags = reinterpret_cast<int *>(ws_at(h, L.off_flags2));
     w2.err = err;
-    const int tbw = narrow_band_of(b, flags);
+    const int tbw = narrow_band_of(b, flags, fp64_stages);
     if (tbw > 0 && sizeof(S) == 8 && fp64_stages) {
         if ((rc = stage2_chase_hier_fp64(reinterpret_cast<const double *>(W), n, ldw, b, tbw, AB,
                                          reinterpret_cast<double *>(ws_at(h, L.off_ab2)), dd, de, w2, s, h->num_sms,
@@ -1200,7 +1204,7 @@ int group_launches(avs_handle *h, const BatchLayout &L, int64_t n, int b, int cn
     double *dd = reinterpret_cast<double *>(base + L.d);
     double *de = reinterpret_cast<double *>(base + L.e);
     // stage 2 as a single call of the same mode runs it (run_stages23)
-    const int tbw = narrow_band_of(b, flags);
+    const int tbw = narrow_band_of(b, flags, sizeof(T) == 8 && f64_stages);
     const bool window = !(flags & AVS_FLAG_CLUSTER_CHASE);
     if constexpr (sizeof(T) == 8) {
         if (f64_stages)
@@ -1344,7 +1348,8 @@ static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const in
         }
         AVS_CUDA_TRY(cudaMemcpyAsync(reinterpret_cast<char *>(h->bws) + L.ptrs, tab, sizeof(void *) * 4 * cnt,
                                      cudaMemcpyHostToDevice, s));
-        const int cflags = flags_of(opts) & (AVS_FLAG_ONE_STAGE_CHASE | AVS_FLAG_BAND32 | AVS_FLAG_CLUSTER_CHASE);
+        const int cflags = flags_of(opts) & (AVS_FLAG_ONE_STAGE_CHASE | AVS_FLAG_BAND32 | AVS_FLAG_CLUSTER_CHASE |
+                                             AVS_FLAG_HIER_CHASE);
         const auto key = std::make_tuple(gn, gb, cnt,
                                          (bidiag ? 1 : 0) + (sizeof(T) == 8 ? 2 : 0) + (dfu ? 4 : 0) + (f64s ? 8 : 0) +
                                              (cflags << 4));

@@ -79,15 +79,18 @@ extern "C" {
  * override that choice. */
 #define AVS_FLAG_FP64_STAGES 1
 #define AVS_FLAG_DF64_STAGES 2
-/* Stage 2 of the single-matrix calls is hierarchical by default, as the
+/* Stage 2 is hierarchical by default in the FP32-class modes, as the
  * reference's bidiag! (BRD/src/bulgechasing2.jl:22-45) and the halving of
  * bidiagonalize (KAbasedSVD/src/bulgechasing.jl:33-42): a blocked band
- * reduction (T rows per sweep, compact-WY applies; FP32 arithmetic in the
- * FP32-class modes, FP64 with FP64 stages) takes the band of width tile (64,
- * 128 or 256) to width 16, then the element chase takes it to the
- * bidiagonal.  These flags change that: */
+ * reduction (T rows per sweep, compact-WY applies, FP32 arithmetic) takes the
+ * band of width tile (64, 128 or 256) to width 16, then the element chase
+ * (double-float) takes it to the bidiagonal.  With FP64 stages the element
+ * chase runs from the band of width tile (the FP64 block stage is slower on
+ * GB300's FP64 pipe) unless AVS_FLAG_HIER_CHASE asks for the hierarchy (FP64
+ * block stage).  Batched groups make the same choices as single calls. */
 #define AVS_FLAG_ONE_STAGE_CHASE 4 /* element chase straight from the band of width tile */
 #define AVS_FLAG_BAND32 8          /* intermediate band of width 32 instead of 16 */
+#define AVS_FLAG_HIER_CHASE 32     /* hierarchical stage 2 with FP64 stages too */
 /* The element chase of the narrow band runs G sweeps per CTA inside a
  * shared-memory window by default; this flag runs it with one thread-block
  * cluster per sweep on the band in global memory instead. */

@@ -73,9 +73,9 @@ def test_band_stage_rejects_pairs(avs_mod, torch_cuda):
 @pytest.mark.parametrize("dtype,tile,prec,tol", [(np.float64, 64, "fp64", 1e-12), (np.float64, 256, "fp64", 1e-12),
                                                  (np.float32, 128, "fp32", 1e-5), (np.float32, 256, "bf16x3", 1e-5)])
 def test_pipeline_hierarchical_vs_one_stage(avs_mod, torch_cuda, dtype, tile, prec, tol):
-    """The default (hierarchical) stage 2 and the one-stage element chase
-    (AVS_FLAG_ONE_STAGE_CHASE) give the same values within the mode's
-    tolerance, and both match LAPACK."""
+    """The hierarchical stage 2 (band 16 and band 32) and the one-stage
+    element chase (AVS_FLAG_ONE_STAGE_CHASE) give the same values within the
+    mode's tolerance, and all match LAPACK."""
     import ctypes
     n = 1024
     rng = np.random.default_rng(tile + n)
@@ -83,7 +83,9 @@ def test_pipeline_hierarchical_vs_one_stage(avs_mod, torch_cuda, dtype, tile, pr
     lap = sl.svdvals(a.astype(np.float64))
     dA = avs_mod.to_device(a)
     outs = []
-    for flags in (0, 4, 8):
+    # FP64 stages run the hierarchy only on request (AVS_FLAG_HIER_CHASE = 32)
+    hier = 32 if dtype == np.float64 else 0
+    for flags in (hier, 4, hier | 8):
         torch = torch_cuda
         sig = torch.empty(n, dtype=dA.dtype, device=dA.device)
         o = avs_mod.Opts(avs_mod.PREC[prec], flags, 0.0, None)
