@@ -19,9 +19,10 @@
 // in slot c mod W).  A producer warp moves the band between the window and
 // global memory: before tick t it has loaded (cp.async, 16-byte chunks, L2
 // only) every column the tick touches, and it prefetches the columns of tick
-// t+2; after tick t it writes back the columns that no sweep of the group
-// touches again (those left of the trailing sweep's next pivot), and every
-// few ticks it publishes that boundary in retired[g] (release).  The next
+// t+3; after tick t it marks as retired the columns that no sweep of the
+// group touches again (those left of the trailing sweep's next pivot).  A
+// publisher warp writes retired columns back and publishes the boundary in
+// retired[g] (fence, release), off the ticks' critical path.  The next
 // group's producer loads a column only once retired[g] has passed it, so it
 // sees every update of this group, and this group never touches a column
 // again once it is retired: the result is the sequential chase's, bit for
@@ -46,9 +47,9 @@ struct WinCfg {
     static constexpr int LDW = 3 * BW + 2;      // window column stride (16-byte multiple; odd stride - 1)
     static constexpr int W = 2 * G * BW + 2 * BW;  // window columns (span of a group's ops + prefetch)
     static constexpr int NC = 32 * G;           // compute threads
-    static constexpr int NT = NC + 32;          // + the producer warp
+    static constexpr int NB = NC + 32;          // threads of the tick barriers: compute warps + producer
+    static constexpr int NT = NC + 64;          // + the producer and the publisher warps
     static constexpr int CHUNKS = LDAB * 8 / 16;  // 16-byte chunks per column
-    static constexpr int PUB = 4;               // ticks between publications of the retired boundary
     static_assert(BW % 2 == 0 && BW <= 32, "window chase band");
     static constexpr size_t smem_bytes() { return 8 * ((size_t)W * LDW + (size_t)G * 32); }
 };
@@ -63,6 +64,42 @@ __device__ __forceinline__ void cp_wait_prev() { asm volatile("cp.async.wait_gro
 __device__ __forceinline__ void bar_sync(int id, int cnt) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(cnt) : "memory"); }
 __device__ __forceinline__ void bar_arrive(int id, int cnt) {
     asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(cnt) : "memory");
+}
+
+__device__ __forceinline__ int ld_volatile_shared(const int *p) { return *(const volatile int *)p; }
+__device__ __forceinline__ void st_volatile_shared(int *p, int v) { *(volatile int *)p = v; }
+__device__ __forceinline__ int ld_relaxed(const int *p) {
+    int v;
+    asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+// Bounded waits on a shared-memory counter written by another warp of the CTA
+// (kWaitNs of %globaltimer, kSpinLimit polls); on timeout kDevTimeout.
+__device__ __forceinline__ bool wait_shared_geq(const int *p, int target, int *err) {
+    const unsigned long long t0 = global_ns();
+    for (long long it = 0; ld_volatile_shared(p) < target; ++it) {
+        if (it > kSpinLimit || ((it & 255) == 255 && (long long)(global_ns() - t0) > kWaitNs)) {
+            atomicCAS(err, kDevOk, kDevTimeout);
+            return false;
+        }
+        __nanosleep(32);
+    }
+    return true;
+}
+// returns the counter once it exceeds v (or v after a timeout)
+__device__ __forceinline__ int wait_shared_gt(const int *p, int v, int *err) {
+    const unsigned long long t0 = global_ns();
+    for (long long it = 0;; ++it) {
+        const int x = ld_volatile_shared(p);
+        if (x > v) return x;
+        if (it > kSpinLimit || ((it & 255) == 255 && (long long)(global_ns() - t0) > kWaitNs)) {
+            atomicCAS(err, kDevOk, kDevTimeout);
+            return v;
+        }
+        __nanosleep(32);
+    }
 }
 
 template <typename S>
@@ -103,6 +140,7 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
     St *win = reinterpret_cast<St *>(smem_raw);  // [W][LDW]
     V *vbuf = reinterpret_cast<V *>(win + (size_t)W * LDW);  // [G][32]
     __shared__ int s_g;
+    __shared__ int s_ret, s_wb;  // columns below s_ret are retired by the group; below s_wb written back
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int nsweeps = (int)(n - 1);
     const int ngroups = (nsweeps + G - 1) / G;
@@ -119,6 +157,11 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
         St *ab = ab_base + (size_t)zb * sAB;
         int *retired = retired_base + (size_t)zb * sRet;
         const int j0 = g * G;
+        if (tid == 0) {
+            s_ret = j0 + 1;
+            s_wb = j0 + 1;
+        }
+        __syncthreads();
         const int gs = min(G, nsweeps - j0);
         int nticks = 0;
         for (int i = 0; i < gs; ++i) nticks = max(nticks, 4 * i + wops<BW>(n, j0 + i));
@@ -142,72 +185,91 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
         };
 
         if (wid == G) {
-            // ---------------- producer warp ----------------
-            int lo_wb = j0 + 1;   // columns below are written back
-            int issued = j0 + 1;  // columns below are requested (cp.async)
-            int rp = (g == 0) ? (int)n : 0;  // last seen retired[g-1]
-            int pub = j0 + 1;     // last published boundary
-            for (int t = 0; t <= nticks; ++t) {
+            // ---------------- producer warp: global -> window ----------------
+            int issued = j0 + 1;               // columns below are requested (cp.async)
+            int rp = (g == 0) ? (int)n : 0;    // retired[g-1] as last observed (acquired)
+            int rp_next = rp;                  // a relaxed read in flight, acquired when used
+            for (int t = 0; t < nticks; ++t) {
                 if (t > 0) {
-                    bar_sync(2, NT);  // compute warps finished tick t-1
-                    const int lo = min(retire_after(t - 1), issued);
-                    // write back the retired columns (16-byte chunks)
-                    for (int q = lane; q < (lo - lo_wb) * Cfg::CHUNKS; q += 32) {
-                        const int c = lo_wb + q / Cfg::CHUNKS, h = q % Cfg::CHUNKS;
-                        const uint4 v = *reinterpret_cast<const uint4 *>(win + (size_t)(c % W) * LDW + 2 * h);
-                        *reinterpret_cast<uint4 *>(ab + (size_t)c * LDAB + 2 * h) = v;
-                    }
-                    lo_wb = lo;
-                    __syncwarp();  // the slots just written back may be refilled below
-                }
-                if (t < nticks) {
-                    const int need = tick_need(t);
-                    const int pre = max(need, tick_need(t + 2));
-                    bool urgent = issued < need;
-                    if (urgent && rp < need) {
-                        if (lane == 0) wait_geq(retired + g - 1, need, err);
-                        __syncwarp();
-                        rp = max(need, __shfl_sync(0xffffffffu, lane == 0 ? ld_acquire(retired + g - 1) : 0, 0));
-                    }
-                    if (need > lo_wb + W && lane == 0) atomicCAS(err, kDevOk, kDevInternal);  // cannot happen
-                    const int tgt = max(issued, min(min(pre, rp), min(lo_wb + W, (int)n)));
-                    for (int q = lane; q < (tgt - issued) * Cfg::CHUNKS; q += 32) {
-                        const int c = issued + q / Cfg::CHUNKS, h = q % Cfg::CHUNKS;
-                        cp_async16(win + (size_t)(c % W) * LDW + 2 * h, ab + (size_t)c * LDAB + 2 * h);
-                    }
-                    cp_commit();
-                    issued = tgt;
-                    if (urgent) cp_wait_all();
-                    else cp_wait_prev();
-                    __syncwarp();
-                    __threadfence_block();
-                    bar_arrive(1, NT);  // the columns of tick t are in the window
-                    // refresh the view of the previous group without waiting on it
-                    if (g > 0 && rp < (int)n && lane == 0) rp = max(rp, ld_acquire(retired + g - 1));
-                    rp = __shfl_sync(0xffffffffu, rp, 0);
-                }
-                if ((t % Cfg::PUB == Cfg::PUB - 1 || t == nticks) && lo_wb > pub) {
-                    __syncwarp();
+                    bar_sync(2, Cfg::NB);  // compute warps finished tick t-1
                     if (lane == 0) {
-                        __threadfence();
-                        st_release(retired + g, t == nticks ? (int)n : lo_wb);
+                        __threadfence_block();
+                        st_volatile_shared(&s_ret, min(retire_after(t - 1), issued));
                     }
-                    pub = lo_wb;
+                }
+                const int need = tick_need(t);
+                const int pre = max(need, tick_need(t + 3));
+                const int rpn = __shfl_sync(0xffffffffu, rp_next, 0);  // lane 0's read of last tick
+                if (rpn > rp) {  // the previous group retired more: acquire before reading it
+                    fence_acq_rel_gpu();
+                    rp = rpn;
+                }
+                const bool urgent = issued < need;
+                if (urgent && rp < need) {
+                    if (lane == 0) wait_geq(retired + g - 1, need, err);
+                    __syncwarp();
+                    rp = max(need, __shfl_sync(0xffffffffu, lane == 0 ? ld_acquire(retired + g - 1) : 0, 0));
+                }
+                // slots of columns below wb + W are free (their columns are written back)
+                int tgt = max(issued, min(min(pre, rp), (int)n));
+                if (tgt > ld_volatile_shared(&s_wb) + W) {
+                    if (urgent) {  // the columns of this tick: wait for the publisher's copies (bounded)
+                        if (lane == 0) wait_shared_geq(&s_wb, need - W, err);
+                        __syncwarp();
+                    }
+                    tgt = max(issued, min(tgt, ld_volatile_shared(&s_wb) + W));
+                }
+                for (int q = lane; q < (tgt - issued) * Cfg::CHUNKS; q += 32) {
+                    const int c = issued + q / Cfg::CHUNKS, h = q % Cfg::CHUNKS;
+                    cp_async16(win + (size_t)(c % W) * LDW + 2 * h, ab + (size_t)c * LDAB + 2 * h);
+                }
+                cp_commit();
+                issued = tgt;
+                if (urgent) cp_wait_all();
+                else cp_wait_prev();
+                __syncwarp();
+                __threadfence_block();
+                bar_arrive(1, Cfg::NB);  // the columns of tick t are in the window
+                // look at the previous group again (lane 0; the value is used next tick,
+                // so the read's latency overlaps the tick)
+                if (g > 0 && rp < (int)n && lane == 0) rp_next = ld_relaxed(retired + g - 1);
+            }
+            bar_sync(2, Cfg::NB);  // the last tick
+            cp_wait_all();
+            if (lane == 0) {
+                __threadfence_block();
+                st_volatile_shared(&s_ret, (int)n);  // everything is retired
+            }
+        } else if (wid == G + 1) {
+            // ---------------- publisher warp: window -> global, retired[g] ----------------
+            int wb = j0 + 1;
+            for (;;) {
+                int r = wb;
+                if (lane == 0) r = wait_shared_gt(&s_ret, wb, err);
+                r = __shfl_sync(0xffffffffu, r, 0);
+                if (r <= wb) break;  // only after a timeout (recorded)
+                __threadfence_block();
+                for (int q = lane; q < (r - wb) * Cfg::CHUNKS; q += 32) {
+                    const int c = wb + q / Cfg::CHUNKS, h = q % Cfg::CHUNKS;
+                    const uint4 v = *reinterpret_cast<const uint4 *>(win + (size_t)(c % W) * LDW + 2 * h);
+                    *reinterpret_cast<uint4 *>(ab + (size_t)c * LDAB + 2 * h) = v;
                 }
                 __syncwarp();
+                wb = r;
+                if (lane == 0) {
+                    st_volatile_shared(&s_wb, wb);  // the slots may be refilled
+                    __threadfence();
+                    st_release(retired + g, wb);
+                }
+                if (wb >= (int)n) break;
             }
-            cp_wait_all();  // no copy into the window may outlive the group
-            if (lane == 0 && pub < (int)n) {
-                __threadfence();
-                st_release(retired + g, (int)n);
-            }
-        } else {
+                } else {
             // ---------------- compute warps: warp wid runs sweep j0 + wid ----------------
             const int j = j0 + wid;
             const int ops = (wid < gs) ? wops<BW>(n, j) : 0;
             V *sv = vbuf + wid * 32;
             for (int t = 0; t < nticks; ++t) {
-                bar_sync(1, NT);  // the tick's columns are loaded; the previous tick is done
+                bar_sync(1, Cfg::NB);  // the tick's columns are loaded; the previous tick is done
                 const int k = t - 4 * wid;
                 if (k >= 0 && k < ops) {
                     const WOp o = wop<BW>(n, j, k);
@@ -263,7 +325,7 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                 }
                 __syncwarp();
                 __threadfence_block();
-                bar_arrive(2, NT);  // tick t done
+                bar_arrive(2, Cfg::NB);  // tick t done
             }
         }
         __syncthreads();
