@@ -107,6 +107,32 @@ struct Vec4<double> {
 __device__ __forceinline__ float ldg_cg(const float *p) { return __ldcg(p); }
 __device__ __forceinline__ double ldg_cg(const double *p) { return __ldcg(p); }
 
+// Staging copy global (L2) -> shared of COUNT elements spread over NT threads:
+// element idx = tid + u * NT comes from src(idx) (nullptr: zero) and goes to
+// dst(idx).  The loads of a batch of 8 are all in flight before the first
+// store, so a thread waits for about one L2 latency per batch instead of one
+// per element.
+template <typename R, int NT, int COUNT, typename Src, typename Dst>
+__device__ __forceinline__ void stage_in(int tid, Src src, Dst dst) {
+    constexpr int PER = (COUNT + NT - 1) / NT;
+    constexpr int BATCH = PER < 8 ? PER : 8;
+#pragma unroll
+    for (int u0 = 0; u0 < PER; u0 += BATCH) {
+        R v[BATCH];
+#pragma unroll
+        for (int u = 0; u < BATCH; ++u) {
+            const int idx = tid + (u0 + u) * NT;
+            const R *p = (u0 + u < PER && idx < COUNT) ? src(idx) : nullptr;
+            v[u] = p ? ldg_cg(p) : R(0);
+        }
+#pragma unroll
+        for (int u = 0; u < BATCH; ++u) {
+            const int idx = tid + (u0 + u) * NT;
+            if (u0 + u < PER && idx < COUNT) dst(idx, v[u]);
+        }
+    }
+}
+
 __device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arrive.aligned;" ::: "memory"); }
 __device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.aligned;" ::: "memory"); }
 
@@ -214,7 +240,7 @@ __device__ __forceinline__ void build_t(const R *s_tau, const R *gram, R *Tm) {
 }
 
 template <int B, int T, typename R, int C>
-__global__ void __launch_bounds__(256) band_stage_kernel(R *ab_base, int64_t n, int64_t ldab, int *ticket,
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) band_stage_kernel(R *ab_base, int64_t n, int64_t ldab, int *ticket,
                                                           int *done_base, int *err, int batch, int64_t sAB,
                                                           int64_t sDone) {
     using Cfg = BandCfg<B, T, C>;
@@ -261,16 +287,17 @@ __global__ void __launch_bounds__(256) band_stage_kernel(R *ab_base, int64_t n, 
                 const int64_t r_lo = rho + T + (int64_t)q * RPC;
                 const int64_t r_hi = (c0 + B < n) ? c0 + B : n;
                 // panel (QR form): P[k][c'] = A(rho + k, c0 + c')
-                for (int idx = tid; idx < T * B; idx += NT) {
-                    const int k = idx % T, cc = idx / T;
-                    P[k * LDP + cc] = (cc < L) ? ldg_cg(at(rho + k, c0 + cc)) : R(0);
-                }
+                stage_in<R, NT, T * B>(
+                    tid, [&](int idx) -> const R * { return (idx / T < L) ? at(rho + idx % T, c0 + idx / T) : nullptr; },
+                    [&](int idx, R v) { P[(idx % T) * LDP + idx / T] = v; });
                 // this CTA's rows of the apply, column-major [c][r]
-                for (int idx = tid; idx < RPC * B; idx += NT) {
-                    const int rr = idx % RPC, cc = idx / RPC;
-                    const int64_t r = r_lo + rr;
-                    As[cc * Cfg::LDA_R + rr] = (cc < L && r < r_hi) ? ldg_cg(at(r, c0 + cc)) : R(0);
-                }
+                stage_in<R, NT, RPC * B>(
+                    tid,
+                    [&](int idx) -> const R * {
+                        const int rr = idx % RPC, cc = idx / RPC;
+                        return (cc < L && r_lo + rr < r_hi) ? at(r_lo + rr, c0 + cc) : nullptr;
+                    },
+                    [&](int idx, R v) { As[(idx / RPC) * Cfg::LDA_R + idx % RPC] = v; });
                 __syncthreads();
                 cl_arrive();  // done reading the pivot rows
                 panel_qr<R, B, T, NW>(P, s_tau, gram);
@@ -300,6 +327,7 @@ __global__ void __launch_bounds__(256) band_stage_kernel(R *ab_base, int64_t n, 
                         for (int a = 0; a < KPT; ++a)
 #pragma unroll
                             for (int b2 = 0; b2 < 4; ++b2) acc[a][b2] = R(0);
+#pragma unroll 2
                         for (int c = 0; c < B; c += 4) {
                             R a4[4][4], v4[KPT][4];
 #pragma unroll
@@ -390,16 +418,20 @@ __global__ void __launch_bounds__(256) band_stage_kernel(R *ab_base, int64_t n, 
                 const int64_t cc_lo = c0 + T + (int64_t)q * RPC;
                 const int64_t c_hi = (c0 + 2 * B < n) ? c0 + 2 * B : n;
                 // panel: P[k][i] = A(c0 + i, c0 + k)
-                for (int idx = tid; idx < T * B; idx += NT) {
-                    const int i = idx % B, k = idx / B;
-                    P[k * LDP + i] = (i < L && k < Tc) ? ldg_cg(at(c0 + i, c0 + k)) : R(0);
-                }
+                stage_in<R, NT, T * B>(
+                    tid,
+                    [&](int idx) -> const R * {
+                        return (idx % B < L && idx / B < Tc) ? at(c0 + idx % B, c0 + idx / B) : nullptr;
+                    },
+                    [&](int idx, R v) { P[(idx / B) * LDP + idx % B] = v; });
                 // this CTA's columns of the apply, column-major [cc][i]
-                for (int idx = tid; idx < RPC * B; idx += NT) {
-                    const int i = idx % B, cc = idx / B;
-                    const int64_t c = cc_lo + cc;
-                    As[cc * Cfg::LDA_L + i] = (i < L && c < c_hi) ? ldg_cg(at(c0 + i, c)) : R(0);
-                }
+                stage_in<R, NT, RPC * B>(
+                    tid,
+                    [&](int idx) -> const R * {
+                        const int i = idx % B, cc = idx / B;
+                        return (i < L && cc_lo + cc < c_hi) ? at(c0 + i, cc_lo + cc) : nullptr;
+                    },
+                    [&](int idx, R v) { As[(idx / B) * Cfg::LDA_L + idx % B] = v; });
                 __syncthreads();
                 cl_arrive();  // done reading the pivot columns
                 panel_qr<R, B, T, NW>(P, s_tau, gram);
@@ -429,6 +461,7 @@ __global__ void __launch_bounds__(256) band_stage_kernel(R *ab_base, int64_t n, 
                         for (int a = 0; a < KPT; ++a)
 #pragma unroll
                             for (int b2 = 0; b2 < 4; ++b2) acc[a][b2] = R(0);
+#pragma unroll 2
                         for (int i = 0; i < B; i += 4) {
                             R a4[4][4], v4[KPT][4];
 #pragma unroll

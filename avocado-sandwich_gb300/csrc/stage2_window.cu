@@ -60,7 +60,8 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
 }
 __device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-__device__ __forceinline__ void cp_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_wait_group() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 __device__ __forceinline__ void bar_sync(int id, int cnt) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(cnt) : "memory"); }
 __device__ __forceinline__ void bar_arrive(int id, int cnt) {
     asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(cnt) : "memory");
@@ -73,7 +74,6 @@ __device__ __forceinline__ int ld_relaxed(const int *p) {
     asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
-__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
 // Bounded waits on a shared-memory counter written by another warp of the CTA
 // (kWaitNs of %globaltimer, kSpinLimit polls); on timeout kDevTimeout.
@@ -188,7 +188,8 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
             // ---------------- producer warp: global -> window ----------------
             int issued = j0 + 1;               // columns below are requested (cp.async)
             int rp = (g == 0) ? (int)n : 0;    // retired[g-1] as last observed (acquired)
-            int rp_next = rp;                  // a relaxed read in flight, acquired when used
+            int rp_next = rp;                  // lane 0: a relaxed read in flight, used next tick
+            int hist1 = j0 + 1;                // columns requested before last tick's copies
             for (int t = 0; t < nticks; ++t) {
                 if (t > 0) {
                     bar_sync(2, Cfg::NB);  // compute warps finished tick t-1
@@ -199,11 +200,11 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                 }
                 const int need = tick_need(t);
                 const int pre = max(need, tick_need(t + 3));
-                const int rpn = __shfl_sync(0xffffffffu, rp_next, 0);  // lane 0's read of last tick
-                if (rpn > rp) {  // the previous group retired more: acquire before reading it
-                    fence_acq_rel_gpu();
-                    rp = rpn;
-                }
+                // lane 0's read of the previous group's boundary, issued last tick.  The
+                // copies of the columns it releases are issued only once the value has
+                // arrived (their range depends on it) and read L2, where the previous
+                // group's writes were made visible before its release.
+                rp = max(rp, __shfl_sync(0xffffffffu, rp_next, 0));
                 const bool urgent = issued < need;
                 if (urgent && rp < need) {
                     if (lane == 0) wait_geq(retired + g - 1, need, err);
@@ -224,9 +225,14 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                     cp_async16(win + (size_t)(c % W) * LDW + 2 * h, ab + (size_t)c * LDAB + 2 * h);
                 }
                 cp_commit();
+                // wait only for the copy groups that hold the columns of tick t (one
+                // group is committed per tick; issued / hist1: requested before this
+                // tick's and last tick's group)
+                if (hist1 >= need) cp_wait_group<2>();  // in groups committed two or more ticks ago
+                else if (issued >= need) cp_wait_group<1>();  // ... one tick ago
+                else cp_wait_group<0>();
+                hist1 = issued;
                 issued = tgt;
-                if (urgent) cp_wait_all();
-                else cp_wait_prev();
                 __syncwarp();
                 __threadfence_block();
                 bar_arrive(1, Cfg::NB);  // the columns of tick t are in the window
