@@ -300,25 +300,55 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                         if (lane < L) sv[lane] = (lane == 0) ? Ar::one() : Ar::mul(x, scal);
                         __syncwarp();
                         if (!Ar::iszero(tau)) {
+                            // column c0 + i sits in slot s0 + i (wrapping at W): one modulo per op
+                            const int s0 = o.c0 % W;
                             if (rop) {
+                                // lane = row r: A(r, c0 + i) at slot(c0 + i) * LDW + (r - c0 - i + KU);
+                                // from column to column the address moves by LDW - 1 (- W LDW at the wrap)
                                 for (int r = rho + 1 + lane; r <= o.c1; r += 32) {
+                                    St *p0 = win + (size_t)s0 * LDW + (r - o.c0 + KU);
+                                    V xv[BW];
                                     typename Ar::Acc a = Ar::acc_zero();
-                                    for (int i = 0; i < L; ++i) Ar::acc_add(a, Ar::lds(A(r, o.c0 + i)), sv[i]);
+                                    {
+                                        St *p = p0;
+#pragma unroll
+                                        for (int i = 0; i < BW; ++i) {
+                                            if (i < L) {
+                                                xv[i] = Ar::lds(p);
+                                                Ar::acc_add(a, xv[i], sv[i]);
+                                            }
+                                            p += LDW - 1;
+                                            if (s0 + i + 1 == W) p -= (size_t)W * LDW;
+                                        }
+                                    }
                                     const V w = Ar::mul(Ar::acc_value(a), tau);
-                                    for (int i = 0; i < L; ++i) {
-                                        St *p = A(r, o.c0 + i);
-                                        Ar::st(p, Ar::sub(Ar::lds(p), Ar::mul(w, sv[i])));
+                                    St *p = p0;
+#pragma unroll
+                                    for (int i = 0; i < BW; ++i) {
+                                        if (i < L) Ar::st(p, Ar::sub(xv[i], Ar::mul(w, sv[i])));
+                                        p += LDW - 1;
+                                        if (s0 + i + 1 == W) p -= (size_t)W * LDW;
                                     }
                                 }
                             } else {
+                                // lane = column c: rows c0 .. c0+L-1 contiguous from A(c0, c)
                                 for (int c = o.c0 + 1 + lane; c <= o.hi; c += 32) {
+                                    int sl = s0 + (c - o.c0);
+                                    sl -= (sl >= W) ? W : 0;
+                                    St *p = win + (size_t)sl * LDW + (o.c0 - c + KU);
+                                    V xv[BW];
                                     typename Ar::Acc a = Ar::acc_zero();
-                                    for (int i = 0; i < L; ++i) Ar::acc_add(a, sv[i], Ar::lds(A(o.c0 + i, c)));
-                                    const V w = Ar::mul(Ar::acc_value(a), tau);
-                                    for (int i = 0; i < L; ++i) {
-                                        St *p = A(o.c0 + i, c);
-                                        Ar::st(p, Ar::sub(Ar::lds(p), Ar::mul(w, sv[i])));
+#pragma unroll
+                                    for (int i = 0; i < BW; ++i) {
+                                        if (i < L) {
+                                            xv[i] = Ar::lds(p + i);
+                                            Ar::acc_add(a, sv[i], xv[i]);
+                                        }
                                     }
+                                    const V w = Ar::mul(Ar::acc_value(a), tau);
+#pragma unroll
+                                    for (int i = 0; i < BW; ++i)
+                                        if (i < L) Ar::st(p + i, Ar::sub(xv[i], Ar::mul(w, sv[i])));
                                 }
                             }
                         }
