@@ -294,3 +294,24 @@ def test_cpu_band_bidiagonal_restatement(oracle_mod, n, b):
     s32 = sl.svdvals(a.astype(np.float32).astype(np.float64))
     assert np.max(np.abs(sig - s32)) / s32[0] < 1e-12
     assert set(ts) == {"stage1", "stage2", "stage3"} and min(ts.values()) >= 0
+
+
+@pytest.mark.parametrize("n,cbw,tbw", [(96, 32, 8), (200, 64, 16), (256, 64, 16), (300, 128, 32)])
+def test_brd_stage_reduces_band(n, cbw, tbw):
+    """One stage of the BRD bidiag! restatement (oracle/brd.py ``stage``, the
+    parity reference of the GPU band reduction): the result is an upper band
+    of width tbw exactly (zeros elsewhere), with the singular values of the
+    input band (LAPACK), and running the stages cbw -> tbw -> 1 gives the
+    bidiagonal of ``bidiag`` with the same values."""
+    import scipy.linalg as sl
+    from oracle import brd
+    rng = np.random.default_rng(n + cbw)
+    a = np.triu(np.tril(rng.standard_normal((n, n)), cbw))
+    b = brd.stage(a, cbw, tbw)
+    i, j = np.indices(b.shape)
+    assert np.max(np.abs(b[(j - i > tbw) | (j < i)])) == 0.0
+    s = sl.svdvals(a)
+    assert np.max(np.abs(sl.svdvals(b) - s)) <= 1e-12 * s[0]
+    c = brd.stage(b, tbw, 1)
+    assert np.max(np.abs(c[(j - i > 1) | (j < i)])) == 0.0
+    assert np.max(np.abs(sl.svdvals(c) - s)) <= 1e-12 * s[0]
