@@ -17,8 +17,8 @@ enum DeviceError : int {
     kDevInternal = 3,  // a kernel found its own bookkeeping inconsistent
 };
 
-// Bounds of any dependency wait: at most kSpinLimit polls (two acquire loads
-// and a 64 ns sleep each, about 1 us with the loads' latency) and at most
+// Bounds of any dependency wait: at most kSpinLimit polls (an acquire load and
+// a 32 ns sleep each, about 1 us with the load's latency) and at most
 // kWaitNs of %globaltimer, whichever comes first -- far beyond any legitimate
 // wait, short enough that a lost dependency returns AVS_ERR_TIMEOUT instead of
 // hanging the GPU.
@@ -65,12 +65,14 @@ __device__ __forceinline__ bool wait_geq_n(const int *flag, int target, int *err
     const unsigned long long t0 = global_ns();
     for (long long it = 0;; ++it) {
         if (ld_acquire(flag) >= target) return true;
-        if (ld_acquire(err) != kDevOk) return false;
-        if (it > kSpinLimit || ((it & 63) == 63 && (long long)(global_ns() - t0) > limit_ns)) {
-            atomicCAS(err, kDevOk, kDevTimeout);
-            return false;
+        if ((it & 15) == 15) {  // another CTA's failure, the bounds: every 16 polls
+            if (ld_acquire(err) != kDevOk) return false;
+            if (it > kSpinLimit || (long long)(global_ns() - t0) > limit_ns) {
+                atomicCAS(err, kDevOk, kDevTimeout);
+                return false;
+            }
         }
-        __nanosleep(64);
+        __nanosleep(32);
     }
 }
 __device__ __forceinline__ bool wait_geq(const int *flag, int target, int *err) {

@@ -136,6 +136,28 @@ __device__ __forceinline__ void stage_in(int tid, Src src, Dst dst) {
 __device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arrive.aligned;" ::: "memory"); }
 __device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.aligned;" ::: "memory"); }
 
+// Scalars of the LAPACK-convention reflector of x = (alpha, x2) with s =
+// ||x2||^2 > 0: beta = -sign(alpha) ||x||, tau = (beta - alpha) / beta =
+// 1 + |alpha| / ||x||, scal = 1 / (alpha - beta).  FP32: the norm from the
+// hardware reciprocal square root with one Newton step (about 0.5 ulp), the
+// reciprocals correctly rounded -- a short dependent chain on the panel's
+// critical path; FP64: divisions and sqrt.
+__device__ __forceinline__ void reflector_scalars(float alpha, float s, float &tau, float &beta, float &scal) {
+    const float a2s = fmaf(alpha, alpha, s);
+    const float r = rsqrtf(a2s);
+    float nrm = a2s * r;
+    nrm = fmaf(0.5f * r, fmaf(-nrm, nrm, a2s), nrm);
+    beta = alpha >= 0.0f ? -nrm : nrm;
+    scal = __frcp_rn(alpha - beta);
+    tau = fmaf(fabsf(alpha), __frcp_rn(nrm), 1.0f);
+}
+__device__ __forceinline__ void reflector_scalars(double alpha, double s, double &tau, double &beta, double &scal) {
+    const double nrm = sqrt(fma(alpha, alpha, s));
+    beta = alpha >= 0.0 ? -nrm : nrm;
+    tau = (beta - alpha) / beta;
+    scal = 1.0 / (alpha - beta);
+}
+
 // Householder QR of the panel P (B rows x T columns, column k at P + k*LDP,
 // zero rows below the valid part), LAPACK convention per column: beta =
 // -sign(alpha) ||x||, v = x / (alpha - beta) below the diagonal, v_k = 1,
@@ -170,12 +192,7 @@ __device__ __forceinline__ void panel_qr(R *P, R *s_tau, R *gram) {
             s = warp_sum(s);
             const R alpha = __shfl_sync(0xffffffffu, x[jk][k / 32], k % 32);
             R tau = R(0), beta = alpha, scal = R(0);
-            if (s > R(0)) {
-                const R nrm = sqrt(fma(alpha, alpha, s));
-                beta = alpha >= R(0) ? -nrm : nrm;
-                tau = (beta - alpha) / beta;
-                scal = R(1) / (alpha - beta);
-            }
+            if (s > R(0)) reflector_scalars(alpha, s, tau, beta, scal);
 #pragma unroll
             for (int u = 0; u < RPL; ++u) {
                 const int i = lane + 32 * u;
@@ -548,7 +565,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) band_stage_kernel
                     }
                 }
             }
-            __threadfence();
+            // the op's stores, made visible at GPU scope by one fence per CTA (after
+            // the CTA barrier), then the cluster barrier, then the release
+            __syncthreads();
+            if (tid == 0) __threadfence();
             cluster.sync();
             if (q == 0 && tid == 0) st_release(done + sw, op + 1);
         }
