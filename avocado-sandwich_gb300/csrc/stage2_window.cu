@@ -186,59 +186,70 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
 
         if (wid == G) {
             // ---------------- producer warp: global -> window ----------------
+            // Between "tick t-1 done" and "tick t's columns are in" only the wait
+            // for copies issued earlier sits on the ticks' critical path; the
+            // bookkeeping and the prefetch of the next ticks come after the
+            // hand-off, while the compute warps run tick t.
             int issued = j0 + 1;               // columns below are requested (cp.async)
-            int rp = (g == 0) ? (int)n : 0;    // retired[g-1] as last observed (acquired)
+            int rp = (g == 0) ? (int)n : 0;    // retired[g-1] as last observed
             int rp_next = rp;                  // lane 0: a relaxed read in flight, used next tick
-            int hist1 = j0 + 1;                // columns requested before last tick's copies
-            for (int t = 0; t < nticks; ++t) {
-                if (t > 0) {
-                    bar_sync(2, Cfg::NB);  // compute warps finished tick t-1
-                    if (lane == 0) {
-                        __threadfence_block();
-                        st_volatile_shared(&s_ret, min(retire_after(t - 1), issued));
-                    }
+            int before_last = j0 + 1;          // columns requested before the last copy group
+            // copies of the columns [from, to) into their slots (one column per step, lanes over chunks)
+            auto copy_in = [&](int from, int to) {
+                int sl = from % W;
+                for (int c = from; c < to; ++c) {
+                    for (int h = lane; h < Cfg::CHUNKS; h += 32)
+                        cp_async16(win + (size_t)sl * LDW + 2 * h, ab + (size_t)c * LDAB + 2 * h);
+                    if (++sl == W) sl = 0;
                 }
+            };
+            for (int t = 0; t < nticks; ++t) {
+                if (t > 0) bar_sync(2, Cfg::NB);  // compute warps finished tick t-1
                 const int need = tick_need(t);
-                const int pre = max(need, tick_need(t + 3));
+                if (issued < need) {
+                    // not prefetched (the previous group was behind): load now
+                    if (rp < need) {
+                        if (lane == 0) wait_geq(retired + g - 1, need, err);
+                        __syncwarp();
+                        rp = max(need, __shfl_sync(0xffffffffu, lane == 0 ? ld_acquire(retired + g - 1) : 0, 0));
+                    }
+                    if (need > ld_volatile_shared(&s_wb) + W) {  // free slots (bounded wait on the publisher)
+                        if (lane == 0) wait_shared_geq(&s_wb, need - W, err);
+                        __syncwarp();
+                    }
+                    copy_in(issued, need);
+                    cp_commit();
+                    before_last = issued;
+                    issued = need;
+                    cp_wait_all();
+                } else if (before_last >= need) {
+                    cp_wait_group<1>();  // in groups committed before the last one
+                } else {
+                    cp_wait_all();
+                }
+                __syncwarp();
+                __threadfence_block();
+                bar_arrive(1, Cfg::NB);  // the columns of tick t are in the window
+                // ---- off the critical path ----
+                if (t > 0 && lane == 0) {
+                    __threadfence_block();
+                    st_volatile_shared(&s_ret, min(retire_after(t - 1), issued));
+                }
                 // lane 0's read of the previous group's boundary, issued last tick.  The
                 // copies of the columns it releases are issued only once the value has
                 // arrived (their range depends on it) and read L2, where the previous
                 // group's writes were made visible before its release.
                 rp = max(rp, __shfl_sync(0xffffffffu, rp_next, 0));
-                const bool urgent = issued < need;
-                if (urgent && rp < need) {
-                    if (lane == 0) wait_geq(retired + g - 1, need, err);
-                    __syncwarp();
-                    rp = max(need, __shfl_sync(0xffffffffu, lane == 0 ? ld_acquire(retired + g - 1) : 0, 0));
-                }
-                // slots of columns below wb + W are free (their columns are written back)
-                int tgt = max(issued, min(min(pre, rp), (int)n));
-                if (tgt > ld_volatile_shared(&s_wb) + W) {
-                    if (urgent) {  // the columns of this tick: wait for the publisher's copies (bounded)
-                        if (lane == 0) wait_shared_geq(&s_wb, need - W, err);
-                        __syncwarp();
-                    }
-                    tgt = max(issued, min(tgt, ld_volatile_shared(&s_wb) + W));
-                }
-                for (int q = lane; q < (tgt - issued) * Cfg::CHUNKS; q += 32) {
-                    const int c = issued + q / Cfg::CHUNKS, h = q % Cfg::CHUNKS;
-                    cp_async16(win + (size_t)(c % W) * LDW + 2 * h, ab + (size_t)c * LDAB + 2 * h);
-                }
-                cp_commit();
-                // wait only for the copy groups that hold the columns of tick t (one
-                // group is committed per tick; issued / hist1: requested before this
-                // tick's and last tick's group)
-                if (hist1 >= need) cp_wait_group<2>();  // in groups committed two or more ticks ago
-                else if (issued >= need) cp_wait_group<1>();  // ... one tick ago
-                else cp_wait_group<0>();
-                hist1 = issued;
-                issued = tgt;
-                __syncwarp();
-                __threadfence_block();
-                bar_arrive(1, Cfg::NB);  // the columns of tick t are in the window
-                // look at the previous group again (lane 0; the value is used next tick,
-                // so the read's latency overlaps the tick)
                 if (g > 0 && rp < (int)n && lane == 0) rp_next = ld_relaxed(retired + g - 1);
+                // prefetch the columns of the next three ticks that the previous group
+                // has retired and whose slots are free
+                const int tgt = min(min(tick_need(t + 3), rp), min(ld_volatile_shared(&s_wb) + W, (int)n));
+                if (tgt > issued) {
+                    copy_in(issued, tgt);
+                    cp_commit();
+                    before_last = issued;
+                    issued = tgt;
+                }
             }
             bar_sync(2, Cfg::NB);  // the last tick
             cp_wait_all();
@@ -255,10 +266,15 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                 r = __shfl_sync(0xffffffffu, r, 0);
                 if (r <= wb) break;  // only after a timeout (recorded)
                 __threadfence_block();
-                for (int q = lane; q < (r - wb) * Cfg::CHUNKS; q += 32) {
-                    const int c = wb + q / Cfg::CHUNKS, h = q % Cfg::CHUNKS;
-                    const uint4 v = *reinterpret_cast<const uint4 *>(win + (size_t)(c % W) * LDW + 2 * h);
-                    *reinterpret_cast<uint4 *>(ab + (size_t)c * LDAB + 2 * h) = v;
+                {
+                    int sl = wb % W;
+                    for (int c = wb; c < r; ++c) {
+                        for (int h = lane; h < Cfg::CHUNKS; h += 32) {
+                            const uint4 v = *reinterpret_cast<const uint4 *>(win + (size_t)sl * LDW + 2 * h);
+                            *reinterpret_cast<uint4 *>(ab + (size_t)c * LDAB + 2 * h) = v;
+                        }
+                        if (++sl == W) sl = 0;
+                    }
                 }
                 __syncwarp();
                 wb = r;
