@@ -69,7 +69,8 @@ class Report(ctypes.Structure):
     _fields_ = [("t_total_ms", ctypes.c_double), ("t_stage1_ms", ctypes.c_double), ("t_stage2_ms", ctypes.c_double),
                 ("t_stage3_ms", ctypes.c_double), ("t_h2d_ms", ctypes.c_double), ("t_d2h_ms", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int64), ("workspace_bytes", ctypes.c_int64),
-                ("precision", ctypes.c_int32), ("status", ctypes.c_int32), ("t_update_ms", ctypes.c_double)]
+                ("precision", ctypes.c_int32), ("status", ctypes.c_int32), ("t_update_ms", ctypes.c_double),
+                ("t_band_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

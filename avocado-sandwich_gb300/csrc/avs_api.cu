@@ -28,7 +28,7 @@ struct avs_handle {
     cudaStream_t stream = nullptr;
     void *ws = nullptr;
     size_t ws_bytes = 0;
-    cudaEvent_t ev[6] = {};
+    cudaEvent_t ev[7] = {};  // 6: after the blocked band reduction of stage 2
     int *h_err = nullptr;  // pinned status word
     // batched path: its own grow-only workspace, pinned pointer tables,
     // captured graphs per group shape, autotuned tiles per order n
@@ -246,7 +246,8 @@ float ev_ms(cudaEvent_t a, cudaEvent_t b) {
 // the stages and ev[3] at the end; the status word is the layout's.
 template <typename S, typename TO>
 int run_stages23(avs_handle *h, const Layout &L, int64_t n, int b, const S *W, int64_t ldw, TO *sigma_out,
-                 double rel_tol, bool fp64_stages, cudaStream_t s, int64_t *launches, int flags) {
+                 double rel_tol, bool fp64_stages, cudaStream_t s, int64_t *launches, int flags,
+                 bool *band_ran = nullptr) {
     int rc;
     int *err = reinterpret_cast<int *>(ws_at(h, L.off_err));
     double *AB = reinterpret_cast<double *>(ws_at(h, L.off_ab));
@@ -259,15 +260,17 @@ int run_stages23(avs_handle *h, const Layout &L, int64_t n, int b, const S *W, i
     if (tbw > 0 && sizeof(S) == 8 && fp64_stages) {
         if ((rc = stage2_chase_hier_fp64(reinterpret_cast<const double *>(W), n, ldw, b, tbw, AB,
                                          reinterpret_cast<double *>(ws_at(h, L.off_ab2)), dd, de, w2, s, h->num_sms,
-                                         launches, !(flags & AVS_FLAG_CLUSTER_CHASE))) != AVS_SUCCESS)
+                                         launches, !(flags & AVS_FLAG_CLUSTER_CHASE), h->ev[6])) != AVS_SUCCESS)
             return rc;
+        if (band_ran) *band_ran = true;
     } else if (tbw > 0 && sizeof(S) == 4 && !fp64_stages) {
         // the FP32 band of width b in the first half of AB (3b x n floats)
         if ((rc = stage2_chase_hier_df(reinterpret_cast<const float *>(W), n, ldw, b, tbw,
                                        reinterpret_cast<float *>(AB), reinterpret_cast<float2 *>(ws_at(h, L.off_ab2)),
-                                       dd, de, w2, s, h->num_sms, launches, !(flags & AVS_FLAG_CLUSTER_CHASE))) !=
-            AVS_SUCCESS)
+                                       dd, de, w2, s, h->num_sms, launches, !(flags & AVS_FLAG_CLUSTER_CHASE),
+                                       h->ev[6])) != AVS_SUCCESS)
             return rc;
+        if (band_ran) *band_ran = true;
     } else if (fp64_stages) {
         if ((rc = extract_band_compact<S>(W, n, ldw, b, AB, L.ldab, s)) != AVS_SUCCESS) return rc;
         ++*launches;
@@ -334,10 +337,11 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
         if ((rc = stage1_ge2bnd<S>(W, n, n, b, w1, s, &launches)) != AVS_SUCCESS) return rc;
     }
     AVS_CUDA_TRY(cudaEventRecord(h->ev[1], s));
+    bool band_ran = false;
     {
         NvtxRange r("avs stages 2-3: chase, bisection");
         if ((rc = run_stages23<S, TO>(h, L, n, b, W, n, sigma_out, rel_tol, fp64_stages, s, &launches,
-                                      chase_flags)) !=
+                                      chase_flags, &band_ran)) !=
             AVS_SUCCESS)
             return rc;
     }
@@ -349,6 +353,7 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
         rep->t_stage3_ms = ev_ms(h->ev[2], h->ev[3]);
         rep->t_total_ms = ev_ms(h->ev[0], h->ev[3]);
         rep->t_update_ms = 0.0;
+        rep->t_band_ms = band_ran ? ev_ms(h->ev[1], h->ev[6]) : 0.0;
         for (int q = 0; q < upd_used; ++q) rep->t_update_ms += ev_ms(h->upd_ev[2 * q], h->upd_ev[2 * q + 1]);
         rep->kernel_launches = launches;
         rep->workspace_bytes = (int64_t)h->ws_bytes;

@@ -240,12 +240,13 @@ int band_to_dense(const R *dAB, int64_t n, int bw, int64_t ldab, R *dA, int64_t 
 // _fp64: FP64 throughout.  dAB1 holds 3 bw x n elements, dAB2 3 tbw x n.
 // window: the narrow band's element chase by the windowed multi-sweep kernel
 // (stage2_window.cu) instead of the cluster kernel.
+// after_band (optional): recorded on s between the band reduction and the chase.
 int stage2_chase_hier_df(const float *dW, int64_t n, int64_t ldw, int bw, int tbw, float *dAB1, float2 *dAB2,
                          double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches,
-                         bool window);
+                         bool window, cudaEvent_t after_band = nullptr);
 int stage2_chase_hier_fp64(const double *dW, int64_t n, int64_t ldw, int bw, int tbw, double *dAB1, double *dAB2,
                            double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms,
-                           int64_t *launches, bool window);
+                           int64_t *launches, bool window, cudaEvent_t after_band = nullptr);
 // Element chase of a narrow band (width 8, 16 or 32; compact storage, ldab =
 // 3 bw) with G sweeps per CTA in a shared-memory window (stage2_window.cu).
 bool chase_window_supported(int bw);

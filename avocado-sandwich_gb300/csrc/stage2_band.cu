@@ -467,7 +467,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) band_stage_kernel
                     if (i <= k) P[k * LDP + i] = (i == k) ? R(1) : R(0);
                 }
                 __syncthreads();
-                // Z = V^T A: thread = 4 columns x KPT reflectors
+                // Z = V^T A: thread = 4 columns (g + cc NG4: lanes one column apart, so
+                // their column reads spread over the banks) x KPT reflectors
                 {
                     constexpr int KPT = Cfg::KPT;
                     const int g = tid % Cfg::NG4, kg = tid / Cfg::NG4;
@@ -482,7 +483,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) band_stage_kernel
                         for (int i = 0; i < B; i += 4) {
                             R a4[4][4], v4[KPT][4];
 #pragma unroll
-                            for (int cc = 0; cc < 4; ++cc) Vec4<R>::ld(As + (4 * g + cc) * Cfg::LDA_L + i, a4[cc]);
+                            for (int cc = 0; cc < 4; ++cc)
+                                Vec4<R>::ld(As + (g + cc * Cfg::NG4) * Cfg::LDA_L + i, a4[cc]);
 #pragma unroll
                             for (int kk = 0; kk < KPT; ++kk) Vec4<R>::ld(P + (k0 + kk) * LDP + i, v4[kk]);
 #pragma unroll
@@ -496,7 +498,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) band_stage_kernel
 #pragma unroll
                         for (int kk = 0; kk < KPT; ++kk)
 #pragma unroll
-                            for (int cc = 0; cc < 4; ++cc) Wy[(k0 + kk) * LDW + 4 * g + cc] = acc[kk][cc];
+                            for (int cc = 0; cc < 4; ++cc) Wy[(k0 + kk) * LDW + g + cc * Cfg::NG4] = acc[kk][cc];
                     }
                 }
                 __syncthreads();
@@ -515,7 +517,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) band_stage_kernel
                             for (int l = 0; l <= k; ++l) {
                                 const R t = Tm[l * (T + 1) + k];
 #pragma unroll
-                                for (int cc = 0; cc < 4; ++cc) y[kk][cc] = fma(t, Wy[l * LDW + 4 * g + cc], y[kk][cc]);
+                                for (int cc = 0; cc < 4; ++cc)
+                                    y[kk][cc] = fma(t, Wy[l * LDW + g + cc * Cfg::NG4], y[kk][cc]);
                             }
                         }
                     }
@@ -524,7 +527,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) band_stage_kernel
 #pragma unroll
                         for (int kk = 0; kk < KPT; ++kk)
 #pragma unroll
-                            for (int cc = 0; cc < 4; ++cc) Wy[(k0 + kk) * LDW + 4 * g + cc] = y[kk][cc];
+                            for (int cc = 0; cc < 4; ++cc) Wy[(k0 + kk) * LDW + g + cc * Cfg::NG4] = y[kk][cc];
                     }
                 }
                 __syncthreads();

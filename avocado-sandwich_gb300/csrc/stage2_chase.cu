@@ -693,11 +693,12 @@ template int stage2_chase_df<double>(const double *, int64_t, int64_t, int, floa
 // element chase tbw -> 1 above.
 int stage2_chase_hier_df(const float *dW, int64_t n, int64_t ldw, int bw, int tbw, float *dAB1, float2 *dAB2,
                          double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches,
-                         bool window) {
+                         bool window, cudaEvent_t after_band) {
     const int64_t ldab1 = 3 * (int64_t)bw, ldab2 = 3 * (int64_t)tbw;
     int rc;
     if ((rc = dense_to_band<float, float>(dW, n, ldw, 0, bw, dAB1, ldab1, 0, 1, s)) != AVS_SUCCESS) return rc;
     if ((rc = band_stage<float>(dAB1, n, bw, tbw, ldab1, w, s, num_sms, 1, 0, 0)) != AVS_SUCCESS) return rc;
+    if (after_band) AVS_CUDA_TRY(cudaEventRecord(after_band, s));
     if ((rc = band_to_band<float, float2>(dAB1, n, bw, ldab1, 0, tbw, dAB2, ldab2, 0, 1, s)) != AVS_SUCCESS)
         return rc;
     if (window && chase_window_supported(tbw)) {
@@ -715,11 +716,12 @@ int stage2_chase_hier_df(const float *dW, int64_t n, int64_t ldw, int bw, int tb
 
 int stage2_chase_hier_fp64(const double *dW, int64_t n, int64_t ldw, int bw, int tbw, double *dAB1, double *dAB2,
                            double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms,
-                           int64_t *launches, bool window) {
+                           int64_t *launches, bool window, cudaEvent_t after_band) {
     const int64_t ldab1 = 3 * (int64_t)bw, ldab2 = 3 * (int64_t)tbw;
     int rc;
     if ((rc = dense_to_band<double, double>(dW, n, ldw, 0, bw, dAB1, ldab1, 0, 1, s)) != AVS_SUCCESS) return rc;
     if ((rc = band_stage<double>(dAB1, n, bw, tbw, ldab1, w, s, num_sms, 1, 0, 0)) != AVS_SUCCESS) return rc;
+    if (after_band) AVS_CUDA_TRY(cudaEventRecord(after_band, s));
     if ((rc = band_to_band<double, double>(dAB1, n, bw, ldab1, 0, tbw, dAB2, ldab2, 0, 1, s)) != AVS_SUCCESS)
         return rc;
     if (window && chase_window_supported(tbw)) {

@@ -42,7 +42,7 @@ extern "C" {
 #endif
 
 #define AVS_VERSION_MAJOR 0
-#define AVS_VERSION_MINOR 1
+#define AVS_VERSION_MINOR 2
 
 /* ---- status codes -------------------------------------------------------- */
 #define AVS_SUCCESS 0
@@ -119,6 +119,8 @@ typedef struct avs_report {
     int32_t status;
     double t_update_ms;  /* tensor-core modes: the trailing updates inside stage 1 (copies of Y,
                             the two tcgen05 GEMMs and the chain), summed over the half-steps */
+    double t_band_ms;    /* hierarchical stage 2: the blocked band reduction (band extraction
+                            included); the element chase is t_stage2_ms - t_band_ms */
 } avs_report;
 
 /* ---- handle ---------------------------------------------------------------- */
