@@ -403,10 +403,13 @@ def kernel_arch(device=0):
     return bv.value, pv.value
 
 
-def chase_rate(device=0, fp64=False):
-    """Measured compute roof of the bulge chase (flops/s, 4 per element step)."""
+def chase_rate(device=0, fp64=False, arith=None):
+    """Measured compute roof of the chase arithmetic (flops/s, 4 per element
+    step): double-float by default, FP64 with fp64=True, or arith in
+    {"df64", "fp64", "fp32"} (fp32: the blocked band reduction's arithmetic)."""
+    mode = {"df64": 0, "fp64": 1, "fp32": 2}[arith] if arith else (1 if fp64 else 0)
     r = ctypes.c_double(0.0)
-    _check(lib().avs_measure_chase_rate(int(device), 1 if fp64 else 0, ctypes.byref(r)), "avs_measure_chase_rate")
+    _check(lib().avs_measure_chase_rate(int(device), mode, ctypes.byref(r)), "avs_measure_chase_rate")
     return r.value
 
 

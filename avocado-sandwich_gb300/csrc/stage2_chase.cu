@@ -568,14 +568,42 @@ __global__ void __launch_bounds__(512) chase_rate_kernel(typename ChaseAr<S>::St
     Ar::st(out + blockIdx.x * (int64_t)blockDim.x + threadIdx.x, acc);
 }
 
+// The same element steps in plain FP32 (the arithmetic of the blocked band
+// reduction's applies in the FP32-class modes).
+__global__ void __launch_bounds__(512) fp32_rate_kernel(float *out, int iters) {
+    constexpr int K = 16;
+    float vals[K], sv[K];
+    const float seed = 1.0f + 1e-3f * (float)(threadIdx.x & 63);
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        vals[k] = seed + 0.01f * k;
+        sv[k] = 0.5f / (k + 1);
+    }
+    for (int it = 0; it < iters; ++it) {
+        float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+        for (int k = 0; k < K; k += 2) {
+            a0 = fmaf(vals[k], sv[k], a0);
+            a1 = fmaf(vals[k + 1], sv[k + 1], a1);
+        }
+        const float w = (a0 + a1) * 1e-3f;
+#pragma unroll
+        for (int k = 0; k < K; ++k) vals[k] = fmaf(-w, sv[k], vals[k]);
+    }
+    float acc = 0.f;
+#pragma unroll
+    for (int k = 0; k < K; ++k) acc += vals[k];
+    out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = acc;
+}
+
 }  // namespace
 
-// Measured rate (flops/s, 4 per element step) of the chase arithmetic in FP64
-// (fp64 != 0) or double-float, all SMs busy, timed with events; the output
-// buffer is allocated and freed here.
+// Measured rate (flops/s, 4 per element step) of the chase arithmetic in
+// double-float (mode 0), FP64 (1) or FP32 (2), all SMs busy, timed with events;
+// the output buffer is allocated and freed here.
 int stage2_rate(int fp64, int num_sms, double *flops_per_s) {
     const int threads = 512, blocks = num_sms * 4;
-    const int iters = fp64 ? 256 : 8192;
+    const int iters = fp64 == 1 ? 256 : (fp64 == 2 ? 32768 : 8192);
     void *out = nullptr;
     AVS_CUDA_TRY(cudaMalloc(&out, sizeof(double) * (size_t)blocks * threads));
     cudaEvent_t e0, e1;
@@ -584,8 +612,10 @@ int stage2_rate(int fp64, int num_sms, double *flops_per_s) {
     float best = 1e30f;
     for (int rep = 0; rep < 4; ++rep) {  // first launch warms up
         cudaEventRecord(e0);
-        if (fp64)
+        if (fp64 == 1)
             chase_rate_kernel<double><<<blocks, threads>>>(reinterpret_cast<double *>(out), iters);
+        else if (fp64 == 2)
+            fp32_rate_kernel<<<blocks, threads>>>(reinterpret_cast<float *>(out), iters);
         else
             chase_rate_kernel<df64><<<blocks, threads>>>(reinterpret_cast<float2 *>(out), iters);
         cudaEventRecord(e1);

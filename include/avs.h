@@ -341,7 +341,8 @@ int avs_kernel_arch(int device, int32_t *binary_version, int32_t *ptx_version);
 /* Diagnostics (no counterpart in the reference): the compute roof of the bulge
  * chase on `device` -- flops per second of its inner arithmetic (compensated
  * dot products and reflector updates, 4 flops per element step) in
- * double-float (fp64 == 0) or FP64, from registers on every SM.  The call
+ * double-float (fp64 == 0), FP64 (fp64 == 1) or FP32 (fp64 == 2: the
+ * arithmetic of the blocked band reduction), from registers on every SM.  The call
  * allocates and frees a small output buffer and synchronises the device. */
 int avs_measure_chase_rate(int device, int32_t fp64, double *flops_per_s);
 
