@@ -300,29 +300,87 @@ def chase_flops(n, bw):
     return float(total)
 
 
-def chase_roofline(args, stage2_ms, fp64_stages=False):
-    """Roofline of the bulge chase against its measured compute roof: the chase's
-    arithmetic (double-float compensated dots and updates) from registers on every
-    SM (avs_measure_chase_rate).  Its band (n x 3b x 8 bytes) stays in L2, so HBM
-    bytes are reported beside it, not as the bound."""
+def _panel_qr_flops(m, t):
+    """Householder QR of an m x t panel (m rows, t reflectors): per reflector k
+    the norm (2(m-k)), its application to the t-k-1 columns right of it
+    (4(m-k) each) and the Gram column v_j^T v_k of the compact-WY factor (2(m-k)
+    for each j < k), plus the factor's recurrence (k^2)."""
+    k = np.arange(min(t, max(m - 1, 0)))
+    mk = m - k
+    return float(np.sum(2 * mk + 4 * mk * (t - k - 1) + 2 * mk * k + k * k))
+
+
+def band_stage_flops(n, bw, tbw):
+    """Algorithmic flops of the blocked band reduction bw -> tbw (stage2_band.cu,
+    the reference's bidiag! stage): per sweep s (rows p = s tbw ..) and step m
+    (c0 = p + tbw + m bw), the R op -- QR of the L x tbw panel (L = min(bw, n -
+    c0)) and the compact-WY apply to its Mr = min(c0 + bw, n) - rho - tbw rows:
+    W = A V (2 Mr L tbw), Y = W T (Mr tbw^2), A -= Y V^T (2 Mr L tbw) -- and the
+    L op -- QR of the L x tbw panel and the apply to Mc = min(c0 + 2bw, n) - c0 -
+    tbw columns (4 L Mc tbw + Mc tbw^2).  About 8 n^2 bw."""
+    total = 0.0
+    nsw = (n - 2 - tbw) // tbw + 1 if n - 2 - tbw >= 0 else 0
+    panel = {}
+    for sw in range(nsw):
+        p = sw * tbw
+        nsteps = (n - 2 - p - tbw) // bw + 1
+        m = np.arange(nsteps)
+        c0 = p + tbw + m * bw
+        L = np.minimum(bw, n - c0)
+        rho = np.where(m == 0, p, c0 - bw)
+        mr = np.minimum(c0 + bw, n) - rho - tbw
+        mc = np.maximum(np.minimum(c0 + 2 * bw, n) - c0 - tbw, 0)
+        total += float(np.sum(4.0 * mr * L * tbw + mr * tbw * tbw + 4.0 * L * mc * tbw + mc * tbw * tbw))
+        for l_ in L:
+            l_ = int(l_)
+            if l_ not in panel:
+                panel[l_] = _panel_qr_flops(l_, tbw)
+            total += 2 * panel[l_]
+    return total
+
+
+NARROW_BAND = 16  # the hierarchical stage 2 reduces the band to this width, then chases it
+
+
+def chase_roofline(args, chase_ms, bw, fp64_stages=False, kernel="chase_win_kernel (band 16 -> bidiagonal)"):
+    """Roofline of the element bulge chase against its measured compute roof:
+    the chase's arithmetic (double-float compensated dots and updates) from
+    registers on every SM (avs_measure_chase_rate).  Its band (n x 3 bw x 8
+    bytes) stays in L2 and shared memory, so HBM bytes are reported beside it,
+    not as the bound."""
     import avs
     hbm, _, src = load_peaks()
-    n, b = args.n, args.tile
-    flops = chase_flops(n, b)
+    n = args.n
+    flops = chase_flops(n, bw)
     peak = avs.chase_rate(0, fp64=fp64_stages) / 1e12
-    t = stage2_ms / 1e3
+    t = chase_ms / 1e3
     ach = flops / t / 1e12
-    byts = n * (b + 1) * 8.0 + 2 * n * 8.0
-    traffic = load_traffic().get("stage2")
+    byts = n * (bw + 1) * 8.0 + 2 * n * 8.0
     return {"bound": "compute (double-float on the FP32 pipe)" if not fp64_stages else "compute (FP64)",
-            "kernel": "chase_cluster_kernel (band -> bidiagonal)", "achieved": ach, "peak": peak,
-            "unit": "TFLOP/s", "frac": ach / peak, "traffic": traffic,
-            "algorithmic": "chase_flops(n, b) = sum over sweeps j and steps m of 4L(rows + cols) + 6L = %.4e flops "
-                           "per launch (n=%d, b=%d), one launch per SVD, over the stage-2 event time" % (flops, n, b),
+            "kernel": kernel, "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+            "traffic": load_traffic().get("chase"), "ms": chase_ms,
+            "algorithmic": "chase_flops(n, bw) = sum over sweeps j and steps m of 4L(rows + cols) + 6L = %.4e flops "
+                           "per launch (n=%d, band %d), one launch per SVD, over the chase's event time"
+                           % (flops, n, bw),
             "peak_source": "measured: avs_measure_chase_rate (the chase's df64 arithmetic from registers, all SMs)",
             "hbm": {"algorithmic_bytes": byts, "achieved_gbs": byts / t / 1e9, "peak_gbs": hbm,
                     "frac": byts / t / 1e9 / hbm, "peak_source": src + " HBM copy",
-                    "note": "band stays in L2; HBM is not the bound"}}
+                    "note": "band stays in L2 / shared memory; HBM is not the bound"}}
+
+
+def band_roofline(args, band_ms, tbw=NARROW_BAND):
+    """Roofline of the blocked band reduction tile -> tbw (band_stage_kernel,
+    FP32 SIMT compact-WY applies) against the measured FP32 rate."""
+    import avs
+    flops = band_stage_flops(args.n, args.tile, tbw)
+    peak = avs.chase_rate(0, arith="fp32") / 1e12
+    ach = flops / (band_ms / 1e3) / 1e12
+    return {"bound": "compute (FP32 pipe)", "kernel": "band_stage_kernel (band %d -> %d)" % (args.tile, tbw),
+            "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak, "ms": band_ms,
+            "traffic": load_traffic().get("band_stage"),
+            "algorithmic": "band_stage_flops(n, %d, %d) = %.4e flops per launch (panels, compact-WY factors, "
+                           "W = A V, Y = W T, A -= Y V^T per op; about 8 n^2 b)" % (args.tile, tbw, flops),
+            "peak_source": "measured: avs_measure_chase_rate(fp32) (FP32 FMA steps from registers, all SMs)"}
 
 
 def tensor_roofline(args, update_ms):
@@ -513,6 +571,7 @@ def main():
         torch.distributed.barrier()
     stage = {"stage1": 0.0, "stage2": 0.0, "stage3": 0.0}
     update_ms = 0.0
+    band_ms = 0.0
     launches = 0
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(local) as clk:
@@ -524,6 +583,7 @@ def main():
             stage["stage2"] += rep.t_stage2_ms
             stage["stage3"] += rep.t_stage3_ms
             update_ms += rep.t_update_ms
+            band_ms += rep.t_band_ms
             launches += rep.kernel_launches
         end.record()
         torch.cuda.synchronize()
@@ -537,6 +597,7 @@ def main():
     sigma = s.double().cpu().numpy()
     stage = {k: v / args.steps for k, v in stage.items()}
     update_ms /= args.steps
+    band_ms /= args.steps
     per_svd = ms / 1e3 / args.steps
 
     # e2e: host matrix in, host sigma out, through avs_svdvals_s
@@ -555,8 +616,17 @@ def main():
             "data": "synthetic N(0,1/n), numpy PCG64 seed 4 + 1000*rank, rounded to float32",
             "config": dict(workload_desc(args), parallelism="replicas" if world > 1 else "single"),
             "stage_ms": stage, "gpu_launches": int(launches), "clocks": clk.summary(), "e2e": e2e}
-    line["roofline"] = chase_roofline(args, stage["stage2"]) if rank == 0 else None
+    hier = band_ms > 0.0
+    chase_ms = stage["stage2"] - band_ms
+    if rank == 0:
+        chase = chase_roofline(args, chase_ms, NARROW_BAND if hier else args.tile,
+                               kernel="chase_win_kernel (band %d -> bidiagonal)" % NARROW_BAND if hier
+                               else "chase_cluster_kernel (band %d -> bidiagonal)" % args.tile)
+        line["roofline"] = chase
+        if hier:
+            line["roofline_band_stage"] = band_roofline(args, band_ms)
     line["dominant_stage"] = max(stage, key=stage.get)
+    line["stage2_split_ms"] = {"band_reduction": band_ms, "element_chase": chase_ms}
     line["roofline_tensor_updates"] = tensor_roofline(args, update_ms)
     line["gflops"] = gflops_report(args, per_svd)
 
