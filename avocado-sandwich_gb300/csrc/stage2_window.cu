@@ -47,7 +47,7 @@ struct WinCfg {
     static constexpr int LDW = 3 * BW + 2;      // window column stride (16-byte multiple; odd stride - 1)
     static constexpr int W = 2 * G * BW + 2 * BW;  // window columns (span of a group's ops + prefetch)
     static constexpr int NC = 64 * G;           // compute threads: two warps per sweep
-    static constexpr int NB = NC + 32;          // threads of the tick barriers: compute warps + producer
+    static constexpr int D = 4;                 // ticks of the mbarrier ring (producer lookahead)
     static constexpr int NT = NC + 64;          // + the producer and the publisher warps
     static constexpr int CHUNKS = LDAB * 8 / 16;  // 16-byte chunks per column
     static_assert(BW % 2 == 0 && BW <= 32, "window chase band");
@@ -68,6 +68,28 @@ __device__ __forceinline__ void bar_arrive(int id, int cnt) {
     asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(cnt) : "memory");
 }
 
+// mbarriers of the tick ring: the producer's copies arrive on them
+// (cp.async.mbarrier.arrive.noinc: when all of the lane's earlier copies have
+// landed), the compute warps wait on the phase of their tick
+__device__ __forceinline__ void mbar_init(unsigned long long *m, unsigned cnt) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(m)), "r"(cnt) : "memory");
+}
+__device__ __forceinline__ void mbar_inval(unsigned long long *m) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(m)) : "memory");
+}
+__device__ __forceinline__ void cp_async_mbar_arrive(unsigned long long *m) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_addr(m)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *m, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(m)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
 __device__ __forceinline__ int ld_volatile_shared(const int *p) { return *(const volatile int *)p; }
 __device__ __forceinline__ void st_volatile_shared(int *p, int v) { *(volatile int *)p = v; }
 __device__ __forceinline__ int ld_relaxed(const int *p) {
@@ -86,6 +108,18 @@ __device__ __forceinline__ bool wait_shared_geq(const int *p, int target, int *e
             return false;
         }
         __nanosleep(32);
+    }
+    return true;
+}
+// Bounded wait for a phase of an mbarrier (kWaitNs, kSpinLimit polls); on
+// timeout kDevTimeout and false.
+__device__ __forceinline__ bool mbar_wait(unsigned long long *m, unsigned parity, int *err) {
+    const unsigned long long t0 = global_ns();
+    for (long long it = 0; !mbar_try_wait(m, parity); ++it) {
+        if (it > kSpinLimit || ((it & 63) == 63 && (long long)(global_ns() - t0) > kWaitNs)) {
+            atomicCAS(err, kDevOk, kDevTimeout);
+            return false;
+        }
     }
     return true;
 }
@@ -141,8 +175,11 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
     St *win = reinterpret_cast<St *>(smem_raw);  // [W][LDW]
     V *vbuf = reinterpret_cast<V *>(win + (size_t)W * LDW);  // [2G][32]: each compute warp's reflector
     __shared__ int s_g;
-    __shared__ int s_ret, s_wb;  // columns below s_ret are retired by the group; below s_wb written back
+    __shared__ int s_tick, s_wb;  // ticks the compute warps have finished; columns below s_wb written back
+    __shared__ __align__(8) unsigned long long s_full[Cfg::D];  // tick t's columns are in: phase t / D of [t % D]
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0)
+        for (int d = 0; d < Cfg::D; ++d) mbar_init(&s_full[d], 32);
     const int nsweeps = (int)(n - 1);
     const int ngroups = (nsweeps + G - 1) / G;
     auto A = [&](int r, int c) -> St * { return win + (size_t)(c % W) * LDW + (r - c + KU); };
@@ -159,7 +196,7 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
         int *retired = retired_base + (size_t)zb * sRet;
         const int j0 = g * G;
         if (tid == 0) {
-            s_ret = j0 + 1;
+            s_tick = 0;
             s_wb = j0 + 1;
         }
         __syncthreads();
@@ -187,14 +224,12 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
 
         if (wid == 2 * G) {
             // ---------------- producer warp: global -> window ----------------
-            // Between "tick t-1 done" and "tick t's columns are in" only the wait
-            // for copies issued earlier sits on the ticks' critical path; the
-            // bookkeeping and the prefetch of the next ticks come after the
-            // hand-off, while the compute warps run tick t.
+            // Each tick's copies arrive on the tick's mbarrier as they land; the
+            // producer runs up to D - 1 ticks ahead of the compute warps (the
+            // mbarrier ring) and never sits between two ticks.
             int issued = j0 + 1;               // columns below are requested (cp.async)
             int rp = (g == 0) ? (int)n : 0;    // retired[g-1] as last observed
             int rp_next = rp;                  // lane 0: a relaxed read in flight, used next tick
-            int before_last = j0 + 1;          // columns requested before the last copy group
             // copies of the columns [from, to) into their slots (one column per step, lanes over chunks)
             auto copy_in = [&](int from, int to) {
                 int sl = from % W;
@@ -205,8 +240,11 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                 }
             };
             for (int t = 0; t < nticks; ++t) {
-                if (t > 0) bar_sync(2, Cfg::NB);  // compute warps finished tick t-1
                 const int need = tick_need(t);
+                if (t >= Cfg::D) {  // the ring slot of tick t is free once the compute warps are past tick t - D
+                    if (lane == 0) wait_shared_geq(&s_tick, t - Cfg::D + 1, err);
+                    __syncwarp();
+                }
                 if (issued < need) {
                     // not prefetched (the previous group was behind): load now
                     if (rp < need) {
@@ -219,23 +257,9 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                         __syncwarp();
                     }
                     copy_in(issued, need);
-                    cp_commit();
-                    before_last = issued;
                     issued = need;
-                    cp_wait_all();
-                } else if (before_last >= need) {
-                    cp_wait_group<1>();  // in groups committed before the last one
-                } else {
-                    cp_wait_all();
                 }
-                __syncwarp();
-                __threadfence_block();
-                bar_arrive(1, Cfg::NB);  // the columns of tick t are in the window
-                // ---- off the critical path ----
-                if (t > 0 && lane == 0) {
-                    __threadfence_block();
-                    st_volatile_shared(&s_ret, min(retire_after(t - 1), issued));
-                }
+                cp_async_mbar_arrive(&s_full[t % Cfg::D]);  // tick t: when this lane's copies so far have landed
                 // lane 0's read of the previous group's boundary, issued last tick.  The
                 // copies of the columns it releases are issued only once the value has
                 // arrived (their range depends on it) and read L2, where the previous
@@ -247,27 +271,25 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                 const int tgt = min(min(tick_need(t + 3), rp), min(ld_volatile_shared(&s_wb) + W, (int)n));
                 if (tgt > issued) {
                     copy_in(issued, tgt);
-                    cp_commit();
-                    before_last = issued;
                     issued = tgt;
                 }
             }
-            bar_sync(2, Cfg::NB);  // the last tick
             cp_wait_all();
-            if (lane == 0) {
-                __threadfence_block();
-                st_volatile_shared(&s_ret, (int)n);  // everything is retired
-            }
         } else if (wid == 2 * G + 1) {
             // ---------------- publisher warp: window -> global, retired[g] ----------------
-            int wb = j0 + 1;
+            // Follows the compute warps' progress: after tick t-1 the columns left
+            // of retire_after(t-1) are final for this group; they are written back
+            // and the boundary is released for the next group.
+            int wb = j0 + 1, seen = 0;
             for (;;) {
-                int r = wb;
-                if (lane == 0) r = wait_shared_gt(&s_ret, wb, err);
-                r = __shfl_sync(0xffffffffu, r, 0);
-                if (r <= wb) break;  // only after a timeout (recorded)
-                __threadfence_block();
-                {
+                int tk = seen;
+                if (lane == 0) tk = wait_shared_gt(&s_tick, seen, err);
+                tk = __shfl_sync(0xffffffffu, tk, 0);
+                if (tk <= seen) break;  // only after a timeout (recorded)
+                seen = tk;
+                const int r = (tk >= nticks) ? (int)n : retire_after(tk - 1);
+                if (r > wb) {
+                    __threadfence_block();
                     int sl = wb % W;
                     for (int c = wb; c < r; ++c) {
                         for (int h = lane; h < Cfg::CHUNKS; h += 32) {
@@ -276,17 +298,17 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                         }
                         if (++sl == W) sl = 0;
                     }
+                    __syncwarp();
+                    wb = r;
+                    if (lane == 0) {
+                        st_volatile_shared(&s_wb, wb);  // the slots may be refilled
+                        __threadfence();
+                        st_release(retired + g, wb);
+                    }
                 }
-                __syncwarp();
-                wb = r;
-                if (lane == 0) {
-                    st_volatile_shared(&s_wb, wb);  // the slots may be refilled
-                    __threadfence();
-                    st_release(retired + g, wb);
-                }
-                if (wb >= (int)n) break;
+                if (tk >= nticks) break;
             }
-                } else {
+        } else {
             // ---------------- compute warps: warps 2i and 2i+1 run sweep j0 + i ----------------
             // Both warps of a pair form the same reflector (same data, same code:
             // the same bits); each applies it to half of the op's rows (R op) or
@@ -297,7 +319,12 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
             const int ops = (sw < gs) ? wops<BW>(n, j) : 0;
             V *sv = vbuf + wid * 32;
             for (int t = 0; t < nticks; ++t) {
-                bar_sync(1, Cfg::NB);  // the tick's columns are loaded; the previous tick is done
+                bar_sync(1, Cfg::NC);  // every compute warp is done with tick t-1
+                if (wid == 0 && lane == 0) {
+                    __threadfence_block();
+                    st_volatile_shared(&s_tick, t);  // ticks < t are done (publisher, producer)
+                }
+                mbar_wait(&s_full[t % Cfg::D], (unsigned)(t / Cfg::D) & 1u, err);  // tick t's columns are in
                 const int k = t - 4 * sw;
                 if (k >= 0 && k < ops) {
                     const WOp o = wop<BW>(n, j, k);
@@ -388,11 +415,20 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                     }
                 }
                 __syncwarp();
+            }
+            bar_sync(1, Cfg::NC);
+            if (wid == 0 && lane == 0) {
                 __threadfence_block();
-                bar_arrive(2, Cfg::NB);  // tick t done
+                st_volatile_shared(&s_tick, nticks);  // all ticks done
             }
         }
         __syncthreads();
+        if (tid == 0) {  // fresh phases for the next group
+            for (int d = 0; d < Cfg::D; ++d) {
+                mbar_inval(&s_full[d]);
+                mbar_init(&s_full[d], 32);
+            }
+        }
     }
 }
 
