@@ -236,7 +236,10 @@ def from_device(t):
 STAGES = {"auto": 0, "fp64": 1, "df64": 2}
 
 
-def my_CU_svdval(A, block_size, precision=None, report=None, handle=None, rel_tol=0.0, stages="auto"):
+FLAGS = {"one_stage_chase": 4, "band32": 8, "cluster_chase": 16, "hier_chase": 32}
+
+
+def my_CU_svdval(A, block_size, precision=None, report=None, handle=None, rel_tol=0.0, stages="auto", flags=0):
     """Singular values (descending) of the square matrix A with tile ``block_size``.
 
     ``A`` is a numpy array (the ``Matrix{Float32}`` method, host copies inside
@@ -248,7 +251,7 @@ def my_CU_svdval(A, block_size, precision=None, report=None, handle=None, rel_to
     "df64" (AVS_FLAG_FP64_STAGES / AVS_FLAG_DF64_STAGES).
     """
     h = handle or default_handle()
-    o = Opts(_prec(precision), STAGES[stages], float(rel_tol), None)
+    o = Opts(_prec(precision), STAGES[stages] | int(flags), float(rel_tol), None)
     r = report if report is not None else Report()
     if _is_torch_cuda(A):
         import torch

@@ -184,9 +184,11 @@ def test_zero_and_degenerate_inputs(avs_mod, torch_cuda):
 
 @pytest.mark.parametrize("n,b", [(512, 32), (1024, 64), (2048, 128), (2048, 256)])
 def test_double_float_stages_match_fp64_stages(avs_mod, torch_cuda, n, b):
-    """The bulge chase and bisection in double-float arithmetic (default for
-    FP32-class modes) agree with the FP64 stages; on FP64 tiles the
-    double-float stages stay within 1e-12 of the known spectrum."""
+    """The element chase and bisection in double-float arithmetic agree with
+    the FP64 stages on the same band (1e-9); on FP64 tiles the double-float
+    stages stay within 1e-12 of the known spectrum.  The default FP32-class
+    stage 2 (FP32 block stage to band 16, then the double-float chase) stays
+    at FP32 level of the FP64 stages."""
     from avs import workloads
     a, sig = workloads.geometric_spectrum(n, 21, 22, 1e-6)
     s64 = avs_mod.my_CU_svdval(a, b, stages="fp64")
@@ -195,9 +197,12 @@ def test_double_float_stages_match_fp64_stages(avs_mod, torch_cuda, n, b):
     assert rel_err(sdf, sig) < 1e-12
     a32 = a.astype(np.float32)
     s32_64 = avs_mod.my_CU_svdval(a32, b, stages="fp64")
-    s32_df = avs_mod.my_CU_svdval(a32, b)
+    s32_df = avs_mod.my_CU_svdval(a32, b, flags=avs_mod.FLAGS["one_stage_chase"])
     assert rel_err(s32_df, s32_64) < 1e-9
     assert rel_err(s32_df, sig) < 1e-5
+    s32_h = avs_mod.my_CU_svdval(a32, b)  # hierarchical for tiles >= 64
+    assert rel_err(s32_h, s32_64) < 1e-6
+    assert rel_err(s32_h, sig) < 1e-5
 
 
 @pytest.mark.parametrize("n,b", [(512, 128), (1024, 128), (1024, 256), (2048, 256)])
