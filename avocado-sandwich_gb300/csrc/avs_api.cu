@@ -92,7 +92,8 @@ Layout make_layout(int64_t n, int b, size_t elem, size_t stage_elem, int tc_fmt 
     o = align_up(o + sizeof(int) * (size_t)(n + 4));
     L.ldab = 3 * (int64_t)b;
     L.off_ab = o;
-    o = align_up(o + sizeof(double) * (size_t)L.ldab * (size_t)n);
+    // the one-stage chase's band (3b x n) or the block stage's (band_ldab(b) x n)
+    o = align_up(o + sizeof(double) * (size_t)band_stride(b, n));
     L.off_ab2 = o;  // the narrow band of the hierarchical chase (width <= kMaxNarrowBand)
     o = align_up(o + sizeof(double) * (size_t)(3 * kMaxNarrowBand) * (size_t)n);
     L.off_d = o;
@@ -855,9 +856,9 @@ int band_reduce_dev(avs_handle *h, int64_t n, int32_t bw, int32_t tbw, R *dB, in
     if (n == 0) return AVS_SUCCESS;
     AVS_CUDA_TRY(cudaSetDevice(h->device));
     const Layout L = make_layout(n, 1, 8, 0);
-    const int64_t ldab = 3 * (int64_t)bw;
+    const int64_t ldab = band_ldab(bw);
     const size_t ab_off = align_up(L.total);
-    const size_t fl_off = align_up(ab_off + sizeof(R) * (size_t)ldab * (size_t)n);
+    const size_t fl_off = align_up(ab_off + sizeof(R) * (size_t)band_stride(bw, n));
     int rc = ensure_ws(h, align_up(fl_off + sizeof(int) * (size_t)(n + 4)));
     if (rc != AVS_SUCCESS) return rc;
     cudaStream_t s = h->stream;
@@ -1101,7 +1102,7 @@ BatchLayout batch_layout(int64_t n, int b, int cnt, size_t elem = 4) {
     L.tblk = take(elem * (size_t)cnt * (nt + 1) * (b / 16) * 256);
     L.tfull = take(b >= 128 ? elem * (size_t)cnt * (nt + 1) * b * b : 0);
     L.f1 = take(sizeof(int) * (size_t)cnt * (2 * nt + 4));
-    L.ab = take(sizeof(float2) * (size_t)cnt * 3 * b * n);
+    L.ab = take(sizeof(double) * (size_t)cnt * (size_t)band_stride(b, n));
     L.ab2 = take(sizeof(double) * (size_t)cnt * 3 * kMaxNarrowBand * n);  // narrow band of the hierarchical chase
     L.f2 = take(sizeof(int) * ((size_t)cnt * (n + 1) + 4));
     L.d = take(sizeof(double) * (size_t)cnt * n);

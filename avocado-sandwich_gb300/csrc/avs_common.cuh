@@ -220,8 +220,15 @@ int stage2_chase_df_batched(const float *dW, int64_t n, int bw, int batch, float
 int stage2_chase_df_batched(const double *dW, int64_t n, int bw, int batch, float2 *dAB, int64_t ldab, double *dd,
                             double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches,
                             bool window);
-// Blocked band reduction bw -> tbw (stage2_band.cu), on a compact band
-// (A(r, c) at dAB[(r - c + 2bw - 1) + c * ldab], ldab >= 3 bw)
+// Blocked band reduction bw -> tbw (stage2_band.cu), on a compact band with
+// 16-byte aligned column segments: A(r, c) at dAB[(r - c + band_ku(bw)) + c *
+// ldab], ldab = band_ldab(bw) (rows c-2bw .. c+bw of column c; a segment that
+// starts at a row divisible by 4 starts on 16 bytes).
+__host__ __device__ constexpr int band_ku(int bw) { return 2 * bw; }
+__host__ __device__ constexpr int64_t band_ldab(int bw) { return 3 * (int64_t)bw + 1; }
+// elements from one matrix's compact band to the next in a batch (a multiple
+// of 4, so every matrix's segments stay on 16 bytes)
+__host__ __device__ constexpr int64_t band_stride(int bw, int64_t n) { return (band_ldab(bw) * n + 3) / 4 * 4; }
 template <typename R>
 int band_stage(R *dAB, int64_t n, int bw, int tbw, int64_t ldab, const Stage2Work &w, cudaStream_t s, int num_sms,
                int batch, int64_t sAB, int64_t sDone);

@@ -28,9 +28,11 @@
 // the compact-WY factor T (LAPACK xLARFT, forward, columnwise), then applies
 // the block reflector to its share of the rows (R op) or columns (L op) as
 // two small GEMMs on the FP32 (or FP64) pipe, operands in shared memory.
-// The band is the compact storage of the element chase, A(r, c) at
-// AB[(r - c + 2B - 1) + c * ldab], ldab >= 3B: rows c-2B+1 .. c+B-1 of
-// column c (band, upper bulge up to 2B-1, lower bulge up to B-1).
+// The band is in compact storage A(r, c) at AB[(r - c + 2B) + c * ldab],
+// ldab = 3B + 1 (band_ku / band_ldab): rows c-2B .. c+B of column c (band,
+// upper bulge up to 2B-1, lower bulge up to B-1), laid out so that every
+// column segment an op moves starts on 16 bytes: staging and write-back move
+// 16-byte vectors.
 //
 // Arithmetic: the element type R throughout (FP32 for the FP32-class modes,
 // FP64 for the FP64 path), reflector scalars included.
@@ -104,31 +106,64 @@ struct Vec4<double> {
     }
 };
 
-__device__ __forceinline__ float ldg_cg(const float *p) { return __ldcg(p); }
-__device__ __forceinline__ double ldg_cg(const double *p) { return __ldcg(p); }
+// 16-byte vectors of the element type: 4 floats or 2 doubles.
+template <typename R>
+struct Vec16;
+template <>
+struct Vec16<float> {
+    static constexpr int N = 4;
+    static __device__ __forceinline__ void ld(const float *p, float (&o)[4]) {
+        const float4 v = __ldcg(reinterpret_cast<const float4 *>(p));
+        o[0] = v.x;
+        o[1] = v.y;
+        o[2] = v.z;
+        o[3] = v.w;
+    }
+    static __device__ __forceinline__ void st(float *p, const float (&v)[4]) {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+};
+template <>
+struct Vec16<double> {
+    static constexpr int N = 2;
+    static __device__ __forceinline__ void ld(const double *p, double (&o)[2]) {
+        const double2 v = __ldcg(reinterpret_cast<const double2 *>(p));
+        o[0] = v.x;
+        o[1] = v.y;
+    }
+    static __device__ __forceinline__ void st(double *p, const double (&v)[2]) {
+        *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+    }
+};
 
-// Staging copy global (L2) -> shared of COUNT elements spread over NT threads:
-// element idx = tid + u * NT comes from src(idx) (nullptr: zero) and goes to
-// dst(idx).  The loads of a batch of 8 are all in flight before the first
-// store, so a thread waits for about one L2 latency per batch instead of one
-// per element.
-template <typename R, int NT, int COUNT, typename Src, typename Dst>
-__device__ __forceinline__ void stage_in(int tid, Src src, Dst dst) {
-    constexpr int PER = (COUNT + NT - 1) / NT;
+// Staging copy global (L2) -> shared of NV 16-byte vectors spread over NT
+// threads: vector idx = tid + u * NT comes from src(idx) (nullptr: zeros) and
+// goes to dst(idx, v).  The loads of a batch of 8 are all in flight before the
+// first store, so a thread waits for about one L2 latency per batch instead of
+// one per vector.
+template <typename R, int NT, int NV, typename Src, typename Dst>
+__device__ __forceinline__ void stage_in_vec(int tid, Src src, Dst dst) {
+    constexpr int N = Vec16<R>::N;
+    constexpr int PER = (NV + NT - 1) / NT;
     constexpr int BATCH = PER < 8 ? PER : 8;
 #pragma unroll
     for (int u0 = 0; u0 < PER; u0 += BATCH) {
-        R v[BATCH];
+        R v[BATCH][N];
 #pragma unroll
         for (int u = 0; u < BATCH; ++u) {
             const int idx = tid + (u0 + u) * NT;
-            const R *p = (u0 + u < PER && idx < COUNT) ? src(idx) : nullptr;
-            v[u] = p ? ldg_cg(p) : R(0);
+            const R *p = (u0 + u < PER && idx < NV) ? src(idx) : nullptr;
+            if (p) {
+                Vec16<R>::ld(p, v[u]);
+            } else {
+#pragma unroll
+                for (int e = 0; e < N; ++e) v[u][e] = R(0);
+            }
         }
 #pragma unroll
         for (int u = 0; u < BATCH; ++u) {
             const int idx = tid + (u0 + u) * NT;
-            if (u0 + u < PER && idx < COUNT) dst(idx, v[u]);
+            if (u0 + u < PER && idx < NV) dst(idx, v[u]);
         }
     }
 }
@@ -262,7 +297,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) band_stage_kernel
                                                           int64_t sDone) {
     using Cfg = BandCfg<B, T, C>;
     constexpr int NT = Cfg::NT, NW = Cfg::NW, LDP = Cfg::LDP, RPC = Cfg::RPC, LDW = Cfg::LDW;
-    constexpr int ku = 2 * B - 1;
+    constexpr int ku = band_ku(B);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R *P = reinterpret_cast<R *>(smem_raw);  // [T][LDP] panel (QR form), then V
     R *As = P + T * LDP;                      // apply staging
@@ -303,18 +338,36 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) band_stage_kernel
                 const int64_t rho = (m == 0) ? p : c0 - B;
                 const int64_t r_lo = rho + T + (int64_t)q * RPC;
                 const int64_t r_hi = (c0 + B < n) ? c0 + B : n;
-                // panel (QR form): P[k][c'] = A(rho + k, c0 + c')
-                stage_in<R, NT, T * B>(
-                    tid, [&](int idx) -> const R * { return (idx / T < L) ? at(rho + idx % T, c0 + idx / T) : nullptr; },
-                    [&](int idx, R v) { P[(idx % T) * LDP + idx / T] = v; });
-                // this CTA's rows of the apply, column-major [c][r]
-                stage_in<R, NT, RPC * B>(
+                constexpr int VN = Vec16<R>::N;
+                // panel (QR form): P[k][c'] = A(rho + k, c0 + c'); column c' of the
+                // pivot rows is T / VN vectors
+                stage_in_vec<R, NT, T / VN * B>(
                     tid,
                     [&](int idx) -> const R * {
-                        const int rr = idx % RPC, cc = idx / RPC;
-                        return (cc < L && r_lo + rr < r_hi) ? at(r_lo + rr, c0 + cc) : nullptr;
+                        const int cc = idx / (T / VN), pt = idx % (T / VN);
+                        return (cc < L) ? at(rho + pt * VN, c0 + cc) : nullptr;
                     },
-                    [&](int idx, R v) { As[(idx / RPC) * Cfg::LDA_R + idx % RPC] = v; });
+                    [&](int idx, const R(&v)[VN]) {
+                        const int cc = idx / (T / VN), pt = idx % (T / VN);
+#pragma unroll
+                        for (int e = 0; e < VN; ++e) P[(pt * VN + e) * LDP + cc] = v[e];
+                    });
+                // this CTA's rows of the apply, column-major [c][r] (a vector that
+                // starts below r_hi ends below c0 + B, inside the column's segment;
+                // its rows at or past r_hi are zeroed)
+                stage_in_vec<R, NT, RPC / VN * B>(
+                    tid,
+                    [&](int idx) -> const R * {
+                        const int cc = idx / (RPC / VN), pt = idx % (RPC / VN);
+                        return (cc < L && r_lo + pt * VN < r_hi) ? at(r_lo + pt * VN, c0 + cc) : nullptr;
+                    },
+                    [&](int idx, R(&v)[VN]) {
+                        const int pt = idx % (RPC / VN);
+#pragma unroll
+                        for (int e = 1; e < VN; ++e)
+                            if (r_lo + pt * VN + e >= r_hi) v[e] = R(0);
+                        Vec16<R>::st(As + (idx / (RPC / VN)) * Cfg::LDA_R + pt * VN, v);
+                    });
                 __syncthreads();
                 cl_arrive();  // done reading the pivot rows
                 panel_qr<R, B, T, NW>(P, s_tau, gram);
@@ -418,14 +471,24 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) band_stage_kernel
                                     acc[rr][c4 + cc] = fma(-y4[rr], v4[cc], acc[rr][c4 + cc]);
                         }
                     }
+                    constexpr int VN = Vec16<R>::N;
 #pragma unroll
                     for (int cc = 0; cc < CPT; ++cc) {
                         const int c = cb + cc;
                         if (c < L) {
 #pragma unroll
-                            for (int rr = 0; rr < 4; ++rr) {
-                                const int64_t r = r_lo + 4 * g + rr;
-                                if (r < r_hi) *at(r, c0 + c) = acc[rr][cc];
+                            for (int r0 = 0; r0 < 4; r0 += VN) {
+                                const int64_t r = r_lo + 4 * g + r0;
+                                if (r + VN <= r_hi) {
+                                    R v[VN];
+#pragma unroll
+                                    for (int e = 0; e < VN; ++e) v[e] = acc[r0 + e][cc];
+                                    Vec16<R>::st(at(r, c0 + c), v);
+                                } else {
+#pragma unroll
+                                    for (int e = 0; e < VN; ++e)
+                                        if (r + e < r_hi) *at(r + e, c0 + c) = acc[r0 + e][cc];
+                                }
                             }
                         }
                     }
@@ -434,21 +497,36 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) band_stage_kernel
                 const int Tc = (int)(n - c0 < T ? n - c0 : (int64_t)T);  // pivot columns
                 const int64_t cc_lo = c0 + T + (int64_t)q * RPC;
                 const int64_t c_hi = (c0 + 2 * B < n) ? c0 + 2 * B : n;
-                // panel: P[k][i] = A(c0 + i, c0 + k)
-                stage_in<R, NT, T * B>(
+                constexpr int VN = Vec16<R>::N;
+                // panel: P[k][i] = A(c0 + i, c0 + k); a vector that starts below L
+                // stays inside the column's segment, its rows at or past L are zeroed
+                stage_in_vec<R, NT, B / VN * T>(
                     tid,
                     [&](int idx) -> const R * {
-                        return (idx % B < L && idx / B < Tc) ? at(c0 + idx % B, c0 + idx / B) : nullptr;
+                        const int k = idx / (B / VN), pt = idx % (B / VN);
+                        return (pt * VN < L && k < Tc) ? at(c0 + pt * VN, c0 + k) : nullptr;
                     },
-                    [&](int idx, R v) { P[(idx / B) * LDP + idx % B] = v; });
+                    [&](int idx, R(&v)[VN]) {
+                        const int pt = idx % (B / VN);
+#pragma unroll
+                        for (int e = 1; e < VN; ++e)
+                            if (pt * VN + e >= L) v[e] = R(0);
+                        Vec16<R>::st(P + (idx / (B / VN)) * LDP + pt * VN, v);
+                    });
                 // this CTA's columns of the apply, column-major [cc][i]
-                stage_in<R, NT, RPC * B>(
+                stage_in_vec<R, NT, B / VN * RPC>(
                     tid,
                     [&](int idx) -> const R * {
-                        const int i = idx % B, cc = idx / B;
-                        return (i < L && cc_lo + cc < c_hi) ? at(c0 + i, cc_lo + cc) : nullptr;
+                        const int cc = idx / (B / VN), pt = idx % (B / VN);
+                        return (pt * VN < L && cc_lo + cc < c_hi) ? at(c0 + pt * VN, cc_lo + cc) : nullptr;
                     },
-                    [&](int idx, R v) { As[(idx / B) * Cfg::LDA_L + idx % B] = v; });
+                    [&](int idx, R(&v)[VN]) {
+                        const int pt = idx % (B / VN);
+#pragma unroll
+                        for (int e = 1; e < VN; ++e)
+                            if (pt * VN + e >= L) v[e] = R(0);
+                        Vec16<R>::st(As + (idx / (B / VN)) * Cfg::LDA_L + pt * VN, v);
+                    });
                 __syncthreads();
                 cl_arrive();  // done reading the pivot columns
                 panel_qr<R, B, T, NW>(P, s_tau, gram);
@@ -555,14 +633,24 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) band_stage_kernel
                                     acc[ii][c4 + cc] = fma(-v4[ii], y4[cc], acc[ii][c4 + cc]);
                         }
                     }
+                    constexpr int VN = Vec16<R>::N;
 #pragma unroll
                     for (int cc = 0; cc < CPT; ++cc) {
                         const int64_t c = cc_lo + cb + cc;
                         if (c < c_hi) {
 #pragma unroll
-                            for (int ii = 0; ii < 4; ++ii) {
-                                const int i = 4 * ig + ii;
-                                if (i < L) *at(c0 + i, c) = acc[ii][cc];
+                            for (int i0 = 0; i0 < 4; i0 += VN) {
+                                const int i = 4 * ig + i0;
+                                if (i + VN <= L) {
+                                    R v[VN];
+#pragma unroll
+                                    for (int e = 0; e < VN; ++e) v[e] = acc[i0 + e][cc];
+                                    Vec16<R>::st(at(c0 + i, c), v);
+                                } else {
+#pragma unroll
+                                    for (int e = 0; e < VN; ++e)
+                                        if (i + e < L) *at(c0 + i + e, c) = acc[i0 + e][cc];
+                                }
                             }
                         }
                     }
@@ -614,13 +702,13 @@ int launch_band_stage(R *dAB, int64_t n, int64_t ldab, const Stage2Work &w, cuda
 }
 
 // dense (leading dimension lda, matrix stride sA) -> compact band of width
-// bw (ku = 2bw - 1), zeros outside 0 <= c - r <= bw
+// bw (ku = band_ku(bw)), zeros outside 0 <= c - r <= bw
 template <typename TI, typename R>
 __global__ void dense_to_band_kernel(const TI *a, int64_t n, int64_t lda, int64_t sA, int bw, R *ab, int64_t ldab,
                                      int64_t sAB) {
     const int64_t c = blockIdx.x;
     const int64_t zb = blockIdx.y;
-    const int ku = 2 * bw - 1;
+    const int ku = band_ku(bw);
     const TI *az = a + zb * sA;
     R *abz = ab + zb * sAB + c * ldab;
     for (int i = threadIdx.x; i < ldab; i += blockDim.x) {
@@ -637,7 +725,7 @@ __global__ void band_to_band_kernel(const R *ab1, int64_t n, int bw1, int64_t ld
                                     int64_t ldab2, int64_t sAB2) {
     const int64_t c = blockIdx.x;
     const int64_t zb = blockIdx.y;
-    const int ku1 = 2 * bw1 - 1, ku2 = 2 * bw2 - 1;
+    const int ku1 = band_ku(bw1), ku2 = 2 * bw2 - 1;
     const R *src = ab1 + zb * sAB1;
     St *dst = ab2 + zb * sAB2 + c * ldab2;
     for (int i = threadIdx.x; i < ldab2; i += blockDim.x) {
@@ -654,11 +742,11 @@ __global__ void band_to_band_kernel(const R *ab1, int64_t n, int bw1, int64_t ld
 }
 
 // compact band (width bw storage) -> dense column-major n x n: every entry the
-// compact storage holds (rows c-2bw+1 .. c+bw-1 of column c), zeros elsewhere
+// compact storage holds (rows c-2bw .. c+bw of column c), zeros elsewhere
 template <typename R>
 __global__ void band_to_dense_kernel(const R *ab, int64_t n, int bw, int64_t ldab, R *a, int64_t lda) {
     const int64_t c = blockIdx.x;
-    const int ku = 2 * bw - 1;
+    const int ku = band_ku(bw);
     for (int64_t r = threadIdx.x; r < n; r += blockDim.x) {
         const int64_t i = ku + r - c;
         a[r + c * lda] = (i >= 0 && i < ldab) ? ab[i + c * ldab] : R(0);
@@ -679,7 +767,7 @@ template <typename R>
 int band_stage(R *dAB, int64_t n, int bw, int tbw, int64_t ldab, const Stage2Work &w, cudaStream_t s, int num_sms,
                int batch, int64_t sAB, int64_t sDone) {
     if (n < 3) return AVS_SUCCESS;
-    if (ldab < 3 * (int64_t)bw) return AVS_ERR_INTERNAL;
+    if (ldab != band_ldab(bw)) return AVS_ERR_INTERNAL;
     AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)((n + 1) * (int64_t)batch + 1), s));
 #define AVS_BAND_CASE(BB, TT)                                                                                   \
     if (bw == BB && tbw == TT)                                                                                  \

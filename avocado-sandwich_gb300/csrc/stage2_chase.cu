@@ -724,7 +724,7 @@ template int stage2_chase_df<double>(const double *, int64_t, int64_t, int, floa
 int stage2_chase_hier_df(const float *dW, int64_t n, int64_t ldw, int bw, int tbw, float *dAB1, float2 *dAB2,
                          double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms, int64_t *launches,
                          bool window, cudaEvent_t after_band) {
-    const int64_t ldab1 = 3 * (int64_t)bw, ldab2 = 3 * (int64_t)tbw;
+    const int64_t ldab1 = band_ldab(bw), ldab2 = 3 * (int64_t)tbw;
     int rc;
     if ((rc = dense_to_band<float, float>(dW, n, ldw, 0, bw, dAB1, ldab1, 0, 1, s)) != AVS_SUCCESS) return rc;
     if ((rc = band_stage<float>(dAB1, n, bw, tbw, ldab1, w, s, num_sms, 1, 0, 0)) != AVS_SUCCESS) return rc;
@@ -747,7 +747,7 @@ int stage2_chase_hier_df(const float *dW, int64_t n, int64_t ldw, int bw, int tb
 int stage2_chase_hier_fp64(const double *dW, int64_t n, int64_t ldw, int bw, int tbw, double *dAB1, double *dAB2,
                            double *dd, double *de, const Stage2Work &w, cudaStream_t s, int num_sms,
                            int64_t *launches, bool window, cudaEvent_t after_band) {
-    const int64_t ldab1 = 3 * (int64_t)bw, ldab2 = 3 * (int64_t)tbw;
+    const int64_t ldab1 = band_ldab(bw), ldab2 = 3 * (int64_t)tbw;
     int rc;
     if ((rc = dense_to_band<double, double>(dW, n, ldw, 0, bw, dAB1, ldab1, 0, 1, s)) != AVS_SUCCESS) return rc;
     if ((rc = band_stage<double>(dAB1, n, bw, tbw, ldab1, w, s, num_sms, 1, 0, 0)) != AVS_SUCCESS) return rc;
@@ -805,8 +805,8 @@ __global__ void bidiag_out_batched(const typename ChaseAr<S>::St *ab, int64_t n,
 
 // Batched stage 2, the same choices as a single call's run_stages23 (so a
 // matrix's values do not depend on its batch): tbw > 0: the blocked band
-// reduction bw -> tbw (arithmetic T, band dAB as T elements, 3 bw x n per
-// matrix), then the element chase of the narrow band (dAB2, 3 tbw x n per
+// reduction bw -> tbw (arithmetic T, band dAB as T elements, band_stride(bw,
+// n) per matrix), then the element chase of the narrow band (dAB2, 3 tbw x n per
 // matrix); tbw == 0: the element chase from width bw.  window: the element
 // chase in the shared-memory window (bands 8/16/32) instead of clusters.
 template <typename T, typename S>
@@ -816,7 +816,7 @@ int stage2_chase_batched(const T *dW, int64_t n, int bw, int batch, typename Cha
     using St = typename ChaseAr<S>::St;
     if (tbw > 0) {
         T *ab1 = reinterpret_cast<T *>(dAB);
-        const int64_t ldab1 = 3 * (int64_t)bw, sAB1 = ldab1 * n, ldab2 = 3 * (int64_t)tbw, sAB2 = ldab2 * n;
+        const int64_t ldab1 = band_ldab(bw), sAB1 = band_stride(bw, n), ldab2 = 3 * (int64_t)tbw, sAB2 = ldab2 * n;
         int rc;
         if ((rc = dense_to_band<T, T>(dW, n, n, n * n, bw, ab1, ldab1, sAB1, batch, s)) != AVS_SUCCESS) return rc;
         if ((rc = band_stage<T>(ab1, n, bw, tbw, ldab1, w, s, num_sms, batch, sAB1, n + 1)) != AVS_SUCCESS)

@@ -46,13 +46,12 @@ struct WinCfg {
     static constexpr int LDAB = 3 * BW;         // storage rows per column (global)
     static constexpr int LDW = 3 * BW + 2;      // window column stride (16-byte multiple; odd stride - 1)
     static constexpr int W = 2 * G * BW + 2 * BW;  // window columns (span of a group's ops + prefetch)
-    static constexpr int NC = 64 * G;           // compute threads: two warps per sweep
+    static constexpr int NC = 32 * G;           // compute threads: one warp per sweep
     static constexpr int D = 4;                 // ticks of the mbarrier ring (producer lookahead)
     static constexpr int NT = NC + 64;          // + the producer and the publisher warps
     static constexpr int CHUNKS = LDAB * 8 / 16;  // 16-byte chunks per column
     static_assert(BW % 2 == 0 && BW <= 32, "window chase band");
-    static constexpr size_t smem_bytes() { return 8 * ((size_t)W * LDW + (size_t)2 * G * 32); }
-    static_assert(G <= 13, "pair barriers 3 .. 3 + G - 1");
+    static constexpr size_t smem_bytes() { return 8 * ((size_t)W * LDW + (size_t)G * 32); }
 };
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -173,7 +172,7 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
     constexpr int KU = Cfg::KU, LDW = Cfg::LDW, W = Cfg::W, NC = Cfg::NC, NT = Cfg::NT, LDAB = Cfg::LDAB;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     St *win = reinterpret_cast<St *>(smem_raw);  // [W][LDW]
-    V *vbuf = reinterpret_cast<V *>(win + (size_t)W * LDW);  // [2G][32]: each compute warp's reflector
+    V *vbuf = reinterpret_cast<V *>(win + (size_t)W * LDW);  // [G][32]: each compute warp's reflector
     __shared__ int s_g;
     __shared__ int s_tick, s_wb;  // ticks the compute warps have finished; columns below s_wb written back
     __shared__ __align__(8) unsigned long long s_full[Cfg::D];  // tick t's columns are in: phase t / D of [t % D]
@@ -222,7 +221,7 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
             return lo;
         };
 
-        if (wid == 2 * G) {
+        if (wid == G) {
             // ---------------- producer warp: global -> window ----------------
             // Each tick's copies arrive on the tick's mbarrier as they land; the
             // producer runs up to D - 1 ticks ahead of the compute warps (the
@@ -275,7 +274,7 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                 }
             }
             cp_wait_all();
-        } else if (wid == 2 * G + 1) {
+        } else if (wid == G + 1) {
             // ---------------- publisher warp: window -> global, retired[g] ----------------
             // Follows the compute warps' progress: after tick t-1 the columns left
             // of retire_after(t-1) are final for this group; they are written back
@@ -309,12 +308,10 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                 if (tk >= nticks) break;
             }
         } else {
-            // ---------------- compute warps: warps 2i and 2i+1 run sweep j0 + i ----------------
-            // Both warps of a pair form the same reflector (same data, same code:
-            // the same bits); each applies it to half of the op's rows (R op) or
-            // columns (L op); the pair meets before the pivot row/column (the
-            // reflector's input) is overwritten.
-            const int sw = wid >> 1, half = wid & 1;
+            // ---------------- compute warps: warp i runs sweep j0 + i ----------------
+            // (one warp per sweep: measured faster than two warps sharing a sweep's
+            // reflector and halving its apply, 239 vs 300 ms at n = 16384)
+            const int sw = wid;
             const int j = j0 + sw;
             const int ops = (sw < gs) ? wops<BW>(n, j) : 0;
             V *sv = vbuf + wid * 32;
@@ -348,15 +345,13 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                         }
                         if (lane < L) sv[lane] = (lane == 0) ? Ar::one() : Ar::mul(x, scal);
                         __syncwarp();
-                        if (!Ar::iszero(tau) && lane < BW) {
+                        if (!Ar::iszero(tau)) {
                             // column c0 + i sits in slot s0 + i (wrapping at W): one modulo per op
                             const int s0 = o.c0 % W;
                             if (rop) {
-                                // lane = row r (this warp's half of rho+1 .. c1): A(r, c0 + i) at
-                                // slot(c0 + i) * LDW + (r - c0 - i + KU); from column to column the
-                                // address moves by LDW - 1 (- W LDW at the wrap)
-                                const int r = rho + 1 + half * BW + lane;
-                                if (r <= o.c1) {
+                                // lane = row r: A(r, c0 + i) at slot(c0 + i) * LDW + (r - c0 - i + KU);
+                                // from column to column the address moves by LDW - 1 (- W LDW at the wrap)
+                                for (int r = rho + 1 + lane; r <= o.c1; r += 32) {
                                     St *p0 = win + (size_t)s0 * LDW + (r - o.c0 + KU);
                                     V xv[BW];
                                     typename Ar::Acc a = Ar::acc_zero();
@@ -382,10 +377,8 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                                     }
                                 }
                             } else {
-                                // lane = column c (this warp's half of c0+1 .. hi): rows c0 .. c0+L-1
-                                // contiguous from A(c0, c)
-                                const int c = o.c0 + 1 + half * BW + lane;
-                                if (c <= o.hi) {
+                                // lane = column c: rows c0 .. c0+L-1 contiguous from A(c0, c)
+                                for (int c = o.c0 + 1 + lane; c <= o.hi; c += 32) {
                                     int sl = s0 + (c - o.c0);
                                     sl -= (sl >= W) ? W : 0;
                                     St *p = win + (size_t)sl * LDW + (o.c0 - c + KU);
@@ -405,10 +398,9 @@ __global__ void __launch_bounds__(WinCfg<BW, G>::NT, 1)
                                 }
                             }
                         }
-                        // the pivot row / column: beta and zeros, once both warps of the pair
-                        // have read it
-                        bar_sync(3 + sw, 64);
-                        if (half == 0 && lane < L) {
+                        // the pivot row / column: beta and zeros (every lane has read it:
+                        // the norm's shuffles came after the reads)
+                        if (lane < L) {
                             St *p = rop ? A(rho, o.c0 + lane) : A(o.c0 + lane, o.c0);
                             Ar::st(p, lane == 0 ? beta : Ar::zero());
                         }
