@@ -26,6 +26,8 @@ struct avs_handle {
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t aux = nullptr;  // stage 1's lookahead stream (panels and T builds)
+    cudaEvent_t la_ev[3] = {};   // its hand-off events
     void *ws = nullptr;
     size_t ws_bytes = 0;
     cudaEvent_t ev[7] = {};  // 6: after the blocked band reduction of stage 2
@@ -193,9 +195,14 @@ int narrow_band_of(int b, int flags, bool fp64) {
     return band_stage_supported(b, t) ? t : 0;
 }
 
-double bisect_tol(bool f64, const avs_opts *opts) {
+// Bisection width relative to ||B||: 2 eps in FP64; 4e-14 in double-float
+// when the tiles are FP64 (FP64X2: FP64-level results); 1e-10 in double-float
+// for the FP32-class modes, whose values carry the ~1e-7..1e-5 error of their
+// FP32 stage 1: the bracket is then 1000x below FP32's unit roundoff and the
+// multisection stops four passes earlier.
+double bisect_tol(bool f64, bool fp32_tiles, const avs_opts *opts) {
     if (opts && opts->bisect_rel_tol > 0) return opts->bisect_rel_tol;
-    return f64 ? 2.0 * DBL_EPSILON : 4e-14;
+    return f64 ? 2.0 * DBL_EPSILON : (fp32_tiles ? 1e-10 : 4e-14);
 }
 
 int check_common(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, const void *A, const void *sigma) {
@@ -321,9 +328,13 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
     w1.tc_split = tc_split;
     w1.tc_ws = tc_split ? ws_at(h, L.off_tc) : nullptr;
     w1.df_update = df_update ? 1 : 0;
+    w1.aux = h->aux;
+    w1.la_fork = h->la_ev[0];
+    w1.la_panel = h->la_ev[1];
+    w1.la_tb = h->la_ev[2];
     int upd_used = 0;
     if (tc_split && rep) {
-        const int pairs = (int)(2 * (n / b));
+        const int pairs = (int)(6 * (n / b));  // three parts per half-step
         while ((int)h->upd_ev.size() < 2 * pairs) {
             cudaEvent_t e;
             AVS_CUDA_TRY(cudaEventCreate(&e));
@@ -383,7 +394,7 @@ int svdvals_dev(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile, 
     const Layout L = make_layout(n, tile, elem, 0, split);
     if ((rc = ensure_ws(h, L.total)) != AVS_SUCCESS) return rc;
     const bool f64 = fp64_stages(prec, opts);
-    const double tol = bisect_tol(f64, opts);
+    const double tol = bisect_tol(f64, elem == 4, opts);
     if (elem == 8)
         return run_pipeline<double, TI, TO>(h, L, n, tile, dA, lda, dsigma, tol, f64, 0, s, rep, df_update_of(prec),
                                             flags_of(opts));
@@ -440,7 +451,7 @@ int svdvals_host(avs_handle *h, int64_t m, int64_t n, int64_t lda, int32_t tile,
                                    (size_t)n, cudaMemcpyHostToDevice, s));
     avs_report r2{};
     const bool f64 = fp64_stages(prec, opts);
-    const double tol = bisect_tol(f64, opts);
+    const double tol = bisect_tol(f64, elem == 4, opts);
     T *dout = reinterpret_cast<T *>(ws_at(h, L.off_out));
     if (elem == 8)
         rc = run_pipeline<double, T, T>(h, L, n, tile, stage, n, dout, tol, f64, 0, s, &r2, df_update_of(prec),
@@ -507,7 +518,9 @@ int avs_create(avs_handle **out, int device) {
     AVS_CUDA_TRY(cudaSetDevice(device));
     AVS_CUDA_TRY(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device));
     AVS_CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    AVS_CUDA_TRY(cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking));
     for (auto &e : h->ev) AVS_CUDA_TRY(cudaEventCreate(&e));
+    for (auto &e : h->la_ev) AVS_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     AVS_CUDA_TRY(cudaMallocHost(&h->h_err, sizeof(int)));
     *h->h_err = 0;
     *out = h;
@@ -526,6 +539,12 @@ int avs_destroy(avs_handle *h) {
     if (h->bws) cudaFree(h->bws);
     if (h->pinned) cudaFreeHost(h->pinned);
     for (cudaEvent_t e : h->upd_ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : h->la_ev)
+        if (e) cudaEventDestroy(e);
+    if (h->aux) {
+        cudaStreamSynchronize(h->aux);
+        cudaStreamDestroy(h->aux);
+    }
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return AVS_SUCCESS;
@@ -813,8 +832,9 @@ int ooc_call(avs_handle *h, int64_t n, int64_t lda, int32_t tile, T *A, T *sigma
             if ((r = band_to_device<T>(A, n, lda, tile, band, s)) != AVS_SUCCESS) return r;
             const bool f64 = fp64_stages(prec, opts);
             T *dout = reinterpret_cast<T *>(ws_at(h, L.off_out));
-            if ((r = run_stages23<T, T>(h, L, n, tile, band + tile, tile, dout, bisect_tol(f64, opts), f64, s,
-                                        &launches, opts ? opts->flags : 0)) != AVS_SUCCESS)
+            const double tol = bisect_tol(f64, sizeof(T) == 4, opts);
+            if ((r = run_stages23<T, T>(h, L, n, tile, band + tile, tile, dout, tol, f64, s, &launches,
+                                        opts ? opts->flags : 0)) != AVS_SUCCESS)
                 return r;
             AVS_CUDA_TRY(cudaMemcpyAsync(sigma, dout, sizeof(T) * (size_t)n, cudaMemcpyDeviceToHost, s));
         } else {
@@ -1331,7 +1351,7 @@ static int batched_call(avs_handle *h, int32_t count, const int64_t *n, const in
     // double-float stages 2-3 (FP64 stages on AVS_FLAG_FP64_STAGES), as its single call
     const bool dfu = sizeof(T) == 8 && opts && df_update_of(opts->precision);
     const bool f64s = sizeof(T) == 8 && (!dfu || (opts->flags & AVS_FLAG_FP64_STAGES));
-    const double tol = bisect_tol(f64s, opts);
+    const double tol = bisect_tol(f64s, sizeof(T) == 4, opts);
     // pinned layout: one status word per group (16 ints apart), then the pointer tables
     int *h_status = reinterpret_cast<int *>(h->pinned);
     void **tab = reinterpret_cast<void **>(h_status + 16 * (groups.size() + 1));

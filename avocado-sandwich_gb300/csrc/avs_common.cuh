@@ -123,6 +123,12 @@ struct Stage1Work {
     // blocks / full T / flag block at the given strides (elements, ints)
     int batch = 1;
     int64_t sA = 0, sTau = 0, sTblk = 0, sTfull = 0, sFlags = 0;
+    // optional (tensor-core path): a second stream and three events on which
+    // the next half-step's panel and T build run while the current trailing
+    // update finishes (lookahead); without them everything runs on the
+    // caller's stream in the same order
+    cudaStream_t aux = nullptr;
+    cudaEvent_t la_fork = nullptr, la_panel = nullptr, la_tb = nullptr;
 };
 template <typename T>
 int stage1_tbuild(const T *dA, int64_t lda, int b, int layout, int pr, int pc, int P, const Stage1Work &w,
@@ -146,11 +152,16 @@ int stage1_tc_planes_block(const float *x, int64_t n, int64_t r0, int64_t j0, in
                            cudaStream_t s);
 int stage1_tc_transpose(const float *src, float *dst, int64_t n, int64_t i0, int64_t j0, int fmt, const TcBufs &tb,
                         cudaStream_t s);
+// transpose of the box rows [i0, i0 + ni) x columns [j0, j0 + nj) of src
+// (ld n) into dst, with dst's operand planes (multiples of 32)
+int stage1_tc_transpose_box(const float *src, float *dst, int64_t n, int64_t i0, int64_t ni, int64_t j0, int64_t nj,
+                            int fmt, const TcBufs &tb, cudaStream_t s);
+enum TcParts : int { kTcS = 1, kTcChain = 2, kTcUpdate = 4, kTcAll = 7 };
 int stage1_tc_update(float *x, int64_t n, int b, int pr, int pc, int P, const Stage1Work &w, const TcBufs &tb,
-                     cudaStream_t s, int64_t *launches);
+                     cudaStream_t s, int64_t *launches, int parts = kTcAll, float *xt_out = nullptr);
 int stage1_chain_tc2(float *x, int64_t n, int b, int pr, int pc, int P, const float *tfull, void *t_hi, void *t_lo,
                      const void *y_hi, const void *y_lo, const float *S, int64_t ntr, void *w_hi, void *w_lo, int fmt,
-                     int *err, cudaStream_t s);
+                     int *err, cudaStream_t s, float *xt_out = nullptr);
 
 template <typename T>
 int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const Stage1Work &w,

@@ -37,6 +37,7 @@ struct ChainTcArgs {
     void *w_hi, *w_lo;  // [P][ntr][b] operand planes of W_p
     int fmt;
     int *err;
+    float *xt;  // optional: the final top strip transposed, xt[(j0 + c) + (top0 + l) * n]
 };
 
 template <int B, bool SPLIT, bool BF16>
@@ -50,7 +51,8 @@ struct CCfg {
     static constexpr int ZPLANE = NKB * ZT;       // bytes of one B plane
     static constexpr int AT = 128 * 128;          // bytes of one A tile (128 rows x 128 B)
     static constexpr int ASTAGE = HALVES * PL * AT;
-    static constexpr int TOP = B * NS * 4;        // FP32 top strip
+    static constexpr int TS = B + 1;              // top strip: column stride (padded for the transposed read)
+    static constexpr int TOP = TS * NS * 4;       // FP32 top strip
     static constexpr int SMEM = 1024 + PL * ZPLANE + 2 * ASTAGE + TOP;
     static constexpr int TCOLS = HALVES * NS;     // TMEM columns of the accumulator
     static constexpr int TALLOC = TCOLS < 32 ? 32 : TCOLS;
@@ -70,7 +72,7 @@ __global__ void __launch_bounds__(CNT, 1)
     uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_dyn) + 1023) & ~(uintptr_t)1023);
     uint8_t *zbuf = base;                               // B operand planes
     uint8_t *abuf = zbuf + C::PL * C::ZPLANE;           // A ring: [stage][half][plane]
-    float *top = reinterpret_cast<float *>(abuf + 2 * C::ASTAGE);  // [c][l]
+    float *top = reinterpret_cast<float *>(abuf + 2 * C::ASTAGE);  // [c][l], column stride TS
     const int tid = threadIdx.x, wid = tid >> 5, lane = tid & 31;
     const int64_t js = (int64_t)blockIdx.x * NS;
     const int64_t j0 = (int64_t)(args.pc + 1) * B + js;
@@ -104,7 +106,7 @@ __global__ void __launch_bounds__(CNT, 1)
 #pragma unroll
         for (int i = 0; i < E; ++i) {
             const int idx = tid + CNT * i;
-            top[idx] = v[i];  // top[c * B + l]
+            top[(idx / B) * C::TS + idx % B] = v[i];
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(CNT, 1)
 #pragma unroll
         for (int i = 0; i < E; ++i) {
             const int idx = tid + CNT * i, c = idx / B, l = idx % B;
-            put_z(c, l, p > 0 ? sv[i] + top[idx] : sv[i]);
+            put_z(c, l, p > 0 ? sv[i] + top[c * C::TS + l] : sv[i]);
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
@@ -243,7 +245,7 @@ __global__ void __launch_bounds__(CNT, 1)
                 read_acc(h, v);
                 const int l = h * 128 + 32 * wid + lane;
 #pragma unroll
-                for (int c = 0; c < NS; ++c) top[c * B + l] -= v[c];
+                for (int c = 0; c < NS; ++c) top[c * C::TS + l] -= v[c];
             }
         } else {
             for (int h = 0; h < C::HALVES; ++h) {
@@ -252,7 +254,7 @@ __global__ void __launch_bounds__(CNT, 1)
                 const int l = h * 128 + 32 * wid + lane;
 #pragma unroll
                 for (int c = 0; c < NS; ++c) {
-                    top[c * B + l] -= v[c];
+                    top[c * C::TS + l] -= v[c];
                     if (ok) tc::put_operand(args.fmt, args.w_hi, args.w_lo, ((int64_t)p * args.ntr + js + c) * B + l, v[c]);
                 }
             }
@@ -265,7 +267,14 @@ __global__ void __launch_bounds__(CNT, 1)
 #pragma unroll
         for (int i = 0; i < E; ++i) {
             const int idx = tid + CNT * i, c = idx / B, l = idx % B;
-            args.x[(top0 + l) + (j0 + c) * n] = top[idx];
+            args.x[(top0 + l) + (j0 + c) * n] = top[c * C::TS + l];
+        }
+        if (args.xt) {  // a warp writes 32 consecutive columns of one row: 128 bytes
+#pragma unroll
+            for (int i = 0; i < E; ++i) {
+                const int idx = tid + CNT * i, c = idx % NS, l = idx / NS;
+                args.xt[(j0 + c) + (top0 + l) * n] = top[c * C::TS + l];
+            }
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -300,7 +309,7 @@ int launch_chain_tc(const ChainTcArgs &a, const CUtensorMap (&m)[4], cudaStream_
 // the Y planes [P][t][l] (tile 0 = the masked GEQRT Y0).
 int stage1_chain_tc2(float *x, int64_t n, int b, int pr, int pc, int P, const float *tfull, void *t_hi, void *t_lo,
                      const void *y_hi, const void *y_lo, const float *S, int64_t ntr, void *w_hi, void *w_lo, int fmt,
-                     int *err, cudaStream_t s) {
+                     int *err, cudaStream_t s, float *xt_out) {
     if (ntr <= 0) return AVS_SUCCESS;
     if (ntr % NS) return AVS_ERR_INTERNAL;
     tplanes_kernel<<<512, 256, 0, s>>>(tfull, (int64_t)P * b * b, fmt, t_hi, t_lo);
@@ -312,7 +321,7 @@ int stage1_chain_tc2(float *x, int64_t n, int b, int pr, int pc, int P, const fl
         tc::Operand op{const_cast<void *>(planes[i]), nullptr, b, (int64_t)P * b, b};
         if (!tc::make_tmap(&m[i], op, op.hi, 128, bf)) return AVS_ERR_INTERNAL;
     }
-    ChainTcArgs a{x, n, pr, pc, P, S, ntr, w_hi, w_lo, fmt, err};
+    ChainTcArgs a{x, n, pr, pc, P, S, ntr, w_hi, w_lo, fmt, err, xt_out};
     if (b == 256) {
         if (fmt == tc::kTF32) return launch_chain_tc<256, false, false>(a, m, s);
         if (fmt == tc::kTF32X3) return launch_chain_tc<256, true, false>(a, m, s);

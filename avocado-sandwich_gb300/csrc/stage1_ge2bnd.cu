@@ -855,13 +855,14 @@ int copy_tau_out(void *out, const Stage1Work &w, int nt, int k, int first, int P
 
 }  // namespace
 
-// Tensor-core trailing update of one half-step, bracketed by a pair of the
-// caller's events when it asked for timing.
+// Tensor-core trailing update (the parts of stage1_tc_update in `parts`) of
+// one half-step, bracketed by a pair of the caller's events when it asked for
+// timing.
 int timed_update(float *X, int64_t n, int b, int pr, int pc, int P, const Stage1Work &w, const TcBufs &tb,
-                 cudaStream_t s, int64_t *launches) {
+                 cudaStream_t s, int64_t *launches, int parts = kTcAll, float *xt_out = nullptr) {
     const bool timed = w.ev_pairs && w.ev_used && *w.ev_used < w.ev_cap;
     if (timed) AVS_CUDA_TRY(cudaEventRecord(w.ev_pairs[2 * *w.ev_used], s));
-    const int rc = stage1_tc_update(X, n, b, pr, pc, P, w, tb, s, launches);
+    const int rc = stage1_tc_update(X, n, b, pr, pc, P, w, tb, s, launches, parts, xt_out);
     if (rc != AVS_SUCCESS) return rc;
     if (timed) {
         AVS_CUDA_TRY(cudaEventRecord(w.ev_pairs[2 * *w.ev_used + 1], s));
@@ -870,38 +871,98 @@ int timed_update(float *X, int64_t n, int b, int pr, int pc, int P, const Stage1
     return AVS_SUCCESS;
 }
 
+// The lookahead's stream hand-offs: `from` records ev, `to` waits for it
+// (nothing when both are the caller's stream).
+int hand_off(cudaStream_t from, cudaStream_t to, cudaEvent_t ev) {
+    if (from == to || !ev) return AVS_SUCCESS;
+    AVS_CUDA_TRY(cudaEventRecord(ev, from));
+    AVS_CUDA_TRY(cudaStreamWaitEvent(to, ev, 0));
+    return AVS_SUCCESS;
+}
+
 // GE2BND with tensor-core trailing updates (FP32 tiles, b = 128 or 256, one
 // matrix, lda = n): QR half-steps on X, LQ half-steps as QR half-steps on the
-// transposed trailing block in tb.xt.
+// transposed trailing block in XT.
+//
+// Lookahead: the next half-step's panel works on the top tile row that the
+// chain of the current update has just finished (the chain writes it into the
+// other buffer as well, transposed), so the panel and its T build run on the
+// aux stream while the caller's stream finishes the update (A_p -= Y_p W_p and
+// the transpose of the rows below).  The Y copies and S_p = Y_p^T A_p need the
+// panel only and run beside the T build; the chain waits for both.  Every
+// kernel touches the same data in the same order as without the overlap:
+//   QR half-step k: panel/tbuild on X column tile k; the chain writes X row
+//     tile k (columns >= k+1) and its transpose, XT column tile k; then the
+//     LQ panel (XT column tile k) overlaps the update of X rows >= k+1 and the
+//     transpose X -> XT of rows and columns >= k+1.
+//   LQ half-step k: the chain writes XT row tile k+1 and its transpose, X
+//     column tile k+1 (rows >= k+1) = the next QR panel, which overlaps the
+//     update of XT rows >= k+2 and the transposes back (XT rows >= k+2, and
+//     the one tile XT(k+1, k) -> X(k, k+1)).
 int stage1_ge2bnd_tc(float *X, int64_t n, int b, const Stage1Work &w, cudaStream_t s, int64_t *launches) {
     const int nt = (int)(n / b);
     const int fmt = w.tc_split;
     const TcBufs tb = stage1_tc_carve(w.tc_ws, n, b, fmt);
     float *XT = tb.xt;
+    const bool la = w.aux && w.la_fork && w.la_panel && w.la_tb;
+    cudaStream_t a = la ? w.aux : s;
     int rc;
     if ((rc = stage1_tc_planes(X, n, fmt, tb, s)) != AVS_SUCCESS) return rc;
-    for (int k = 0; k < nt; ++k) {
-        const int64_t kb = (int64_t)k * b, k1b = (int64_t)(k + 1) * b;
-        const int P = nt - k;
-        if ((rc = launch_panel<float, 0>(X, n, b, k, k, P, 0, w, s)) != AVS_SUCCESS) return rc;
-        if ((rc = copy_tau_out<float>(w.tau_q_out, w, nt, k, k, P, b, s)) != AVS_SUCCESS) return rc;
-        if (launches) *launches += 1;
-        if (k == nt - 1) break;  // no trailing columns left
-        if ((rc = stage1_tbuild<float>(X, n, b, 0, k, k, P, w, s)) != AVS_SUCCESS) return rc;
-        if ((rc = timed_update(X, n, b, k, k, P, w, tb, s, launches)) != AVS_SUCCESS) return rc;
-        if (launches) *launches += 1;
-        // X rows kb.., columns k1b.. -> XT rows k1b.., columns kb..
-        if ((rc = stage1_tc_transpose(X, XT, n, kb, k1b, fmt, tb, s)) != AVS_SUCCESS) return rc;
-        const int PL = nt - k - 1;
-        if ((rc = launch_panel<float, 0>(XT, n, b, k + 1, k, PL, 0, w, s)) != AVS_SUCCESS) return rc;
-        if ((rc = copy_tau_out<float>(w.tau_p_out, w, nt, k, k + 1, PL, b, s)) != AVS_SUCCESS) return rc;
-        if ((rc = stage1_tbuild<float>(XT, n, b, 0, k + 1, k, PL, w, s)) != AVS_SUCCESS) return rc;
-        if ((rc = timed_update(XT, n, b, k + 1, k, PL, w, tb, s, launches)) != AVS_SUCCESS) return rc;
-        // and back: XT rows k1b.., columns kb.. -> X rows kb.., columns k1b..
-        if ((rc = stage1_tc_transpose(XT, X, n, k1b, kb, fmt, tb, s)) != AVS_SUCCESS) return rc;
-        if (launches) *launches += 4;
+    // panel + tau copy + T build of one half-step on the aux stream, with the
+    // hand-offs back to the caller's stream after the panel and after the T build
+    auto panel_tb = [&](float *M, int pr, int pc, int P, void *tau_out, int k, int first) -> int {
+        int r;
+        if ((r = hand_off(s, a, la ? w.la_fork : nullptr)) != AVS_SUCCESS) return r;
+        if ((r = launch_panel<float, 0>(M, n, b, pr, pc, P, 0, w, a)) != AVS_SUCCESS) return r;
+        if ((r = copy_tau_out<float>(tau_out, w, nt, k, first, P, b, a)) != AVS_SUCCESS) return r;
+        if (la) AVS_CUDA_TRY(cudaEventRecord(w.la_panel, a));
+        if ((int64_t)(pc + 1) * b < n && (r = stage1_tbuild<float>(M, n, b, 0, pr, pc, P, w, a)) != AVS_SUCCESS)
+            return r;
+        if (la) AVS_CUDA_TRY(cudaEventRecord(w.la_tb, a));
+        if (launches) *launches += 2;
+        return AVS_SUCCESS;
+    };
+    // the head of a half-step's update: S after the panel, the chain after the T build
+    auto head = [&](float *M, int pr, int pc, int P, float *other) -> int {
+        int r;
+        if (la) AVS_CUDA_TRY(cudaStreamWaitEvent(s, w.la_panel, 0));
+        if ((r = timed_update(M, n, b, pr, pc, P, w, tb, s, launches, kTcS)) != AVS_SUCCESS) return r;
+        if (la) AVS_CUDA_TRY(cudaStreamWaitEvent(s, w.la_tb, 0));
+        return timed_update(M, n, b, pr, pc, P, w, tb, s, launches, kTcChain, other);
+    };
+    auto finish = [&](int r) -> int {  // the aux stream joins the caller's before any return
+        if (la) {
+            cudaEventRecord(w.la_fork, a);
+            cudaStreamWaitEvent(s, w.la_fork, 0);
+        }
+        return r;
+    };
+    if ((rc = panel_tb(X, 0, 0, nt, w.tau_q_out, 0, 0)) != AVS_SUCCESS) return finish(rc);
+    for (int k = 0; k + 1 < nt; ++k) {
+        const int64_t k1b = (int64_t)(k + 1) * b, k2b = (int64_t)(k + 2) * b;
+        const int P = nt - k, PL = nt - k - 1;
+        // QR half-step k (its panel and T build are done or in flight on aux)
+        if ((rc = head(X, k, k, P, XT)) != AVS_SUCCESS) return finish(rc);
+        if ((rc = panel_tb(XT, k + 1, k, PL, w.tau_p_out, k, k + 1)) != AVS_SUCCESS) return finish(rc);
+        if ((rc = timed_update(X, n, b, k, k, P, w, tb, s, launches, kTcUpdate)) != AVS_SUCCESS) return finish(rc);
+        // X rows, columns >= k+1 -> XT
+        if ((rc = stage1_tc_transpose_box(X, XT, n, k1b, n - k1b, k1b, n - k1b, fmt, tb, s)) != AVS_SUCCESS)
+            return finish(rc);
+        // LQ half-step k
+        if ((rc = head(XT, k + 1, k, PL, X)) != AVS_SUCCESS) return finish(rc);
+        if ((rc = panel_tb(X, k + 1, k + 1, P - 1, w.tau_q_out, k + 1, k + 1)) != AVS_SUCCESS) return finish(rc);
+        if ((rc = timed_update(XT, n, b, k + 1, k, PL, w, tb, s, launches, kTcUpdate)) != AVS_SUCCESS)
+            return finish(rc);
+        // and back: XT rows >= k+2 (all columns >= k) -> X, and the LQ panel's top tile
+        if ((rc = stage1_tc_transpose_box(XT, X, n, k2b, n - k2b, (int64_t)k * b, n - (int64_t)k * b, fmt, tb, s)) !=
+            AVS_SUCCESS)
+            return finish(rc);
+        if ((rc = stage1_tc_transpose_box(XT, X, n, k1b, b, (int64_t)k * b, b, fmt, tb, s)) != AVS_SUCCESS)
+            return finish(rc);
+        if (launches) *launches += 3;
     }
-    return AVS_SUCCESS;
+    // the last QR panel (one tile, no trailing columns) ran on aux
+    return finish(AVS_SUCCESS);
 }
 
 template <typename T>

@@ -135,48 +135,68 @@ int stage1_tc_transpose(const float *src, float *dst, int64_t n, int64_t i0, int
     return AVS_SUCCESS;
 }
 
+int stage1_tc_transpose_box(const float *src, float *dst, int64_t n, int64_t i0, int64_t ni, int64_t j0, int64_t nj,
+                            int fmt, const TcBufs &tb, cudaStream_t s) {
+    if (ni <= 0 || nj <= 0) return AVS_SUCCESS;
+    if (ni % 32 || nj % 32 || i0 + ni > n || j0 + nj > n) return AVS_ERR_INTERNAL;
+    transpose_kernel<<<dim3((unsigned)(ni / 32), (unsigned)(nj / 32)), dim3(32, 8), 0, s>>>(src, dst, n, i0, j0, fmt,
+                                                                                          tb.ph, tb.pl);
+    AVS_CUDA_TRY(cudaGetLastError());
+    return AVS_SUCCESS;
+}
+
 // Trailing update of the QR half-step with panel (pr, pc) and P tiles on the
-// column-major n x n matrix x (ld n), after the panel and the T build.
+// column-major n x n matrix x (ld n), after the panel and the T build.  parts
+// selects the steps (a caller that overlaps other work with the update runs
+// them separately): kTcS = Y copies and S_p = Y_p^T A_p (needs the panel
+// only), kTcChain = the chain (needs the T factors; writes the top tile row,
+// and its transpose into xt_out when given), kTcUpdate = A_p -= Y_p W_p.
 int stage1_tc_update(float *x, int64_t n, int b, int pr, int pc, int P, const Stage1Work &w, const TcBufs &tb,
-                     cudaStream_t s, int64_t *launches) {
+                     cudaStream_t s, int64_t *launches, int parts, float *xt_out) {
     const int fmt = w.tc_split;
     const int64_t r0 = (int64_t)pr * b, c0 = (int64_t)pc * b, j0 = (int64_t)(pc + 1) * b;
     const int64_t ntr = n - j0;
     if (ntr <= 0) return AVS_SUCCESS;
     int rc;
-    ycopy_kernel<<<dim3(b / 32, b / 32, P), dim3(32, 8), 0, s>>>(x, n, r0, c0, b, fmt, tb.ych, tb.ycl, tb.yrh,
-                                                                tb.yrl);
-    AVS_CUDA_TRY(cudaGetLastError());
     const int nkb = b * tc::fmt_bytes(fmt) / 128;
-    // S_p = Y_p^T A_p, p = 0..P-1 (A_0 = the top tile row)
-    {
-        tc::Operand A{tb.ych, tb.ycl, b, (int64_t)P * b, b};
-        tc::Operand B{tb.ph, tb.pl, n, n, n};
-        tc::GemmDesc g{};
-        g.p0 = 0;
-        g.a_y0 = 0;
-        g.a_yp = b;
-        g.b_x0 = (int)r0;
-        g.b_xp = b;
-        g.b_y0 = (int)j0;
-        g.b_yp = 0;
-        g.nkb = nkb;
-        g.epi = tc::kEpiStore;
-        g.out = tb.S;
-        g.ld_out = b;
-        g.o_row0 = 0;
-        g.o_rowp = 0;
-        g.o_col0 = 0;
-        g.o_colp = ntr;
-        g.err = w.err;
-        if ((rc = tc::gemm(fmt, A, B, g, b, (int)ntr, P, s)) != AVS_SUCCESS) return rc;
+    if (parts & kTcS) {
+        ycopy_kernel<<<dim3(b / 32, b / 32, P), dim3(32, 8), 0, s>>>(x, n, r0, c0, b, fmt, tb.ych, tb.ycl, tb.yrh,
+                                                                    tb.yrl);
+        AVS_CUDA_TRY(cudaGetLastError());
+        // S_p = Y_p^T A_p, p = 0..P-1 (A_0 = the top tile row)
+        {
+            tc::Operand A{tb.ych, tb.ycl, b, (int64_t)P * b, b};
+            tc::Operand B{tb.ph, tb.pl, n, n, n};
+            tc::GemmDesc g{};
+            g.p0 = 0;
+            g.a_y0 = 0;
+            g.a_yp = b;
+            g.b_x0 = (int)r0;
+            g.b_xp = b;
+            g.b_y0 = (int)j0;
+            g.b_yp = 0;
+            g.nkb = nkb;
+            g.epi = tc::kEpiStore;
+            g.out = tb.S;
+            g.ld_out = b;
+            g.o_row0 = 0;
+            g.o_rowp = 0;
+            g.o_col0 = 0;
+            g.o_colp = ntr;
+            g.err = w.err;
+            if ((rc = tc::gemm(fmt, A, B, g, b, (int)ntr, P, s)) != AVS_SUCCESS) return rc;
+        }
+        if (launches) *launches += 2;
     }
     // chain along the tiles (top tile row, W_p)
-    if ((rc = stage1_chain_tc2(x, n, b, pr, pc, P, static_cast<const float *>(w.tfull), tb.th, tb.tl, tb.yrh, tb.yrl,
-                               tb.S, ntr, tb.wh, tb.wl, fmt, w.err, s)) != AVS_SUCCESS)
-        return rc;
+    if (parts & kTcChain) {
+        if ((rc = stage1_chain_tc2(x, n, b, pr, pc, P, static_cast<const float *>(w.tfull), tb.th, tb.tl, tb.yrh,
+                                   tb.yrl, tb.S, ntr, tb.wh, tb.wl, fmt, w.err, s, xt_out)) != AVS_SUCCESS)
+            return rc;
+        if (launches) *launches += 2;
+    }
     // A_p -= Y_p W_p, p = 1..P-1
-    if (P > 1) {
+    if ((parts & kTcUpdate) && P > 1) {
         tc::Operand A{tb.yrh, tb.yrl, b, (int64_t)P * b, b};
         tc::Operand B{tb.wh, tb.wl, b, (int64_t)P * ntr, b};
         tc::GemmDesc g{};
@@ -197,8 +217,8 @@ int stage1_tc_update(float *x, int64_t n, int b, int pr, int pc, int P, const St
         g.o_colp = 0;
         g.err = w.err;
         if ((rc = tc::gemm(fmt, A, B, g, b, (int)ntr, P - 1, s)) != AVS_SUCCESS) return rc;
+        if (launches) *launches += 1;
     }
-    if (launches) *launches += (P > 1) ? 5 : 4;
     return AVS_SUCCESS;
 }
 

@@ -102,7 +102,8 @@ typedef struct avs_opts {
     int32_t precision;      /* AVS_PREC_* (0 = default for the entry point's type) */
     int32_t flags;          /* AVS_FLAG_* (0 = defaults) */
     double bisect_rel_tol;  /* bisection width relative to ||B|| (0 = 2 * DBL_EPSILON in FP64,
-                               4e-14 in double-float) */
+                               4e-14 in double-float on FP64 tiles, 1e-10 in double-float
+                               for the FP32-class modes) */
     void *stream;           /* cudaStream_t for the _dev entry points (NULL = handle stream) */
 } avs_opts;
 
