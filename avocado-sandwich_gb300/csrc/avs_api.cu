@@ -518,7 +518,13 @@ int avs_create(avs_handle **out, int device) {
     AVS_CUDA_TRY(cudaSetDevice(device));
     AVS_CUDA_TRY(cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, device));
     AVS_CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
-    AVS_CUDA_TRY(cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking));
+    {
+        // the lookahead stream at the highest priority: the panels are a latency-bound chain on
+        // few SMs, and the block scheduler then places them ahead of the update's tiles
+        int least = 0, greatest = 0;
+        AVS_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        AVS_CUDA_TRY(cudaStreamCreateWithPriority(&h->aux, cudaStreamNonBlocking, greatest));
+    }
     for (auto &e : h->ev) AVS_CUDA_TRY(cudaEventCreate(&e));
     for (auto &e : h->la_ev) AVS_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     AVS_CUDA_TRY(cudaMallocHost(&h->h_err, sizeof(int)));

@@ -123,10 +123,10 @@ struct Stage1Work {
     // blocks / full T / flag block at the given strides (elements, ints)
     int batch = 1;
     int64_t sA = 0, sTau = 0, sTblk = 0, sTfull = 0, sFlags = 0;
-    // optional (tensor-core path): a second stream and three events on which
-    // the next half-step's panel and T build run while the current trailing
-    // update finishes (lookahead); without them everything runs on the
-    // caller's stream in the same order
+    // optional (tensor-core path): a second stream (high priority) and three
+    // events on which the next half-step's panel and T build run while the
+    // current trailing update finishes (lookahead); without them everything
+    // runs on the caller's stream in the same order
     cudaStream_t aux = nullptr;
     cudaEvent_t la_fork = nullptr, la_panel = nullptr, la_tb = nullptr;
 };
