@@ -334,7 +334,7 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
     w1.la_tb = h->la_ev[2];
     int upd_used = 0;
     if (tc_split && rep) {
-        const int pairs = (int)(6 * (n / b));  // three parts per half-step
+        const int pairs = (int)(8 * (n / b));  // four parts per half-step
         while ((int)h->upd_ev.size() < 2 * pairs) {
             cudaEvent_t e;
             AVS_CUDA_TRY(cudaEventCreate(&e));

@@ -143,6 +143,7 @@ struct TcBufs {
     float *S;         // [nt][n][b] S_p = Y_p^T A_p
     void *wh, *wl;    // [nt][n][b] W_p planes
     void *th, *tl;    // [nt][b][b] T_p planes
+    int *ready;       // [nt + 1] per-tile counters of finished chain strips
     size_t bytes;
 };
 TcBufs stage1_tc_carve(void *ws, int64_t n, int b, int fmt);
@@ -156,12 +157,18 @@ int stage1_tc_transpose(const float *src, float *dst, int64_t n, int64_t i0, int
 // (ld n) into dst, with dst's operand planes (multiples of 32)
 int stage1_tc_transpose_box(const float *src, float *dst, int64_t n, int64_t i0, int64_t ni, int64_t j0, int64_t nj,
                             int fmt, const TcBufs &tb, cudaStream_t s);
-enum TcParts : int { kTcS = 1, kTcChain = 2, kTcUpdate = 4, kTcAll = 7 };
+enum TcParts : int { kTcS = 1, kTcChain = 2, kTcUpdate = 4, kTcPlanes = 8, kTcAll = 15 };
+// columns of the chain's strips: the chain signals a tile of the top row
+// (ready[tile] += 1 per strip, b / kChainStrip strips per tile) once the
+// strip's final values are in memory
+constexpr int kChainStrip = 32;
 int stage1_tc_update(float *x, int64_t n, int b, int pr, int pc, int P, const Stage1Work &w, const TcBufs &tb,
-                     cudaStream_t s, int64_t *launches, int parts = kTcAll, float *xt_out = nullptr);
-int stage1_chain_tc2(float *x, int64_t n, int b, int pr, int pc, int P, const float *tfull, void *t_hi, void *t_lo,
-                     const void *y_hi, const void *y_lo, const float *S, int64_t ntr, void *w_hi, void *w_lo, int fmt,
-                     int *err, cudaStream_t s, float *xt_out = nullptr);
+                     cudaStream_t s, int64_t *launches, int parts = kTcAll, float *xt_out = nullptr,
+                     int *ready = nullptr);
+int stage1_chain_tplanes(const float *tfull, int b, int P, int fmt, void *t_hi, void *t_lo, cudaStream_t s);
+int stage1_chain_tc2(float *x, int64_t n, int b, int pr, int pc, int P, void *t_hi, void *t_lo, const void *y_hi,
+                     const void *y_lo, const float *S, int64_t ntr, void *w_hi, void *w_lo, int fmt, int *err,
+                     cudaStream_t s, float *xt_out = nullptr, int *ready = nullptr);
 
 template <typename T>
 int stage1_update_full(T *dA, int64_t lda, int64_t n, int b, int layout, int pr, int pc, int P, const Stage1Work &w,

@@ -25,7 +25,7 @@
 namespace avs {
 namespace {
 
-constexpr int NS = 32;   // strip columns
+constexpr int NS = kChainStrip;  // strip columns
 constexpr int CNT = 128; // threads: 4 warps = the 4 TMEM lane quadrants
 
 struct ChainTcArgs {
@@ -38,6 +38,7 @@ struct ChainTcArgs {
     int fmt;
     int *err;
     float *xt;  // optional: the final top strip transposed, xt[(j0 + c) + (top0 + l) * n]
+    int *ready; // optional: ready[strip / (B / NS)] += 1 once the strip's values are in memory
 };
 
 template <int B, bool SPLIT, bool BF16>
@@ -276,9 +277,15 @@ __global__ void __launch_bounds__(CNT, 1)
                 args.xt[(j0 + c) + (top0 + l) * n] = top[c * C::TS + l];
             }
         }
+        if (args.ready) __threadfence();  // this thread's values, before the strip is released
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
+    // release the strip to the panel that waits for its tile
+    if (args.ready && tid == 0 && ok) {
+        __threadfence();
+        atomicAdd(args.ready + blockIdx.x / (B / NS), 1);
+    }
     if (wid == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(C::TALLOC));
 }
 
@@ -304,16 +311,22 @@ int launch_chain_tc(const ChainTcArgs &a, const CUtensorMap (&m)[4], cudaStream_
 
 }  // namespace
 
-// Chain of one half-step on the tensor cores.  tfull: [P][b*b] FP32 T factors
-// (T(l, l') at l + l'*b); t_hi/t_lo: scratch for their operand planes; yrow:
-// the Y planes [P][t][l] (tile 0 = the masked GEQRT Y0).
-int stage1_chain_tc2(float *x, int64_t n, int b, int pr, int pc, int P, const float *tfull, void *t_hi, void *t_lo,
-                     const void *y_hi, const void *y_lo, const float *S, int64_t ntr, void *w_hi, void *w_lo, int fmt,
-                     int *err, cudaStream_t s, float *xt_out) {
-    if (ntr <= 0) return AVS_SUCCESS;
-    if (ntr % NS) return AVS_ERR_INTERNAL;
+// Operand planes of the T factors of one half-step (tfull: [P][b*b] FP32, T(l,
+// l') at l + l'*b) into t_hi/t_lo.
+int stage1_chain_tplanes(const float *tfull, int b, int P, int fmt, void *t_hi, void *t_lo, cudaStream_t s) {
     tplanes_kernel<<<512, 256, 0, s>>>(tfull, (int64_t)P * b * b, fmt, t_hi, t_lo);
     AVS_CUDA_TRY(cudaGetLastError());
+    return AVS_SUCCESS;
+}
+
+// Chain of one half-step on the tensor cores.  t_hi/t_lo: the T factors'
+// operand planes (stage1_chain_tplanes); yrow: the Y planes [P][t][l] (tile 0 =
+// the masked GEQRT Y0).
+int stage1_chain_tc2(float *x, int64_t n, int b, int pr, int pc, int P, void *t_hi, void *t_lo, const void *y_hi,
+                     const void *y_lo, const float *S, int64_t ntr, void *w_hi, void *w_lo, int fmt, int *err,
+                     cudaStream_t s, float *xt_out, int *ready) {
+    if (ntr <= 0) return AVS_SUCCESS;
+    if (ntr % NS) return AVS_ERR_INTERNAL;
     const bool bf = tc::fmt_bf16(fmt), split = tc::fmt_split(fmt);
     CUtensorMap m[4];
     const void *planes[4] = {t_hi, split ? t_lo : t_hi, y_hi, split ? y_lo : y_hi};
@@ -321,7 +334,7 @@ int stage1_chain_tc2(float *x, int64_t n, int b, int pr, int pc, int P, const fl
         tc::Operand op{const_cast<void *>(planes[i]), nullptr, b, (int64_t)P * b, b};
         if (!tc::make_tmap(&m[i], op, op.hi, 128, bf)) return AVS_ERR_INTERNAL;
     }
-    ChainTcArgs a{x, n, pr, pc, P, S, ntr, w_hi, w_lo, fmt, err, xt_out};
+    ChainTcArgs a{x, n, pr, pc, P, S, ntr, w_hi, w_lo, fmt, err, xt_out, ready};
     if (b == 256) {
         if (fmt == tc::kTF32) return launch_chain_tc<256, false, false>(a, m, s);
         if (fmt == tc::kTF32X3) return launch_chain_tc<256, true, false>(a, m, s);

@@ -62,6 +62,8 @@ struct PanelArgs {
     int *ticket;
     int *progress;   // [2P]: diagonal block handed on, trailing top rows handed on
     int *err;
+    const int *ready;  // optional: role p's tile is final once ready[p] >= ready_need
+    int ready_need;
     int64_t sA, sTau, sTblk, sFlags;  // per-matrix strides (blockIdx.y = matrix)
 };
 
@@ -284,6 +286,11 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
     T *tblk_out = reinterpret_cast<T *>(args.tblk) + zb * args.sTblk + (size_t)p * nb * kIB * kIB;
     const int t = tid;  // my row (b <= 256)
 
+    if (args.ready) {  // the tile is still being written by the previous update's chain
+        if (tid == 0) s_ok = wait_geq(args.ready + p, args.ready_need, args.err);
+        __syncthreads();
+        if (!s_ok) return;
+    }
     int *full = progress + args.P;  // per role: block cb's trailing top rows are final
     for (int cb = 0; cb < nb; ++cb) {
         const int c0 = cb * kIB;
@@ -780,7 +787,7 @@ __global__ void __launch_bounds__(kNT) update_kernel(UpdateArgs args) {
 
 template <typename T, int LAYOUT>
 int launch_panel(T *dA, int64_t lda, int b, int pr, int pc, int P, int first_role, const Stage1Work &w,
-                 cudaStream_t s) {
+                 cudaStream_t s, const int *ready = nullptr) {
     static std::atomic<bool> attr_set{false};
     const size_t smem = panel3_smem_bytes<T>(b);
     if (!attr_set) {
@@ -807,6 +814,8 @@ int launch_panel(T *dA, int64_t lda, int b, int pr, int pc, int P, int first_rol
     a.sTau = w.sTau;
     a.sTblk = w.sTblk;
     a.sFlags = w.sFlags;
+    a.ready = ready;
+    a.ready_need = b / kChainStrip;
     panel3_kernel<T, LAYOUT><<<dim3(P - first_role, batch), kNT, smem, s>>>(a);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
@@ -859,10 +868,11 @@ int copy_tau_out(void *out, const Stage1Work &w, int nt, int k, int first, int P
 // one half-step, bracketed by a pair of the caller's events when it asked for
 // timing.
 int timed_update(float *X, int64_t n, int b, int pr, int pc, int P, const Stage1Work &w, const TcBufs &tb,
-                 cudaStream_t s, int64_t *launches, int parts = kTcAll, float *xt_out = nullptr) {
+                 cudaStream_t s, int64_t *launches, int parts = kTcAll, float *xt_out = nullptr,
+                 int *ready = nullptr) {
     const bool timed = w.ev_pairs && w.ev_used && *w.ev_used < w.ev_cap;
     if (timed) AVS_CUDA_TRY(cudaEventRecord(w.ev_pairs[2 * *w.ev_used], s));
-    const int rc = stage1_tc_update(X, n, b, pr, pc, P, w, tb, s, launches, parts, xt_out);
+    const int rc = stage1_tc_update(X, n, b, pr, pc, P, w, tb, s, launches, parts, xt_out, ready);
     if (rc != AVS_SUCCESS) return rc;
     if (timed) {
         AVS_CUDA_TRY(cudaEventRecord(w.ev_pairs[2 * *w.ev_used + 1], s));
@@ -871,30 +881,23 @@ int timed_update(float *X, int64_t n, int b, int pr, int pc, int P, const Stage1
     return AVS_SUCCESS;
 }
 
-// The lookahead's stream hand-offs: `from` records ev, `to` waits for it
-// (nothing when both are the caller's stream).
-int hand_off(cudaStream_t from, cudaStream_t to, cudaEvent_t ev) {
-    if (from == to || !ev) return AVS_SUCCESS;
-    AVS_CUDA_TRY(cudaEventRecord(ev, from));
-    AVS_CUDA_TRY(cudaStreamWaitEvent(to, ev, 0));
-    return AVS_SUCCESS;
-}
-
 // GE2BND with tensor-core trailing updates (FP32 tiles, b = 128 or 256, one
 // matrix, lda = n): QR half-steps on X, LQ half-steps as QR half-steps on the
 // transposed trailing block in XT.
 //
 // Lookahead: the next half-step's panel works on the top tile row that the
-// chain of the current update has just finished (the chain writes it into the
-// other buffer as well, transposed), so the panel and its T build run on the
-// aux stream while the caller's stream finishes the update (A_p -= Y_p W_p and
-// the transpose of the rows below).  The Y copies and S_p = Y_p^T A_p need the
-// panel only and run beside the T build; the chain waits for both.  Every
-// kernel touches the same data in the same order as without the overlap:
-//   QR half-step k: panel/tbuild on X column tile k; the chain writes X row
-//     tile k (columns >= k+1) and its transpose, XT column tile k; then the
-//     LQ panel (XT column tile k) overlaps the update of X rows >= k+1 and the
-//     transpose X -> XT of rows and columns >= k+1.
+// chain of the current update computes (the chain writes it into the other
+// buffer as well, transposed, and counts finished strips per tile), so the
+// panel runs on the aux stream (high priority) beside the chain, each role
+// waiting for its own tile, and beside the rest of the update (A_p -= Y_p W_p
+// and the transpose of the rows below) on the caller's stream; its T build
+// follows on aux.  The Y copies and S_p = Y_p^T A_p need the panel only and
+// run beside the T build; the chain waits for both.  Every kernel touches the
+// same data in the same order as without the overlap:
+//   QR half-step k: the chain writes X row tile k (columns >= k+1) and its
+//     transpose, XT column tile k = the LQ panel, which overlaps the rest of
+//     the update of X rows >= k+1 and the transpose X -> XT of rows and
+//     columns >= k+1.
 //   LQ half-step k: the chain writes XT row tile k+1 and its transpose, X
 //     column tile k+1 (rows >= k+1) = the next QR panel, which overlaps the
 //     update of XT rows >= k+2 and the transposes back (XT rows >= k+2, and
@@ -906,14 +909,22 @@ int stage1_ge2bnd_tc(float *X, int64_t n, int b, const Stage1Work &w, cudaStream
     float *XT = tb.xt;
     const bool la = w.aux && w.la_fork && w.la_panel && w.la_tb;
     cudaStream_t a = la ? w.aux : s;
-    int rc;
+    int rc, dev = 0, sms = 0;
+    AVS_CUDA_TRY(cudaGetDevice(&dev));
+    AVS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     if ((rc = stage1_tc_planes(X, n, fmt, tb, s)) != AVS_SUCCESS) return rc;
-    // panel + tau copy + T build of one half-step on the aux stream, with the
-    // hand-offs back to the caller's stream after the panel and after the T build
-    auto panel_tb = [&](float *M, int pr, int pc, int P, void *tau_out, int k, int first) -> int {
+    // panel + tau copy + T build of one half-step on the aux stream, after the
+    // caller's stream has reached this point (or the point where it recorded
+    // la_fork: forked = true); hand-offs back after the panel and after the T
+    // build
+    auto panel_tb = [&](float *M, int pr, int pc, int P, void *tau_out, int k, int first, const int *ready,
+                        bool forked = false) -> int {
         int r;
-        if ((r = hand_off(s, a, la ? w.la_fork : nullptr)) != AVS_SUCCESS) return r;
-        if ((r = launch_panel<float, 0>(M, n, b, pr, pc, P, 0, w, a)) != AVS_SUCCESS) return r;
+        if (la) {
+            if (!forked) AVS_CUDA_TRY(cudaEventRecord(w.la_fork, s));
+            AVS_CUDA_TRY(cudaStreamWaitEvent(a, w.la_fork, 0));
+        }
+        if ((r = launch_panel<float, 0>(M, n, b, pr, pc, P, 0, w, a, ready)) != AVS_SUCCESS) return r;
         if ((r = copy_tau_out<float>(tau_out, w, nt, k, first, P, b, a)) != AVS_SUCCESS) return r;
         if (la) AVS_CUDA_TRY(cudaEventRecord(w.la_panel, a));
         if ((int64_t)(pc + 1) * b < n && (r = stage1_tbuild<float>(M, n, b, 0, pr, pc, P, w, a)) != AVS_SUCCESS)
@@ -922,13 +933,26 @@ int stage1_ge2bnd_tc(float *X, int64_t n, int b, const Stage1Work &w, cudaStream
         if (launches) *launches += 2;
         return AVS_SUCCESS;
     };
-    // the head of a half-step's update: S after the panel, the chain after the T build
-    auto head = [&](float *M, int pr, int pc, int P, float *other) -> int {
+    // one half-step's update on the caller's stream, with the next panel
+    // (on M2, panel tile (pr2, pc2), P2 tiles) started beside its chain
+    auto half_step = [&](float *M, int pr, int pc, int P, float *M2, int pr2, int pc2, int P2, void *tau_out,
+                         int k2, int first2) -> int {
         int r;
         if (la) AVS_CUDA_TRY(cudaStreamWaitEvent(s, w.la_panel, 0));
         if ((r = timed_update(M, n, b, pr, pc, P, w, tb, s, launches, kTcS)) != AVS_SUCCESS) return r;
         if (la) AVS_CUDA_TRY(cudaStreamWaitEvent(s, w.la_tb, 0));
-        return timed_update(M, n, b, pr, pc, P, w, tb, s, launches, kTcChain, other);
+        // The panel starts beside the chain (its roles wait for their tiles)
+        // only while its P2 CTAs, on at most P2 SMs, leave at least half of the
+        // SMs to the chain; otherwise after it.  The chain is launched first:
+        // where the two streams share a hardware queue the panel then simply
+        // runs after it, so the panel's waits never hold the chain back.
+        int *ready = (la && 2 * P2 <= sms) ? tb.ready : nullptr;
+        if ((r = timed_update(M, n, b, pr, pc, P, w, tb, s, launches, kTcPlanes, nullptr, ready)) != AVS_SUCCESS)
+            return r;
+        if (ready) AVS_CUDA_TRY(cudaEventRecord(w.la_fork, s));
+        if ((r = timed_update(M, n, b, pr, pc, P, w, tb, s, launches, kTcChain, M2, ready)) != AVS_SUCCESS) return r;
+        if ((r = panel_tb(M2, pr2, pc2, P2, tau_out, k2, first2, ready, ready != nullptr)) != AVS_SUCCESS) return r;
+        return timed_update(M, n, b, pr, pc, P, w, tb, s, launches, kTcUpdate);
     };
     auto finish = [&](int r) -> int {  // the aux stream joins the caller's before any return
         if (la) {
@@ -937,21 +961,17 @@ int stage1_ge2bnd_tc(float *X, int64_t n, int b, const Stage1Work &w, cudaStream
         }
         return r;
     };
-    if ((rc = panel_tb(X, 0, 0, nt, w.tau_q_out, 0, 0)) != AVS_SUCCESS) return finish(rc);
+    if ((rc = panel_tb(X, 0, 0, nt, w.tau_q_out, 0, 0, nullptr)) != AVS_SUCCESS) return finish(rc);
     for (int k = 0; k + 1 < nt; ++k) {
         const int64_t k1b = (int64_t)(k + 1) * b, k2b = (int64_t)(k + 2) * b;
         const int P = nt - k, PL = nt - k - 1;
-        // QR half-step k (its panel and T build are done or in flight on aux)
-        if ((rc = head(X, k, k, P, XT)) != AVS_SUCCESS) return finish(rc);
-        if ((rc = panel_tb(XT, k + 1, k, PL, w.tau_p_out, k, k + 1)) != AVS_SUCCESS) return finish(rc);
-        if ((rc = timed_update(X, n, b, k, k, P, w, tb, s, launches, kTcUpdate)) != AVS_SUCCESS) return finish(rc);
+        // QR half-step k (its panel and T build done or in flight on aux), the LQ panel beside it
+        if ((rc = half_step(X, k, k, P, XT, k + 1, k, PL, w.tau_p_out, k, k + 1)) != AVS_SUCCESS) return finish(rc);
         // X rows, columns >= k+1 -> XT
         if ((rc = stage1_tc_transpose_box(X, XT, n, k1b, n - k1b, k1b, n - k1b, fmt, tb, s)) != AVS_SUCCESS)
             return finish(rc);
-        // LQ half-step k
-        if ((rc = head(XT, k + 1, k, PL, X)) != AVS_SUCCESS) return finish(rc);
-        if ((rc = panel_tb(X, k + 1, k + 1, P - 1, w.tau_q_out, k + 1, k + 1)) != AVS_SUCCESS) return finish(rc);
-        if ((rc = timed_update(XT, n, b, k + 1, k, PL, w, tb, s, launches, kTcUpdate)) != AVS_SUCCESS)
+        // LQ half-step k, the next QR panel beside it
+        if ((rc = half_step(XT, k + 1, k, PL, X, k + 1, k + 1, P - 1, w.tau_q_out, k + 1, k + 1)) != AVS_SUCCESS)
             return finish(rc);
         // and back: XT rows >= k+2 (all columns >= k) -> X, and the LQ panel's top tile
         if ((rc = stage1_tc_transpose_box(XT, X, n, k2b, n - k2b, (int64_t)k * b, n - (int64_t)k * b, fmt, tb, s)) !=

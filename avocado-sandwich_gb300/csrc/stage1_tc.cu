@@ -114,6 +114,7 @@ TcBufs stage1_tc_carve(void *ws, int64_t n, int b, int fmt) {
     t.wl = take(two ? e * (size_t)nt * b * n : 0);
     t.th = take(e * (size_t)nt * b * b);
     t.tl = take(two ? e * (size_t)nt * b * b : 0);
+    t.ready = static_cast<int *>(take(sizeof(int) * (size_t)(nt + 1)));
     t.bytes = o;
     return t;
 }
@@ -149,10 +150,12 @@ int stage1_tc_transpose_box(const float *src, float *dst, int64_t n, int64_t i0,
 // column-major n x n matrix x (ld n), after the panel and the T build.  parts
 // selects the steps (a caller that overlaps other work with the update runs
 // them separately): kTcS = Y copies and S_p = Y_p^T A_p (needs the panel
-// only), kTcChain = the chain (needs the T factors; writes the top tile row,
-// and its transpose into xt_out when given), kTcUpdate = A_p -= Y_p W_p.
+// only), kTcPlanes = the T factors' operand planes (needs the T build; zeroes
+// the ready counters when given), kTcChain = the chain (writes the top tile
+// row, and its transpose into xt_out when given, counting finished strips per
+// tile in ready), kTcUpdate = A_p -= Y_p W_p.
 int stage1_tc_update(float *x, int64_t n, int b, int pr, int pc, int P, const Stage1Work &w, const TcBufs &tb,
-                     cudaStream_t s, int64_t *launches, int parts, float *xt_out) {
+                     cudaStream_t s, int64_t *launches, int parts, float *xt_out, int *ready) {
     const int fmt = w.tc_split;
     const int64_t r0 = (int64_t)pr * b, c0 = (int64_t)pc * b, j0 = (int64_t)(pc + 1) * b;
     const int64_t ntr = n - j0;
@@ -188,12 +191,19 @@ int stage1_tc_update(float *x, int64_t n, int b, int pr, int pc, int P, const St
         }
         if (launches) *launches += 2;
     }
+    if (parts & kTcPlanes) {
+        if (ready) AVS_CUDA_TRY(cudaMemsetAsync(ready, 0, sizeof(int) * (size_t)(n / b + 1), s));
+        if ((rc = stage1_chain_tplanes(static_cast<const float *>(w.tfull), b, P, fmt, tb.th, tb.tl, s)) !=
+            AVS_SUCCESS)
+            return rc;
+        if (launches) *launches += 1;
+    }
     // chain along the tiles (top tile row, W_p)
     if (parts & kTcChain) {
-        if ((rc = stage1_chain_tc2(x, n, b, pr, pc, P, static_cast<const float *>(w.tfull), tb.th, tb.tl, tb.yrh,
-                                   tb.yrl, tb.S, ntr, tb.wh, tb.wl, fmt, w.err, s, xt_out)) != AVS_SUCCESS)
+        if ((rc = stage1_chain_tc2(x, n, b, pr, pc, P, tb.th, tb.tl, tb.yrh, tb.yrl, tb.S, ntr, tb.wh, tb.wl, fmt,
+                                   w.err, s, xt_out, ready)) != AVS_SUCCESS)
             return rc;
-        if (launches) *launches += 2;
+        if (launches) *launches += 1;
     }
     // A_p -= Y_p W_p, p = 1..P-1
     if ((parts & kTcUpdate) && P > 1) {
