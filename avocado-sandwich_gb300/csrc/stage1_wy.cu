@@ -166,6 +166,178 @@ __global__ void __launch_bounds__(kWNT) tbuild_kernel(TBuildArgs args) {
 }
 
 // ---------------------------------------------------------------------------
+// T build in shared memory (FP32 tiles).  One CTA per tile, the same T as
+// tbuild_kernel with T's upper block triangle held in shared memory, packed by
+// 16-column blocks (column block J: rows 0 .. 16(J+1), column-major, at
+// offset 256 J (J+1) / 2):
+//   1. the Gram blocks G_IJ = Y_I^T Y_J (I < J) in two passes over the tile's
+//      rows (8 x 8 output tiles per thread, rows of Y staged 32 at a time with
+//      the next chunk's loads in flight during the current chunk's products),
+//      written straight into their places in the packed T;
+//   2. the diagonal blocks T_JJ from the panel;
+//   3. column blocks J = 1.. in order: H = G[0:c0, J] T_JJ, then
+//      T[0:c0, J] = -T[0:c0, 0:c0] H, one thread per row, every operand in
+//      shared memory (the recurrence is latency-bound when it reads T back
+//      from global memory);
+//   4. T to tfull (zeros below the diagonal blocks), coalesced.
+constexpr int kTbKC = 32;  // rows of Y per staged chunk
+
+__host__ __device__ constexpr int tb_off(int J) { return 256 * J * (J + 1) / 2; }
+inline size_t tbuild_f32_smem(int b) {
+    const int nb = b / kWIB;
+    return sizeof(float) * ((size_t)tb_off(nb) + (size_t)kTbKC * (b + 4));
+}
+
+template <int LAYOUT>
+__global__ void __launch_bounds__(kWNT) tbuild_f32_kernel(TBuildArgs args) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int b = args.b;
+    const int nb = b / kWIB;
+    const int p = blockIdx.x + args.first_role;
+    const int64_t zb = blockIdx.y;
+    const bool geqrt = (p == 0);
+    const int tid = threadIdx.x;
+    View<const float, LAYOUT> V{reinterpret_cast<const float *>(args.a) + zb * args.sA, args.lda};
+    const int64_t row0 = (int64_t)(args.pr + p) * b;
+    const int64_t col0 = (int64_t)args.pc * b;
+    float *Tf = reinterpret_cast<float *>(args.tfull) + zb * args.sTfull + (size_t)p * b * b;
+    const float *tb = reinterpret_cast<const float *>(args.tblk) + zb * args.sTblk + (size_t)p * nb * kWIB * kWIB;
+    float *Tp = reinterpret_cast<float *>(smem_raw);  // packed upper block triangle
+    float *ch = Tp + tb_off(nb);                        // [kTbKC][b + 4] rows of Y, then H
+    const int ldc = b + 4;
+    auto tp = [&](int r, int i) -> float & {  // T(r, i), r < 16 (i / 16 + 1)
+        const int J = i / kWIB;
+        return Tp[tb_off(J) + (i % kWIB) * (kWIB * (J + 1)) + r];
+    };
+
+    // ---- 1. Gram blocks
+    const int ntiles = 2 * nb * (nb - 1);  // 8 x 8 tiles: 4 per block pair
+    const int per = kTbKC * b / kWNT;      // staged values per thread and chunk
+    for (int base = 0; base < ntiles; base += kWNT) {
+        const int u = base + tid;
+        int l0 = -1, i0 = -1;
+        if (u < ntiles) {
+            const int pair = u >> 2;
+            int J = 1;
+            while (J * (J + 1) / 2 <= pair) ++J;
+            const int I = pair - J * (J - 1) / 2;
+            l0 = I * kWIB + 8 * ((u >> 1) & 1);
+            i0 = J * kWIB + 8 * (u & 1);
+        }
+        float g[8][8];
+#pragma unroll
+        for (int x = 0; x < 8; ++x)
+#pragma unroll
+            for (int y = 0; y < 8; ++y) g[x][y] = 0.0f;
+        // staged value e of this thread: (k, m) = (k_0 + e dk, m_0 + e dm), one
+        // pointer stepped by a fixed stride (coalesced along the tile's storage)
+        const int k_0 = (LAYOUT == 0) ? tid % kTbKC : tid / b;
+        const int m_0 = (LAYOUT == 0) ? tid / kTbKC : tid % b;
+        const int dk = (LAYOUT == 0) ? 0 : kWNT / b;
+        const int dm = (LAYOUT == 0) ? kWNT / kTbKC : 0;
+        const int64_t dp = (LAYOUT == 0) ? (int64_t)dm * args.lda : (int64_t)dk * args.lda;
+        float nx[32];
+        auto fetch = [&](int k0) {
+            const float *ptr = &V(row0 + k0 + k_0, col0 + m_0);
+#pragma unroll
+            for (int e = 0; e < 32; ++e) {
+                if (e < per) {
+                    float v = __ldcg(ptr + e * dp);
+                    if (geqrt) {
+                        const int t = k0 + k_0 + e * dk, m = m_0 + e * dm;
+                        v = (t == m) ? 1.0f : (t > m ? v : 0.0f);
+                    }
+                    nx[e] = v;
+                }
+            }
+        };
+        fetch(0);
+        for (int k0 = 0; k0 < b; k0 += kTbKC) {
+            __syncthreads();  // the previous chunk's products are done
+#pragma unroll
+            for (int e = 0; e < 32; ++e)
+                if (e < per) ch[(k_0 + e * dk) * ldc + m_0 + e * dm] = nx[e];
+            __syncthreads();
+            if (k0 + kTbKC < b) fetch(k0 + kTbKC);
+            if (l0 >= 0) {
+#pragma unroll 4
+                for (int k = 0; k < kTbKC; ++k) {
+                    const float4 a0 = *reinterpret_cast<const float4 *>(ch + k * ldc + l0);
+                    const float4 a1 = *reinterpret_cast<const float4 *>(ch + k * ldc + l0 + 4);
+                    const float4 c0 = *reinterpret_cast<const float4 *>(ch + k * ldc + i0);
+                    const float4 c1 = *reinterpret_cast<const float4 *>(ch + k * ldc + i0 + 4);
+                    const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+                    const float c[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+#pragma unroll
+                    for (int x = 0; x < 8; ++x)
+#pragma unroll
+                        for (int y = 0; y < 8; ++y) g[x][y] = fmaf(a[x], c[y], g[x][y]);
+                }
+            }
+        }
+        if (l0 >= 0) {
+#pragma unroll
+            for (int y = 0; y < 8; ++y)
+#pragma unroll
+                for (int x = 0; x < 8; ++x) tp(l0 + x, i0 + y) = g[x][y];
+        }
+    }
+    // ---- 2. diagonal blocks
+    for (int idx = tid; idx < nb * kWIB * kWIB; idx += kWNT) {
+        const int J = idx / (kWIB * kWIB), e = idx % (kWIB * kWIB), r = e % kWIB, q = e / kWIB;
+        tp(J * kWIB + r, J * kWIB + q) = tb[idx];
+    }
+    __syncthreads();
+    // ---- 3. column blocks
+    float *H = ch;  // [c0][16]
+    for (int J = 1; J < nb; ++J) {
+        const int c0 = J * kWIB;
+        const int r = tid;
+        if (r < c0) {  // H[r] = G[r, J] T_JJ (T_JJ upper triangular)
+            float gq[kWIB], h[kWIB];
+#pragma unroll
+            for (int q = 0; q < kWIB; ++q) gq[q] = tp(r, c0 + q);
+#pragma unroll
+            for (int q = 0; q < kWIB; ++q) {
+                float v = 0.0f;
+#pragma unroll
+                for (int qq = 0; qq <= q; ++qq) v = fmaf(gq[qq], tp(c0 + qq, c0 + q), v);
+                h[q] = v;
+            }
+#pragma unroll
+            for (int q = 0; q < kWIB; q += 4)
+                *reinterpret_cast<float4 *>(H + r * kWIB + q) = make_float4(h[q], h[q + 1], h[q + 2], h[q + 3]);
+        }
+        __syncthreads();
+        if (r < c0) {  // T[r, J] = -sum_{m >= block start of r} T(r, m) H[m]
+            float acc[kWIB];
+#pragma unroll
+            for (int q = 0; q < kWIB; ++q) acc[q] = 0.0f;
+            for (int m = (r / kWIB) * kWIB; m < c0; ++m) {
+                const float t = tp(r, m);
+                const float4 *hm = reinterpret_cast<const float4 *>(H + m * kWIB);
+#pragma unroll
+                for (int q4 = 0; q4 < kWIB / 4; ++q4) {
+                    const float4 hv = hm[q4];
+                    acc[4 * q4] = fmaf(t, hv.x, acc[4 * q4]);
+                    acc[4 * q4 + 1] = fmaf(t, hv.y, acc[4 * q4 + 1]);
+                    acc[4 * q4 + 2] = fmaf(t, hv.z, acc[4 * q4 + 2]);
+                    acc[4 * q4 + 3] = fmaf(t, hv.w, acc[4 * q4 + 3]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < kWIB; ++q) tp(r, c0 + q) = -acc[q];
+        }
+        __syncthreads();
+    }
+    // ---- 4. out, zeros below the diagonal blocks
+    for (int idx = tid; idx < b * b; idx += kWNT) {
+        const int l = idx % b, i = idx / b;
+        Tf[l + (size_t)i * b] = (l < kWIB * (i / kWIB + 1)) ? tp(l, i) : 0.0f;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Trailing update with full T.
 struct UpdFullArgs {
     void *a;
@@ -431,6 +603,18 @@ int launch_upd_full_any(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, co
 template <typename T, int LAYOUT>
 int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const Stage1Work &w, cudaStream_t s,
                   int first_role = 0) {
+    if constexpr (sizeof(T) == 4) {
+        static std::atomic<bool> attr32{false};
+        if (!attr32) {
+            AVS_CUDA_TRY(cudaFuncSetAttribute(tbuild_f32_kernel<LAYOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)tbuild_f32_smem(256)));
+            attr32 = true;
+        }
+        TBuildArgs a{dA, lda, b, pr, pc, P, w.tblk, w.tfull, w.sA, w.sTblk, w.sTfull, first_role};
+        tbuild_f32_kernel<LAYOUT><<<dim3(P - first_role, w.batch > 0 ? w.batch : 1), kWNT, tbuild_f32_smem(b), s>>>(a);
+        AVS_CUDA_TRY(cudaGetLastError());
+        return AVS_SUCCESS;
+    }
     static std::atomic<bool> attr{false};
     const size_t smem = sizeof(T) * (size_t)32 * (256 + 1) > sizeof(T) * (size_t)256 * 256 / 16
                             ? sizeof(T) * (size_t)32 * (256 + 1)

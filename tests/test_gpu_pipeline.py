@@ -185,7 +185,8 @@ def test_zero_and_degenerate_inputs(avs_mod, torch_cuda):
 @pytest.mark.parametrize("n,b", [(512, 32), (1024, 64), (2048, 128), (2048, 256)])
 def test_double_float_stages_match_fp64_stages(avs_mod, torch_cuda, n, b):
     """The element chase and bisection in double-float arithmetic agree with
-    the FP64 stages on the same band (1e-9); on FP64 tiles the double-float
+    the FP64 stages on the same band (1e-9 normwise, plus one unit of the FP32
+    output's rounding); on FP64 tiles the double-float
     stages stay within 1e-12 of the known spectrum.  The default FP32-class
     stage 2 (FP32 block stage to band 16, then the double-float chase) stays
     at FP32 level of the FP64 stages."""
@@ -198,7 +199,9 @@ def test_double_float_stages_match_fp64_stages(avs_mod, torch_cuda, n, b):
     a32 = a.astype(np.float32)
     s32_64 = avs_mod.my_CU_svdval(a32, b, stages="fp64")
     s32_df = avs_mod.my_CU_svdval(a32, b, flags=avs_mod.FLAGS["one_stage_chase"])
-    assert rel_err(s32_df, s32_64) < 1e-9
+    # normwise 1e-9, plus the FP32 output's own rounding (a value on a rounding
+    # boundary may land one unit apart)
+    assert np.all(np.abs(s32_df - s32_64) <= 1e-9 * s32_64[0] + np.spacing(s32_64))
     assert rel_err(s32_df, sig) < 1e-5
     s32_h = avs_mod.my_CU_svdval(a32, b)  # hierarchical for tiles >= 64
     assert rel_err(s32_h, s32_64) < 1e-6
