@@ -602,6 +602,7 @@ def main():
 
     # e2e: host matrix in, host sigma out, through avs_svdvals_s
     e2e_times = []
+    s_host = None
     for _ in range(args.e2e_steps):
         t0 = time.perf_counter()
         s_host = avs.my_CU_svdval(a_host, b, precision=args.precision, handle=h)
@@ -634,7 +635,8 @@ def main():
     s64 = None
     lapack = lapack_reference(args, a_host) if extras else None
     acc = {"mode": args.precision, "tolerance_normwise": 1e-5,
-           "host_vs_device_max_diff": float(np.max(np.abs(s_host.astype(np.float64) - sigma)))}
+           "host_vs_device_max_diff": (float(np.max(np.abs(s_host.astype(np.float64) - sigma)))
+                                       if s_host is not None else None)}
     if lapack is not None:
         acc["vs_lapack_dgesdd"] = errors(sigma, lapack)
         acc["lapack_source"] = "tests/golden/sigma_n16384_seed4.npz (dgesdd on the same float32 matrix, SHA-256 checked)"
