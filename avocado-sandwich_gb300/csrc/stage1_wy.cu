@@ -456,9 +456,9 @@ __device__ __forceinline__ void gemm(const UpdCtx<T, LAYOUT, B, WW, CT> &ctx, in
     __syncthreads();
 }
 
-template <typename T, int LAYOUT, int B, typename CT = T>
+template <typename T, int LAYOUT, int B, typename CT = T, int WW = WCfg<T>::W>
 __global__ void __launch_bounds__(kWNT) update_full_kernel(UpdFullArgs args) {
-    using C = UCfg<T, B>;
+    using C = UCfg<T, B, WW>;
     static_assert(sizeof(CT) == sizeof(T), "compute type of the element's size");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CT *Top = reinterpret_cast<CT *>(smem_raw);    // LDB x W, column-major
@@ -513,7 +513,7 @@ __global__ void __launch_bounds__(kWNT) update_full_kernel(UpdFullArgs args) {
     CT acc[8][C::CB];
     CT apr[8][C::CB];
     for (int p = args.first_role; p < args.P; ++p) {
-        UpdCtx<T, LAYOUT, B, WCfg<T>::W, CT> ctx;
+        UpdCtx<T, LAYOUT, B, WW, CT> ctx;
         ctx.V = V;
         ctx.Tf = reinterpret_cast<const T *>(args.tfull) + zb * args.sTfull + (size_t)p * B * B;
         ctx.row0 = (int64_t)(args.pr + p) * B;
@@ -570,14 +570,14 @@ size_t upd_full_smem() {
     return sizeof(T) * (2 * (size_t)C::LDB * C::W + 2 * (size_t)C::KC * C::LDC);
 }
 
-template <typename T, int LAYOUT, int B, typename CT = T>
+template <typename T, int LAYOUT, int B, typename CT = T, int WW = WCfg<T>::W>
 int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const Stage1Work &w, cudaStream_t s,
                     int first_role) {
-    using C = UCfg<T, B>;
+    using C = UCfg<T, B, WW>;
     static std::atomic<bool> attr{false};
-    const size_t smem = upd_full_smem<T, B>();
+    const size_t smem = upd_full_smem<T, B, WW>();
     if (!attr) {
-        AVS_CUDA_TRY(cudaFuncSetAttribute(update_full_kernel<T, LAYOUT, B, CT>,
+        AVS_CUDA_TRY(cudaFuncSetAttribute(update_full_kernel<T, LAYOUT, B, CT, WW>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
@@ -585,17 +585,34 @@ int launch_upd_full(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const 
     if (ncols <= 0) return AVS_SUCCESS;
     UpdFullArgs a{dA, lda, n, B, pr, pc, P, w.tfull, w.sA, w.sTfull, first_role};
     const unsigned gx = (unsigned)((ncols + C::W - 1) / C::W);
-    update_full_kernel<T, LAYOUT, B, CT><<<dim3(gx, w.batch > 0 ? w.batch : 1), kWNT, smem, s>>>(a);
+    update_full_kernel<T, LAYOUT, B, CT, WW><<<dim3(gx, w.batch > 0 ? w.batch : 1), kWNT, smem, s>>>(a);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
 }
 
 // FP64 tiles: the update in FP64, or in double-float when the work asks for it.
+// FP64 tiles: 32-column strips, or 16 when the 32-column strips (times the
+// batch) would not give every SM two CTAs -- a strip runs its P tiles in
+// sequence, so the strips are the launch's only parallelism.  A column's values
+// do not depend on the strip width (columns are independent, the sums run in
+// the same order), so single and batched calls agree bit for bit.
 template <typename T, int LAYOUT, int B>
 int launch_upd_full_any(T *dA, int64_t lda, int64_t n, int pr, int pc, int P, const Stage1Work &w, cudaStream_t s,
                         int first_role) {
     if constexpr (sizeof(T) == 8) {
-        if (w.df_update) return launch_upd_full<T, LAYOUT, B, dfx>(dA, lda, n, pr, pc, P, w, s, first_role);
+        static int sms = 0;
+        if (sms == 0) {
+            int dev = 0;
+            AVS_CUDA_TRY(cudaGetDevice(&dev));
+            AVS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        }
+        const int64_t ncols = n - (int64_t)(pc + 1) * B;
+        const bool narrow = ((ncols + 31) / 32) * (int64_t)(w.batch > 0 ? w.batch : 1) < 2 * (int64_t)sms;
+        if (w.df_update)
+            return narrow ? launch_upd_full<T, LAYOUT, B, dfx, 16>(dA, lda, n, pr, pc, P, w, s, first_role)
+                          : launch_upd_full<T, LAYOUT, B, dfx>(dA, lda, n, pr, pc, P, w, s, first_role);
+        return narrow ? launch_upd_full<T, LAYOUT, B, T, 16>(dA, lda, n, pr, pc, P, w, s, first_role)
+                      : launch_upd_full<T, LAYOUT, B>(dA, lda, n, pr, pc, P, w, s, first_role);
     }
     return launch_upd_full<T, LAYOUT, B>(dA, lda, n, pr, pc, P, w, s, first_role);
 }
