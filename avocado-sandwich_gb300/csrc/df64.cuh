@@ -106,5 +106,7 @@ __device__ __forceinline__ dfx operator*(dfx a, dfx b) { return dfx(df_mul(a.v, 
 __device__ __forceinline__ dfx operator-(dfx a) { return dfx(df_neg(a.v)); }
 __device__ __forceinline__ dfx &operator+=(dfx &a, dfx b) { return a = a + b; }
 __device__ __forceinline__ dfx &operator-=(dfx &a, dfx b) { return a = a - b; }
+__device__ __forceinline__ bool operator==(dfx a, dfx b) { return a.v.hi == b.v.hi && a.v.lo == b.v.lo; }
+__device__ __forceinline__ bool operator!=(dfx a, dfx b) { return !(a == b); }
 
 }  // namespace avs

@@ -41,6 +41,8 @@
 #include <cmath>
 #include <cstdio>
 
+#include <type_traits>
+
 #include "avs_common.cuh"
 #include "df64.cuh"
 
@@ -184,6 +186,71 @@ struct PScal<float> {
     }
 };
 
+// FP64 tiles in double-float arithmetic (AVS_PREC_FP64X2): the same closed
+// forms with alpha and the results as double-float values.
+struct PScalarsD {
+    df64 nu, tau, tc, f, inv, beta;
+};
+
+__device__ __forceinline__ PScalarsD pscal_df(df64 s, df64 alpha) {
+    PScalarsD r;
+    const df64 x = df_add(s, df_mul(alpha, alpha));  // n1^2
+    const df64 z{0.0f, 0.0f};
+    if (x.hi <= 0.0f) {  // zero column: identity reflector
+        r.nu = r.tau = r.tc = r.f = r.inv = z;
+        r.beta = alpha;
+        return r;
+    }
+    // 1/n1 and 1/nu: FP32 estimates refined by one Newton step in double-float
+    const float y0 = rsqrtf(x.hi);
+    const df64 e = df_sub(df64{1.0f, 0.0f}, df_mul(x, two_prod(y0, y0)));
+    const df64 rn1 = df_add(df64{y0, 0.0f}, df_mul_f(e, 0.5f * y0));
+    const df64 n1 = df_mul(x, rn1);
+    const bool neg = df_lt0(alpha);
+    const df64 nu = neg ? df_sub(alpha, n1) : df_add(alpha, n1);  // |nu| = |alpha| + n1 > 0
+    const df64 inv = df_rcp(nu);
+    const df64 anu = neg ? df_neg(nu) : nu;
+    const df64 ainv = neg ? df_neg(inv) : inv;
+    r.nu = nu;
+    r.tau = df_mul(anu, rn1);
+    r.tc = neg ? df_neg(rn1) : rn1;
+    r.inv = inv;
+    r.f = df_mul(rn1, ainv);
+    r.beta = neg ? n1 : df_neg(n1);
+    return r;
+}
+
+template <>
+struct PScal<dfx> {
+    using Acc = df64;
+    static __device__ __forceinline__ Acc zero() { return df64{0.0f, 0.0f}; }
+    static __device__ __forceinline__ Acc sq(dfx x, Acc a) { return df_add(a, df_mul(x.v, x.v)); }
+    static __device__ __forceinline__ Acc shfl_add(Acc a, int o) {
+        return df_add(a, df64{__shfl_xor_sync(0xffffffffu, a.hi, o), __shfl_xor_sync(0xffffffffu, a.lo, o)});
+    }
+    static __device__ __forceinline__ Acc shfl_add_local(Acc a, Acc b) { return df_add(a, b); }
+    static __device__ __forceinline__ void compute(Acc s, dfx alpha, dfx *out) {
+        const PScalarsD r = pscal_df(s, alpha.v);
+        out[0] = dfx(r.nu); out[1] = dfx(r.tc); out[2] = dfx(r.f); out[3] = dfx(r.inv); out[4] = dfx(r.beta);
+        out[5] = dfx(r.tau);
+    }
+};
+
+// Warp shuffles and finiteness of the panel's compute types.
+__device__ __forceinline__ float vshfl_xor(float v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double vshfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ dfx vshfl_xor(dfx v, int o) {
+    return dfx(df64{__shfl_xor_sync(0xffffffffu, v.v.hi, o), __shfl_xor_sync(0xffffffffu, v.v.lo, o)});
+}
+__device__ __forceinline__ float vshfl(float v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ double vshfl(double v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+__device__ __forceinline__ dfx vshfl(dfx v, int src) {
+    return dfx(df64{__shfl_sync(0xffffffffu, v.v.hi, src), __shfl_sync(0xffffffffu, v.v.lo, src)});
+}
+__device__ __forceinline__ bool vfinite(float v) { return isfinite(v); }
+__device__ __forceinline__ bool vfinite(double v) { return isfinite(v); }
+__device__ __forceinline__ bool vfinite(dfx v) { return isfinite(v.v.hi) && isfinite(v.v.lo); }
+
 // ---------------------------------------------------------------------------
 // Panel kernel (roles, schedule and outputs as described at the top):
 //   * every thread owns one row of the 16-column slice (b <= 256 rows, 256
@@ -246,24 +313,24 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-template <typename T, int LAYOUT>
+template <typename T, int LAYOUT, typename CT = T>
 __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int b = args.b;
     const int nb = b / kIB;
     const int ldx = ldpad(b);
-    using Acc = typename PScal<T>::Acc;
+    using Acc = typename PScal<CT>::Acc;
     Acc *spart = reinterpret_cast<Acc *>(smem_raw);         // 8 warps
-    T *stau = reinterpret_cast<T *>(smem_raw + sizeof(double) * 16);
-    T *scal = stau + kIB;                                    // 16
-    T *X = scal + 16;                                        // ldx * kIB (column-major)
-    T *Yr = X + (size_t)ldx * kIB;                           // b * kIB (row-major: Yr[t*16 + l])
-    T *Rt = Yr + (size_t)b * kIB;                            // kIB * b, Rt[l + j*kIB]
-    T *Ws = Rt + (size_t)kIB * b;                            // kIB * b, Ws[l + j*kIB]
-    T *Tm = Ws + (size_t)kIB * b;                            // kIB * kIB, Tm[l + i*kIB]
-    T *G = Tm + kIB * kIB;                                   // kIB * kIB
-    T *part = G + kIB * kIB;                                 // 2 x 8 * kIB (double-buffered)
-    T *dsum = part + 16 * kIB;                               // end of the small arrays
+    CT *stau = reinterpret_cast<CT *>(smem_raw + sizeof(double) * 16);
+    CT *scal = stau + kIB;                                    // 16
+    CT *X = scal + 16;                                        // ldx * kIB (column-major)
+    CT *Yr = X + (size_t)ldx * kIB;                           // b * kIB (row-major: Yr[t*16 + l])
+    CT *Rt = Yr + (size_t)b * kIB;                            // kIB * b, Rt[l + j*kIB]
+    CT *Ws = Rt + (size_t)kIB * b;                            // kIB * b, Ws[l + j*kIB]
+    CT *Tm = Ws + (size_t)kIB * b;                            // kIB * kIB, Tm[l + i*kIB]
+    CT *G = Tm + kIB * kIB;                                   // kIB * kIB
+    CT *part = G + kIB * kIB;                                 // 2 x 8 * kIB (double-buffered)
+    CT *dsum = part + 16 * kIB;                               // end of the small arrays
     // C chunks (16-byte aligned): LAYOUT 0 [column][row], LAYOUT 1 [row][column]
     T *cbuf0 = reinterpret_cast<T *>((reinterpret_cast<uintptr_t>(dsum + 2 * kIB + 8) + 15) & ~(uintptr_t)15);
 
@@ -300,7 +367,7 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
         for (int idx = tid; idx < b * kIB; idx += kNT) {
             int tt, l;
             if (LAYOUT == 0) { tt = idx % b; l = idx / b; } else { l = idx % kIB; tt = idx / kIB; }
-            X[tt + l * ldx] = __ldcg(&V(row0 + tt, col0 + c0 + l));
+            X[tt + l * ldx] = CT(__ldcg(&V(row0 + tt, col0 + c0 + l)));
         }
         const int jbase = c0 + kIB;
         const int nrest = b - jbase;
@@ -351,7 +418,7 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
             for (int idx = tid; idx < kIB * kIB; idx += kNT) {
                 int l, j;
                 if (LAYOUT == 0) { l = idx % kIB; j = idx / kIB; } else { j = idx % kIB; l = idx / kIB; }
-                Rt[l + (c0 + j) * kIB] = __ldcg(&V(top0 + c0 + l, col0 + c0 + j));
+                Rt[l + (c0 + j) * kIB] = CT(__ldcg(&V(top0 + c0 + l, col0 + c0 + j)));
             }
         }
         __syncthreads();
@@ -363,36 +430,36 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
         // updates) after the step's barrier, so warp 0 keeps the updated pivot
         // row in registers and stores it after the next barrier: no later step
         // reads that row before the Gram matrix below.
-        T *pend_at = nullptr;
-        T pend_v = T(0);
+        CT *pend_at = nullptr;
+        CT pend_v = CT(0);
         for (int i = 0; i < kIB; ++i) {
             const int c = c0 + i;
             const int pb = i & 1;
             if (geqrt && c == b - 1) {
-                if (tid == 0) stau[i] = T(0);
+                if (tid == 0) stau[i] = CT(0);
                 continue;
             }
             const bool live = (t < b) && (geqrt ? (t > c) : true);
-            const T x = live ? X[t + i * ldx] : T(0);
-            T pv[kIB];
+            const CT x = live ? X[t + i * ldx] : CT(0);
+            CT pv[kIB];
 #pragma unroll
-            for (int jj = 0; jj < kIB; ++jj) pv[jj] = (live && jj > i) ? x * X[t + jj * ldx] : T(0);
-            Acc sq = PScal<T>::zero();
-            if (live) sq = PScal<T>::sq(x, sq);
+            for (int jj = 0; jj < kIB; ++jj) pv[jj] = (live && jj > i) ? x * X[t + jj * ldx] : CT(0);
+            Acc sq = PScal<CT>::zero();
+            if (live) sq = PScal<CT>::sq(x, sq);
             // warp reduce-scatter of pv[0..15]: lane L ends with the warp sum of pv[L & 15]
 #pragma unroll
             for (int h = 8; h >= 1; h >>= 1) {
                 const bool upper = (lane & h) != 0;
 #pragma unroll
                 for (int q = 0; q < h; ++q) {
-                    const T send = upper ? pv[q] : pv[q + h];
-                    const T keep = upper ? pv[q + h] : pv[q];
-                    pv[q] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+                    const CT send = upper ? pv[q] : pv[q + h];
+                    const CT keep = upper ? pv[q + h] : pv[q];
+                    pv[q] = keep + vshfl_xor(send, h);
                 }
             }
-            pv[0] += __shfl_xor_sync(0xffffffffu, pv[0], 16);
+            pv[0] += vshfl_xor(pv[0], 16);
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) sq = PScal<T>::shfl_add(sq, o);
+            for (int o = 16; o > 0; o >>= 1) sq = PScal<CT>::shfl_add(sq, o);
             if (lane < kIB) part[pb * 8 * kIB + wid * kIB + lane] = pv[0];  // lane L holds index L & 15
             if (lane == 0) spart[pb * 8 + wid] = sq;
             __syncthreads();
@@ -400,57 +467,57 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                 *pend_at = pend_v;
                 pend_at = nullptr;
             }
-            const T alpha = geqrt ? X[c + i * ldx] : Rt[i + c * kIB];
-            T out[6];
-            if constexpr (sizeof(T) == 4) {
+            const CT alpha = geqrt ? X[c + i * ldx] : Rt[i + c * kIB];
+            CT out[6];
+            if constexpr (!std::is_same<CT, double>::value) {
                 // FP32 tiles: every lane forms the (double-float) scalars -- no
                 // divergence, and the loads below overlap them.  The 8 warp
                 // partials are summed by a 3-level shuffle tree; df_add is
                 // commutative, so every lane of every warp gets the same sum.
                 Acc s_all = spart[pb * 8 + (lane & 7)];
-                s_all = PScal<T>::shfl_add(s_all, 1);
-                s_all = PScal<T>::shfl_add(s_all, 2);
-                s_all = PScal<T>::shfl_add(s_all, 4);
-                PScal<T>::compute(s_all, alpha, out);
-                if (!isfinite(out[5]) || !isfinite(out[0])) {
+                s_all = PScal<CT>::shfl_add(s_all, 1);
+                s_all = PScal<CT>::shfl_add(s_all, 2);
+                s_all = PScal<CT>::shfl_add(s_all, 4);
+                PScal<CT>::compute(s_all, alpha, out);
+                if (!vfinite(out[5]) || !vfinite(out[0])) {
                     if (tid == 0) atomicCAS(args.err, kDevOk, kDevNonfinite);
-                    out[5] = out[1] = out[2] = out[3] = T(0);
+                    out[5] = out[1] = out[2] = out[3] = CT(0);
                     out[4] = alpha;
                 }
             } else {
                 // FP64 tiles: lane 0 of each warp forms the scalars (FP64 is
                 // costly on every lane), the warp reads them with shuffles
                 if (lane == 0) {
-                    Acc s_all = PScal<T>::zero();
+                    Acc s_all = PScal<CT>::zero();
 #pragma unroll
-                    for (int w = 0; w < kNT / 32; ++w) s_all = PScal<T>::shfl_add_local(s_all, spart[pb * 8 + w]);
-                    PScal<T>::compute(s_all, alpha, out);
-                    if (!isfinite(out[5]) || !isfinite(out[0])) {
+                    for (int w = 0; w < kNT / 32; ++w) s_all = PScal<CT>::shfl_add_local(s_all, spart[pb * 8 + w]);
+                    PScal<CT>::compute(s_all, alpha, out);
+                    if (!vfinite(out[5]) || !vfinite(out[0])) {
                         if (tid == 0) atomicCAS(args.err, kDevOk, kDevNonfinite);
-                        out[5] = out[1] = out[2] = out[3] = T(0);
+                        out[5] = out[1] = out[2] = out[3] = CT(0);
                         out[4] = alpha;
                     }
                 }
 #pragma unroll
-                for (int q = 0; q < 6; ++q) out[q] = __shfl_sync(0xffffffffu, out[q], 0);
+                for (int q = 0; q < 6; ++q) out[q] = vshfl(out[q], 0);
             }
             // column sums of the 16 dot products: lane L sums column L & 15
-            T dmine = T(0);
+            CT dmine = CT(0);
 #pragma unroll
             for (int w = 0; w < kNT / 32; ++w) dmine += part[pb * 8 * kIB + w * kIB + (lane & 15)];
-            T rvr[kIB];
+            CT rvr[kIB];
 #pragma unroll
             for (int jj = 0; jj < kIB; ++jj) rvr[jj] = geqrt ? X[c + jj * ldx] : Rt[i + (c0 + jj) * kIB];
-            const T tv = out[5];
+            const CT tv = out[5];
             if (tid == 0) stau[i] = tv;
-            if (tv == T(0)) {
-                if (live) X[t + i * ldx] = T(0);
+            if (tv == CT(0)) {
+                if (live) X[t + i * ldx] = CT(0);
                 continue;  // the next step reads only own rows until its barrier
             }
-            const T nu = out[0], tc = out[1], f = out[2], inv = out[3];
-            T dsv[kIB];
+            const CT nu = out[0], tc = out[1], f = out[2], inv = out[3];
+            CT dsv[kIB];
 #pragma unroll
-            for (int jj = 0; jj < kIB; ++jj) dsv[jj] = __shfl_sync(0xffffffffu, dmine, jj);
+            for (int jj = 0; jj < kIB; ++jj) dsv[jj] = vshfl(dmine, jj);
             if (live) {
 #pragma unroll
                 for (int jj = 0; jj < kIB; ++jj)
@@ -472,7 +539,7 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
             for (int idx = tid; idx < kIB * kIB; idx += kNT) {
                 int l, jx;
                 if (LAYOUT == 0) { l = idx % kIB; jx = idx / kIB; } else { jx = idx % kIB; l = idx / kIB; }
-                V(top0 + c0 + l, col0 + c0 + jx) = Rt[l + (c0 + jx) * kIB];
+                V(top0 + c0 + l, col0 + c0 + jx) = (T)Rt[l + (c0 + jx) * kIB];
             }
             __syncthreads();
             if (tid == 0) {
@@ -481,7 +548,7 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
             }
         }
 
-        // ---- Gram matrix of the block's reflectors, T (warp 0), masked Y
+        // ---- Gram matrix of the block's reflectors, CT (warp 0), masked Y
         {
             const int pi = tid >> 1, h = tid & 1;
             int l = -1, i = 0;
@@ -492,21 +559,21 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                     acc += ii;
                 }
             }
-            T pt = T(0);
+            CT pt = CT(0);
             if (l >= 0) {
                 const int half = (b + 1) / 2;
                 const int tlo = h * half, thi = min(b, tlo + half);
                 for (int tt = tlo; tt < thi; ++tt)
                     if (geqrt ? (tt > c0 + i) : true) pt += X[tt + l * ldx] * X[tt + i * ldx];
             }
-            pt += __shfl_xor_sync(0xffffffffu, pt, 1);
-            if (l >= 0 && h == 0) G[l + i * kIB] = pt + (geqrt ? X[c0 + i + l * ldx] : T(0));
+            pt += vshfl_xor(pt, 1);
+            if (l >= 0 && h == 0) G[l + i * kIB] = pt + (geqrt ? X[c0 + i + l * ldx] : CT(0));
         }
-        if (tid < kIB * kIB) Tm[tid] = T(0);
+        if (tid < kIB * kIB) Tm[tid] = CT(0);
         for (int idx = tid; idx < b * kIB; idx += kNT) {
             const int tt = idx / kIB, l = idx % kIB;
-            T y = X[tt + l * ldx];
-            if (geqrt) y = (tt == c0 + l) ? T(1) : (tt > c0 + l ? y : T(0));
+            CT y = X[tt + l * ldx];
+            if (geqrt) y = (tt == c0 + l) ? CT(1) : (tt > c0 + l ? y : CT(0));
             Yr[tt * kIB + l] = y;
         }
         __syncthreads();
@@ -515,7 +582,7 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
             __syncwarp();
             for (int i = 1; i < kIB; ++i) {
                 if (lane < i) {
-                    T acc = T(0);
+                    CT acc = CT(0);
                     for (int m = lane; m < i; ++m) acc += Tm[lane + m * kIB] * G[m + i * kIB];
                     Tm[lane + i * kIB] = -stau[i] * acc;
                 }
@@ -525,26 +592,26 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
         for (int idx = tid; idx < b * kIB; idx += kNT) {
             int tt, l;
             if (LAYOUT == 0) { tt = idx % b; l = idx / b; } else { l = idx % kIB; tt = idx / kIB; }
-            if (!geqrt || tt >= c0) V(row0 + tt, col0 + c0 + l) = X[tt + l * ldx];
+            if (!geqrt || tt >= c0) V(row0 + tt, col0 + c0 + l) = (T)X[tt + l * ldx];
         }
-        if (tid < kIB) tau_out[c0 + tid] = stau[tid];
+        if (tid < kIB) tau_out[c0 + tid] = (T)stau[tid];
         __syncthreads();
         if (geqrt && tid == 0) {  // the block's rows of the top tile are written back above
             __threadfence();
             st_release(progress, cb + 1);
         }
-        if (tid < kIB * kIB) tblk_out[(size_t)cb * kIB * kIB + tid] = Tm[tid];
+        if (tid < kIB * kIB) tblk_out[(size_t)cb * kIB * kIB + tid] = (T)Tm[tid];
 
         // ---- apply to the rest of the tile
         if (nrest > 0) {
-            // (a) Z = Y^T C: the rows tstart..b-1 of C stream through shared
+            // (a) Z = Y^CT C: the rows tstart..b-1 of C stream through shared
             // memory in chunks of CR rows (cp.async ring of NBUF chunks, issued
             // since the block started); thread j owns column j and all 16
             // reflectors (Y rows broadcast).
             {
-                T z[kIB];
+                CT z[kIB];
 #pragma unroll
-                for (int l = 0; l < kIB; ++l) z[l] = T(0);
+                for (int l = 0; l < kIB; ++l) z[l] = CT(0);
                 for (int ch = 0; ch < nch; ++ch) {
                     cp_async_wait<NBUF - 1>();
                     __syncthreads();
@@ -554,8 +621,8 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                     const int j = tid;
                     if (j < nrest) {
                         for (int r = 0; r < rows; ++r) {
-                            const T cv = LAYOUT == 0 ? buf[j * cld + r] : buf[r * cld + j];
-                            const T *yrow = Yr + (t0 + r) * kIB;
+                            const CT cv = CT(LAYOUT == 0 ? buf[j * cld + r] : buf[r * cld + j]);
+                            const CT *yrow = Yr + (t0 + r) * kIB;
 #pragma unroll
                             for (int l = 0; l < kIB; ++l) z[l] += yrow[l] * cv;
                         }
@@ -578,13 +645,13 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                 for (int idx = tid; idx < kIB * nrest; idx += kNT) {
                     int l, j;
                     if (LAYOUT == 0) { l = idx % kIB; j = idx / kIB; } else { j = idx % nrest; l = idx / nrest; }
-                    Rt[l + (jbase + j) * kIB] = __ldcg(&V(top0 + c0 + l, col0 + jbase + j));
+                    Rt[l + (jbase + j) * kIB] = CT(__ldcg(&V(top0 + c0 + l, col0 + jbase + j)));
                 }
                 __syncthreads();
             }
-            // (b) W = T^T (Z + top rows); top rows -= W
+            // (b) W = CT^CT (Z + top rows); top rows -= W
             for (int jr = tid; jr < nrest; jr += kNT) {
-                T zc[kIB];
+                CT zc[kIB];
 #pragma unroll
                 for (int l = 0; l < kIB; ++l) {
                     zc[l] = Ws[l + jr * kIB];
@@ -592,7 +659,7 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                 }
 #pragma unroll
                 for (int l = 0; l < kIB; ++l) {
-                    T acc = T(0);
+                    CT acc = CT(0);
 #pragma unroll
                     for (int m = 0; m <= l; ++m) acc += Tm[m + l * kIB] * zc[m];
                     Ws[l + jr * kIB] = acc;
@@ -606,7 +673,7 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                 for (int idx = tid; idx < kIB * nrest; idx += kNT) {
                     int l, jx;
                     if (LAYOUT == 0) { l = idx % kIB; jx = idx / kIB; } else { jx = idx % nrest; l = idx / nrest; }
-                    V(top0 + c0 + l, col0 + jbase + jx) = Rt[l + (jbase + jx) * kIB];
+                    V(top0 + c0 + l, col0 + jbase + jx) = (T)Rt[l + (jbase + jx) * kIB];
                 }
                 __syncthreads();
                 if (tid == 0) {
@@ -617,21 +684,21 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
             // (c) C -= Y W: thread owns row t; 16 columns per group, the next
             // group's loads issued before the current group's arithmetic
             if (t >= tstart && t < b) {
-                T yv[kIB];
+                CT yv[kIB];
 #pragma unroll
                 for (int l = 0; l < kIB; ++l) yv[l] = Yr[t * kIB + l];
-                T cur[16], nxt[16];
-                auto load16 = [&](int jr, T (&v)[16]) {
+                CT cur[16], nxt[16];
+                auto load16 = [&](int jr, CT (&v)[16]) {
                     if (LAYOUT == 0) {
 #pragma unroll
-                        for (int q = 0; q < 16; ++q) v[q] = __ldcg(&V(row0 + t, col0 + jbase + jr + q));
+                        for (int q = 0; q < 16; ++q) v[q] = CT(__ldcg(&V(row0 + t, col0 + jbase + jr + q)));
                     } else {
 #pragma unroll
                         for (int q4 = 0; q4 < 4; ++q4) {
                             T w4[4];
                             ld4(&V(row0 + t, col0 + jbase + jr + 4 * q4), w4);
 #pragma unroll
-                            for (int q = 0; q < 4; ++q) v[4 * q4 + q] = w4[q];
+                            for (int q = 0; q < 4; ++q) v[4 * q4 + q] = CT(w4[q]);
                         }
                     }
                 };
@@ -640,17 +707,17 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
                     if (jr + 16 < nrest) load16(jr + 16, nxt);
 #pragma unroll
                     for (int q = 0; q < 16; ++q) {
-                        T s2 = T(0);
+                        CT s2 = CT(0);
 #pragma unroll
                         for (int l = 0; l < kIB; ++l) s2 += yv[l] * Ws[l + (jr + q) * kIB];
                         cur[q] -= s2;
                     }
                     if (LAYOUT == 0) {
 #pragma unroll
-                        for (int q = 0; q < 16; ++q) V(row0 + t, col0 + jbase + jr + q) = cur[q];
+                        for (int q = 0; q < 16; ++q) V(row0 + t, col0 + jbase + jr + q) = (T)cur[q];
                     } else {
 #pragma unroll
-                        for (int q = 0; q < 16; ++q) V(row0 + t, col0 + jbase + jr + q) = cur[q];
+                        for (int q = 0; q < 16; ++q) V(row0 + t, col0 + jbase + jr + q) = (T)cur[q];
                     }
 #pragma unroll
                     for (int q = 0; q < 16; ++q) cur[q] = nxt[q];
@@ -785,14 +852,23 @@ __global__ void __launch_bounds__(kNT) update_kernel(UpdateArgs args) {
     store_strip(Top, top0);
 }
 
+// FP64 tiles with the double-float trailing updates (AVS_PREC_FP64X2) run
+// the panel in double-float arithmetic too (CT = dfx: FP64 storage, each value
+// converted on load and rounded back on store); GB300 issues FP64 at 1/64 of
+// the FP32 rate and the panel's reflectors and applies are FP64-issue-bound.
 template <typename T, int LAYOUT>
 int launch_panel(T *dA, int64_t lda, int b, int pr, int pc, int P, int first_role, const Stage1Work &w,
                  cudaStream_t s, const int *ready = nullptr) {
     static std::atomic<bool> attr_set{false};
     const size_t smem = panel3_smem_bytes<T>(b);
+    const bool dfp = sizeof(T) == 8 && w.df_update;
     if (!attr_set) {
         AVS_CUDA_TRY(cudaFuncSetAttribute(panel3_kernel<T, LAYOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)panel3_smem_bytes<T>(256)));
+        if constexpr (sizeof(T) == 8)
+            AVS_CUDA_TRY(cudaFuncSetAttribute(panel3_kernel<T, LAYOUT, dfx>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)panel3_smem_bytes<T>(256)));
         attr_set = true;
     }
     const int batch = w.batch > 0 ? w.batch : 1;
@@ -816,6 +892,13 @@ int launch_panel(T *dA, int64_t lda, int b, int pr, int pc, int P, int first_rol
     a.sFlags = w.sFlags;
     a.ready = ready;
     a.ready_need = b / kChainStrip;
+    if constexpr (sizeof(T) == 8) {
+        if (dfp) {
+            panel3_kernel<T, LAYOUT, dfx><<<dim3(P - first_role, batch), kNT, smem, s>>>(a);
+            AVS_CUDA_TRY(cudaGetLastError());
+            return AVS_SUCCESS;
+        }
+    }
     panel3_kernel<T, LAYOUT><<<dim3(P - first_role, batch), kNT, smem, s>>>(a);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
