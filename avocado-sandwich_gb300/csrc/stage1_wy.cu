@@ -18,6 +18,7 @@
 // a register-blocked GEMM (8 rows x CB columns per thread, K = b streamed
 // through shared memory in chunks that the next chunk's loads overlap).
 #include <algorithm>
+#include <type_traits>
 
 #include "avs_common.cuh"
 #include "df64.cuh"
@@ -433,6 +434,39 @@ __device__ __forceinline__ void gemm(const UpdCtx<T, LAYOUT, B, WW, CT> &ctx, in
             }
         }
         const int k0 = ch * C::KC;
+        if constexpr (std::is_same<CT, dfx>::value) {
+            // double-float: compensated accumulation (Dot2, Ogita-Rump-Oishi) on
+            // the pairs (s, c) = (acc.hi, acc.lo): the product's error terms and
+            // the sum's rounding error go to c, renormalised once per call below
+#pragma unroll 4
+            for (int k = 0; k < C::KC; ++k) {
+                CT av[8], bv[C::CB];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) av[i] = cur[k * C::LDC + m0 + C::TM * i];
+#pragma unroll
+                for (int j = 0; j < C::CB; ++j) {
+                    bv[j] = Bop[(k0 + k) + (c0 + j) * C::LDB];
+                    if (neg) bv[j] = -bv[j];
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+#pragma unroll
+                    for (int j = 0; j < C::CB; ++j) {
+                        const df64 x = av[i].v, y = bv[j].v;
+                        const float pr = __fmul_rn(x.hi, y.hi);
+                        float ep = __fmaf_rn(x.hi, y.hi, -pr);
+                        ep = __fmaf_rn(x.hi, y.lo, ep);
+                        ep = __fmaf_rn(x.lo, y.hi, ep);
+                        df64 &a = acc[i][j].v;
+                        const float t = __fadd_rn(a.hi, pr);
+                        const float z = __fsub_rn(t, a.hi);
+                        const float es = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(t, z)), __fsub_rn(pr, z));
+                        a.hi = t;
+                        a.lo = __fadd_rn(a.lo, __fadd_rn(es, ep));
+                    }
+            }
+            continue;
+        }
 #pragma unroll 4
         for (int k = 0; k < C::KC; ++k) {
             CT av[8], bv[C::CB];
@@ -452,6 +486,12 @@ __device__ __forceinline__ void gemm(const UpdCtx<T, LAYOUT, B, WW, CT> &ctx, in
                     for (int j = 0; j < C::CB; ++j) acc[i][j] += av[i] * bv[j];
             }
         }
+    }
+    if constexpr (std::is_same<CT, dfx>::value) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < C::CB; ++j) acc[i][j].v = two_sum(acc[i][j].v.hi, acc[i][j].v.lo);
     }
     __syncthreads();
 }
