@@ -26,7 +26,6 @@ namespace avs {
 namespace {
 
 constexpr int NS = kChainStrip;  // strip columns
-constexpr int CNT = 128; // threads: 4 warps = the 4 TMEM lane quadrants
 
 struct ChainTcArgs {
     float *x;
@@ -43,6 +42,9 @@ struct ChainTcArgs {
 
 template <int B, bool SPLIT, bool BF16>
 struct CCfg {
+    // threads: one warp per TMEM lane quadrant (b = 128: two CTAs fit an SM),
+    // or two (b = 256: one CTA per SM, so eight warps hide the epilogue's latency)
+    static constexpr int CNT = B == 256 ? 256 : 128;
     static constexpr int EB = BF16 ? 2 : 4;
     static constexpr int BK = 128 / EB;           // K elements per 128-byte block
     static constexpr int NKB = B / BK;            // K blocks
@@ -60,12 +62,13 @@ struct CCfg {
 };
 
 template <int B, bool SPLIT, bool BF16>
-__global__ void __launch_bounds__(CNT, 1)
+__global__ void __launch_bounds__(CCfg<B, SPLIT, BF16>::CNT, 1)
     chain_tc_kernel(const __grid_constant__ CUtensorMap tT_hi, const __grid_constant__ CUtensorMap tT_lo,
                     const __grid_constant__ CUtensorMap tY_hi, const __grid_constant__ CUtensorMap tY_lo,
                     ChainTcArgs args) {
     using C = CCfg<B, SPLIT, BF16>;
     using namespace tc;
+    constexpr int CNT = C::CNT;
     extern __shared__ uint8_t smem_dyn[];
     __shared__ uint64_t full[2], empty[2], done;
     __shared__ uint32_t tmem_base;
@@ -195,16 +198,25 @@ __global__ void __launch_bounds__(CNT, 1)
                     rna_tf32(z - __uint_as_float(h));
         }
     };
-    // accumulator rows owned by this thread: l = h*128 + 32*wid + lane, columns 0..31
-    auto read_acc = [&](int h, float (&v)[NS]) {
-        float a[16], b2[16];
-        const uint32_t ta = tmem + ((uint32_t)(32 * wid) << 16) + (uint32_t)(h * NS);
-        tmem_ld16(ta, a);
-        tmem_ld16(ta + 16, b2);
+    // The accumulator part this thread reads back: warp w reads TMEM lanes
+    // 32 (w % 4) ..; the two warps of a lane quadrant take the two 128-row
+    // halves (b = 256) or the two 16-column halves of the strip (b = 128).
+    // Row my_l, columns my_c0 .. my_c0 + EC - 1.
+    constexpr int GRP = CNT / 128;
+    constexpr bool BY_HALF = C::HALVES >= GRP;
+    constexpr int EC = BY_HALF ? NS : NS / GRP;
+    const int quad = wid & 3, grp = wid >> 2;
+    const int my_h = BY_HALF ? grp : 0;
+    const int my_c0 = BY_HALF ? 0 : grp * EC;
+    const int my_l = my_h * 128 + 32 * quad + lane;
+    auto read_acc = [&](float (&v)[EC]) {
+        const uint32_t ta = tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)(my_h * NS + my_c0);
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            v[q] = a[q];
-            v[16 + q] = b2[q];
+        for (int c16 = 0; c16 < EC; c16 += 16) {
+            float a[16];
+            tmem_ld16(ta + c16, a);
+#pragma unroll
+            for (int q = 0; q < 16; ++q) v[c16 + q] = a[q];
         }
     };
 
@@ -229,35 +241,32 @@ __global__ void __launch_bounds__(CNT, 1)
         product(&tT_hi, &tT_lo, p * B);  // W = T_p^T Z
         if (p == 0) {
             // W0 becomes the strip operand of Top -= Y0 W0
-            for (int h = 0; h < C::HALVES; ++h) {
-                float v[NS];
-                read_acc(h, v);
-                const int l = h * 128 + 32 * wid + lane;
+            {
+                float v[EC];
+                read_acc(v);
 #pragma unroll
-                for (int c = 0; c < NS; ++c) put_z(c, l, v[c]);
+                for (int c = 0; c < EC; ++c) put_z(my_c0 + c, my_l, v[c]);
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             product(&tY_hi, &tY_lo, 0);  // Y0 W0
-            for (int h = 0; h < C::HALVES; ++h) {
-                float v[NS];
-                read_acc(h, v);
-                const int l = h * 128 + 32 * wid + lane;
+            {
+                float v[EC];
+                read_acc(v);
 #pragma unroll
-                for (int c = 0; c < NS; ++c) top[c * C::TS + l] -= v[c];
+                for (int c = 0; c < EC; ++c) top[(my_c0 + c) * C::TS + my_l] -= v[c];
             }
         } else {
-            for (int h = 0; h < C::HALVES; ++h) {
-                float v[NS];
-                read_acc(h, v);
-                const int l = h * 128 + 32 * wid + lane;
+            float v[EC];
+            read_acc(v);
 #pragma unroll
-                for (int c = 0; c < NS; ++c) {
-                    top[c * C::TS + l] -= v[c];
-                    if (ok) tc::put_operand(args.fmt, args.w_hi, args.w_lo, ((int64_t)p * args.ntr + js + c) * B + l, v[c]);
-                }
+            for (int c = 0; c < EC; ++c) {
+                top[(my_c0 + c) * C::TS + my_l] -= v[c];
+                if (ok)
+                    tc::put_operand(args.fmt, args.w_hi, args.w_lo, ((int64_t)p * args.ntr + js + my_c0 + c) * B + my_l,
+                                    v[c]);
             }
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -304,7 +313,7 @@ int launch_chain_tc(const ChainTcArgs &a, const CUtensorMap (&m)[4], cudaStream_
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
         attr = true;
     }
-    chain_tc_kernel<B, SPLIT, BF16><<<(unsigned)(a.ntr / NS), CNT, C::SMEM, s>>>(m[0], m[1], m[2], m[3], a);
+    chain_tc_kernel<B, SPLIT, BF16><<<(unsigned)(a.ntr / NS), C::CNT, C::SMEM, s>>>(m[0], m[1], m[2], m[3], a);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
 }
