@@ -27,9 +27,12 @@
  * runtime errors.  A Julia binding turns AVS_ERR_NOT_IMPLEMENTED into
  * error("Not implemented").
  *
- * Threading: a handle owns one CUDA stream and a grow-only device workspace;
- * calls on one handle are serialised by the caller (one handle per host
- * thread).  Entry points block until their results are ready.
+ * Threading: a handle owns one CUDA stream, a second (highest-priority)
+ * stream on which stage 1 of the tensor-core modes runs its next panel ahead
+ * (joined back before the call returns; ordered after the caller's stream by
+ * events, so capture and stream semantics are the caller's), and a grow-only
+ * device workspace; calls on one handle are serialised by the caller (one
+ * handle per host thread).  Entry points block until their results are ready.
  */
 #ifndef AVS_H
 #define AVS_H
@@ -273,9 +276,10 @@ int avs_bidiag_svals_dev(avs_handle *h, int64_t n, const double *dd, const doubl
  * default stream), and synchronises that stream before it returns, so the
  * values are in dsigma on return.  Its scratch is a static device array in the
  * library (~512 KiB per GPU, held until exit), so n <= 65536; larger n returns
- * AVS_ERR_TOO_LARGE.  The first call on a device looks the array's address up:
- * make that first call before any stream capture begins.  Calls share the
- * array: calls that overlap on the GPU race on it. */
+ * AVS_ERR_TOO_LARGE.  The first call on a device looks the array's address up.
+ * Because every call synchronises its stream, no call can be recorded by a
+ * stream capture (CUDA graph).  Calls share the array: calls that overlap on
+ * the GPU race on it. */
 int avs_bidiag_svals_noalloc(int64_t n, const double *dd, const double *de, double *dsigma, double rel_tol,
                              void *stream);
 
