@@ -48,7 +48,7 @@ struct TBuildArgs {
 
 // ---------------------------------------------------------------------------
 // T build.  One CTA per tile.
-template <typename T, int LAYOUT>
+template <typename T, int LAYOUT, typename CT = T>
 __global__ void __launch_bounds__(kWNT) tbuild_kernel(TBuildArgs args) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int b = args.b;
@@ -63,9 +63,9 @@ __global__ void __launch_bounds__(kWNT) tbuild_kernel(TBuildArgs args) {
     T *Tf = reinterpret_cast<T *>(args.tfull) + zb * args.sTfull + (size_t)p * b * b;
     const T *tb = reinterpret_cast<const T *>(args.tblk) + zb * args.sTblk + (size_t)p * nb * kWIB * kWIB;
 
-    // ---- 1. G(l, i) = y_l^T y_i for l < i in different 16-blocks, into Tf
+    // ---- 1. G(l, i) = y_l^CT y_i for l < i in different 16-blocks, into Tf
     constexpr int KC = 32;
-    T *chunk = reinterpret_cast<T *>(smem_raw);  // KC x (b + 1)
+    CT *chunk = reinterpret_cast<CT *>(smem_raw);  // KC x (b + 1)
     const int ldc = b + 1;
     // 4 x 4 micro-blocks (lb, ib) of G with block16(lb*4) < block16(ib*4)
     const int nmb = b / 4;
@@ -82,25 +82,25 @@ __global__ void __launch_bounds__(kWNT) tbuild_kernel(TBuildArgs args) {
                 acc += cnt;
             }
         }
-        T g[4][4];
+        CT g[4][4];
 #pragma unroll
         for (int x = 0; x < 4; ++x)
 #pragma unroll
-            for (int y = 0; y < 4; ++y) g[x][y] = T(0);
+            for (int y = 0; y < 4; ++y) g[x][y] = CT(0);
         for (int k0 = 0; k0 < b; k0 += KC) {
             __syncthreads();
             for (int idx = tid; idx < KC * b; idx += kWNT) {
                 int k, m;
                 if (LAYOUT == 0) { k = idx % KC; m = idx / KC; } else { m = idx % b; k = idx / b; }
                 const int t = k0 + k;
-                T v = V(row0 + t, col0 + m);
-                if (geqrt) v = (t == m) ? T(1) : (t > m ? v : T(0));
+                CT v = CT(V(row0 + t, col0 + m));
+                if (geqrt) v = (t == m) ? CT(1) : (t > m ? v : CT(0));
                 chunk[k * ldc + m] = v;
             }
             __syncthreads();
             if (lb >= 0) {
                 for (int k = 0; k < KC; ++k) {
-                    T a[4], c[4];
+                    CT a[4], c[4];
 #pragma unroll
                     for (int x = 0; x < 4; ++x) a[x] = chunk[k * ldc + lb * 4 + x];
 #pragma unroll
@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(kWNT) tbuild_kernel(TBuildArgs args) {
 #pragma unroll
             for (int x = 0; x < 4; ++x)
 #pragma unroll
-                for (int y = 0; y < 4; ++y) Tf[(lb * 4 + x) + (size_t)(ibk * 4 + y) * b] = g[x][y];
+                for (int y = 0; y < 4; ++y) Tf[(lb * 4 + x) + (size_t)(ibk * 4 + y) * b] = (T)g[x][y];
         }
     }
     __syncthreads();
@@ -128,38 +128,38 @@ __global__ void __launch_bounds__(kWNT) tbuild_kernel(TBuildArgs args) {
         else if (bl > bi) Tf[l + (size_t)i * b] = T(0);
     }
     __syncthreads();
-    // ---- 3. column blocks J = 1..nb-1: T[0:c0, J] = -T[0:c0,0:c0] G[0:c0, J] T_JJ.
+    // ---- 3. column blocks J = 1..nb-1: CT[0:c0, J] = -CT[0:c0,0:c0] G[0:c0, J] T_JJ.
     // G's block (in Tf's column block J) and T_JJ are staged in shared memory;
-    // thread r owns row r: 16 accumulators over m (T upper triangular, zeros
-    // below the diagonal), one coalesced load of T(r, m) per m, then the 16 x 16
+    // thread r owns row r: 16 accumulators over m (CT upper triangular, zeros
+    // below the diagonal), one coalesced load of CT(r, m) per m, then the 16 x 16
     // product with T_JJ in registers.
-    T *Gs = chunk;              // c0 x kWIB, Gs[m * kWIB + q]
-    T *TJ = Gs + b * kWIB;      // kWIB x kWIB, TJ[qq + q * kWIB]
+    CT *Gs = chunk;              // c0 x kWIB, Gs[m * kWIB + q]
+    CT *TJ = Gs + b * kWIB;      // kWIB x kWIB, TJ[qq + q * kWIB]
     for (int J = 1; J < nb; ++J) {
         const int c0 = J * kWIB;
         for (int idx = tid; idx < c0 * kWIB; idx += kWNT) {
             const int m = idx % c0, q = idx / c0;
-            Gs[m * kWIB + q] = Tf[m + (size_t)(c0 + q) * b];
+            Gs[m * kWIB + q] = CT(Tf[m + (size_t)(c0 + q) * b]);
         }
-        for (int idx = tid; idx < kWIB * kWIB; idx += kWNT) TJ[idx] = tb[(size_t)J * kWIB * kWIB + idx];
+        for (int idx = tid; idx < kWIB * kWIB; idx += kWNT) TJ[idx] = CT(tb[(size_t)J * kWIB * kWIB + idx]);
         __syncthreads();
         const int r = tid;
         if (r < c0) {
-            T acc[kWIB];
+            CT acc[kWIB];
 #pragma unroll
-            for (int q = 0; q < kWIB; ++q) acc[q] = T(0);
+            for (int q = 0; q < kWIB; ++q) acc[q] = CT(0);
 #pragma unroll 8
             for (int m = 0; m < c0; ++m) {
-                const T t = Tf[r + (size_t)m * b];
+                const CT t = CT(Tf[r + (size_t)m * b]);
 #pragma unroll
                 for (int q = 0; q < kWIB; ++q) acc[q] += t * Gs[m * kWIB + q];
             }
 #pragma unroll
             for (int q = 0; q < kWIB; ++q) {
-                T v = T(0);
+                CT v = CT(0);
 #pragma unroll
                 for (int qq = 0; qq < kWIB; ++qq) v += acc[qq] * TJ[qq + q * kWIB];
-                Tf[r + (size_t)(c0 + q) * b] = -v;
+                Tf[r + (size_t)(c0 + q) * b] = (T)(-v);
             }
         }
         __syncthreads();
@@ -679,9 +679,21 @@ int launch_tbuild(const T *dA, int64_t lda, int b, int pr, int pc, int P, const 
     if (!attr) {
         AVS_CUDA_TRY(
             cudaFuncSetAttribute(tbuild_kernel<T, LAYOUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if constexpr (sizeof(T) == 8)
+            AVS_CUDA_TRY(cudaFuncSetAttribute(tbuild_kernel<T, LAYOUT, dfx>,
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
     TBuildArgs a{dA, lda, b, pr, pc, P, w.tblk, w.tfull, w.sA, w.sTblk, w.sTfull, first_role};
+    if constexpr (sizeof(T) == 8) {
+        // FP64 tiles with the double-float updates: the T build in double-float
+        // too (FP64 storage; GB300 issues FP64 at 1/64 of the FP32 rate)
+        if (w.df_update) {
+            tbuild_kernel<T, LAYOUT, dfx><<<dim3(P - first_role, w.batch > 0 ? w.batch : 1), kWNT, smem, s>>>(a);
+            AVS_CUDA_TRY(cudaGetLastError());
+            return AVS_SUCCESS;
+        }
+    }
     tbuild_kernel<T, LAYOUT><<<dim3(P - first_role, w.batch > 0 ? w.batch : 1), kWNT, smem, s>>>(a);
     AVS_CUDA_TRY(cudaGetLastError());
     return AVS_SUCCESS;
