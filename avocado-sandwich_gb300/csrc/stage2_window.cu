@@ -457,7 +457,11 @@ static int chase_window(typename ChaseAr<S>::St *dAB, int64_t n, int bw, const S
     AVS_CUDA_TRY(cudaMemsetAsync(w.flags, 0, sizeof(int) * (size_t)((n + 1) * (int64_t)batch + 1), s));
     switch (bw) {
         case 8: return launch_win<8, S, 8>(dAB, n, w, s, num_sms, batch, sAB);
-        case 16: return launch_win<16, S, 8>(dAB, n, w, s, num_sms, batch, sAB);
+        // band 16: 8 sweeps per CTA for one matrix (n = 16384: 322 ms of stage 2 against 334 with 4); 4 for
+        // batches, whose matrices give the launch enough groups (512 matrices of order 256: 31.8 against
+        // 35.8 ms); the values do not depend on it
+        case 16: return batch > 1 ? launch_win<16, S, 4>(dAB, n, w, s, num_sms, batch, sAB)
+                                  : launch_win<16, S, 8>(dAB, n, w, s, num_sms, batch, sAB);
         case 32: return launch_win<32, S, 3>(dAB, n, w, s, num_sms, batch, sAB);
         default: return AVS_ERR_UNSUPPORTED;
     }
