@@ -400,8 +400,8 @@ def tensor_roofline(args, update_ms):
 
 
 def gflops_report(args, seconds):
-    """The benchmark spec's convention: (8/3) n^3 flops of the band reduction per
-    SVD over the whole SVD's time, against the FP64 and TF32 compute roofs."""
+    """The usual convention for a bidiagonal reduction: (8/3) n^3 flops per SVD
+    over the whole SVD's time, against the FP64 and TF32 compute roofs."""
     _, bf16, src = load_peaks()
     f = 8.0 / 3.0 * float(args.n) ** 3
     g = f / seconds / 1e9
@@ -416,7 +416,8 @@ def gflops_report(args, seconds):
 
 def run_modes(args, A, h, s64, lapack):
     """The other precision modes on the same matrix (one warm-up, one timed call),
-    and the headline mode with FP64 stages 2 and 3 (the benchmark spec's form)."""
+    and the headline mode with FP64 stages 2 and 3 (Householder generation's
+    neighbours, the chase and the bisection, in FP64)."""
     import avs
     out = {}
     legs = [(p, "auto") for p in ("tf32x3", "tf32", "bf16x3", "bf16", "fp32") if p != args.precision]
