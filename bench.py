@@ -416,8 +416,8 @@ def gflops_report(args, seconds):
 
 def run_modes(args, A, h, s64, lapack):
     """The other precision modes on the same matrix (one warm-up, one timed call),
-    and the headline mode with FP64 stages 2 and 3 (Householder generation's
-    neighbours, the chase and the bisection, in FP64)."""
+    and the headline mode with FP64 stages 2 and 3 (the bulge chase and the
+    bisection in FP64 arithmetic)."""
     import avs
     out = {}
     legs = [(p, "auto") for p in ("tf32x3", "tf32", "bf16x3", "bf16", "fp32") if p != args.precision]
