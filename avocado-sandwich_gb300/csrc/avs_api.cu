@@ -1,6 +1,7 @@
 // C ABI of the GB300 tiled SVD: handle, workspace, argument checks and the
 // three-stage pipeline behind my_CU_svdval (CUDAbasedSVD/SVD_GPU.jl:257-283).
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cstdio>
 #include <cstdlib>
@@ -305,6 +306,18 @@ int run_stages23(avs_handle *h, const Layout &L, int64_t n, int b, const S *W, i
     return AVS_SUCCESS;
 }
 
+// Calls of the process whose stage 1 may run a panel that waits on the GPU
+// for its tiles beside the chain; only a call that starts while no other one
+// runs does so (the flag is held until the call's stream is synchronised).
+std::atomic<int> g_lookahead_calls{0};
+struct LookaheadSlot {
+    bool on, solo;
+    explicit LookaheadSlot(bool use) : on(use), solo(use && g_lookahead_calls.fetch_add(1) == 0) {}
+    ~LookaheadSlot() {
+        if (on) g_lookahead_calls.fetch_sub(1);
+    }
+};
+
 // The pipeline on device data.  S = tile storage type.  src holds the input
 // (type TI, leading dimension lds) on the device; sigma_out (type TO) on the device.
 template <typename S, typename TI, typename TO>
@@ -332,6 +345,8 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
     w1.la_fork = h->la_ev[0];
     w1.la_panel = h->la_ev[1];
     w1.la_tb = h->la_ev[2];
+    const LookaheadSlot slot(tc_split != 0);
+    w1.la_ready = slot.solo;
     int upd_used = 0;
     if (tc_split && rep) {
         const int pairs = (int)(8 * (n / b));  // four parts per half-step

@@ -129,6 +129,10 @@ struct Stage1Work {
     // runs on the caller's stream in the same order
     cudaStream_t aux = nullptr;
     cudaEvent_t la_fork = nullptr, la_panel = nullptr, la_tb = nullptr;
+    // the panel may start beside the chain, waiting for its tiles, only when
+    // no other such call of the process runs at the same time (waiting panels
+    // of several calls could hold every SM their chains need)
+    bool la_ready = false;
 };
 template <typename T>
 int stage1_tbuild(const T *dA, int64_t lda, int b, int layout, int pr, int pc, int P, const Stage1Work &w,

@@ -1026,10 +1026,11 @@ int stage1_ge2bnd_tc(float *X, int64_t n, int b, const Stage1Work &w, cudaStream
         if (la) AVS_CUDA_TRY(cudaStreamWaitEvent(s, w.la_tb, 0));
         // The panel starts beside the chain (its roles wait for their tiles)
         // only while its P2 CTAs, on at most P2 SMs, leave at least half of the
-        // SMs to the chain; otherwise after it.  The chain is launched first:
+        // SMs to the chain and no other call of the process does the same
+        // (w.la_ready); otherwise after it.  The chain is launched first:
         // where the two streams share a hardware queue the panel then simply
         // runs after it, so the panel's waits never hold the chain back.
-        int *ready = (la && 2 * P2 <= sms) ? tb.ready : nullptr;
+        int *ready = (la && w.la_ready && 2 * P2 <= sms) ? tb.ready : nullptr;
         if ((r = timed_update(M, n, b, pr, pc, P, w, tb, s, launches, kTcPlanes, nullptr, ready)) != AVS_SUCCESS)
             return r;
         if (ready) AVS_CUDA_TRY(cudaEventRecord(w.la_fork, s));
