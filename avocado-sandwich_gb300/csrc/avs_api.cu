@@ -306,16 +306,30 @@ int run_stages23(avs_handle *h, const Layout &L, int64_t n, int b, const S *W, i
     return AVS_SUCCESS;
 }
 
-// Calls of the process whose stage 1 may run a panel that waits on the GPU
-// for its tiles beside the chain; only a call that starts while no other one
-// runs does so (the flag is held until the call's stream is synchronised).
-std::atomic<int> g_lookahead_calls{0};
+// Panel CTAs that calls of the process may keep waiting on the GPU for their
+// tiles beside their chains.  A call reserves its largest panel (nt - 1 CTAs)
+// for its whole duration, and only if all reservations together stay within
+// half of the SMs: the chains of all running calls then always have the other
+// half (waiting panels hold their SMs; every other kernel finishes by itself).
+// Held until the call's stream is synchronised.
+std::atomic<int> g_lookahead_ctas{0};
 struct LookaheadSlot {
-    bool on, solo;
-    explicit LookaheadSlot(bool use) : on(use), solo(use && g_lookahead_calls.fetch_add(1) == 0) {}
-    ~LookaheadSlot() {
-        if (on) g_lookahead_calls.fetch_sub(1);
+    int held = 0;
+    LookaheadSlot(int want, int limit) {
+        if (want <= 0) return;
+        int cur = g_lookahead_ctas.load();
+        while (cur + want <= limit) {
+            if (g_lookahead_ctas.compare_exchange_weak(cur, cur + want)) {
+                held = want;
+                break;
+            }
+        }
     }
+    ~LookaheadSlot() {
+        if (held) g_lookahead_ctas.fetch_sub(held);
+    }
+    LookaheadSlot(const LookaheadSlot &) = delete;
+    LookaheadSlot &operator=(const LookaheadSlot &) = delete;
 };
 
 // The pipeline on device data.  S = tile storage type.  src holds the input
@@ -345,8 +359,8 @@ int run_pipeline(avs_handle *h, const Layout &L, int64_t n, int b, const TI *src
     w1.la_fork = h->la_ev[0];
     w1.la_panel = h->la_ev[1];
     w1.la_tb = h->la_ev[2];
-    const LookaheadSlot slot(tc_split != 0);
-    w1.la_ready = slot.solo;
+    const LookaheadSlot slot(tc_split ? (int)(n / b) - 1 : 0, h->num_sms / 2);
+    w1.la_ready = slot.held > 0;
     int upd_used = 0;
     if (tc_split && rep) {
         const int pairs = (int)(8 * (n / b));  // four parts per half-step

@@ -130,8 +130,8 @@ struct Stage1Work {
     cudaStream_t aux = nullptr;
     cudaEvent_t la_fork = nullptr, la_panel = nullptr, la_tb = nullptr;
     // the panel may start beside the chain, waiting for its tiles, only when
-    // no other such call of the process runs at the same time (waiting panels
-    // of several calls could hold every SM their chains need)
+    // the call holds a reservation of its panel CTAs (the waiting panels of
+    // all running calls together stay within half of the SMs)
     bool la_ready = false;
 };
 template <typename T>

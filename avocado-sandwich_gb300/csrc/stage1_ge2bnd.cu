@@ -1026,8 +1026,9 @@ int stage1_ge2bnd_tc(float *X, int64_t n, int b, const Stage1Work &w, cudaStream
         if (la) AVS_CUDA_TRY(cudaStreamWaitEvent(s, w.la_tb, 0));
         // The panel starts beside the chain (its roles wait for their tiles)
         // only while its P2 CTAs, on at most P2 SMs, leave at least half of the
-        // SMs to the chain and no other call of the process does the same
-        // (w.la_ready); otherwise after it.  The chain is launched first:
+        // SMs to the chain and the call holds its reservation (w.la_ready: the
+        // waiting panels of all running calls within half of the SMs);
+        // otherwise after it.  The chain is launched first:
         // where the two streams share a hardware queue the panel then simply
         // runs after it, so the panel's waits never hold the chain back.
         int *ready = (la && w.la_ready && 2 * P2 <= sms) ? tb.ready : nullptr;
