@@ -26,7 +26,11 @@
 // next role reads only in its own apply), so the step between roles is one
 // reflector loop.  Roles are handed out by an atomic ticket in launch order,
 // so a role only ever waits on a role already running: no co-residency
-// assumption, and every wait is bounded.
+// assumption, and every wait is bounded.  The panel computes in its tile type,
+// except with the double-float trailing updates of FP64 tiles (AVS_PREC_FP64X2),
+// where it computes in double-float too (FP64 storage).  In the lookahead of the
+// tensor-core path (stage1_ge2bnd_tc) a role may also wait for its own tile,
+// which the previous update's chain finishes on the other stream.
 //
 // Trailing update kernel.  One CTA owns a column strip of the trailing matrix,
 // keeps the strip of the top tile row in shared memory, and applies the GEQRT
@@ -322,15 +326,15 @@ __global__ void __launch_bounds__(kNT) panel3_kernel(PanelArgs args) {
     using Acc = typename PScal<CT>::Acc;
     Acc *spart = reinterpret_cast<Acc *>(smem_raw);         // 8 warps
     CT *stau = reinterpret_cast<CT *>(smem_raw + sizeof(double) * 16);
-    CT *scal = stau + kIB;                                    // 16
-    CT *X = scal + 16;                                        // ldx * kIB (column-major)
-    CT *Yr = X + (size_t)ldx * kIB;                           // b * kIB (row-major: Yr[t*16 + l])
-    CT *Rt = Yr + (size_t)b * kIB;                            // kIB * b, Rt[l + j*kIB]
-    CT *Ws = Rt + (size_t)kIB * b;                            // kIB * b, Ws[l + j*kIB]
-    CT *Tm = Ws + (size_t)kIB * b;                            // kIB * kIB, Tm[l + i*kIB]
-    CT *G = Tm + kIB * kIB;                                   // kIB * kIB
-    CT *part = G + kIB * kIB;                                 // 2 x 8 * kIB (double-buffered)
-    CT *dsum = part + 16 * kIB;                               // end of the small arrays
+    CT *scal = stau + kIB;                                   // 16
+    CT *X = scal + 16;                                       // ldx * kIB (column-major)
+    CT *Yr = X + (size_t)ldx * kIB;                          // b * kIB (row-major: Yr[t*16 + l])
+    CT *Rt = Yr + (size_t)b * kIB;                           // kIB * b, Rt[l + j*kIB]
+    CT *Ws = Rt + (size_t)kIB * b;                           // kIB * b, Ws[l + j*kIB]
+    CT *Tm = Ws + (size_t)kIB * b;                           // kIB * kIB, Tm[l + i*kIB]
+    CT *G = Tm + kIB * kIB;                                  // kIB * kIB
+    CT *part = G + kIB * kIB;                                // 2 x 8 * kIB (double-buffered)
+    CT *dsum = part + 16 * kIB;                              // end of the small arrays
     // C chunks (16-byte aligned): LAYOUT 0 [column][row], LAYOUT 1 [row][column]
     T *cbuf0 = reinterpret_cast<T *>((reinterpret_cast<uintptr_t>(dsum + 2 * kIB + 8) + 15) & ~(uintptr_t)15);
 
