@@ -16,7 +16,9 @@
 // for b = 256) lives in tensor memory.  Both factors are triangular (T_p^T
 // and Y0 lower triangular in (row, k)), so the K blocks right of the first
 // half's diagonal block are skipped.  Top stays in shared memory (FP32) for
-// the whole chain.
+// the whole chain; at the end it goes to the matrix and, transposed, to the
+// other buffer (the next half-step's panel column), and each strip raises its
+// tile's counter so that panel can start on the tiles already finished.
 #include <cuda_bf16.h>
 
 #include "avs_common.cuh"

@@ -11,12 +11,17 @@
 //
 // tbuild_kernel forms T_p (b x b, upper triangular) from the 16 x 16 diagonal
 // blocks the panel kernel produced and the Gram matrix G = Y_p^T Y_p:
-// T[0:c0, J] = -T[0:c0, 0:c0] G[0:c0, J] T_JJ for the column blocks J.
+// T[0:c0, J] = -T[0:c0, 0:c0] G[0:c0, J] T_JJ for the column blocks J (FP64
+// tiles; in double-float with the double-float updates); tbuild_f32_kernel
+// forms the same T for FP32 tiles with T's upper block triangle in shared
+// memory.
 //
 // update_full_kernel: one CTA per column strip keeps the strip of the top tile
 // row in shared memory for the whole half-step; each of the three products is
 // a register-blocked GEMM (8 rows x CB columns per thread, K = b streamed
-// through shared memory in chunks that the next chunk's loads overlap).
+// through shared memory in chunks that the next chunk's loads overlap).  FP64
+// tiles use 16-column strips when 32-column strips would leave SMs idle; in
+// double-float the products accumulate with the compensated dot product.
 #include <algorithm>
 #include <type_traits>
 
