@@ -5,6 +5,7 @@ import ctypes
 import os
 import re
 
+import numpy as np
 import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -143,3 +144,18 @@ def test_ooc_plan_host_logic(avs_mod):
 def test_selftest_timeout_argument_check(avs_mod):
     assert avs_mod.lib().avs_selftest_timeout(None) == -1
     assert b"CUDA runtime error" in avs_mod.lib().avs_strerror(1)
+
+
+def test_serve_plan_host_logic(avs_mod):
+    """The serving plan is host arithmetic: FP64 requests share batched calls
+    in the double-float FP64X2 mode; FP32 requests of order >= 2048 run alone
+    with the split-BF16 tensor-core update (tile 128); smaller FP32 requests
+    share batched FP32 calls, tile 32 up to order 256 and 64 up to 1024."""
+    assert avs_mod.serve_plan(4096, np.float64) == (128, "fp64x2", True)
+    assert avs_mod.serve_plan(8192, np.float32) == (128, "bf16x3", False)
+    assert avs_mod.serve_plan(2048, np.float32) == (128, "bf16x3", False)
+    assert avs_mod.serve_plan(1024, np.float32) == (64, "fp32", True)
+    assert avs_mod.serve_plan(256, np.float32) == (32, "fp32", True)
+    assert avs_mod.serve_plan(96, np.float32)[0] == 32
+    # an explicit tile is kept
+    assert avs_mod.serve_plan(1024, np.float32, 128) == (128, "fp32", True)
